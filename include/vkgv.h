@@ -1,0 +1,340 @@
+/*
+ * vkgv.h — C ABI of the GB300 meshlet visibility-buffer path.
+ *
+ * This library replaces the Vulkan draw path of one headless vk_gltf_viewer
+ * frame: task-shader meshlet culling, mesh-shader + fixed-function
+ * visibility-buffer rasterisation, the HiZ min-pyramid reduction and the
+ * visibility-buffer resolve.  The scene is consumed in the renderer's own
+ * buffer layout (shaders/mesh_common.h.glsl:20-126,
+ * shaders/visbuffer/visbuffer.h.glsl:20-56), with every buffer device address
+ * being a CUDA device pointer instead of a VkDeviceAddress.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (VKGV_OK ...).  No C++
+ *     exception crosses this boundary.  vkgv_last_error() explains the last
+ *     non-OK status of a context.
+ *   - The caller owns the scene, the cameras and every per-view output.  The
+ *     context owns scratch (survivor lists, triangle bins, counters).
+ *   - Calls are ordered on the CUDA stream passed in (a cudaStream_t given as
+ *     void*; NULL is the legacy default stream).  A context is used by one
+ *     host thread at a time, as the reference records its frame from one
+ *     thread (src/vk_gltf_viewer/application.cpp:604-1280).
+ *   - Device pointers are passed as uint64_t device addresses, mirroring the
+ *     reference's buffer_reference push constants.
+ */
+#ifndef VKGV_H
+#define VKGV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum vkgv_status {
+    VKGV_OK = 0,
+    VKGV_INVALID_ARG = 1,    /* null pointer, zero-size view, bad flag mix  */
+    VKGV_OUT_OF_MEMORY = 2,  /* scratch allocation failed                   */
+    VKGV_LIMIT_EXCEEDED = 3, /* draw count >= 2^25, view > 8192 px, ...     */
+    VKGV_TIMEOUT = 4,        /* a bounded device wait ran out               */
+    VKGV_CUDA_ERROR = 5,     /* a CUDA runtime call failed                  */
+    VKGV_DEVICE_FAULT = 6    /* the device status word recorded a violation */
+};
+
+/* ------------------------------------------------------------- constants */
+/* shaders/mesh_common.h.glsl:36-38 */
+#define VKGV_MAX_VERTICES 64u
+#define VKGV_MAX_PRIMITIVES 126u
+#define VKGV_MAX_MESHLETS 102u
+/* src/vk_gltf_viewer/assets.cpp:324 — the builder's triangle limit */
+#define VKGV_BUILDER_MAX_TRIANGLES 124u
+/* shaders/visbuffer/visbuffer.h.glsl:15-16, 67 */
+#define VKGV_TRIANGLE_BITS 7u
+#define VKGV_DRAW_INDEX_BITS 25u
+#define VKGV_VISBUFFER_CLEAR 0xFFFFFFFFu
+/* shaders/resource_table.h.glsl:23 */
+#define VKGV_INVALID_HANDLE 0xFFFFFFFFu
+/* largest view edge; keeps 28.8 fixed-point coordinates inside int32 */
+#define VKGV_MAX_VIEW_DIM 8192u
+
+/* ---------------------------------------------------- scene layout (A7) */
+/* Byte-exact mirrors of the GLSL scalar-layout structs. */
+
+/* glsl::Meshlet, shaders/mesh_common.h.glsl:49-58 — 36 bytes */
+typedef struct vkgv_meshlet {
+    uint32_t vertex_offset;   /* first entry in the vertex-index stream   */
+    uint32_t triangle_offset; /* first byte in the triangle-index stream  */
+    uint8_t vertex_count;
+    uint8_t triangle_count;
+    uint8_t _pad[2];
+    float aabb_extents[3];
+    float aabb_center[3];
+} vkgv_meshlet;
+
+/* glsl::Vertex, shaders/mesh_common.h.glsl:60-71 — 24 bytes */
+typedef struct vkgv_vertex {
+    float position[3];
+    uint8_t color[4];   /* unpacked as color / 255 (mesh_common.h.glsl:74-76) */
+    uint8_t normal[3];  /* unpacked as normal / 127 - 1 (mesh_common.h.glsl:78-80) */
+    uint8_t _pad;
+    uint16_t uv[2];     /* IEEE binary16 */
+} vkgv_vertex;
+
+/* glsl::MeshletDraw, shaders/mesh_common.h.glsl:96-100 — 12 bytes */
+typedef struct vkgv_meshlet_draw {
+    uint32_t primitive_index;
+    uint32_t meshlet_index;
+    uint32_t transform_index;
+} vkgv_meshlet_draw;
+
+/* glsl::Primitive, shaders/mesh_common.h.glsl:102-113 — 64 bytes, align 8 */
+typedef struct vkgv_primitive {
+    uint64_t vertex_index_buffer;    /* uint32 per meshlet vertex            */
+    uint64_t primitive_index_buffer; /* uint8 triplets, meshlet-local        */
+    uint64_t vertex_buffer;          /* vkgv_vertex                          */
+    uint64_t meshlet_buffer;         /* vkgv_meshlet                         */
+    float aabb_extents[3];
+    float aabb_center[3];
+    uint32_t meshlet_count;
+    uint32_t material_index;
+} vkgv_primitive;
+
+/* glsl::Material, shaders/mesh_common.h.glsl:115-126 — 48 bytes */
+typedef struct vkgv_material {
+    float albedo_factor[4];
+    uint32_t albedo_index; /* index into the scene's texture table, or VKGV_INVALID_HANDLE */
+    float uv_offset[2];
+    float uv_scale[2];
+    float uv_rotation;
+    float alpha_cutoff;
+    uint32_t double_sided;
+} vkgv_material;
+
+/* glsl::Camera, shaders/mesh_common.h.glsl:20-27 — 352 bytes.
+ * Matrices are column-major (m[column*4 + row]). */
+typedef struct vkgv_camera {
+    float prev_view_projection[16];
+    float prev_occlusion_view_projection[16];
+    float view_projection[16];
+    float occlusion_view_projection[16];
+    float frustum[6][4];
+} vkgv_camera;
+
+/* Texture descriptor: the bindless sampled-image table entry that
+ * Material.albedoIndex names (shaders/resource_table.h.glsl:11). */
+enum vkgv_texture_format {
+    VKGV_TEXTURE_RGBA8 = 0,  /* 4 x uint8, sampled as UNORM then toLinear() */
+    VKGV_TEXTURE_RGB32F = 1  /* 3 x float, linear                            */
+};
+typedef struct vkgv_texture {
+    uint64_t data;       /* device address of texel (0,0)            */
+    uint32_t width;
+    uint32_t height;
+    uint32_t format;     /* vkgv_texture_format                      */
+    uint32_t row_pitch;  /* texels between rows (>= width)           */
+} vkgv_texture;
+
+/* HiZ pyramid: one R32_SFLOAT image with a full mip chain
+ * (src/vk_gltf_viewer/application.cpp:472-529).  Mip 0 is (W>>1) x (H>>1);
+ * mip k is max(1, (W>>1)>>k) x max(1, (H>>1)>>k); the mips are packed back
+ * to back starting at `data`.  levels = floor(log2(max(W, H))). */
+typedef struct vkgv_pyramid {
+    uint64_t data;
+    uint32_t width;   /* mip-0 width  = W >> 1 */
+    uint32_t height;  /* mip-0 height = H >> 1 */
+    uint32_t levels;  /* 0 = no pyramid */
+    uint32_t _pad;
+} vkgv_pyramid;
+
+/* The scene half of glsl::VisbufferPushConstants
+ * (shaders/visbuffer/visbuffer.h.glsl:37-47) plus the texture table. */
+typedef struct vkgv_scene {
+    uint64_t draw_buffer;        /* vkgv_meshlet_draw[meshlet_draw_count] */
+    uint64_t transform_buffer;   /* float[16] per node, column-major      */
+    uint64_t primitive_buffer;   /* vkgv_primitive[]                      */
+    uint64_t material_buffer;    /* vkgv_material[]                       */
+    uint64_t texture_table;      /* vkgv_texture[texture_count] or 0      */
+    uint32_t meshlet_draw_count;
+    uint32_t texture_count;
+} vkgv_scene;
+
+/* One headless view: the camera half of the push constants plus the
+ * per-view images of the visbuffer, resolve and HiZ passes. */
+typedef struct vkgv_view {
+    uint64_t camera_buffer;      /* device address of one vkgv_camera       */
+    uint32_t width;
+    uint32_t height;
+    vkgv_pyramid prev_pyramid;   /* read by the occlusion test; levels 0 = none */
+    vkgv_pyramid pyramid;        /* written from this frame's depth          */
+    uint64_t depth_id;           /* uint64[W*H]: (depth bits << 32) | (id + 1); 0 = clear */
+    uint64_t visbuffer;          /* uint32[W*H] visbuffer IDs, or 0          */
+    uint64_t color;              /* uint32[W*H] RGBA8 (R in the low byte), or 0 */
+    uint64_t survivors;          /* uint32[survivor_capacity] drawn draw indices, or 0 */
+    uint64_t survivor_count;     /* uint32 counter, or 0                     */
+    uint32_t survivor_capacity;
+    uint32_t _pad;
+} vkgv_view;
+
+/* ------------------------------------------------------------ frame flags */
+enum vkgv_frame_flags {
+    VKGV_CULL_FRUSTUM = 1u << 0,        /* isAabbInFrustum (culling.h.glsl:8-19)     */
+    VKGV_CULL_OCCLUSION = 1u << 1,      /* HiZ test vs prev_pyramid (task.glsl:54-65) */
+    VKGV_CULL_TWO_PASS = 1u << 2,       /* re-test pass-1 occlusion rejects vs this frame's pyramid */
+    VKGV_CULL_CONE = 1u << 3,           /* conservative meshlet normal-cone test     */
+    VKGV_RESOLVE_FLAT = 1u << 4,        /* visbuffer_resolve.comp.glsl               */
+    VKGV_RESOLVE_TEXTURED = 1u << 5,    /* barycentrics + texture resolve            */
+    VKGV_BUILD_PYRAMID = 1u << 6,       /* HiZ reduce chain into view.pyramid        */
+    VKGV_WRITE_IDS = 1u << 7,           /* write the uint32 visbuffer image          */
+    VKGV_SKIP_CLEAR = 1u << 8,          /* depth_id already cleared by the caller    */
+    /* The reference frame: application.cpp:764-1003. */
+    VKGV_FRAME_REFERENCE = (1u << 0) | (1u << 1) | (1u << 4) | (1u << 6) | (1u << 7)
+};
+
+/* --------------------------------------------------------------- context */
+typedef struct vkgv_ctx vkgv_ctx;
+typedef struct vkgv_graph vkgv_graph;
+
+typedef struct vkgv_config {
+    int32_t device;                  /* CUDA device ordinal                       */
+    uint32_t bin_size;               /* raster bin edge in pixels: 8/16/32, 0 = default */
+    uint32_t meshlets_per_cta;       /* meshlets per raster CTA: 1/2/4, 0 = default */
+    uint32_t big_triangle_capacity;  /* binned-triangle queue entries, 0 = default */
+    uint32_t spin_limit;             /* bounded device waits, 0 = default         */
+    uint32_t _reserved[3];
+} vkgv_config;
+
+/* Replaces Application's device/pass initialisation
+ * (src/vk_gltf_viewer/application.cpp:181-576). */
+int vkgv_create(const vkgv_config* config, vkgv_ctx** out_ctx);
+int vkgv_destroy(vkgv_ctx* ctx);
+/* Human-readable reason of the last non-OK status on ctx (never NULL). */
+const char* vkgv_last_error(const vkgv_ctx* ctx);
+/* Reads and clears the device status word (first recorded violation). */
+int vkgv_device_status(vkgv_ctx* ctx, uint32_t* out_code, uint32_t* out_detail);
+
+/* One frame for `view_count` views: clear, cull (1 or 2 passes), raster,
+ * pyramid, resolve as selected by `flags`.  Replaces the command recording
+ * of Application::run (src/vk_gltf_viewer/application.cpp:764-1003).
+ * view_count > 1 runs the batched path (all views in each launch). */
+int vkgv_frame(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views,
+               uint32_t view_count, uint32_t flags, void* stream);
+
+/* Stage entry points (each replaces one recorded pass). */
+/* Clears depth_id to 0 and resets the survivor counter
+ * (attachment clears, application.cpp:772-808). */
+int vkgv_clear(vkgv_ctx* ctx, const vkgv_view* view, void* stream);
+/* Task shader (shaders/visbuffer/visbuffer.task.glsl:25-76): appends the
+ * surviving draw indices to view->survivors.  pass 1 tests against
+ * view->prev_pyramid with prevOcclusionViewProjection; pass 2 re-tests the
+ * pass-1 occlusion rejects against view->pyramid with
+ * occlusionViewProjection. */
+int vkgv_cull(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view,
+              uint32_t flags, uint32_t pass, void* stream);
+/* Mesh shader + raster + fragment shader
+ * (shaders/visbuffer/visbuffer.mesh.glsl:30-104, visbuffer.frag.glsl:28-39):
+ * rasterises draw_list[first .. *draw_count) into view->depth_id with a
+ * 64-bit max, the order-independent equivalent of the GREATER_OR_EQUAL
+ * depth test (application.cpp:333).  draw_list/draw_count are device
+ * addresses; pass 0 for both to use view->survivors. */
+int vkgv_raster(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view,
+                uint64_t draw_list, uint64_t draw_count, uint32_t first, void* stream);
+/* HiZ reduce chain (shaders/hiz_reduce.comp.glsl, application.cpp:951-1003):
+ * view->depth_id -> view->pyramid. */
+int vkgv_hiz_reduce(vkgv_ctx* ctx, const vkgv_view* view, void* stream);
+/* Resolve (shaders/visbuffer/visbuffer_resolve.comp.glsl:17-41): writes
+ * view->color (and view->visbuffer with VKGV_WRITE_IDS).  flags selects
+ * VKGV_RESOLVE_FLAT or VKGV_RESOLVE_TEXTURED. */
+int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view,
+                 uint32_t flags, void* stream);
+
+/* GPU stage zones, the analogue of the reference's GPU profiler zones
+ * (TracyVkZone at application.cpp:765, 919, 952).  While enabled, every
+ * vkgv_frame outside graph capture records a CUDA event at each stage
+ * boundary; vkgv_stage_times waits for the last such frame and returns the
+ * milliseconds of each stage in this order: clear, cull pass 1, meshlet
+ * raster pass 1, binned raster pass 1, pyramid pass 1, cull pass 2,
+ * meshlet raster pass 2, binned raster pass 2, pyramid, resolve, finalise
+ * (VKGV_STAGE_COUNT entries; 0 for stages that did not run). */
+#define VKGV_STAGE_COUNT 11u
+int vkgv_set_profiling(vkgv_ctx* ctx, int32_t enable);
+int vkgv_stage_times(vkgv_ctx* ctx, float* out_ms, uint32_t count);
+
+/* Pyramid geometry for a W x H view: levels and total float count. */
+int vkgv_pyramid_layout(uint32_t width, uint32_t height, uint32_t* out_levels,
+                        uint64_t* out_float_count);
+
+/* Captures one vkgv_frame into a CUDA graph (the buffers named by scene and
+ * views are baked in; camera contents may change between launches). */
+int vkgv_graph_capture(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views,
+                       uint32_t view_count, uint32_t flags, vkgv_graph** out_graph);
+int vkgv_graph_launch(vkgv_graph* graph, void* stream);
+int vkgv_graph_destroy(vkgv_graph* graph);
+
+/* ---------------------------------------------- host scene producers (A15) */
+/* Replace the glTF import + meshletiser (src/vk_gltf_viewer/assets.cpp:288-430)
+ * for procedural scenes, and the camera update (src/vk_gltf_viewer/camera.cpp). */
+typedef struct vkgv_mesh vkgv_mesh;
+
+typedef struct vkgv_mesh_info {
+    uint32_t vertex_count;
+    uint32_t triangle_count;
+    uint32_t meshlet_count;
+    uint32_t vertex_index_count;     /* entries in the vertex-index stream   */
+    uint32_t primitive_index_bytes;  /* bytes in the triangle-index stream   */
+    float position_scale;            /* dequantisation scale a node matrix must apply
+                                        (KHR_mesh_quantization); 1 when unquantised */
+    const vkgv_vertex* vertices;
+    const float* positions;          /* float3 per vertex (unquantised source) */
+    const float* uvs;                /* float2 per vertex                      */
+    const uint32_t* indices;         /* uint32 x 3 per triangle                */
+    const vkgv_meshlet* meshlets;
+    const uint32_t* vertex_indices;
+    const uint8_t* primitive_indices;
+    float aabb_extents[3];
+    float aabb_center[3];
+} vkgv_mesh_info;
+
+/* Icosahedron subdivided `level` times onto the unit sphere
+ * (20 * 4^level triangles). */
+vkgv_mesh* vkgv_mesh_icosphere(uint32_t level);
+/* Torus (ring radius R, tube radius r) with seg_major x seg_minor quads,
+ * displaced along the normal by seeded value noise of amplitude noise_amp.
+ * quantize != 0 stores positions as KHR_mesh_quantization int16-normalised
+ * values (dequantised into vkgv_vertex.position) and normals as int8. */
+vkgv_mesh* vkgv_mesh_torus(float R, float r, uint32_t seg_major, uint32_t seg_minor,
+                           float noise_amp, uint64_t seed, int32_t quantize);
+/* Displaces an icosphere-like mesh along its normalised position by seeded
+ * value noise (amplitude amp). */
+int vkgv_mesh_displace(vkgv_mesh* mesh, float amp, uint64_t seed);
+/* Mesh from caller arrays (positions float3, indices uint32 x 3). */
+vkgv_mesh* vkgv_mesh_from_arrays(const float* positions, uint32_t vertex_count,
+                                 const uint32_t* indices, uint32_t triangle_count);
+/* Sets per-vertex RGBA8 colours and binary16 UVs from float arrays
+ * (either may be NULL). */
+int vkgv_mesh_set_attributes(vkgv_mesh* mesh, const float* rgba, const float* uv);
+/* Greedy meshletiser with the reference limits (64 vertices / 124
+ * triangles; assets.cpp:323-341); also computes each meshlet AABB
+ * (assets.cpp:348-372). */
+int vkgv_mesh_build_meshlets(vkgv_mesh* mesh, uint32_t max_vertices, uint32_t max_triangles);
+int vkgv_mesh_get_info(const vkgv_mesh* mesh, vkgv_mesh_info* out);
+void vkgv_mesh_free(vkgv_mesh* mesh);
+
+/* Camera update (src/vk_gltf_viewer/camera.cpp:170-193): shifts the current
+ * matrices into prev*, writes VP = reverseZ * perspectiveRH_ZO(y-flip) *
+ * lookAtRH, copies it to occlusionViewProjection and extracts the six
+ * frustum planes. */
+int vkgv_camera_update(vkgv_camera* camera, const float eye[3], const float target[3],
+                       const float up[3], float fovy_radians, float aspect,
+                       float znear, float zfar);
+/* Frustum planes of a view-projection (camera.cpp:70-84). */
+int vkgv_frustum_planes(const float view_projection[16], float out_planes[24]);
+
+/* Library version string. */
+const char* vkgv_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VKGV_H */

@@ -1,0 +1,233 @@
+"""ctypes binding of the CPU oracle (oracle.c).  TEST INFRASTRUCTURE ONLY:
+imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+as the checker, never by the product package.
+
+Parity status: the oracle is pinned by hand-derived known-answer cases only;
+parity with the reference renderer's own execution is unpinned (it needs a
+Vulkan mesh-shader device, which does not exist here).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+
+CULL_FRUSTUM = 1 << 0
+CULL_OCCLUSION = 1 << 1
+CULL_TWO_PASS = 1 << 2
+CULL_CONE = 1 << 3
+RESOLVE_FLAT = 1 << 4
+RESOLVE_TEXTURED = 1 << 5
+BUILD_PYRAMID = 1 << 6
+
+
+class OrcPrimitive(C.Structure):
+    _fields_ = [("vertex_indices", C.c_void_p), ("primitive_indices", C.c_void_p), ("vertices", C.c_void_p),
+                ("meshlets", C.c_void_p), ("aabb_extents", C.c_float * 3), ("aabb_center", C.c_float * 3),
+                ("meshlet_count", C.c_uint32), ("material_index", C.c_uint32)]
+
+
+class OrcTexture(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("format", C.c_uint32),
+                ("row_pitch", C.c_uint32)]
+
+
+class OrcScene(C.Structure):
+    _fields_ = [("draws", C.c_void_p), ("draw_count", C.c_uint32), ("transforms", C.c_void_p),
+                ("primitives", C.c_void_p), ("materials", C.c_void_p), ("textures", C.c_void_p),
+                ("texture_count", C.c_uint32)]
+
+
+class OrcPyramid(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("levels", C.c_uint32)]
+
+
+_lib = None
+
+
+def build() -> Path:
+    """Compiles the oracle with its Makefile (gcc, no fast-math)."""
+    res = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    return LIB
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        lib = C.CDLL(str(LIB))
+        P = C.c_void_p
+        U32 = C.c_uint32
+        lib.orc_set_threads.argtypes = [C.c_int]
+        lib.orc_get_threads.restype = C.c_int
+        lib.orc_pyramid_levels.restype = U32
+        lib.orc_pyramid_levels.argtypes = [U32, U32]
+        lib.orc_pyramid_floats.restype = C.c_uint64
+        lib.orc_pyramid_floats.argtypes = [U32, U32]
+        lib.orc_cull.argtypes = [P, P, P, U32, U32, P, U32, P, P, P, P]
+        lib.orc_raster.argtypes = [P, P, U32, U32, P, U32, P]
+        lib.orc_hiz.argtypes = [P, U32, U32, P]
+        lib.orc_resolve.argtypes = [P, P, U32, U32, P, U32, P, P]
+        lib.orc_frame.argtypes = [P, P, U32, U32, P, U32, P, P, P, P, P, P]
+        lib.orc_from_linear.restype = C.c_float
+        lib.orc_from_linear.argtypes = [C.c_float]
+        lib.orc_to_linear.restype = C.c_float
+        lib.orc_to_linear.argtypes = [C.c_float]
+        lib.orc_unorm8.restype = U32
+        lib.orc_unorm8.argtypes = [C.c_float]
+        lib.orc_raster_triangle.argtypes = [P, P, P, U32, U32, U32, P]
+        lib.orc_min_sample.restype = C.c_float
+        lib.orc_min_sample.argtypes = [P, U32, U32, C.c_float, C.c_float]
+        lib.orc_frustum_visible.restype = C.c_int
+        lib.orc_frustum_visible.argtypes = [P, P, P]
+        _lib = lib
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    load().orc_set_threads(int(n))
+
+
+def _addr(a: np.ndarray) -> int:
+    return int(a.ctypes.data)
+
+
+class OracleScene:
+    """orc_scene over the host arrays of a HostScene (kept alive here)."""
+
+    def __init__(self, host):
+        self.host = host
+        self._keep = []
+        prims = (OrcPrimitive * len(host.meshes))()
+        for p, m in enumerate(host.meshes):
+            arrs = [np.ascontiguousarray(m.vertex_indices), np.ascontiguousarray(m.primitive_indices),
+                    np.ascontiguousarray(m.vertices), np.ascontiguousarray(m.meshlets)]
+            self._keep += arrs
+            prims[p].vertex_indices, prims[p].primitive_indices, prims[p].vertices, prims[p].meshlets = map(_addr, arrs)
+            prims[p].aabb_extents[:] = [float(x) for x in m.aabb_extents]
+            prims[p].aabb_center[:] = [float(x) for x in m.aabb_center]
+            prims[p].meshlet_count = m.meshlet_count
+            prims[p].material_index = host.prim_materials[p]
+        self.prims = prims
+        self.draws = np.ascontiguousarray(host.draws, np.uint32)
+        self.transforms = np.ascontiguousarray(host.transforms, np.float32)
+        self.materials = np.ascontiguousarray(host.materials)
+        texs = (OrcTexture * max(1, len(host.textures)))()
+        for i, t in enumerate(host.textures):
+            d = np.ascontiguousarray(t.data)
+            self._keep.append(d)
+            texs[i].data = _addr(d)
+            texs[i].width, texs[i].height, texs[i].format, texs[i].row_pitch = t.width, t.height, t.format, t.width
+        self.texs = texs
+        self.s = OrcScene(draws=_addr(self.draws), draw_count=host.draw_count, transforms=_addr(self.transforms),
+                          primitives=C.addressof(prims), materials=_addr(self.materials),
+                          textures=C.addressof(texs), texture_count=len(host.textures))
+
+    @property
+    def ptr(self):
+        return C.addressof(self.s)
+
+
+def pyramid_floats(w: int, h: int) -> int:
+    return int(load().orc_pyramid_floats(w, h))
+
+
+def pyramid_levels(w: int, h: int) -> int:
+    return int(load().orc_pyramid_levels(w, h))
+
+
+def cull(os_: OracleScene, cam, w: int, h: int, flags: int, pass_: int = 1, pyramid: np.ndarray | None = None,
+         candidates: np.ndarray | None = None):
+    """Returns (survivors, occlusion_rejects) as uint32 arrays."""
+    lib = load()
+    n = os_.host.draw_count if candidates is None else int(candidates.size)
+    surv = np.zeros(max(1, n), np.uint32)
+    rej = np.zeros(max(1, n), np.uint32)
+    ns, nr = C.c_uint32(), C.c_uint32()
+    pyr = None
+    if pyramid is not None:
+        pyramid = np.ascontiguousarray(pyramid, np.float32)
+        pyr = OrcPyramid(_addr(pyramid), w >> 1, h >> 1, pyramid_levels(w, h))
+    cand = None if candidates is None else np.ascontiguousarray(candidates, np.uint32)
+    lib.orc_cull(os_.ptr, C.addressof(cam), C.addressof(pyr) if pyr is not None else None, flags, pass_,
+                 _addr(cand) if cand is not None else None, n, _addr(surv), C.addressof(ns), _addr(rej),
+                 C.addressof(nr))
+    return surv[: ns.value].copy(), rej[: nr.value].copy()
+
+
+def raster(os_: OracleScene, cam, w: int, h: int, draws: np.ndarray, depth_id: np.ndarray | None = None):
+    lib = load()
+    draws = np.ascontiguousarray(draws, np.uint32)
+    if depth_id is None:
+        depth_id = np.zeros(w * h, np.uint64)
+    lib.orc_raster(os_.ptr, C.addressof(cam), w, h, _addr(draws) if draws.size else None, draws.size,
+                   _addr(depth_id))
+    return depth_id
+
+
+def hiz(depth_id: np.ndarray, w: int, h: int) -> np.ndarray:
+    pyr = np.zeros(max(1, pyramid_floats(w, h)), np.float32)
+    load().orc_hiz(_addr(np.ascontiguousarray(depth_id, np.uint64)), w, h, _addr(pyr))
+    return pyr
+
+
+def resolve(os_: OracleScene, cam, w: int, h: int, depth_id: np.ndarray, textured: bool = False):
+    ids = np.zeros(w * h, np.uint32)
+    rgba = np.zeros(w * h, np.uint32)
+    load().orc_resolve(os_.ptr, C.addressof(cam), w, h, _addr(np.ascontiguousarray(depth_id, np.uint64)),
+                       1 if textured else 0, _addr(ids), _addr(rgba))
+    return ids, rgba
+
+
+def frame(os_: OracleScene, cam, w: int, h: int, flags: int, prev_pyramid: np.ndarray | None = None):
+    """Whole frame; returns dict with depth_id, ids, rgba, pyramid, survivors."""
+    lib = load()
+    depth = np.zeros(w * h, np.uint64)
+    ids = np.zeros(w * h, np.uint32)
+    rgba = np.zeros(w * h, np.uint32)
+    pyr = np.zeros(max(1, pyramid_floats(w, h)), np.float32)
+    surv = np.zeros(max(1, os_.host.draw_count), np.uint32)
+    ns = C.c_uint32()
+    prev = None
+    if prev_pyramid is not None:
+        prev_pyramid = np.ascontiguousarray(prev_pyramid, np.float32)
+        prev = OrcPyramid(_addr(prev_pyramid), w >> 1, h >> 1, pyramid_levels(w, h))
+    lib.orc_frame(os_.ptr, C.addressof(cam), w, h, C.addressof(prev) if prev is not None else None, flags,
+                  _addr(depth), _addr(ids), _addr(rgba), _addr(pyr), _addr(surv), C.addressof(ns))
+    return {"depth_id": depth, "ids": ids, "rgba": rgba, "pyramid": pyr, "survivors": surv[: ns.value].copy()}
+
+
+def raster_triangle(v0, v1, v2, tri_id: int, w: int, h: int, depth_id: np.ndarray | None = None):
+    if depth_id is None:
+        depth_id = np.zeros(w * h, np.uint64)
+    a = [np.ascontiguousarray(v, np.float32) for v in (v0, v1, v2)]
+    load().orc_raster_triangle(_addr(a[0]), _addr(a[1]), _addr(a[2]), tri_id, w, h, _addr(depth_id))
+    return depth_id
+
+
+def min_sample(img: np.ndarray, u: float, v: float) -> float:
+    img = np.ascontiguousarray(img, np.float32)
+    return float(load().orc_min_sample(_addr(img), img.shape[1], img.shape[0], u, v))
+
+
+def frustum_visible(center, extents, planes) -> bool:
+    c = np.ascontiguousarray(center, np.float32)
+    e = np.ascontiguousarray(extents, np.float32)
+    p = np.ascontiguousarray(planes, np.float32).reshape(24)
+    return bool(load().orc_frustum_visible(_addr(c), _addr(e), _addr(p)))
+
+
+def from_linear(c: float) -> float:
+    return float(load().orc_from_linear(c))
+
+
+def unorm8(c: float) -> int:
+    return int(load().orc_unorm8(c))

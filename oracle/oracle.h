@@ -1,0 +1,146 @@
+/*
+ * oracle.h — CPU restatement of vk_gltf_viewer's meshlet visibility-buffer
+ * path.  TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check and the
+ * CPU-baseline leg of the benchmark call it as the checker.  The product
+ * library never links or calls it.
+ *
+ * Parity status: the reference renderer cannot execute here (it needs a
+ * Vulkan 1.3 mesh-shader device and glslangValidator; no graphics stack
+ * exists on either machine), so the restatement is pinned by hand-derived
+ * known-answer cases (tests/golden/kat_*.json) and by the reference's
+ * constants, not by reference output.  Parity with the reference's own
+ * execution is therefore unpinned beyond those cases.
+ *
+ * Every function follows the reference file:line named in its comment.  The
+ * parts the reference leaves to the Vulkan implementation (rasterisation
+ * rules, depth interpolation, min-reduction sampler footprint, clipping)
+ * are pinned as documented in oracle.c and implemented identically by the
+ * CUDA kernels.
+ */
+#ifndef VKGV_ORACLE_H
+#define VKGV_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Layout restatements (shaders/mesh_common.h.glsl:20-126, scalar layout). */
+typedef struct orc_meshlet {
+    uint32_t vertex_offset, triangle_offset;
+    uint8_t vertex_count, triangle_count, pad_[2];
+    float aabb_extents[3], aabb_center[3];
+} orc_meshlet; /* 36 B */
+
+typedef struct orc_vertex {
+    float position[3];
+    uint8_t color[4];
+    uint8_t normal[3];
+    uint8_t pad_;
+    uint16_t uv[2];
+} orc_vertex; /* 24 B */
+
+typedef struct orc_draw {
+    uint32_t primitive_index, meshlet_index, transform_index;
+} orc_draw; /* 12 B */
+
+typedef struct orc_material {
+    float albedo_factor[4];
+    uint32_t albedo_index;
+    float uv_offset[2], uv_scale[2], uv_rotation, alpha_cutoff;
+    uint32_t double_sided;
+} orc_material; /* 48 B */
+
+typedef struct orc_camera {
+    float prev_vp[16], prev_occlusion_vp[16], vp[16], occlusion_vp[16];
+    float frustum[6][4];
+} orc_camera; /* 352 B */
+
+/* A primitive with host pointers in place of the device addresses. */
+typedef struct orc_primitive {
+    const uint32_t* vertex_indices;
+    const uint8_t* primitive_indices;
+    const orc_vertex* vertices;
+    const orc_meshlet* meshlets;
+    float aabb_extents[3], aabb_center[3];
+    uint32_t meshlet_count, material_index;
+} orc_primitive;
+
+typedef struct orc_texture {
+    const void* data;
+    uint32_t width, height, format, row_pitch; /* format: 0 RGBA8, 1 RGB32F */
+} orc_texture;
+
+typedef struct orc_scene {
+    const orc_draw* draws;
+    uint32_t draw_count;
+    const float* transforms; /* 16 floats per node, column-major */
+    const orc_primitive* primitives;
+    const orc_material* materials;
+    const orc_texture* textures;
+    uint32_t texture_count;
+} orc_scene;
+
+/* Pyramid: mip k is max(1,w0>>k) x max(1,h0>>k) floats, packed. */
+typedef struct orc_pyramid {
+    float* data;
+    uint32_t width, height, levels;
+} orc_pyramid;
+
+enum {
+    ORC_CULL_FRUSTUM = 1u << 0,
+    ORC_CULL_OCCLUSION = 1u << 1,
+    ORC_CULL_TWO_PASS = 1u << 2,
+    ORC_CULL_CONE = 1u << 3,
+    ORC_RESOLVE_FLAT = 1u << 4,
+    ORC_RESOLVE_TEXTURED = 1u << 5,
+    ORC_BUILD_PYRAMID = 1u << 6
+};
+
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+uint32_t orc_pyramid_levels(uint32_t w, uint32_t h);
+uint64_t orc_pyramid_floats(uint32_t w, uint32_t h);
+
+/* Task shader for a candidate list (NULL = all draws).  pass 1 uses
+ * prevOcclusionViewProjection, pass 2 occlusionViewProjection.
+ * Survivors come out in ascending draw order.  rejected receives the draws
+ * that passed the frustum test but failed the occlusion test. */
+void orc_cull(const orc_scene* s, const orc_camera* cam, const orc_pyramid* pyr,
+              uint32_t flags, uint32_t pass, const uint32_t* cand, uint32_t ncand,
+              uint32_t* survivors, uint32_t* nsurv, uint32_t* rejected, uint32_t* nrej);
+
+/* Mesh shader + fixed-function raster + fragment shader for a draw list. */
+void orc_raster(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h,
+                const uint32_t* draws, uint32_t ndraws, uint64_t* depth_id);
+
+/* HiZ reduce chain (hiz_reduce.comp.glsl + application.cpp:951-1003). */
+void orc_hiz(const uint64_t* depth_id, uint32_t w, uint32_t h, float* pyramid);
+
+/* visbuffer_resolve.comp.glsl (flat) or the textured extension. */
+void orc_resolve(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h,
+                 const uint64_t* depth_id, uint32_t textured, uint32_t* ids, uint32_t* rgba);
+
+/* A whole frame with the same pass structure as vkgv_frame. */
+void orc_frame(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h,
+               const orc_pyramid* prev, uint32_t flags, uint64_t* depth_id,
+               uint32_t* ids, uint32_t* rgba, float* pyramid_out,
+               uint32_t* survivors, uint32_t* nsurv);
+
+/* Single-fragment helpers exported for the known-answer tests. */
+float orc_from_linear(float c);
+float orc_to_linear(float c);
+uint32_t orc_unorm8(float c);
+/* Rasterises one clip-space triangle with a given id (KAT entry point). */
+void orc_raster_triangle(const float v0[4], const float v1[4], const float v2[4],
+                         uint32_t id, uint32_t w, uint32_t h, uint64_t* depth_id);
+/* Min-reduction sample of a single-level image (KAT entry point). */
+float orc_min_sample(const float* img, uint32_t w, uint32_t h, float u, float v);
+int orc_frustum_visible(const float center[3], const float extents[3], const float planes[24]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,232 @@
+"""GPU parity of every stage against the CPU oracle, through the C ABI.
+
+Bit-exact: survivor sets, depth|id buffers, visbuffer IDs, HiZ mips.
+Resolve RGBA8: within 1/255 per channel (fromLinear/toLinear use powf, whose
+last-ulp results differ between libm and CUDA)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import binding as ob
+from vk_gltf_viewer_gb300 import abi, scene
+
+from gpu_util import Pair, oracle_flags, orbit_cameras, rgba_close, small_grid, u32, u64, view
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ico(renderer):
+    return Pair(scene.scene_icosphere(6))
+
+
+@pytest.fixture(scope="module")
+def grid(renderer):
+    return Pair(small_grid())
+
+
+def test_cull_frustum_matches_oracle(renderer, ico):
+    w, h = 1280, 720
+    cams = orbit_cameras(6, 3.0, w, h, seed=1) + orbit_cameras(3, 1.3, w, h, seed=2)
+    for cam in cams:
+        v = view(ico, cam, w, h)
+        renderer.clear(ico.dev, v)
+        renderer.cull(ico.dev, v, abi.CULL_FRUSTUM, 1)
+        got = np.sort(v.survivor_list())
+        exp, _ = ob.cull(ico.orc, cam, w, h, ob.CULL_FRUSTUM)
+        assert np.array_equal(got, np.sort(exp))
+
+
+def test_cull_occlusion_matches_oracle(renderer, grid):
+    w, h = 640, 360
+    cam0 = scene.grid_camera(w, h)
+    prev = ob.frame(grid.orc, cam0, w, h, ob.CULL_FRUSTUM | ob.BUILD_PYRAMID)["pyramid"]
+    for cam in orbit_cameras(4, 12.0, w, h, seed=5, centre=tuple(scene.grid_centre() * 0.25)) + [cam0]:
+        v = view(grid, cam, w, h, prev=prev)
+        renderer.clear(grid.dev, v)
+        renderer.cull(grid.dev, v, abi.CULL_FRUSTUM | abi.CULL_OCCLUSION, 1)
+        got = np.sort(v.survivor_list())
+        exp, _ = ob.cull(grid.orc, cam, w, h, ob.CULL_FRUSTUM | ob.CULL_OCCLUSION, 1, pyramid=prev)
+        assert np.array_equal(got, np.sort(exp))
+
+
+@pytest.mark.parametrize("size", [(1280, 720), (333, 257), (64, 64), (1, 1)])
+def test_raster_matches_oracle(renderer, ico, size):
+    w, h = size
+    for cam in orbit_cameras(3, 2.6, w, h, seed=11) + orbit_cameras(2, 1.05, w, h, seed=12):
+        exp_surv, _ = ob.cull(ico.orc, cam, w, h, ob.CULL_FRUSTUM)
+        exp = ob.raster(ico.orc, cam, w, h, exp_surv)
+        v = view(ico, cam, w, h)
+        renderer.clear(ico.dev, v)
+        lst = torch.from_numpy(exp_surv.view(np.int32).copy()).cuda()
+        cnt = torch.tensor([exp_surv.size], dtype=torch.int32, device="cuda")
+        renderer.raster(ico.dev, v, lst, cnt)
+        got = u64(v.depth_id)
+        assert np.array_equal(got, exp), f"{(got != exp).sum()} pixels differ"
+
+
+def test_raster_near_plane_and_guard_band(renderer, grid):
+    """Cameras inside the grid, close to geometry: triangles cross the near
+    plane and extend far past the guard band."""
+    w, h = 800, 600
+    c = scene.grid_centre() * 0.25
+    eyes = [(0.0, 0.05, 0.9), (0.3, 0.0, 0.0), (2.5, 0.2, 1.2)]
+    for e in eyes:
+        cam = scene.camera(e, (e[0] + 1.0, e[1] - 0.1, e[2] + 0.3), (0, 1, 0), 75.0, w / h)
+        exp_surv, _ = ob.cull(grid.orc, cam, w, h, ob.CULL_FRUSTUM)
+        exp = ob.raster(grid.orc, cam, w, h, exp_surv)
+        v = view(grid, cam, w, h)
+        renderer.clear(grid.dev, v)
+        lst = torch.from_numpy(exp_surv.view(np.int32).copy()).cuda()
+        cnt = torch.tensor([exp_surv.size], dtype=torch.int32, device="cuda")
+        renderer.raster(grid.dev, v, lst, cnt)
+        got = u64(v.depth_id)
+        assert np.array_equal(got, exp), f"eye {e}: {(got != exp).sum()} pixels differ"
+    del c
+
+
+@pytest.mark.parametrize("size", [(1920, 1080), (1280, 720), (135, 77), (512, 384), (3, 1), (1, 1), (257, 1025)])
+def test_hiz_matches_oracle(renderer, ico, size):
+    w, h = size
+    rng = np.random.default_rng(w * 7 + h)
+    d = rng.random(w * h, dtype=np.float32)
+    d[rng.random(w * h) < 0.2] = 0.0
+    depth_id = (d.view(np.uint32).astype(np.uint64) << np.uint64(32)) | np.uint64(3)
+    exp = ob.hiz(depth_id, w, h)
+    cam = scene.camera((0, 0, 3), (0, 0, 0), (0, 1, 0), 60, w / h)
+    v = view(ico, cam, w, h)
+    v.depth_id.copy_(torch.from_numpy(depth_id.view(np.int64)).cuda())
+    if v.pyramid is None:
+        pytest.skip("no pyramid for a 1x1 view")
+    v.pyramid.fill_(-1.0)
+    renderer.hiz(ico.dev, v)
+    got = v.pyramid.cpu().numpy()
+    assert np.array_equal(got[: exp.size], exp)
+
+
+@pytest.mark.parametrize("textured", [False, True])
+def test_resolve_matches_oracle(renderer, grid, textured):
+    w, h = 640, 360
+    cam = scene.grid_camera(w, h)
+    out = ob.frame(grid.orc, cam, w, h, ob.CULL_FRUSTUM)
+    v = view(grid, cam, w, h)
+    v.depth_id.copy_(torch.from_numpy(out["depth_id"].view(np.int64)).cuda())
+    flags = (abi.RESOLVE_TEXTURED if textured else abi.RESOLVE_FLAT) | abi.WRITE_IDS
+    renderer.resolve(grid.dev, v, flags)
+    ids, rgba = ob.resolve(grid.orc, cam, w, h, out["depth_id"], textured)
+    assert np.array_equal(u32(v.visbuffer), ids)
+    ok, bad = rgba_close(u32(v.color), rgba)
+    assert ok, f"{bad} pixels off by more than 1/255"
+
+
+FRAME_CASES = {
+    "reference": abi.FRAME_REFERENCE,
+    "two_pass_textured": abi.CULL_FRUSTUM | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID
+    | abi.RESOLVE_TEXTURED | abi.WRITE_IDS,
+}
+
+
+@pytest.mark.parametrize("name", sorted(FRAME_CASES))
+def test_frame_matches_oracle(renderer, grid, name):
+    flags = FRAME_CASES[name]
+    w, h = 960, 540
+    cam0 = scene.grid_camera(w, h)
+    first = ob.frame(grid.orc, cam0, w, h, oracle_flags(flags))
+    cam1 = scene.camera((0.9, 4.0, 4.5), tuple(scene.grid_centre() * 0.25), (0, 1, 0), 75.0, w / h, prev=cam0)
+    exp = ob.frame(grid.orc, cam1, w, h, oracle_flags(flags), prev_pyramid=first["pyramid"])
+    v = view(grid, cam1, w, h, prev=first["pyramid"])
+    renderer.frame(grid.dev, [v], flags)
+    torch.cuda.synchronize()
+    assert np.array_equal(np.sort(v.survivor_list()), np.sort(exp["survivors"]))
+    assert np.array_equal(u64(v.depth_id), exp["depth_id"])
+    assert np.array_equal(u32(v.visbuffer), exp["ids"])
+    assert np.array_equal(v.pyramid.cpu().numpy()[: exp["pyramid"].size], exp["pyramid"])
+    ok, bad = rgba_close(u32(v.color), exp["rgba"])
+    assert ok, f"{bad} pixels off"
+    assert renderer.device_status() == (0, 0)
+
+
+def test_batched_frame_matches_single_views(renderer, grid):
+    flags = abi.CULL_FRUSTUM | abi.BUILD_PYRAMID | abi.RESOLVE_FLAT | abi.WRITE_IDS
+    sizes = [(256, 256), (512, 384), (640, 360), (97, 61), (1024, 576)]
+    centre = scene.grid_centre() * 0.25
+    rng = np.random.default_rng(21)
+    views, exps = [], []
+    for w, h in sizes:
+        d = rng.normal(size=3)
+        eye = centre + 9.0 * d / np.linalg.norm(d)
+        cam = scene.camera(tuple(eye), tuple(centre), scene.safe_up(eye, centre), 75.0, w / h)
+        views.append(view(grid, cam, w, h))
+        exps.append(ob.frame(grid.orc, cam, w, h, oracle_flags(flags)))
+    renderer.frame(grid.dev, views, flags)
+    torch.cuda.synchronize()
+    for v, e in zip(views, exps):
+        assert np.array_equal(u32(v.visbuffer), e["ids"])
+        assert np.array_equal(v.pyramid.cpu().numpy()[: e["pyramid"].size], e["pyramid"])
+        assert np.array_equal(np.sort(v.survivor_list()), np.sort(e["survivors"]))
+
+
+def test_graph_replay_matches_frame(renderer, grid):
+    flags = abi.FRAME_REFERENCE
+    w, h = 640, 360
+    cam = scene.grid_camera(w, h)
+    v = view(grid, cam, w, h)
+    renderer.frame(grid.dev, [v], flags)
+    torch.cuda.synchronize()
+    ref_ids = u32(v.visbuffer).copy()
+    ref_rgba = u32(v.color).copy()
+    g = renderer.capture(grid.dev, [v], flags)
+    v.visbuffer.zero_()
+    v.color.zero_()
+    for _ in range(2):
+        g.launch()
+    torch.cuda.synchronize()
+    assert np.array_equal(u32(v.visbuffer), ref_ids)
+    assert np.array_equal(u32(v.color), ref_rgba)
+    g.close()
+
+
+def test_rerun_is_bit_identical(renderer, grid):
+    w, h = 800, 450
+    cam = scene.grid_camera(w, h)
+    v = view(grid, cam, w, h)
+    renderer.frame(grid.dev, [v], abi.FRAME_REFERENCE)
+    a = u64(v.depth_id).copy()
+    renderer.frame(grid.dev, [v], abi.FRAME_REFERENCE)
+    assert np.array_equal(a, u64(v.depth_id))
+
+
+def test_empty_view(renderer, ico):
+    w, h = 320, 200
+    cam = scene.camera((0, 0, 3), (0, 0, 6), (0, 1, 0), 60, w / h)  # looking away
+    v = view(ico, cam, w, h)
+    renderer.frame(ico.dev, [v], abi.FRAME_REFERENCE)
+    torch.cuda.synchronize()
+    assert np.all(u32(v.visbuffer) == 0xFFFFFFFF)
+    assert np.all(u32(v.color) == 0)
+    assert int(v.survivor_count.item()) == 0
+
+
+def test_invalid_arguments(renderer, ico):
+    cam = scene.camera((0, 0, 3), (0, 0, 0), (0, 1, 0), 60, 1.0)
+    v = view(ico, cam, 64, 64)
+    bad = v.struct(ico.host.draw_count)
+    bad.width = 0
+    import ctypes as C
+    lib = abi.load()
+    assert lib.vkgv_frame(renderer.ctx, C.byref(ico.dev.scene), C.byref(bad), 1, abi.FRAME_REFERENCE, 0) == \
+        abi.INVALID_ARG
+    big = abi.Scene.from_buffer_copy(ico.dev.scene)
+    big.meshlet_draw_count = 1 << 25
+    good = v.struct(ico.host.draw_count)
+    assert lib.vkgv_frame(renderer.ctx, C.byref(big), C.byref(good), 1, abi.FRAME_REFERENCE, 0) == \
+        abi.LIMIT_EXCEEDED
+    nopyr = v.struct(ico.host.draw_count)
+    nopyr.pyramid = abi.Pyramid()
+    assert lib.vkgv_frame(renderer.ctx, C.byref(ico.dev.scene), C.byref(nopyr), 1, abi.FRAME_REFERENCE, 0) == \
+        abi.INVALID_ARG
+    huge = v.struct(ico.host.draw_count)
+    huge.width = 9000
+    assert lib.vkgv_frame(renderer.ctx, C.byref(ico.dev.scene), C.byref(huge), 1, abi.FRAME_REFERENCE, 0) == \
+        abi.LIMIT_EXCEEDED
+    assert b"8192" in lib.vkgv_last_error(renderer.ctx)

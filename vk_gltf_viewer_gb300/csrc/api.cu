@@ -1,0 +1,643 @@
+// C ABI of libvkgv: context, frame orchestration, stage entry points and
+// CUDA-graph capture.  This replaces the per-frame command recording of
+// Application::run (src/vk_gltf_viewer/application.cpp:764-1003) and the pass
+// initialisation of application.cpp:181-576.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+using namespace vkgv;
+
+namespace {
+
+constexpr uint32_t kRing = 4;                 // in-flight frames sharing staging slots
+constexpr uint32_t kCountersPerView = 4;      // see DeviceView::counters
+constexpr uint32_t kGlobalCounters = 8;       // [0] pass-1 big queue, [1] pass-2 big queue
+constexpr uint32_t kDefaultBigCapacity = 1u << 21;
+
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct vkgv_ctx {
+    int device = 0;
+    uint32_t sm_count = 0;
+    vkgv_config cfg{};
+    std::string last_error;
+    RasterConfig raster{};
+
+    uint32_t* status = nullptr;        // 2 words
+    uint32_t* counters = nullptr;      // kGlobalCounters + kCountersPerView * view_cap
+    uint32_t view_cap = 0;
+    DeviceView* d_views[kRing] = {};
+    DeviceView* h_views[kRing] = {};   // pinned staging
+    cudaEvent_t ring_ev[kRing] = {};
+    bool ring_used[kRing] = {};
+    uint32_t ring_pos = 0;
+
+    Scratch survivors;  // per view: capacity draw_count
+    Scratch rejected;   // per view: capacity draw_count
+    BigTri* big = nullptr;
+    uint32_t big_cap = 0;
+    cudaStream_t capture_stream = nullptr;
+    // Buffers replaced by a larger allocation stay alive until destroy, since
+    // a captured graph may still point at them.
+    std::vector<void*> retired_dev;
+    std::vector<void*> retired_host;
+    // GPU stage zones (vkgv_set_profiling)
+    bool profile = false;
+    bool profile_recorded = false;
+    cudaEvent_t zone[VKGV_STAGE_COUNT + 1] = {};
+};
+
+struct vkgv_graph {
+    vkgv_ctx* ctx = nullptr;
+    DeviceView* d_views = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int fail(vkgv_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+int cuda_fail(vkgv_ctx* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, VKGV_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define VKGV_CUDA(ctx, call)                                   \
+    do {                                                       \
+        cudaError_t e__ = (call);                              \
+        if (e__ != cudaSuccess) return cuda_fail(ctx, e__, #call); \
+    } while (0)
+
+bool aligned16(uint64_t p) { return (p & 15u) == 0; }
+
+int ensure_scratch(vkgv_ctx* ctx, Scratch& s, size_t bytes, const char* what) {
+    if (s.bytes >= bytes) return VKGV_OK;
+    if (s.ptr) {
+        ctx->retired_dev.push_back(s.ptr);
+        s.ptr = nullptr;
+        s.bytes = 0;
+    }
+    size_t want = std::max(bytes, size_t(1) << 20);
+    if (cudaMalloc(&s.ptr, want) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, VKGV_OUT_OF_MEMORY, std::string("scratch allocation failed: ") + what);
+    }
+    s.bytes = want;
+    return VKGV_OK;
+}
+
+int ensure_views(vkgv_ctx* ctx, uint32_t n) {
+    if (ctx->view_cap >= n) return VKGV_OK;
+    uint32_t cap = std::max<uint32_t>(n, 16);
+    for (uint32_t i = 0; i < kRing; ++i) {
+        if (ctx->ring_used[i]) VKGV_CUDA(ctx, cudaEventSynchronize(ctx->ring_ev[i]));
+        if (ctx->d_views[i]) ctx->retired_dev.push_back(ctx->d_views[i]);
+        if (ctx->h_views[i]) ctx->retired_host.push_back(ctx->h_views[i]);
+        ctx->d_views[i] = nullptr;
+        ctx->h_views[i] = nullptr;
+        VKGV_CUDA(ctx, cudaMalloc(&ctx->d_views[i], sizeof(DeviceView) * cap));
+        VKGV_CUDA(ctx, cudaMallocHost(&ctx->h_views[i], sizeof(DeviceView) * cap));
+        ctx->ring_used[i] = false;
+    }
+    if (ctx->counters) ctx->retired_dev.push_back(ctx->counters);
+    ctx->counters = nullptr;
+    VKGV_CUDA(ctx, cudaMalloc(&ctx->counters, sizeof(uint32_t) * (kGlobalCounters + kCountersPerView * cap)));
+    VKGV_CUDA(ctx, cudaMemset(ctx->counters, 0, sizeof(uint32_t) * (kGlobalCounters + kCountersPerView * cap)));
+    ctx->view_cap = cap;
+    return VKGV_OK;
+}
+
+int validate_scene(vkgv_ctx* ctx, const vkgv_scene* s) {
+    if (!s) return fail(ctx, VKGV_INVALID_ARG, "scene is NULL");
+    if (s->meshlet_draw_count >= (1u << VKGV_DRAW_INDEX_BITS))
+        return fail(ctx, VKGV_LIMIT_EXCEEDED, "meshlet_draw_count must be < 2^25 (25-bit draw index)");
+    if (s->meshlet_draw_count > 0 &&
+        (!s->draw_buffer || !s->transform_buffer || !s->primitive_buffer || !s->material_buffer))
+        return fail(ctx, VKGV_INVALID_ARG, "scene buffers must be non-NULL");
+    if (s->texture_count > 0 && !s->texture_table)
+        return fail(ctx, VKGV_INVALID_ARG, "texture_table is NULL with texture_count > 0");
+    return VKGV_OK;
+}
+
+int validate_pyramid(vkgv_ctx* ctx, const vkgv_pyramid& p, uint32_t w, uint32_t h, const char* which) {
+    if (p.levels == 0) return VKGV_OK;
+    uint32_t levels = 0;
+    uint64_t floats = 0;
+    vkgv_pyramid_layout(w, h, &levels, &floats);
+    if (!p.data || p.width != (w >> 1) || p.height != (h >> 1) || p.levels != levels)
+        return fail(ctx, VKGV_INVALID_ARG,
+                    std::string(which) + " pyramid must be (W>>1) x (H>>1) with floor(log2(max(W,H))) levels");
+    if (p.data & 3u) return fail(ctx, VKGV_INVALID_ARG, std::string(which) + " pyramid must be 4-byte aligned");
+    return VKGV_OK;
+}
+
+int validate_view(vkgv_ctx* ctx, const vkgv_view& v, uint32_t flags) {
+    if (v.width == 0 || v.height == 0) return fail(ctx, VKGV_INVALID_ARG, "zero-size view");
+    if (v.width > VKGV_MAX_VIEW_DIM || v.height > VKGV_MAX_VIEW_DIM)
+        return fail(ctx, VKGV_LIMIT_EXCEEDED, "view edge exceeds 8192 pixels");
+    if (!v.camera_buffer) return fail(ctx, VKGV_INVALID_ARG, "camera_buffer is NULL");
+    if (!v.depth_id || !aligned16(v.depth_id)) return fail(ctx, VKGV_INVALID_ARG, "depth_id must be 16-byte aligned");
+    int rc = validate_pyramid(ctx, v.prev_pyramid, v.width, v.height, "prev");
+    if (rc) return rc;
+    rc = validate_pyramid(ctx, v.pyramid, v.width, v.height, "output");
+    if (rc) return rc;
+    if ((flags & VKGV_BUILD_PYRAMID) && v.pyramid.levels == 0 && (v.width > 1 || v.height > 1))
+        return fail(ctx, VKGV_INVALID_ARG, "VKGV_BUILD_PYRAMID needs an output pyramid");
+    if ((flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED)) && !v.color)
+        return fail(ctx, VKGV_INVALID_ARG, "resolve requested without a color image");
+    if ((flags & VKGV_WRITE_IDS) && !v.visbuffer)
+        return fail(ctx, VKGV_INVALID_ARG, "VKGV_WRITE_IDS without a visbuffer image");
+    if ((flags & VKGV_RESOLVE_FLAT) && (flags & VKGV_RESOLVE_TEXTURED))
+        return fail(ctx, VKGV_INVALID_ARG, "choose one of VKGV_RESOLVE_FLAT and VKGV_RESOLVE_TEXTURED");
+    if (v.survivors && !v.survivor_count)
+        return fail(ctx, VKGV_INVALID_ARG, "survivors given without survivor_count");
+    return VKGV_OK;
+}
+
+struct Prepared {
+    SceneArgs S;
+    uint32_t max_w = 0, max_h = 0;
+    uint64_t max_px = 0;
+};
+
+// Builds the DeviceView table for `views` into `host` (count n).
+int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, uint32_t n, uint32_t flags,
+                DeviceView* host, Prepared& P) {
+    int rc = validate_scene(ctx, scene);
+    if (rc) return rc;
+    const uint32_t D = scene->meshlet_draw_count;
+    size_t per_view = std::max<size_t>(D, 1) * sizeof(uint32_t);
+    rc = ensure_scratch(ctx, ctx->rejected, per_view * n, "rejected lists");
+    if (rc) return rc;
+    bool need_surv = false;
+    for (uint32_t i = 0; i < n; ++i) need_surv |= views[i].survivors == 0;
+    if (need_surv) {
+        rc = ensure_scratch(ctx, ctx->survivors, per_view * n, "survivor lists");
+        if (rc) return rc;
+    }
+    if (n > ctx->view_cap) return fail(ctx, VKGV_LIMIT_EXCEEDED, "view table too small");
+    P.S.draws = reinterpret_cast<const vkgv_meshlet_draw*>(scene->draw_buffer);
+    P.S.transforms = reinterpret_cast<const float*>(scene->transform_buffer);
+    P.S.prims = reinterpret_cast<const vkgv_primitive*>(scene->primitive_buffer);
+    P.S.mats = reinterpret_cast<const vkgv_material*>(scene->material_buffer);
+    P.S.textures = reinterpret_cast<const vkgv_texture*>(scene->texture_table);
+    P.S.draw_count = D;
+    P.S.texture_count = scene->texture_count;
+    for (uint32_t i = 0; i < n; ++i) {
+        const vkgv_view& v = views[i];
+        rc = validate_view(ctx, v, flags);
+        if (rc) return rc;
+        if (v.survivors && v.survivor_capacity < D)
+            return fail(ctx, VKGV_LIMIT_EXCEEDED, "survivor_capacity must be >= meshlet_draw_count");
+        DeviceView& d = host[i];
+        std::memset(&d, 0, sizeof(d));
+        d.cam = reinterpret_cast<const vkgv_camera*>(v.camera_buffer);
+        d.w = v.width;
+        d.h = v.height;
+        d.prev_pyr = reinterpret_cast<const float*>(v.prev_pyramid.data);
+        d.prev_w0 = v.prev_pyramid.width;
+        d.prev_h0 = v.prev_pyramid.height;
+        d.prev_levels = v.prev_pyramid.levels;
+        d.pyr = reinterpret_cast<float*>(v.pyramid.data);
+        d.pyr_levels = v.pyramid.levels;
+        d.depth_id = reinterpret_cast<unsigned long long*>(v.depth_id);
+        d.ids = reinterpret_cast<uint32_t*>(v.visbuffer);
+        d.rgba = reinterpret_cast<uint32_t*>(v.color);
+        if (v.survivors) {
+            d.survivors = reinterpret_cast<uint32_t*>(v.survivors);
+            d.survivor_count = reinterpret_cast<uint32_t*>(v.survivor_count);
+            d.survivor_capacity = v.survivor_capacity;
+        } else {
+            d.survivors = reinterpret_cast<uint32_t*>(ctx->survivors.ptr) + (size_t)i * std::max<uint32_t>(D, 1);
+            d.survivor_count = reinterpret_cast<uint32_t*>(v.survivor_count);
+            d.survivor_capacity = D;
+        }
+        d.rejected = reinterpret_cast<uint32_t*>(ctx->rejected.ptr) + (size_t)i * std::max<uint32_t>(D, 1);
+        d.counters = ctx->counters + kGlobalCounters + kCountersPerView * i;
+        P.max_w = std::max(P.max_w, v.width);
+        P.max_h = std::max(P.max_h, v.height);
+        P.max_px = std::max<uint64_t>(P.max_px, (uint64_t)v.width * v.height);
+    }
+    return VKGV_OK;
+}
+
+// Takes the next staging slot of the view-table ring, waiting until the
+// frame that last used it has consumed its table.
+int acquire_slot(vkgv_ctx* ctx, int* out_slot, DeviceView** out_dev, DeviceView** out_host) {
+    uint32_t slot = ctx->ring_pos;
+    ctx->ring_pos = (ctx->ring_pos + 1) % kRing;
+    if (ctx->ring_used[slot]) VKGV_CUDA(ctx, cudaEventSynchronize(ctx->ring_ev[slot]));
+    *out_slot = (int)slot;
+    *out_dev = ctx->d_views[slot];
+    *out_host = ctx->h_views[slot];
+    return VKGV_OK;
+}
+
+int commit_views(vkgv_ctx* ctx, int slot, uint32_t n, cudaStream_t stream) {
+    VKGV_CUDA(ctx, cudaMemcpyAsync(ctx->d_views[slot], ctx->h_views[slot], sizeof(DeviceView) * n,
+                                   cudaMemcpyHostToDevice, stream));
+    return VKGV_OK;
+}
+
+int close_slot(vkgv_ctx* ctx, int slot, cudaStream_t stream) {
+    VKGV_CUDA(ctx, cudaEventRecord(ctx->ring_ev[slot], stream));
+    ctx->ring_used[slot] = true;
+    return VKGV_OK;
+}
+
+// Records one frame on `stream` for a device view table.  With `zones`,
+// zones[i] is recorded at the start of stage i and zones[count] at the end.
+void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32_t n, uint32_t flags,
+                  cudaStream_t stream, cudaEvent_t* zones = nullptr) {
+    auto zone = [&](int i) {
+        if (zones) cudaEventRecord(zones[i], stream);
+    };
+    uint32_t* gc = ctx->counters;
+    zone(0);
+    launch_clear(dv, n, (flags & VKGV_SKIP_CLEAR) ? 0 : P.max_px, gc, kGlobalCounters, ctx->sm_count, stream);
+    zone(1);
+    launch_cull(P.S, dv, n, flags, 1, ctx->status, ctx->sm_count, stream);
+    zone(2);
+    RasterLists l1{1, nullptr, nullptr, 0};
+    launch_raster(P.S, dv, n, l1, ctx->raster, ctx->big, gc + 0, ctx->big_cap, ctx->status, ctx->sm_count, stream,
+                  zones ? zones[3] : nullptr);
+    zone(4);
+    const bool two = (flags & VKGV_CULL_TWO_PASS) && (flags & VKGV_CULL_OCCLUSION);
+    if (two) launch_hiz(dv, n, P.max_w, P.max_h, ctx->sm_count, stream);
+    zone(5);
+    if (two) launch_cull(P.S, dv, n, flags, 2, ctx->status, ctx->sm_count, stream);
+    zone(6);
+    if (two) {
+        RasterLists l2{2, nullptr, nullptr, 0};
+        launch_raster(P.S, dv, n, l2, ctx->raster, ctx->big, gc + 1, ctx->big_cap, ctx->status, ctx->sm_count,
+                      stream, zones ? zones[7] : nullptr);
+    } else {
+        zone(7);
+    }
+    zone(8);
+    if (flags & VKGV_BUILD_PYRAMID) launch_hiz(dv, n, P.max_w, P.max_h, ctx->sm_count, stream);
+    zone(9);
+    if (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS))
+        launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
+    zone(10);
+    launch_finalize(dv, n, stream);
+    zone(11);
+}
+
+int check_launch(vkgv_ctx* ctx) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
+    return VKGV_OK;
+}
+
+int two_pass_needs_pyramid(vkgv_ctx* ctx, const vkgv_view* views, uint32_t n, uint32_t flags) {
+    if ((flags & VKGV_CULL_TWO_PASS) && (flags & VKGV_CULL_OCCLUSION))
+        for (uint32_t i = 0; i < n; ++i)
+            if (views[i].prev_pyramid.levels && !views[i].pyramid.levels)
+                return fail(ctx, VKGV_INVALID_ARG, "two-pass culling needs an output pyramid");
+    return VKGV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vkgv_create(const vkgv_config* config, vkgv_ctx** out_ctx) {
+    if (!out_ctx) return VKGV_INVALID_ARG;
+    *out_ctx = nullptr;
+    vkgv_ctx* ctx = new (std::nothrow) vkgv_ctx();
+    if (!ctx) return VKGV_OUT_OF_MEMORY;
+    if (config) ctx->cfg = *config;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        delete ctx;
+        return VKGV_CUDA_ERROR;
+    }
+    if (ctx->cfg.device < 0 || ctx->cfg.device >= ndev) {
+        delete ctx;
+        return VKGV_INVALID_ARG;
+    }
+    ctx->device = ctx->cfg.device;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) {
+        delete ctx;
+        return VKGV_CUDA_ERROR;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    ctx->sm_count = (uint32_t)std::max(sms, 1);
+    uint32_t bin = ctx->cfg.bin_size ? ctx->cfg.bin_size : 32;
+    if (bin != 8 && bin != 16 && bin != 32 && bin != 64) {
+        delete ctx;
+        return VKGV_INVALID_ARG;
+    }
+    uint32_t mpc = ctx->cfg.meshlets_per_cta ? ctx->cfg.meshlets_per_cta : 4;
+    if (mpc != 1 && mpc != 2 && mpc != 4 && mpc != 8) {
+        delete ctx;
+        return VKGV_INVALID_ARG;
+    }
+    ctx->raster.chunk = bin;
+    ctx->raster.small_area = bin * bin > 64 ? 64 : bin * bin;
+    ctx->raster.warps_per_cta = mpc;
+    ctx->raster.blocks_per_view = 0;
+    ctx->big_cap = ctx->cfg.big_triangle_capacity ? ctx->cfg.big_triangle_capacity : kDefaultBigCapacity;
+    bool ok = cudaMalloc(&ctx->status, 2 * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMemset(ctx->status, 0, 2 * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&ctx->big, sizeof(BigTri) * (size_t)ctx->big_cap) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (uint32_t i = 0; ok && i < kRing; ++i)
+        ok = cudaEventCreateWithFlags(&ctx->ring_ev[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        vkgv_destroy(ctx);
+        return VKGV_OUT_OF_MEMORY;
+    }
+    if (ensure_views(ctx, 16) != VKGV_OK) {
+        vkgv_destroy(ctx);
+        return VKGV_OUT_OF_MEMORY;
+    }
+    *out_ctx = ctx;
+    return VKGV_OK;
+}
+
+int vkgv_destroy(vkgv_ctx* ctx) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    for (uint32_t i = 0; i < kRing; ++i) {
+        if (ctx->d_views[i]) cudaFree(ctx->d_views[i]);
+        if (ctx->h_views[i]) cudaFreeHost(ctx->h_views[i]);
+        if (ctx->ring_ev[i]) cudaEventDestroy(ctx->ring_ev[i]);
+    }
+    if (ctx->counters) cudaFree(ctx->counters);
+    if (ctx->status) cudaFree(ctx->status);
+    if (ctx->big) cudaFree(ctx->big);
+    if (ctx->survivors.ptr) cudaFree(ctx->survivors.ptr);
+    if (ctx->rejected.ptr) cudaFree(ctx->rejected.ptr);
+    if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+    for (uint32_t i = 0; i <= VKGV_STAGE_COUNT; ++i)
+        if (ctx->zone[i]) cudaEventDestroy(ctx->zone[i]);
+    for (void* p : ctx->retired_dev) cudaFree(p);
+    for (void* p : ctx->retired_host) cudaFreeHost(p);
+    delete ctx;
+    return VKGV_OK;
+}
+
+const char* vkgv_last_error(const vkgv_ctx* ctx) {
+    if (!ctx) return "null context";
+    return ctx->last_error.c_str();
+}
+
+int vkgv_device_status(vkgv_ctx* ctx, uint32_t* out_code, uint32_t* out_detail) {
+    if (!ctx || !out_code || !out_detail) return VKGV_INVALID_ARG;
+    uint32_t h[2] = {0, 0};
+    VKGV_CUDA(ctx, cudaMemcpy(h, ctx->status, sizeof(h), cudaMemcpyDeviceToHost));
+    VKGV_CUDA(ctx, cudaMemset(ctx->status, 0, sizeof(h)));
+    *out_code = h[0];
+    *out_detail = h[1];
+    return VKGV_OK;
+}
+
+int vkgv_frame(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, uint32_t view_count, uint32_t flags,
+               void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!views || view_count == 0) return fail(ctx, VKGV_INVALID_ARG, "no views");
+    if (view_count > 65535u) return fail(ctx, VKGV_LIMIT_EXCEEDED, "at most 65535 views per frame");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    int rc = two_pass_needs_pyramid(ctx, views, view_count, flags);
+    if (rc) return rc;
+    rc = ensure_views(ctx, view_count);
+    if (rc) return rc;
+    DeviceView *dv, *hv;
+    int slot = 0;
+    rc = acquire_slot(ctx, &slot, &dv, &hv);
+    if (rc) return rc;
+    Prepared P;
+    rc = build_views(ctx, scene, views, view_count, flags, hv, P);
+    if (rc) return rc;
+    rc = commit_views(ctx, slot, view_count, stream);
+    if (rc) return rc;
+    record_frame(ctx, P, dv, view_count, flags, stream, ctx->profile ? ctx->zone : nullptr);
+    if (ctx->profile) ctx->profile_recorded = true;
+    rc = check_launch(ctx);
+    if (rc) return rc;
+    return close_slot(ctx, slot, stream);
+}
+
+int vkgv_set_profiling(vkgv_ctx* ctx, int32_t enable) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (enable && !ctx->zone[0])
+        for (uint32_t i = 0; i <= VKGV_STAGE_COUNT; ++i) VKGV_CUDA(ctx, cudaEventCreate(&ctx->zone[i]));
+    ctx->profile = enable != 0;
+    ctx->profile_recorded = false;
+    return VKGV_OK;
+}
+
+int vkgv_stage_times(vkgv_ctx* ctx, float* out_ms, uint32_t count) {
+    if (!ctx || !out_ms) return VKGV_INVALID_ARG;
+    if (!ctx->profile_recorded) return fail(ctx, VKGV_INVALID_ARG, "no profiled frame recorded");
+    VKGV_CUDA(ctx, cudaEventSynchronize(ctx->zone[VKGV_STAGE_COUNT]));
+    for (uint32_t i = 0; i < count && i < VKGV_STAGE_COUNT; ++i) {
+        float ms = 0.f;
+        VKGV_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->zone[i], ctx->zone[i + 1]));
+        out_ms[i] = ms;
+    }
+    return VKGV_OK;
+}
+
+int vkgv_clear(vkgv_ctx* ctx, const vkgv_view* view, void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!view) return fail(ctx, VKGV_INVALID_ARG, "view is NULL");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    vkgv_scene empty{};
+    DeviceView *dv, *hv;
+    int slot = 0;
+    int rc = acquire_slot(ctx, &slot, &dv, &hv);
+    if (rc) return rc;
+    Prepared P;
+    rc = build_views(ctx, &empty, view, 1, 0, hv, P);
+    if (rc) return rc;
+    rc = commit_views(ctx, slot, 1, stream);
+    if (rc) return rc;
+    launch_clear(dv, 1, P.max_px, ctx->counters, kGlobalCounters, ctx->sm_count, stream);
+    launch_finalize(dv, 1, stream);
+    rc = check_launch(ctx);
+    if (rc) return rc;
+    return close_slot(ctx, slot, stream);
+}
+
+int vkgv_cull(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, uint32_t flags, uint32_t pass,
+              void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!view) return fail(ctx, VKGV_INVALID_ARG, "view is NULL");
+    if (pass != 1 && pass != 2) return fail(ctx, VKGV_INVALID_ARG, "pass must be 1 or 2");
+    if (!view->survivors) return fail(ctx, VKGV_INVALID_ARG, "vkgv_cull needs view->survivors");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    DeviceView *dv, *hv;
+    int slot = 0;
+    int rc = acquire_slot(ctx, &slot, &dv, &hv);
+    if (rc) return rc;
+    Prepared P;
+    rc = build_views(ctx, scene, view, 1, flags & ~(VKGV_BUILD_PYRAMID | VKGV_RESOLVE_FLAT |
+                                                        VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS),
+                         hv, P);
+    if (rc) return rc;
+    rc = commit_views(ctx, slot, 1, stream);
+    if (rc) return rc;
+    launch_cull(P.S, dv, 1, flags, pass, ctx->status, ctx->sm_count, stream);
+    launch_finalize(dv, 1, stream);
+    rc = check_launch(ctx);
+    if (rc) return rc;
+    return close_slot(ctx, slot, stream);
+}
+
+int vkgv_raster(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, uint64_t draw_list,
+                uint64_t draw_count, uint32_t first, void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!view) return fail(ctx, VKGV_INVALID_ARG, "view is NULL");
+    if ((draw_list == 0) != (draw_count == 0))
+        return fail(ctx, VKGV_INVALID_ARG, "draw_list and draw_count must both be set or both be 0");
+    if (!draw_list && (!view->survivors || !view->survivor_count))
+        return fail(ctx, VKGV_INVALID_ARG, "vkgv_raster without a list needs view->survivors and survivor_count");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    DeviceView *dv, *hv;
+    int slot = 0;
+    int rc = acquire_slot(ctx, &slot, &dv, &hv);
+    if (rc) return rc;
+    Prepared P;
+    rc = build_views(ctx, scene, view, 1, 0, hv, P);
+    if (rc) return rc;
+    rc = commit_views(ctx, slot, 1, stream);
+    if (rc) return rc;
+    RasterLists l{0, draw_list ? reinterpret_cast<const uint32_t*>(draw_list) : reinterpret_cast<const uint32_t*>(view->survivors),
+                  draw_count ? reinterpret_cast<const uint32_t*>(draw_count)
+                             : reinterpret_cast<const uint32_t*>(view->survivor_count),
+                  first};
+    VKGV_CUDA(ctx, cudaMemsetAsync(ctx->counters, 0, sizeof(uint32_t), stream));
+    launch_raster(P.S, dv, 1, l, ctx->raster, ctx->big, ctx->counters, ctx->big_cap, ctx->status, ctx->sm_count,
+                  stream);
+    rc = check_launch(ctx);
+    if (rc) return rc;
+    return close_slot(ctx, slot, stream);
+}
+
+int vkgv_hiz_reduce(vkgv_ctx* ctx, const vkgv_view* view, void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!view) return fail(ctx, VKGV_INVALID_ARG, "view is NULL");
+    if (view->pyramid.levels == 0) return fail(ctx, VKGV_INVALID_ARG, "view has no output pyramid");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    vkgv_scene empty{};
+    DeviceView *dv, *hv;
+    int slot = 0;
+    int rc = acquire_slot(ctx, &slot, &dv, &hv);
+    if (rc) return rc;
+    Prepared P;
+    rc = build_views(ctx, &empty, view, 1, VKGV_BUILD_PYRAMID, hv, P);
+    if (rc) return rc;
+    rc = commit_views(ctx, slot, 1, stream);
+    if (rc) return rc;
+    launch_hiz(dv, 1, P.max_w, P.max_h, ctx->sm_count, stream);
+    rc = check_launch(ctx);
+    if (rc) return rc;
+    return close_slot(ctx, slot, stream);
+}
+
+int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, uint32_t flags, void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!view) return fail(ctx, VKGV_INVALID_ARG, "view is NULL");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    DeviceView *dv, *hv;
+    int slot = 0;
+    int rc = acquire_slot(ctx, &slot, &dv, &hv);
+    if (rc) return rc;
+    Prepared P;
+    rc = build_views(ctx, scene, view, 1, flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS),
+                         hv, P);
+    if (rc) return rc;
+    rc = commit_views(ctx, slot, 1, stream);
+    if (rc) return rc;
+    launch_resolve(P.S, dv, 1, P.max_w, P.max_h, flags, stream);
+    rc = check_launch(ctx);
+    if (rc) return rc;
+    return close_slot(ctx, slot, stream);
+}
+
+int vkgv_graph_capture(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, uint32_t view_count,
+                       uint32_t flags, vkgv_graph** out_graph) {
+    if (!ctx || !out_graph) return VKGV_INVALID_ARG;
+    *out_graph = nullptr;
+    if (!views || view_count == 0) return fail(ctx, VKGV_INVALID_ARG, "no views");
+    int rc = two_pass_needs_pyramid(ctx, views, view_count, flags);
+    if (rc) return rc;
+    rc = ensure_views(ctx, view_count);
+    if (rc) return rc;
+    std::vector<DeviceView> host(view_count);
+    Prepared P;
+    rc = build_views(ctx, scene, views, view_count, flags, host.data(), P);
+    if (rc) return rc;
+    vkgv_graph* g = new (std::nothrow) vkgv_graph();
+    if (!g) return fail(ctx, VKGV_OUT_OF_MEMORY, "graph object");
+    g->ctx = ctx;
+    if (cudaMalloc(&g->d_views, sizeof(DeviceView) * view_count) != cudaSuccess ||
+        cudaMemcpy(g->d_views, host.data(), sizeof(DeviceView) * view_count, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        vkgv_graph_destroy(g);
+        return fail(ctx, VKGV_OUT_OF_MEMORY, "graph view table");
+    }
+    cudaStream_t s = ctx->capture_stream;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        vkgv_graph_destroy(g);
+        return cuda_fail(ctx, e, "cudaStreamBeginCapture");
+    }
+    record_frame(ctx, P, g->d_views, view_count, flags, s);
+    e = cudaStreamEndCapture(s, &g->graph);
+    if (e != cudaSuccess) {
+        vkgv_graph_destroy(g);
+        return cuda_fail(ctx, e, "cudaStreamEndCapture");
+    }
+    e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+        vkgv_graph_destroy(g);
+        return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    }
+    *out_graph = g;
+    return VKGV_OK;
+}
+
+int vkgv_graph_launch(vkgv_graph* g, void* stream_) {
+    if (!g || !g->exec) return VKGV_INVALID_ARG;
+    cudaError_t e = cudaGraphLaunch(g->exec, reinterpret_cast<cudaStream_t>(stream_));
+    if (e != cudaSuccess) return cuda_fail(g->ctx, e, "cudaGraphLaunch");
+    return VKGV_OK;
+}
+
+int vkgv_graph_destroy(vkgv_graph* g) {
+    if (!g) return VKGV_INVALID_ARG;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->d_views) {
+        cudaDeviceSynchronize();
+        cudaFree(g->d_views);
+    }
+    delete g;
+    return VKGV_OK;
+}
+
+}  // extern "C"

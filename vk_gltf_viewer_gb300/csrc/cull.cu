@@ -1,0 +1,219 @@
+// Meshlet culling: the task shader (shaders/visbuffer/visbuffer.task.glsl:25-76)
+// as one thread per meshlet draw with warp-ballot compaction.
+//
+// The reference groups 102 draws per task workgroup and compacts them into a
+// uint8 payload with subgroupExclusiveAdd; here every draw is tested once and
+// survivors are appended to a per-view uint32 list with one atomic per warp.
+// The index clamp at visbuffer.task.glsl:41 re-tests draw 101 of a full
+// workgroup in 26 extra lanes and appends it up to 27 times; the duplicates
+// produce identical fragments, so the survivor *set* (what this kernel emits,
+// each draw once) is the reference's.
+#include "kernels.cuh"
+
+namespace vkgv {
+
+namespace {
+
+// Pass-1 corner table of projectAabb (shaders/culling.h.glsl:32-41).
+__constant__ float kCorners[8][3] = {{1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, -1},
+                                     {1, -1, 1},  {1, 1, 1},  {-1, -1, 1}, {-1, 1, 1}};
+
+// Exact floor(log2(m)) clamped to [0, levels-1]; m <= 0 or NaN -> 0,
+// +inf -> levels-1.
+__device__ __forceinline__ int hiz_level(float m, uint32_t levels) {
+    int top = (int)levels - 1;
+    if (!(m > 0.0f)) return 0;
+    if (isinf(m)) return top;
+    int e = (int)((__float_as_uint(m) >> 23) & 0xffu) - 127;  // subnormals give < 0 -> 0
+    return e < 0 ? 0 : (e > top ? top : e);
+}
+
+struct CullResult {
+    bool visible;
+    bool occluded;
+};
+
+__device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceView& V, const float* frustum,
+                                               const float* occl_vp, const float* pyr, uint32_t pw0,
+                                               uint32_t ph0, uint32_t plevels, uint32_t flags, uint32_t d,
+                                               uint32_t* status) {
+    CullResult res{false, false};
+    const vkgv_meshlet_draw dr = S.draws[d];
+    const vkgv_primitive* prim = &S.prims[dr.primitive_index];
+    if (dr.meshlet_index >= prim->meshlet_count) {
+        report(status, kStatusBadIndex, d);
+        return res;
+    }
+    const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
+    const float4* M4 = reinterpret_cast<const float4*>(S.transforms + 16 * (size_t)dr.transform_index);
+    float M[16];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float4 q = __ldg(M4 + c);
+        M[c * 4 + 0] = q.x;
+        M[c * 4 + 1] = q.y;
+        M[c * 4 + 2] = q.z;
+        M[c * 4 + 3] = q.w;
+    }
+    const float e0 = ml->aabb_extents[0], e1 = ml->aabb_extents[1], e2 = ml->aabb_extents[2];
+    float wc4[4];
+    // worldAabbCenter (visbuffer.task.glsl:50)
+    m4v(M, ml->aabb_center[0], ml->aabb_center[1], ml->aabb_center[2], 1.0f, wc4);
+    // getWorldSpaceAabbExtent (culling.h.glsl:22-29)
+    float we[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+        we[j] = fadd(fadd(fmul(fabsf(M[0 * 4 + j]), e0), fmul(fabsf(M[1 * 4 + j]), e1)), fmul(fabsf(M[2 * 4 + j]), e2));
+    // isAabbInFrustum (culling.h.glsl:8-19)
+    if (flags & VKGV_CULL_FRUSTUM) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            const float p0 = frustum[4 * i], p1 = frustum[4 * i + 1], p2 = frustum[4 * i + 2], p3 = frustum[4 * i + 3];
+            float radius = fadd(fadd(fmul(we[0], fabsf(p0)), fmul(we[1], fabsf(p1))), fmul(we[2], fabsf(p2)));
+            float distance = fsub(fadd(fadd(fmul(p0, wc4[0]), fmul(p1, wc4[1])), fmul(p2, wc4[2])), p3);
+            if (-radius > distance) return res;
+        }
+    }
+    if (!pyr) {
+        res.visible = true;
+        return res;
+    }
+    // projectAabb (culling.h.glsl:44-56)
+    float mn0 = 1.0f, mn1 = 1.0f, mn2 = 1.0f, mx0 = -1.0f, mx1 = -1.0f, mx2 = -1.0f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        float px = fadd(fmul(kCorners[i][0], we[0]), wc4[0]);
+        float py = fadd(fmul(kCorners[i][1], we[1]), wc4[1]);
+        float pz = fadd(fmul(kCorners[i][2], we[2]), wc4[2]);
+        float clip[4];
+        m4v(occl_vp, px, py, pz, 1.0f, clip);
+        float ndx = gclamp(fdiv(clip[0], clip[3]), -1.0f, 1.0f);
+        float ndy = gclamp(fdiv(clip[1], clip[3]), -1.0f, 1.0f);
+        float qx = fadd(fmul(ndx, 0.5f), 0.5f), qy = fadd(fmul(ndy, 0.5f), 0.5f);
+        float qz = fdiv(clip[2], clip[3]);
+        mn0 = gmin(mn0, qx);
+        mn1 = gmin(mn1, qy);
+        mn2 = gmin(mn2, qz);
+        mx0 = gmax(mx0, qx);
+        mx1 = gmax(mx1, qy);
+        mx2 = gmax(mx2, qz);
+    }
+    (void)mn2;
+    // HiZ lookup (visbuffer.task.glsl:57-64)
+    float width = fmul(fsub(mx0, mn0), (float)pw0);
+    float height = fmul(fsub(mx1, mn1), (float)ph0);
+    int lvl = hiz_level(gmax(width, height), plevels);
+    float cx = fmul(fadd(mn0, mx0), 0.5f), cy = fmul(fadd(mn1, mx1), 0.5f);
+    uint32_t mw = mip_dim(pw0, (uint32_t)lvl), mh = mip_dim(ph0, (uint32_t)lvl);
+    const float* img = pyr + mip_offset(pw0, ph0, (uint32_t)lvl);
+    int x0 = 0, x1 = 0, y0 = 0, y1 = 0;
+    int nx = footprint_axis(cx, mw, x0, x1);
+    int ny = footprint_axis(cy, mh, y0, y1);
+    float depth = __ldg(img + (size_t)y0 * mw + x0);
+    if (nx == 2) depth = gmin(depth, __ldg(img + (size_t)y0 * mw + x1));
+    if (ny == 2) {
+        depth = gmin(depth, __ldg(img + (size_t)y1 * mw + x0));
+        if (nx == 2) depth = gmin(depth, __ldg(img + (size_t)y1 * mw + x1));
+    }
+    if (depth < mx2) {
+        res.visible = true;
+    } else {
+        res.occluded = true;
+    }
+    return res;
+}
+
+// Appends `flag` lanes' values to list[*counter ...] with one atomic per warp.
+__device__ __forceinline__ void warp_append(bool flag, uint32_t value, uint32_t* list, uint32_t* counter,
+                                            uint32_t capacity, uint32_t* status) {
+    const unsigned mask = __ballot_sync(0xffffffffu, flag);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (flag) {
+        uint32_t slot = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+        if (slot < capacity)
+            list[slot] = value;
+        else
+            report(status, kStatusListOverflow, slot);
+    }
+}
+
+// pass 1: candidates are all draws [0, D); survivors -> survivors[0..),
+//         occlusion rejects -> rejected.
+// pass 2: candidates are rejected[0, counters[1]); survivors are appended at
+//         survivors[counters[0] + ...] via counters[2].
+__global__ void __launch_bounds__(256) k_cull(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags,
+                                              uint32_t pass, uint32_t* status) {
+    const DeviceView& V = views[blockIdx.y];
+    const vkgv_camera* cam = V.cam;
+    __shared__ float s_frustum[24];
+    __shared__ float s_vp[16];
+    if (threadIdx.x < 24) s_frustum[threadIdx.x] = (&cam->frustum[0][0])[threadIdx.x];
+    if (threadIdx.x < 16)
+        s_vp[threadIdx.x] = pass == 1 ? cam->prev_occlusion_view_projection[threadIdx.x]
+                                      : cam->occlusion_view_projection[threadIdx.x];
+    __syncthreads();
+    const float* pyr = nullptr;
+    uint32_t pw0 = 0, ph0 = 0, pl = 0;
+    if (flags & VKGV_CULL_OCCLUSION) {
+        if (pass == 1 && V.prev_pyr && V.prev_levels) {
+            pyr = V.prev_pyr;
+            pw0 = V.prev_w0;
+            ph0 = V.prev_h0;
+            pl = V.prev_levels;
+        } else if (pass == 2 && V.pyr && V.pyr_levels) {
+            pyr = V.pyr;
+            pw0 = V.w >> 1;
+            ph0 = V.h >> 1;
+            pl = V.pyr_levels;
+        }
+    }
+    const bool collect_rejects = pass == 1 && pyr != nullptr && (flags & VKGV_CULL_TWO_PASS);
+    const uint32_t n = pass == 1 ? S.draw_count : V.counters[1];
+    uint32_t* out_counter = pass == 1 ? &V.counters[0] : &V.counters[2];
+    uint32_t* out_list = pass == 1 ? V.survivors : V.survivors + V.counters[0];
+    const uint32_t cap = pass == 1 ? V.survivor_capacity : V.survivor_capacity - min(V.counters[0], V.survivor_capacity);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // Grid-stride with a warp-uniform trip count so the ballots stay converged.
+    const uint32_t start = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t warp_start = start & ~31u;
+    for (uint32_t base = warp_start; base < n; base += stride) {
+        const uint32_t i = base + (threadIdx.x & 31);
+        bool vis = false, occ = false;
+        uint32_t d = 0;
+        if (i < n) {
+            d = pass == 1 ? i : V.rejected[i];
+            if (d < S.draw_count) {
+                CullResult r = cull_one(S, V, s_frustum, s_vp, pyr, pw0, ph0, pl, flags, d, status);
+                vis = r.visible;
+                occ = r.occluded;
+            } else {
+                report(status, kStatusBadIndex, d);
+            }
+        }
+        warp_append(vis, d, out_list, out_counter, cap, status);
+        if (collect_rejects) warp_append(occ, d, V.rejected, &V.counters[1], S.draw_count, status);
+    }
+}
+
+}  // namespace
+
+void launch_cull(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t flags, uint32_t pass,
+                 uint32_t* status, uint32_t sm_count, cudaStream_t stream) {
+    const uint32_t threads = 256;
+    uint32_t want = (S.draw_count + threads - 1) / threads;
+    // pass 2 candidate counts live on the device: cap the grid and stride.
+    uint32_t cap = pass == 1 ? 4096u : 64u;
+    uint32_t per_view = want < cap ? want : cap;
+    uint32_t min_blocks = (sm_count * 8 + nviews - 1) / nviews;
+    if (pass == 1 && per_view < min_blocks && want > per_view) per_view = want < min_blocks ? want : min_blocks;
+    if (per_view == 0) per_view = 1;
+    dim3 grid(per_view, nviews);
+    k_cull<<<grid, threads, 0, stream>>>(S, views, flags, pass, status);
+}
+
+}  // namespace vkgv

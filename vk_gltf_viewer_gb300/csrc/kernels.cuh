@@ -1,0 +1,35 @@
+// Kernel launchers shared between the translation units of libvkgv.
+#pragma once
+
+#include "common.cuh"
+
+namespace vkgv {
+
+struct RasterLists {
+    uint32_t pass;            // 1, 2, or 0 for an explicit list
+    const uint32_t* list;     // explicit list (pass 0)
+    const uint32_t* count;    // explicit count (pass 0), device
+    uint32_t first;           // explicit start (pass 0)
+};
+
+struct RasterConfig {
+    uint32_t small_area;      // bbox pixel area rasterised inline by the lane
+    uint32_t chunk;           // edge of the binned chunk in pixels (8, 16, 32, 64)
+    uint32_t warps_per_cta;   // meshlets in flight per CTA
+    uint32_t blocks_per_view;
+};
+
+void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels, uint32_t* counters,
+                  uint32_t counter_words, uint32_t sm_count, cudaStream_t stream);
+void launch_cull(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t flags, uint32_t pass,
+                 uint32_t* status, uint32_t sm_count, cudaStream_t stream);
+void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews, const RasterLists& lists,
+                   const RasterConfig& cfg, BigTri* big, uint32_t* big_count, uint32_t big_capacity,
+                   uint32_t* status, uint32_t sm_count, cudaStream_t stream, cudaEvent_t between = nullptr);
+void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h, uint32_t sm_count,
+                cudaStream_t stream);
+void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h,
+                    uint32_t flags, cudaStream_t stream);
+void launch_finalize(const DeviceView* views, uint32_t nviews, cudaStream_t stream);
+
+}  // namespace vkgv

@@ -1,0 +1,433 @@
+// Visibility-buffer rasterisation: the mesh shader
+// (shaders/visbuffer/visbuffer.mesh.glsl:30-104), the fixed-function
+// rasteriser with the pipeline state of application.cpp:326-340 / 830-841, and
+// the fragment shader's ID write (shaders/visbuffer/visbuffer.frag.glsl:36).
+//
+// One warp owns one surviving meshlet draw: it transforms the <= 64 meshlet
+// vertices into shared memory, then each lane sets up one triangle at a time
+// (homogeneous backface determinant, outcode reject, near/far and guard-band
+// clipping, 28.8 fixed-point snap, top-left edge functions, depth plane).
+// Small triangles are rasterised by the lane itself; larger ones are cut into
+// chunk x chunk pixel rectangles and binned into a queue that a second
+// kernel drains with one CTA per rectangle.  Every covered sample performs a
+// 64-bit max of (depth bits << 32 | id + 1), which is the order-independent
+// form of the GREATER_OR_EQUAL depth test with ties won by the later draw.
+#include "kernels.cuh"
+
+namespace vkgv {
+
+namespace {
+
+constexpr float kGuard = 256.0f;
+enum : int { OC_XLO = 1, OC_XHI = 2, OC_YLO = 4, OC_YHI = 8, OC_ZLO = 16, OC_ZHI = 32 };
+
+__device__ __forceinline__ int outcode(const float4& v) {
+    int c = 0;
+    if (v.x < -v.w) c |= OC_XLO;
+    if (v.x > v.w) c |= OC_XHI;
+    if (v.y < -v.w) c |= OC_YLO;
+    if (v.y > v.w) c |= OC_YHI;
+    if (v.z < 0.0f) c |= OC_ZLO;
+    if (v.z > v.w) c |= OC_ZHI;
+    return c;
+}
+
+__device__ __forceinline__ bool outside_guard(const float4& v) {
+    float g = fmul(kGuard, v.w);
+    return v.x < -g || v.x > g || v.y < -g || v.y > g;
+}
+
+struct RasterCtx {
+    unsigned long long* depth;
+    uint32_t w, h;
+    float hw, hh;
+    uint32_t view;
+    BigTri* big;
+    uint32_t* big_count;
+    uint32_t big_cap;
+    uint32_t small_area;
+    uint32_t chunk;
+    uint32_t* status;
+};
+
+// Depth-test early-out: the stored value only grows, so a stale read that is
+// already >= v proves the max would not change it.
+__device__ __forceinline__ void plot(unsigned long long* p, unsigned long long v) {
+    if (__ldcg(p) < v) atomicMax(p, v);
+}
+
+__device__ void raster_rect(const int32_t* X, const int32_t* Y, const int32_t* bias, float z0, float pa, float pb,
+                            uint32_t id, int px0, int py0, int px1, int py1, unsigned long long* depth,
+                            uint32_t w) {
+    const unsigned long long lo = (unsigned long long)id + 1ull;
+    const int32_t sx0 = px0 * 256 + 128, sy0 = py0 * 256 + 128;
+    int64_t erow[3], stx[3], sty[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int a = k, b = (k + 1) % 3;
+        const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
+        erow[k] = (int64_t)dx * (sy0 - Y[a]) - (int64_t)dy * (sx0 - X[a]);
+        stx[k] = -(int64_t)dy * 256;
+        sty[k] = (int64_t)dx * 256;
+    }
+    for (int py = py0; py <= py1; ++py) {
+        int64_t e0 = erow[0], e1 = erow[1], e2 = erow[2];
+        const int32_t sy = py * 256 + 128;
+        const float zrow = __fmaf_rn(pb, __int2float_rn(sy - Y[0]), z0);
+        unsigned long long* row = depth + (size_t)py * w;
+        for (int px = px0; px <= px1; ++px) {
+            if (e0 >= bias[0] && e1 >= bias[1] && e2 >= bias[2]) {
+                const int32_t sx = px * 256 + 128;
+                float z = __fmaf_rn(pa, __int2float_rn(sx - X[0]), zrow);
+                if (!(z > 0.0f)) z = 0.0f;
+                if (z > 1.0f) z = 1.0f;
+                plot(row + px, ((unsigned long long)__float_as_uint(z) << 32) | lo);
+            }
+            e0 += stx[0];
+            e1 += stx[1];
+            e2 += stx[2];
+        }
+        erow[0] += sty[0];
+        erow[1] += sty[1];
+        erow[2] += sty[2];
+    }
+}
+
+// Triangle setup on snapped vertices and dispatch to inline or binned raster.
+__device__ void setup_and_raster(int32_t X0, int32_t Y0, float Z0, int32_t X1, int32_t Y1, float Z1, int32_t X2,
+                                 int32_t Y2, float Z2, uint32_t id, const RasterCtx& c) {
+    int64_t A = (int64_t)(X1 - X0) * (Y2 - Y0) - (int64_t)(Y1 - Y0) * (X2 - X0);
+    if (A == 0) return;
+    if (A < 0) {
+        int32_t tx = X1, ty = Y1;
+        float tz = Z1;
+        X1 = X2, Y1 = Y2, Z1 = Z2;
+        X2 = tx, Y2 = ty, Z2 = tz;
+        A = -A;
+    }
+    const int32_t minx = min(X0, min(X1, X2)), maxx = max(X0, max(X1, X2));
+    const int32_t miny = min(Y0, min(Y1, Y2)), maxy = max(Y0, max(Y1, Y2));
+    // ceil((min - 128) / 256) and floor((max - 128) / 256); >> is floor division.
+    int64_t px0 = ((int64_t)minx - 128 + 255) >> 8, px1 = ((int64_t)maxx - 128) >> 8;
+    int64_t py0 = ((int64_t)miny - 128 + 255) >> 8, py1 = ((int64_t)maxy - 128) >> 8;
+    px0 = px0 < 0 ? 0 : px0;
+    py0 = py0 < 0 ? 0 : py0;
+    px1 = px1 > (int64_t)c.w - 1 ? (int64_t)c.w - 1 : px1;
+    py1 = py1 > (int64_t)c.h - 1 ? (int64_t)c.h - 1 : py1;
+    if (px0 > px1 || py0 > py1) return;
+    int32_t X[3] = {X0, X1, X2}, Y[3] = {Y0, Y1, Y2};
+    int32_t bias[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int a = k, b = (k + 1) % 3;
+        const int32_t dx = X[b] - X[a], dy = Y[b] - Y[a];
+        bias[k] = (dy < 0 || (dy == 0 && dx > 0)) ? 0 : 1;
+    }
+    const float dx1 = __int2float_rn(X1 - X0), dy1 = __int2float_rn(Y1 - Y0);
+    const float dx2 = __int2float_rn(X2 - X0), dy2 = __int2float_rn(Y2 - Y0);
+    const float af = __ll2float_rn(A);
+    const float dz1 = fsub(Z1, Z0), dz2 = fsub(Z2, Z0);
+    const float pa = fdiv(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), af);
+    const float pb = fdiv(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), af);
+    const int64_t bw = px1 - px0 + 1, bh = py1 - py0 + 1;
+    if (bw * bh <= (int64_t)c.small_area) {
+        raster_rect(X, Y, bias, Z0, pa, pb, id, (int)px0, (int)py0, (int)px1, (int)py1, c.depth, c.w);
+        return;
+    }
+    const int64_t cs = c.chunk;
+    const int64_t ncx = (bw + cs - 1) / cs, ncy = (bh + cs - 1) / cs;
+    const uint32_t n = (uint32_t)(ncx * ncy);
+    const uint32_t base = atomicAdd(c.big_count, n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const int64_t cx = i % ncx, cy = i / ncx;
+        const int qx0 = (int)(px0 + cx * cs), qy0 = (int)(py0 + cy * cs);
+        const int qx1 = (int)min(px1, px0 + (cx + 1) * cs - 1), qy1 = (int)min(py1, py0 + (cy + 1) * cs - 1);
+        if (base + i < c.big_cap) {
+            BigTri t;
+            t.x[0] = X0, t.x[1] = X1, t.x[2] = X2;
+            t.y[0] = Y0, t.y[1] = Y1, t.y[2] = Y2;
+            t.z0 = Z0, t.pa = pa, t.pb = pb;
+            t.id = id;
+            t.px0 = (uint16_t)qx0, t.py0 = (uint16_t)qy0, t.px1 = (uint16_t)qx1, t.py1 = (uint16_t)qy1;
+            t.view = c.view;
+            t._pad = 0;
+            c.big[base + i] = t;
+        } else {
+            report(c.status, kStatusQueueOverflow, base + i);
+            raster_rect(X, Y, bias, Z0, pa, pb, id, qx0, qy0, qx1, qy1, c.depth, c.w);
+        }
+    }
+}
+
+__device__ __forceinline__ bool snap(const float4& v, const RasterCtx& c, int32_t& X, int32_t& Y, float& Z) {
+    if (!(v.w > 0.0f)) return false;
+    const float xd = fdiv(v.x, v.w), yd = fdiv(v.y, v.w), zd = fdiv(v.z, v.w);
+    const float xf = fadd(fmul(xd, c.hw), c.hw), yf = fadd(fmul(yd, c.hh), c.hh);
+    const float sx = fmul(xf, 256.0f), sy = fmul(yf, 256.0f);
+    if (!(fabsf(sx) < 1073741824.0f) || !(fabsf(sy) < 1073741824.0f)) return false;
+    X = __float2int_rn(sx);
+    Y = __float2int_rn(sy);
+    Z = zd;
+    return true;
+}
+
+__device__ __forceinline__ float plane_dist(const float4& v, int plane) {
+    switch (plane) {
+        case 0: return fsub(v.w, v.z);
+        case 1: return v.z;
+        case 2: return fsub(fmul(kGuard, v.w), v.x);
+        case 3: return fadd(v.x, fmul(kGuard, v.w));
+        case 4: return fsub(fmul(kGuard, v.w), v.y);
+        default: return fadd(v.y, fmul(kGuard, v.w));
+    }
+}
+
+__device__ int clip_poly(const float4* in, int n, float4* out, int plane) {
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+        const float4 a = in[i];
+        const float4 b = in[(i + 1) % n];
+        const float da = plane_dist(a, plane), db = plane_dist(b, plane);
+        const bool ia = da >= 0.0f, ib = db >= 0.0f;
+        if (ia) out[m++] = a;
+        if (ia != ib) {
+            const float t = fdiv(da, fsub(da, db));
+            out[m++] = make_float4(fadd(a.x, fmul(t, fsub(b.x, a.x))), fadd(a.y, fmul(t, fsub(b.y, a.y))),
+                                   fadd(a.z, fmul(t, fsub(b.z, a.z))), fadd(a.w, fmul(t, fsub(b.w, a.w))));
+        }
+    }
+    return m;
+}
+
+// Slow path: homogeneous clipping (near/far, then guard band) and a fan.
+__device__ __noinline__ void raster_clipped(float4 v0, float4 v1, float4 v2, bool clipz, uint32_t id,
+                                            const RasterCtx& c) {
+    float4 bufa[12], bufb[12];
+    bufa[0] = v0, bufa[1] = v1, bufa[2] = v2;
+    float4* cur = bufa;
+    float4* nxt = bufb;
+    int n = 3;
+    if (clipz) {
+        for (int plane = 0; plane < 2 && n >= 3; ++plane) {
+            n = clip_poly(cur, n, nxt, plane);
+            float4* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+    }
+    bool guard = false;
+    for (int k = 0; k < n; ++k) guard |= outside_guard(cur[k]);
+    if (guard) {
+        for (int plane = 2; plane < 6 && n >= 3; ++plane) {
+            n = clip_poly(cur, n, nxt, plane);
+            float4* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+    }
+    if (n < 3) return;
+    int32_t X[12], Y[12];
+    float Z[12];
+    for (int k = 0; k < n; ++k)
+        if (!snap(cur[k], c, X[k], Y[k], Z[k])) return;
+    for (int k = 1; k + 1 < n; ++k)
+        setup_and_raster(X[0], Y[0], Z[0], X[k], Y[k], Z[k], X[k + 1], Y[k + 1], Z[k + 1], id, c);
+}
+
+__device__ __forceinline__ void raster_triangle(const float4& a, const float4& b, const float4& cc, uint32_t id,
+                                                const RasterCtx& c) {
+    const int oc0 = outcode(a), oc1 = outcode(b), oc2 = outcode(cc);
+    if (oc0 & oc1 & oc2) return;
+    const bool clipz = ((oc0 | oc1 | oc2) & (OC_ZLO | OC_ZHI)) != 0;
+    if (clipz || outside_guard(a) || outside_guard(b) || outside_guard(cc)) {
+        raster_clipped(a, b, cc, clipz, id, c);
+        return;
+    }
+    int32_t X0, Y0, X1, Y1, X2, Y2;
+    float Z0, Z1, Z2;
+    if (!snap(a, c, X0, Y0, Z0) || !snap(b, c, X1, Y1, Z1) || !snap(cc, c, X2, Y2, Z2)) return;
+    setup_and_raster(X0, Y0, Z0, X1, Y1, Z1, X2, Y2, Z2, id, c);
+}
+
+struct RasterParams {
+    SceneArgs S;
+    const DeviceView* views;
+    RasterLists lists;
+    BigTri* big;
+    uint32_t* big_count;
+    uint32_t big_cap;
+    uint32_t small_area;
+    uint32_t chunk;
+    uint32_t* status;
+};
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_raster(RasterParams P) {
+    __shared__ float4 s_clip[WARPS][64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t vi = blockIdx.y;
+    const DeviceView& V = P.views[vi];
+    const uint32_t* list;
+    uint32_t count, first = 0;
+    if (P.lists.pass == 1) {
+        list = V.survivors;
+        count = min(V.counters[0], V.survivor_capacity);
+    } else if (P.lists.pass == 2) {
+        const uint32_t c0 = min(V.counters[0], V.survivor_capacity);
+        list = V.survivors + c0;
+        count = min(V.counters[2], V.survivor_capacity - c0);
+    } else {
+        list = P.lists.list;
+        count = *P.lists.count;
+        first = P.lists.first;
+    }
+    RasterCtx c;
+    c.depth = V.depth_id;
+    c.w = V.w;
+    c.h = V.h;
+    c.hw = 0.5f * (float)V.w;
+    c.hh = 0.5f * (float)V.h;
+    c.view = vi;
+    c.big = P.big;
+    c.big_count = P.big_count;
+    c.big_cap = P.big_cap;
+    c.small_area = P.small_area;
+    c.chunk = P.chunk;
+    c.status = P.status;
+    float VP[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) VP[k] = V.cam->view_projection[k];
+    const uint32_t stride = gridDim.x * WARPS;
+    for (uint32_t s = first + blockIdx.x * WARPS + warp; s < count; s += stride) {
+        const uint32_t d = list[s];
+        if (d >= P.S.draw_count) {
+            if (lane == 0) report(P.status, kStatusBadIndex, d);
+            continue;
+        }
+        const vkgv_meshlet_draw dr = P.S.draws[d];
+        const vkgv_primitive* prim = &P.S.prims[dr.primitive_index];
+        const uint32_t mcount = prim->meshlet_count;
+        if (dr.meshlet_index >= mcount) {
+            if (lane == 0) report(P.status, kStatusBadIndex, d);
+            continue;
+        }
+        const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
+        const uint32_t vc = ml->vertex_count, tc = ml->triangle_count;
+        if (vc > 64) {
+            if (lane == 0) report(P.status, kStatusBadIndex, d);
+            continue;
+        }
+        const uint32_t* vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
+        const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset;
+        const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
+        const bool double_sided = P.S.mats[prim->material_index].double_sided != 0;
+        const float4* M4 = reinterpret_cast<const float4*>(P.S.transforms + 16 * (size_t)dr.transform_index);
+        float M[16];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float4 t = __ldg(M4 + q);
+            M[q * 4 + 0] = t.x;
+            M[q * 4 + 1] = t.y;
+            M[q * 4 + 2] = t.z;
+            M[q * 4 + 3] = t.w;
+        }
+        float mvp[16];
+        m4m(VP, M, mvp);
+        const float tdet = det4(M);
+        for (uint32_t k = lane; k < vc; k += 32) {
+            const vkgv_vertex* vx = verts + __ldg(vidx + k);
+            const float2 xy = __ldg(reinterpret_cast<const float2*>(vx->position));
+            const float z = __ldg(&vx->position[2]);
+            float r[4];
+            m4v(mvp, xy.x, xy.y, z, 1.0f, r);
+            s_clip[warp][k] = make_float4(r[0], r[1], r[2], r[3]);
+        }
+        __syncwarp();
+        for (uint32_t t = lane; t < tc; t += 32) {
+            const uint32_t i0 = __ldg(tri + 3 * t), i1 = __ldg(tri + 3 * t + 1), i2 = __ldg(tri + 3 * t + 2);
+            if (i0 >= vc || i1 >= vc || i2 >= vc) {
+                report(P.status, kStatusBadIndex, d);
+                continue;
+            }
+            const float4 a = s_clip[warp][i0], b = s_clip[warp][i1], cc = s_clip[warp][i2];
+            if (!double_sided) {
+                const float det = det3(a.x, a.y, a.w, b.x, b.y, b.w, cc.x, cc.y, cc.w);
+                const bool cull = tdet < 0.0f ? det < 0.0f : det > 0.0f;
+                if (cull) continue;
+            }
+            raster_triangle(a, b, cc, (d << 7) | t, c);
+        }
+        __syncwarp();
+    }
+}
+
+// Drains the binned rectangles: one CTA per rectangle, 64 x 4 threads.
+__global__ void __launch_bounds__(256) k_raster_big(const BigTri* __restrict__ q, const uint32_t* count,
+                                                    uint32_t cap, const DeviceView* __restrict__ views) {
+    const uint32_t n = min(*count, cap);
+    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
+    for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
+        const BigTri t = q[e];
+        const DeviceView& V = views[t.view];
+        unsigned long long* depth = V.depth_id;
+        const uint32_t w = V.w;
+        const unsigned long long lo = (unsigned long long)t.id + 1ull;
+        int32_t bias[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int a = k, b = (k + 1) % 3;
+            const int32_t dx = t.x[b] - t.x[a], dy = t.y[b] - t.y[a];
+            bias[k] = (dy < 0 || (dy == 0 && dx > 0)) ? 0 : 1;
+        }
+        for (int py = t.py0 + ty; py <= (int)t.py1; py += 4) {
+            const int32_t sy = py * 256 + 128;
+            const float zrow = __fmaf_rn(t.pb, __int2float_rn(sy - t.y[0]), t.z0);
+            for (int px = t.px0 + tx; px <= (int)t.px1; px += 64) {
+                const int32_t sx = px * 256 + 128;
+                bool covered = true;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int a = k, b = (k + 1) % 3;
+                    const int64_t ev = (int64_t)(t.x[b] - t.x[a]) * (sy - t.y[a]) -
+                                       (int64_t)(t.y[b] - t.y[a]) * (sx - t.x[a]);
+                    covered = covered && ev >= bias[k];
+                }
+                if (!covered) continue;
+                float z = __fmaf_rn(t.pa, __int2float_rn(sx - t.x[0]), zrow);
+                if (!(z > 0.0f)) z = 0.0f;
+                if (z > 1.0f) z = 1.0f;
+                plot(depth + (size_t)py * w + px, ((unsigned long long)__float_as_uint(z) << 32) | lo);
+            }
+        }
+    }
+}
+
+}  // namespace
+
+void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews, const RasterLists& lists,
+                   const RasterConfig& cfg, BigTri* big, uint32_t* big_count, uint32_t big_capacity,
+                   uint32_t* status, uint32_t sm_count, cudaStream_t stream, cudaEvent_t between) {
+    RasterParams P;
+    P.S = S;
+    P.views = views;
+    P.lists = lists;
+    P.big = big;
+    P.big_count = big_count;
+    P.big_cap = big_capacity;
+    P.small_area = cfg.small_area;
+    P.chunk = cfg.chunk;
+    P.status = status;
+    uint32_t bpv = cfg.blocks_per_view ? cfg.blocks_per_view : (sm_count * 16 + nviews - 1) / nviews;
+    if (bpv == 0) bpv = 1;
+    dim3 grid(bpv, nviews);
+    switch (cfg.warps_per_cta) {
+        case 1: k_raster<1><<<grid, 32, 0, stream>>>(P); break;
+        case 2: k_raster<2><<<grid, 64, 0, stream>>>(P); break;
+        case 8: k_raster<8><<<grid, 256, 0, stream>>>(P); break;
+        default: k_raster<4><<<grid, 128, 0, stream>>>(P); break;
+    }
+    if (between) cudaEventRecord(between, stream);
+    k_raster_big<<<sm_count * 8, 256, 0, stream>>>(big, big_count, big_capacity, views);
+}
+
+}  // namespace vkgv

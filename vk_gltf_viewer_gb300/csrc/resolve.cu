@@ -1,0 +1,240 @@
+// Visibility-buffer resolve (shaders/visbuffer/visbuffer_resolve.comp.glsl:17-41)
+// plus the per-frame clear and the survivor-count finalisation.
+//
+// Flat resolve: per pixel, unpack the ID, fetch draw -> primitive ->
+// material and store fromLinear(albedoFactor) (shaders/srgb.h.glsl:26-32) as
+// RGBA8 UNORM, or 0 where nothing was drawn.  The reference dispatches
+// floor(W/32) x H groups (application.cpp:945), leaving the last W mod 32
+// columns unwritten; every column is written here.
+//
+// Textured resolve (extension, no reference implementation): the commented-out
+// formula of visbuffer.frag.glsl:29-34 — perspective-correct barycentrics of
+// the visible triangle, vertex colour, transformUv (mesh_common.h.glsl:129-135)
+// and a bilinear REPEAT base-colour sample decoded with toLinear.
+#include <cuda_fp16.h>
+
+#include "kernels.cuh"
+
+namespace vkgv {
+
+namespace {
+
+__device__ __forceinline__ float from_linear(float c) {
+    const bool cutoff = c < 0.0031308f;
+    const float higher = 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
+    const float lower = c * 12.92f;
+    return cutoff ? lower : higher;
+}
+
+__device__ __forceinline__ float to_linear(float c) {
+    const bool cutoff = c < 0.04045f;
+    const float higher = powf((c + 0.055f) / 1.055f, 2.4f);
+    const float lower = c / 12.92f;
+    return cutoff ? lower : higher;
+}
+
+__device__ __forceinline__ uint32_t unorm8(float c) {
+    if (!(c > 0.0f)) return 0;
+    if (c > 1.0f) c = 1.0f;
+    return (uint32_t)__float2int_rn(c * 255.0f);
+}
+
+__device__ __forceinline__ uint32_t pack_rgba(const float lin[4]) {
+    return unorm8(from_linear(lin[0])) | (unorm8(from_linear(lin[1])) << 8) | (unorm8(from_linear(lin[2])) << 16) |
+           (unorm8(lin[3]) << 24);
+}
+
+__device__ void sample_texture(const vkgv_texture& t, float u, float v, float out[4]) {
+    const float tx = u * (float)t.width - 0.5f, ty = v * (float)t.height - 0.5f;
+    const float fx = floorf(tx), fy = floorf(ty);
+    const float ax = tx - fx, ay = ty - fy;
+    const long long W = t.width, H = t.height;
+    long long x0 = (long long)fx, y0 = (long long)fy;
+    const long long xs[2] = {((x0 % W) + W) % W, (((x0 + 1) % W) + W) % W};
+    const long long ys[2] = {((y0 % H) + H) % H, (((y0 + 1) % H) + H) % H};
+    float tex[2][2][4];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const size_t idx = (size_t)ys[j] * t.row_pitch + (size_t)xs[i];
+            if (t.format == VKGV_TEXTURE_RGBA8) {
+                const uchar4 p = __ldg(reinterpret_cast<const uchar4*>(t.data) + idx);
+                tex[j][i][0] = (float)p.x / 255.0f;
+                tex[j][i][1] = (float)p.y / 255.0f;
+                tex[j][i][2] = (float)p.z / 255.0f;
+                tex[j][i][3] = (float)p.w / 255.0f;
+            } else {
+                const float* p = reinterpret_cast<const float*>(t.data) + 3 * idx;
+                tex[j][i][0] = __ldg(p);
+                tex[j][i][1] = __ldg(p + 1);
+                tex[j][i][2] = __ldg(p + 2);
+                tex[j][i][3] = 1.0f;
+            }
+        }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float top = tex[0][0][k] + ax * (tex[0][1][k] - tex[0][0][k]);
+        const float bot = tex[1][0][k] + ax * (tex[1][1][k] - tex[1][0][k]);
+        out[k] = top + ay * (bot - top);
+    }
+}
+
+__device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32_t px, uint32_t py, uint32_t id,
+                                 float out[4]) {
+    const uint32_t d = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
+    const vkgv_meshlet_draw dr = S.draws[d];
+    const vkgv_primitive* prim = &S.prims[dr.primitive_index];
+    const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
+    const vkgv_material& mat = S.mats[prim->material_index];
+    const float* Mp = S.transforms + 16 * (size_t)dr.transform_index;
+    float M[16], VP[16], mvp[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        M[k] = __ldg(Mp + k);
+        VP[k] = V.cam->view_projection[k];
+    }
+    m4m(VP, M, mvp);
+    const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset + 3 * t;
+    const uint32_t* vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
+    const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
+    float c[3][4];
+    const vkgv_vertex* vx[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        vx[k] = verts + vidx[tri[k]];
+        m4v(mvp, vx[k]->position[0], vx[k]->position[1], vx[k]->position[2], 1.0f, c[k]);
+    }
+    const float nx = (((float)px + 0.5f) / (float)V.w) * 2.0f - 1.0f;
+    const float ny = (((float)py + 0.5f) / (float)V.h) * 2.0f - 1.0f;
+    float a[3], b[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a[k] = c[k][0] - nx * c[k][3];
+        b[k] = c[k][1] - ny * c[k][3];
+    }
+    float l[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    const float sum = (l[0] + l[1]) + l[2];
+    if (sum != 0.0f) {
+        l[0] /= sum;
+        l[1] /= sum;
+        l[2] /= sum;
+    } else {
+        l[0] = l[1] = l[2] = 1.0f / 3.0f;
+    }
+    float col[4], uv[2];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        col[k] = (l[0] * ((float)vx[0]->color[k] / 255.0f) + l[1] * ((float)vx[1]->color[k] / 255.0f)) +
+                 l[2] * ((float)vx[2]->color[k] / 255.0f);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float h0 = __half2float(__ushort_as_half(vx[0]->uv[k]));
+        const float h1 = __half2float(__ushort_as_half(vx[1]->uv[k]));
+        const float h2 = __half2float(__ushort_as_half(vx[2]->uv[k]));
+        uv[k] = (l[0] * h0 + l[1] * h1) + l[2] * h2;
+    }
+    float sampled[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+    if (mat.albedo_index != VKGV_INVALID_HANDLE && mat.albedo_index < S.texture_count) {
+        const float cs = cosf(mat.uv_rotation), sn = sinf(mat.uv_rotation);
+        const float ru = cs * uv[0] + sn * uv[1], rv = -sn * uv[0] + cs * uv[1];
+        const float tu = ru * mat.uv_scale[0] + mat.uv_offset[0];
+        const float tv = rv * mat.uv_scale[1] + mat.uv_offset[1];
+        const vkgv_texture tex = S.textures[mat.albedo_index];
+        sample_texture(tex, tu, tv, sampled);
+        if (tex.format == VKGV_TEXTURE_RGBA8)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) sampled[k] = to_linear(sampled[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = col[k] * mat.albedo_factor[k] * sampled[k];
+}
+
+template <bool TEXTURED>
+__global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
+    const DeviceView& V = views[blockIdx.y];
+    const uint32_t w = V.w, n = V.w * V.h;
+    uint32_t* ids = (flags & VKGV_WRITE_IDS) ? V.ids : nullptr;
+    uint32_t* rgba = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED)) ? V.rgba : nullptr;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint32_t lo = (uint32_t)__ldcs(V.depth_id + p);
+        const uint32_t id = lo ? lo - 1u : VKGV_VISBUFFER_CLEAR;
+        if (ids) __stcs(ids + p, id);
+        if (!rgba) continue;
+        uint32_t out = 0;
+        if (id != VKGV_VISBUFFER_CLEAR) {
+            float lin[4];
+            if (TEXTURED) {
+                resolve_textured(S, V, p % w, p / w, id, lin);
+            } else {
+                const vkgv_meshlet_draw dr = S.draws[id >> VKGV_TRIANGLE_BITS];
+                const vkgv_material& mat = S.mats[S.prims[dr.primitive_index].material_index];
+                const float4 a = *reinterpret_cast<const float4*>(mat.albedo_factor);
+                lin[0] = a.x;
+                lin[1] = a.y;
+                lin[2] = a.z;
+                lin[3] = a.w;
+            }
+            out = pack_rgba(lin);
+        }
+        __stcs(rgba + p, out);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ views, uint32_t* counters,
+                                               uint32_t counter_words, uint32_t skip_pixels) {
+    const DeviceView& V = views[blockIdx.y];
+    if (blockIdx.x == 0 && threadIdx.x < 4) V.counters[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && blockIdx.y == 0)
+        for (uint32_t i = threadIdx.x; i < counter_words; i += blockDim.x) counters[i] = 0;
+    if (skip_pixels) return;
+    const uint32_t n = V.w * V.h;
+    // 16-byte stores of two pixels; depth_id allocations are 16-byte aligned
+    // when they come from cudaMalloc (checked by the host).
+    ulonglong2* p2 = reinterpret_cast<ulonglong2*>(V.depth_id);
+    const uint32_t n2 = n / 2;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x)
+        __stcg(p2 + i, make_ulonglong2(0ull, 0ull));
+    if ((n & 1u) && blockIdx.x == 0 && threadIdx.x == 0) V.depth_id[n - 1] = 0ull;
+}
+
+__global__ void k_finalize(const DeviceView* __restrict__ views, uint32_t nviews) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nviews) return;
+    const DeviceView& V = views[v];
+    if (!V.survivor_count) return;
+    const uint32_t c0 = min(V.counters[0], V.survivor_capacity);
+    const uint32_t c2 = min(V.counters[2], V.survivor_capacity - c0);
+    *V.survivor_count = c0 + c2;
+}
+
+}  // namespace
+
+void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h,
+                    uint32_t flags, cudaStream_t stream) {
+    const uint64_t px = (uint64_t)max_w * max_h;
+    uint32_t bx = (uint32_t)((px + 255) / 256);
+    if (bx > 65535u) bx = 65535u;
+    dim3 grid(bx, nviews);
+    if (flags & VKGV_RESOLVE_TEXTURED)
+        k_resolve<true><<<grid, 256, 0, stream>>>(S, views, flags);
+    else
+        k_resolve<false><<<grid, 256, 0, stream>>>(S, views, flags);
+}
+
+void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels, uint32_t* counters,
+                  uint32_t counter_words, uint32_t sm_count, cudaStream_t stream) {
+    const bool skip = max_pixels == 0;
+    uint64_t want = (max_pixels / 2 + 255) / 256;
+    uint32_t cap = (sm_count * 16 + nviews - 1) / nviews;
+    if (cap < 1) cap = 1;
+    uint32_t bx = skip ? 1u : (uint32_t)(want < cap ? (want ? want : 1) : cap);
+    dim3 grid(bx, nviews);
+    k_clear<<<grid, 256, 0, stream>>>(views, counters, counter_words, skip ? 1u : 0u);
+}
+
+void launch_finalize(const DeviceView* views, uint32_t nviews, cudaStream_t stream) {
+    k_finalize<<<(nviews + 127) / 128, 128, 0, stream>>>(views, nviews);
+}
+
+}  // namespace vkgv
