@@ -1,0 +1,378 @@
+"""Benchmark of the GB300 meshlet visibility-buffer path.
+
+Metric: views/s at 1920x1080 on the 82M-triangle torus-grid scene (2048
+instances of a 40,000-triangle displaced torus, 843,776 meshlet draws) with
+two-pass frustum + HiZ occlusion culling, visibility-buffer rasterisation,
+HiZ pyramid and textured resolve, one step = one frame through a captured
+CUDA graph.  The batched leg renders 256 views of uneven resolution in one
+graph launch.  Inputs are synthetic (seeded procedural scene and cameras).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank renders its own views (weak scaling, no
+collective on the data path); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "views/s at 1080p, 82M-tri scene: batched vs single-view CUDA; adjoint ms/view"
+WORKLOAD = ("torus grid: 2048 instances x 40,000 tris = 81.92M tris, 843,776 meshlet draws (<=64 verts/"
+            "<=124 tris), 1920x1080, two-pass frustum+HiZ culling, HiZ pyramid, textured resolve, "
+            "steady state (previous frame's pyramid)")
+W1080, H1080 = 1920, 1080
+FLAGS_NAMES = "CULL_FRUSTUM|CULL_OCCLUSION|CULL_TWO_PASS|BUILD_PYRAMID|RESOLVE_TEXTURED|WRITE_IDS"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--batch-views", type=int, default=256)
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.lines: list[str] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- reference
+
+def run_reference(args, rank, world):
+    """The reference's path on the host cores: the CPU restatement of the
+    shader math (the Vulkan renderer itself cannot run here), same workload,
+    all host threads, steady state."""
+    if rank != 0:
+        return
+    import numpy as np
+
+    from oracle import binding as ob
+    from vk_gltf_viewer_gb300 import scene
+
+    threads = os.cpu_count() or 1
+    ob.set_threads(threads)
+    host = scene.scene_torus_grid()
+    cam = scene.grid_camera(W1080, H1080)
+    osc = ob.OracleScene(host)
+    flags = ob.CULL_FRUSTUM | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID | ob.RESOLVE_TEXTURED
+    prev = ob.frame(osc, cam, W1080, H1080, flags)["pyramid"]
+    for _ in range(max(0, args.warmup)):
+        prev = ob.frame(osc, cam, W1080, H1080, flags, prev_pyramid=prev)["pyramid"]
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        prev = ob.frame(osc, cam, W1080, H1080, flags, prev_pyramid=prev)["pyramid"]
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    del np
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "views/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "flags": FLAGS_NAMES},
+        "cpu_baseline": {"value": v, "unit": "views/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} steady-state frames of the workload on {threads} host threads"},
+        "e2e": {"value": v, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the Vulkan renderer needs a mesh-shader graphics device (none on this box); its CPU "
+                "restatement (oracle/oracle.c) is timed instead",
+    }), flush=True)
+
+
+# ------------------------------------------------------------------- ours
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+
+    from vk_gltf_viewer_gb300 import abi, scene
+    from vk_gltf_viewer_gb300 import build as vbuild
+    from vk_gltf_viewer_gb300.renderer import DeviceScene, Renderer, ViewBuffers
+
+    if not vbuild.LIB.exists():
+        vbuild.build()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    r = Renderer(local)
+    host = scene.scene_torus_grid()
+    dev = DeviceScene(host, f"cuda:{local}")
+    flags = (abi.CULL_FRUSTUM | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID | abi.RESOLVE_TEXTURED
+             | abi.WRITE_IDS)
+    cam = scene.grid_camera(W1080, H1080)
+    view = ViewBuffers.allocate(W1080, H1080, cam, host.draw_count, device=f"cuda:{local}", prev_pyramid="alias")
+    # first frame without history, then steady state
+    view.use_prev = False
+    r.frame(dev, [view], flags)
+    view.use_prev = True
+    for _ in range(2):
+        r.frame(dev, [view], flags)
+    torch.cuda.synchronize()
+
+    # per-stage zones of one steady-state frame (outside the timed region)
+    r.set_profiling(True)
+    stage_runs = []
+    for _ in range(5):
+        r.frame(dev, [view], flags)
+        stage_runs.append(r.stage_times())
+    r.set_profiling(False)
+    stages = {k: statistics.median([s[k] for s in stage_runs]) for k in stage_runs[0]}
+
+    graph = r.capture(dev, [view], flags)
+    kernels_per_frame = graph.kernel_count()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    for _ in range(max(3, args.warmup)):
+        graph.launch()
+    torch.cuda.synchronize()
+
+    # ---- timed: single view, device-resident inputs, L2 flushed between steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            starts[i].record(stream)
+            graph.launch()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        # keep sampling a moment under load for the clock record
+        for _ in range(20):
+            graph.launch()
+        torch.cuda.synchronize()
+    per_step = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_local = sum(per_step) / 1000.0
+    t = torch.tensor([t_local], device=f"cuda:{local}")
+    if pg:
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    t_max = float(t.item())
+    value = world * args.steps / t_max
+    ms_per_step = 1000.0 * t_max / args.steps
+    status = r.device_status()
+
+    # ---- e2e through the C ABI with host buffers: camera in, RGBA8 out
+    cam_host = torch.from_numpy(scene.camera_bytes(cam)).pin_memory()
+    rgba_host = torch.empty(W1080 * H1080, dtype=torch.int32).pin_memory()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        view.camera.copy_(cam_host, non_blocking=True)
+        graph.launch()
+        rgba_host.copy_(view.color, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    te = torch.tensor([e0.elapsed_time(e1) / 1000.0], device=f"cuda:{local}")
+    if pg:
+        pg.all_reduce(te, op=pg.ReduceOp.MAX)
+    e2e_value = world * args.steps / float(te.item())
+    graph.close()
+
+    # ---- roofline of the dominant kernel (meshlet raster, pass 1)
+    dominant = max(("raster1", "big1", "cull1", "cull2", "hiz", "resolve", "clear"), key=lambda k: stages[k])
+    surv = int(view.survivor_count.item())
+    mesh = host.meshes[0]
+    g_unique = (36 * mesh.meshlet_count + 4 * mesh.vertex_indices.size + 24 * mesh.vertices.size
+                + mesh.primitive_indices.size)
+    px = W1080 * H1080
+    alg_bytes = {
+        # survivor entry + draw record per meshlet, unique geometry, transforms,
+        # one 8-byte depth|id write-back per pixel
+        "raster1": 16 * surv + g_unique + 64 * host.transforms.shape[0] + 8 * px,
+        # draw list + transforms + meshlet bounds read, survivor/reject lists written
+        "cull1": 12 * host.draw_count + 64 * host.transforms.shape[0] + 36 * mesh.meshlet_count + 8 * surv,
+        "resolve": 8 * px + 4 * px + 4 * px,
+        "hiz": 8 * px + 4 * sum(max(1, (W1080 >> 1) >> k) * max(1, (H1080 >> 1) >> k) for k in range(10)),
+        "clear": 8 * px,
+    }
+    dom_bytes = alg_bytes.get(dominant, alg_bytes["raster1"])
+    dom_ms = stages[dominant]
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    peak, peak_src = 6800.0, "fallback"
+    if peaks_path.exists():
+        peak, peak_src = float(json.loads(peaks_path.read_text())["hbm_gbs"]), "measured"
+    achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / "raster_meshlets_c2_1080p.md"
+    if prof.exists():
+        for line in prof.read_text().splitlines():
+            if line.startswith("dram_bytes_per_launch:"):
+                traffic = int(line.split(":")[1].strip())
+
+    # ---- batched leg: 256 uneven views in one graph launch
+    batched = None
+    if not args.no_batched and args.batch_views > 0:
+        bv = []
+        for bcam, w, h in scene.batch_views(args.batch_views):
+            vb = ViewBuffers.allocate(w, h, bcam, host.draw_count, device=f"cuda:{local}", prev_pyramid="alias",
+                                      survivors=False)
+            bv.append(vb)
+        for vb in bv:
+            vb.use_prev = False
+        r.frame(dev, bv, flags)
+        for vb in bv:
+            vb.use_prev = True
+        r.frame(dev, bv, flags)
+        bgraph = r.capture(dev, bv, flags)
+        for _ in range(2):
+            bgraph.launch()
+        torch.cuda.synchronize()
+        bsteps = max(2, min(args.steps, 5))
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        b0.record(stream)
+        for _ in range(bsteps):
+            bgraph.launch()
+        b1.record(stream)
+        torch.cuda.synchronize()
+        tb = torch.tensor([b0.elapsed_time(b1) / 1000.0], device=f"cuda:{local}")
+        if pg:
+            pg.all_reduce(tb, op=pg.ReduceOp.MAX)
+        bval = world * bsteps * len(bv) / float(tb.item())
+        batched = {"value": bval, "unit": "views/s", "views_per_launch": len(bv), "steps": bsteps,
+                   "ms_per_launch": 1000.0 * float(tb.item()) / bsteps,
+                   "kernels_per_launch": bgraph.kernel_count(),
+                   "speedup_vs_single_view": bval / value,
+                   "mean_pixels_per_view": float(np.mean([vb.width * vb.height for vb in bv])),
+                   "config": "256 poses on a radius-30 sphere around the grid centre, sizes uniform over "
+                             "256^2, 512x384, 1024x576, 1280x720, 1920x1080"}
+        bgraph.close()
+        del bv
+
+    # ---- CPU baseline: the oracle on the host cores, bounded sample
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import binding as ob
+        threads = os.cpu_count() or 1
+        ob.set_threads(threads)
+        osc = ob.OracleScene(host)
+        of = ob.CULL_FRUSTUM | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID | ob.RESOLVE_TEXTURED
+        prev = ob.frame(osc, cam, W1080, H1080, of)["pyramid"]
+        n_cpu = 0
+        tc0 = time.perf_counter()
+        while n_cpu < 3 or (time.perf_counter() - tc0 < 10.0 and n_cpu < 30):
+            prev = ob.frame(osc, cam, W1080, H1080, of, prev_pyramid=prev)["pyramid"]
+            n_cpu += 1
+        tc = time.perf_counter() - tc0
+        cpu = {"value": n_cpu / tc, "unit": "views/s", "cores": threads, "kind": "port",
+               "sample": f"{n_cpu} steady-state frames of the same workload (oracle/oracle.c, {threads} threads)"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "flags": FLAGS_NAMES, "width": W1080, "height": H1080,
+                       "draws": host.draw_count, "triangles": host.triangle_count,
+                       "l2": "256 MiB buffer written between timed steps (outside the events)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "views/s", "h2d_bytes_per_step": 352,
+                    "d2h_bytes_per_step": W1080 * H1080 * 4},
+            "gpu_launches": kernels_per_frame * args.steps,
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                         "algorithmic_bytes": dom_bytes, "kernel_ms": dom_ms},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "stages_ms": stages,
+            "survivors": surv,
+            "device_status": list(status),
+        }
+        if batched:
+            out["batched"] = batched
+        print(json.dumps(out), flush=True)
+    if pg:
+        pg.destroy_process_group()
+    r.close()
+
+
+if __name__ == "__main__":
+    main()

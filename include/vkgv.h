@@ -271,6 +271,8 @@ int vkgv_graph_capture(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* 
                        uint32_t view_count, uint32_t flags, vkgv_graph** out_graph);
 int vkgv_graph_launch(vkgv_graph* graph, void* stream);
 int vkgv_graph_destroy(vkgv_graph* graph);
+/* Number of kernel launches one vkgv_graph_launch performs. */
+int vkgv_graph_kernel_count(const vkgv_graph* graph, uint32_t* out_count);
 
 /* ---------------------------------------------- host scene producers (A15) */
 /* Replace the glTF import + meshletiser (src/vk_gltf_viewer/assets.cpp:288-430)

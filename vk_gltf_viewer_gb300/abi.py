@@ -142,6 +142,7 @@ _PROTOS = {
     "vkgv_graph_capture": (C.c_int, [_P, C.POINTER(Scene), C.POINTER(View), _U32, _U32, C.POINTER(_P)]),
     "vkgv_graph_launch": (C.c_int, [_P, _P]),
     "vkgv_graph_destroy": (C.c_int, [_P]),
+    "vkgv_graph_kernel_count": (C.c_int, [_P, C.POINTER(_U32)]),
     "vkgv_mesh_icosphere": (_P, [_U32]),
     "vkgv_mesh_torus": (_P, [C.c_float, C.c_float, _U32, _U32, C.c_float, _U64, C.c_int32]),
     "vkgv_mesh_displace": (C.c_int, [_P, C.c_float, _U64]),

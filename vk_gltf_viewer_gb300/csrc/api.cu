@@ -628,6 +628,21 @@ int vkgv_graph_launch(vkgv_graph* g, void* stream_) {
     return VKGV_OK;
 }
 
+int vkgv_graph_kernel_count(const vkgv_graph* g, uint32_t* out_count) {
+    if (!g || !g->graph || !out_count) return VKGV_INVALID_ARG;
+    size_t n = 0;
+    if (cudaGraphGetNodes(g->graph, nullptr, &n) != cudaSuccess) return VKGV_CUDA_ERROR;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n && cudaGraphGetNodes(g->graph, nodes.data(), &n) != cudaSuccess) return VKGV_CUDA_ERROR;
+    uint32_t k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    *out_count = k;
+    return VKGV_OK;
+}
+
 int vkgv_graph_destroy(vkgv_graph* g) {
     if (!g) return VKGV_INVALID_ARG;
     if (g->exec) cudaGraphExecDestroy(g->exec);

@@ -205,12 +205,12 @@ __global__ void __launch_bounds__(256) k_cull(SceneArgs S, const DeviceView* __r
 void launch_cull(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t flags, uint32_t pass,
                  uint32_t* status, uint32_t sm_count, cudaStream_t stream) {
     const uint32_t threads = 256;
-    uint32_t want = (S.draw_count + threads - 1) / threads;
-    // pass 2 candidate counts live on the device: cap the grid and stride.
-    uint32_t cap = pass == 1 ? 4096u : 64u;
-    uint32_t per_view = want < cap ? want : cap;
-    uint32_t min_blocks = (sm_count * 8 + nviews - 1) / nviews;
-    if (pass == 1 && per_view < min_blocks && want > per_view) per_view = want < min_blocks ? want : min_blocks;
+    const uint32_t want = (S.draw_count + threads - 1) / threads;
+    // Pass 1 covers every draw once.  Pass-2 candidate counts live on the
+    // device, so its grid fills the GPU and strides over the reject list.
+    const uint32_t fill = (sm_count * 8 + nviews - 1) / nviews;
+    uint32_t per_view = pass == 1 ? want : (want < fill ? want : fill);
+    if (per_view > 65535u) per_view = 65535u;
     if (per_view == 0) per_view = 1;
     dim3 grid(per_view, nviews);
     k_cull<<<grid, threads, 0, stream>>>(S, views, flags, pass, status);

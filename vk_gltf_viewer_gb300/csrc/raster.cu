@@ -50,11 +50,9 @@ struct RasterCtx {
     uint32_t* status;
 };
 
-// Depth-test early-out: the stored value only grows, so a stale read that is
-// already >= v proves the max would not change it.
-__device__ __forceinline__ void plot(unsigned long long* p, unsigned long long v) {
-    if (__ldcg(p) < v) atomicMax(p, v);
-}
+// The depth test: a 64-bit max whose result is not needed (a reduction
+// that does not wait for the L2 round trip).
+__device__ __forceinline__ void plot(unsigned long long* p, unsigned long long v) { atomicMax(p, v); }
 
 __device__ void raster_rect(const int32_t* X, const int32_t* Y, const int32_t* bias, float z0, float pa, float pb,
                             uint32_t id, int px0, int py0, int px1, int py1, unsigned long long* depth,
@@ -94,7 +92,7 @@ __device__ void raster_rect(const int32_t* X, const int32_t* Y, const int32_t* b
 }
 
 // Triangle setup on snapped vertices and dispatch to inline or binned raster.
-__device__ void setup_and_raster(int32_t X0, int32_t Y0, float Z0, int32_t X1, int32_t Y1, float Z1, int32_t X2,
+__device__ __noinline__ void setup_and_raster(int32_t X0, int32_t Y0, float Z0, int32_t X1, int32_t Y1, float Z1, int32_t X2,
                                  int32_t Y2, float Z2, uint32_t id, const RasterCtx& c) {
     int64_t A = (int64_t)(X1 - X0) * (Y2 - Y0) - (int64_t)(Y1 - Y0) * (X2 - X0);
     if (A == 0) return;
@@ -234,21 +232,6 @@ __device__ __noinline__ void raster_clipped(float4 v0, float4 v1, float4 v2, boo
         setup_and_raster(X[0], Y[0], Z[0], X[k], Y[k], Z[k], X[k + 1], Y[k + 1], Z[k + 1], id, c);
 }
 
-__device__ __forceinline__ void raster_triangle(const float4& a, const float4& b, const float4& cc, uint32_t id,
-                                                const RasterCtx& c) {
-    const int oc0 = outcode(a), oc1 = outcode(b), oc2 = outcode(cc);
-    if (oc0 & oc1 & oc2) return;
-    const bool clipz = ((oc0 | oc1 | oc2) & (OC_ZLO | OC_ZHI)) != 0;
-    if (clipz || outside_guard(a) || outside_guard(b) || outside_guard(cc)) {
-        raster_clipped(a, b, cc, clipz, id, c);
-        return;
-    }
-    int32_t X0, Y0, X1, Y1, X2, Y2;
-    float Z0, Z1, Z2;
-    if (!snap(a, c, X0, Y0, Z0) || !snap(b, c, X1, Y1, Z1) || !snap(cc, c, X2, Y2, Z2)) return;
-    setup_and_raster(X0, Y0, Z0, X1, Y1, Z1, X2, Y2, Z2, id, c);
-}
-
 struct RasterParams {
     SceneArgs S;
     const DeviceView* views;
@@ -261,12 +244,41 @@ struct RasterParams {
     uint32_t* status;
 };
 
+// Setup record of one small triangle, shared by the warp while it
+// rasterises all small triangles of a round cooperatively.
+struct TriRec {
+    int32_t x[3], y[3];   // oriented (positive area) snapped vertices, 28.8
+    float z0, pa, pb;     // depth plane
+    float inv_bw;         // 1 / bbox width (exact floor division for bw <= 64)
+    uint32_t id;
+    uint16_t bx0, by0;    // clamped bbox origin (pixels)
+    uint8_t bw, bh;       // clamped bbox extent (pixels, <= 64)
+    uint8_t bias;         // bit k: edge k excludes its samples (not top-left)
+    uint8_t _pad;
+};
+
+constexpr uint8_t kFlagGuard = 1u << 6;
+constexpr uint8_t kFlagSnapped = 1u << 7;
+// Triangles whose unclamped bbox is below this many 28.8 units on both axes
+// keep every edge-function value of their bbox inside int32.
+constexpr int32_t kSmallExtent = 1 << 14;
+
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_raster(RasterParams P) {
+__global__ void __launch_bounds__(WARPS * 32, 8 * 4 / WARPS) k_raster(RasterParams P) {
     __shared__ float4 s_clip[WARPS][64];
+    __shared__ int2 s_xy[WARPS][64];
+    __shared__ float s_z[WARPS][64];
+    __shared__ uint8_t s_fl[WARPS][64];
+    __shared__ TriRec s_tri[WARPS][32];
+    __shared__ uint32_t s_end[WARPS][32];
+    __shared__ float s_mvp[WARPS][16];
+    __shared__ float s_tdet[WARPS];
+    __shared__ float s_vp[16];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t vi = blockIdx.y;
     const DeviceView& V = P.views[vi];
+    if (threadIdx.x < 16) s_vp[threadIdx.x] = V.cam->view_projection[threadIdx.x];
+    __syncthreads();
     const uint32_t* list;
     uint32_t count, first = 0;
     if (P.lists.pass == 1) {
@@ -294,9 +306,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(RasterParams P) {
     c.small_area = P.small_area;
     c.chunk = P.chunk;
     c.status = P.status;
-    float VP[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) VP[k] = V.cam->view_projection[k];
+    float4* clip = s_clip[warp];
+    int2* sxy = s_xy[warp];
+    float* sz = s_z[warp];
+    uint8_t* sfl = s_fl[warp];
+    TriRec* recs = s_tri[warp];
+    uint32_t* ends = s_end[warp];
     const uint32_t stride = gridDim.x * WARPS;
     for (uint32_t s = first + blockIdx.x * WARPS + warp; s < count; s += stride) {
         const uint32_t d = list[s];
@@ -306,8 +321,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(RasterParams P) {
         }
         const vkgv_meshlet_draw dr = P.S.draws[d];
         const vkgv_primitive* prim = &P.S.prims[dr.primitive_index];
-        const uint32_t mcount = prim->meshlet_count;
-        if (dr.meshlet_index >= mcount) {
+        if (dr.meshlet_index >= prim->meshlet_count) {
             if (lane == 0) report(P.status, kStatusBadIndex, d);
             continue;
         }
@@ -321,43 +335,166 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(RasterParams P) {
         const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset;
         const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
         const bool double_sided = P.S.mats[prim->material_index].double_sided != 0;
-        const float4* M4 = reinterpret_cast<const float4*>(P.S.transforms + 16 * (size_t)dr.transform_index);
-        float M[16];
+        // mvp = VP * M, one element per lane (lanes 0-15); lane 16 takes the
+        // sign source determinant(M) of visbuffer.mesh.glsl:71.
+        const float* Mg = P.S.transforms + 16 * (size_t)dr.transform_index;
+        if (lane < 16) {
+            const int cc = lane >> 2, j = lane & 3;
+            const float4 mc = __ldg(reinterpret_cast<const float4*>(Mg) + cc);
+            s_mvp[warp][lane] = fadd(fadd(fadd(fmul(s_vp[0 * 4 + j], mc.x), fmul(s_vp[1 * 4 + j], mc.y)),
+                                          fmul(s_vp[2 * 4 + j], mc.z)),
+                                     fmul(s_vp[3 * 4 + j], mc.w));
+        } else if (lane == 16) {
+            float M[16];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float4 t = __ldg(M4 + q);
-            M[q * 4 + 0] = t.x;
-            M[q * 4 + 1] = t.y;
-            M[q * 4 + 2] = t.z;
-            M[q * 4 + 3] = t.w;
+            for (int q = 0; q < 16; ++q) M[q] = __ldg(Mg + q);
+            s_tdet[warp] = det4(M);
         }
-        float mvp[16];
-        m4m(VP, M, mvp);
-        const float tdet = det4(M);
+        __syncwarp();
+        const float tdet = s_tdet[warp];
+        const float* mvp = s_mvp[warp];
+        // Vertex stage: clip position, outcode, guard flag and the 28.8 snap,
+        // each computed once per meshlet vertex.
         for (uint32_t k = lane; k < vc; k += 32) {
             const vkgv_vertex* vx = verts + __ldg(vidx + k);
             const float2 xy = __ldg(reinterpret_cast<const float2*>(vx->position));
-            const float z = __ldg(&vx->position[2]);
+            const float zz = __ldg(&vx->position[2]);
             float r[4];
-            m4v(mvp, xy.x, xy.y, z, 1.0f, r);
-            s_clip[warp][k] = make_float4(r[0], r[1], r[2], r[3]);
+            m4v(mvp, xy.x, xy.y, zz, 1.0f, r);
+            const float4 cv = make_float4(r[0], r[1], r[2], r[3]);
+            clip[k] = cv;
+            int32_t X = 0, Y = 0;
+            float Z = 0.0f;
+            uint8_t fl = (uint8_t)outcode(cv);
+            if (outside_guard(cv)) fl |= kFlagGuard;
+            if (snap(cv, c, X, Y, Z)) fl |= kFlagSnapped;
+            sxy[k] = make_int2(X, Y);
+            sz[k] = Z;
+            sfl[k] = fl;
         }
         __syncwarp();
-        for (uint32_t t = lane; t < tc; t += 32) {
-            const uint32_t i0 = __ldg(tri + 3 * t), i1 = __ldg(tri + 3 * t + 1), i2 = __ldg(tri + 3 * t + 2);
-            if (i0 >= vc || i1 >= vc || i2 >= vc) {
-                report(P.status, kStatusBadIndex, d);
-                continue;
+        for (uint32_t tbase = 0; tbase < tc; tbase += 32) {
+            const uint32_t t = tbase + lane;
+            uint32_t area = 0;
+            if (t < tc) {
+                const uint32_t i0 = __ldg(tri + 3 * t), i1 = __ldg(tri + 3 * t + 1), i2 = __ldg(tri + 3 * t + 2);
+                bool live = true;
+                if (i0 >= vc || i1 >= vc || i2 >= vc) {
+                    report(P.status, kStatusBadIndex, d);
+                    live = false;
+                }
+                if (live && !double_sided) {
+                    const float4 a = clip[i0], b = clip[i1], cc = clip[i2];
+                    const float det = det3(a.x, a.y, a.w, b.x, b.y, b.w, cc.x, cc.y, cc.w);
+                    live = !(tdet < 0.0f ? det < 0.0f : det > 0.0f);
+                }
+                const uint32_t id = (d << 7) | t;
+                uint8_t f0 = 0, f1 = 0, f2 = 0;
+                if (live) {
+                    f0 = sfl[i0], f1 = sfl[i1], f2 = sfl[i2];
+                    if (f0 & f1 & f2 & 63) live = false;  // outcode reject
+                }
+                if (live && ((f0 | f1 | f2) & (OC_ZLO | OC_ZHI | kFlagGuard))) {
+                    raster_clipped(clip[i0], clip[i1], clip[i2], ((f0 | f1 | f2) & (OC_ZLO | OC_ZHI)) != 0, id, c);
+                    live = false;
+                }
+                if (live && !(f0 & f1 & f2 & kFlagSnapped)) live = false;
+                if (live) {
+                    int2 p0 = sxy[i0], p1 = sxy[i1], p2 = sxy[i2];
+                    float z0 = sz[i0], z1 = sz[i1], z2 = sz[i2];
+                    const int64_t A = (int64_t)(p1.x - p0.x) * (p2.y - p0.y) - (int64_t)(p1.y - p0.y) * (p2.x - p0.x);
+                    const int32_t minx = min(p0.x, min(p1.x, p2.x)), maxx = max(p0.x, max(p1.x, p2.x));
+                    const int32_t miny = min(p0.y, min(p1.y, p2.y)), maxy = max(p0.y, max(p1.y, p2.y));
+                    if (A != 0 && maxx - minx < kSmallExtent && maxy - miny < kSmallExtent) {
+                        int32_t px0 = (minx - 128 + 255) >> 8, px1 = (maxx - 128) >> 8;
+                        int32_t py0 = (miny - 128 + 255) >> 8, py1 = (maxy - 128) >> 8;
+                        px0 = max(px0, 0);
+                        py0 = max(py0, 0);
+                        px1 = min(px1, (int32_t)c.w - 1);
+                        py1 = min(py1, (int32_t)c.h - 1);
+                        if (px0 <= px1 && py0 <= py1) {
+                            const uint32_t bw = (uint32_t)(px1 - px0 + 1), bh = (uint32_t)(py1 - py0 + 1);
+                            if (bw * bh <= c.small_area) {
+                                if (A < 0) {
+                                    const int2 tp = p1;
+                                    p1 = p2;
+                                    p2 = tp;
+                                    const float tz = z1;
+                                    z1 = z2;
+                                    z2 = tz;
+                                }
+                                const int64_t Ap = A < 0 ? -A : A;
+                                TriRec& r = recs[lane];
+                                r.x[0] = p0.x, r.x[1] = p1.x, r.x[2] = p2.x;
+                                r.y[0] = p0.y, r.y[1] = p1.y, r.y[2] = p2.y;
+                                uint8_t bias = 0;
+#pragma unroll
+                                for (int k = 0; k < 3; ++k) {
+                                    const int32_t dx = r.x[(k + 1) % 3] - r.x[k], dy = r.y[(k + 1) % 3] - r.y[k];
+                                    if (!(dy < 0 || (dy == 0 && dx > 0))) bias |= (uint8_t)(1u << k);
+                                }
+                                const float dx1 = __int2float_rn(p1.x - p0.x), dy1 = __int2float_rn(p1.y - p0.y);
+                                const float dx2 = __int2float_rn(p2.x - p0.x), dy2 = __int2float_rn(p2.y - p0.y);
+                                const float af = __ll2float_rn(Ap);
+                                const float dz1 = fsub(z1, z0), dz2 = fsub(z2, z0);
+                                r.z0 = z0;
+                                r.pa = fdiv(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), af);
+                                r.pb = fdiv(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), af);
+                                r.inv_bw = 1.0f / (float)bw;
+                                r.id = id;
+                                r.bx0 = (uint16_t)px0;
+                                r.by0 = (uint16_t)py0;
+                                r.bw = (uint8_t)bw;
+                                r.bh = (uint8_t)bh;
+                                r.bias = bias;
+                                area = bw * bh;
+                            } else {
+                                setup_and_raster(p0.x, p0.y, z0, p1.x, p1.y, z1, p2.x, p2.y, z2, id, c);
+                            }
+                        }
+                    } else if (A != 0) {
+                        setup_and_raster(p0.x, p0.y, z0, p1.x, p1.y, z1, p2.x, p2.y, z2, id, c);
+                    }
+                }
             }
-            const float4 a = s_clip[warp][i0], b = s_clip[warp][i1], cc = s_clip[warp][i2];
-            if (!double_sided) {
-                const float det = det3(a.x, a.y, a.w, b.x, b.y, b.w, cc.x, cc.y, cc.w);
-                const bool cull = tdet < 0.0f ? det < 0.0f : det > 0.0f;
-                if (cull) continue;
+            // Warp-cooperative raster of this round's small triangles: an
+            // inclusive scan of their bbox areas spreads the pixels evenly.
+            uint32_t incl = area;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
             }
-            raster_triangle(a, b, cc, (d << 7) | t, c);
+            ends[lane] = incl;
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
+            for (uint32_t p = lane; p < total; p += 32) {
+                // smallest j with ends[j] > p
+                uint32_t j = 0;
+#pragma unroll
+                for (uint32_t step = 16; step > 0; step >>= 1)
+                    if (ends[j + step - 1] <= p) j += step;
+                const TriRec& r = recs[j];
+                const uint32_t local = p - (ends[j] - (uint32_t)r.bw * r.bh);
+                const uint32_t ly = (uint32_t)(((float)local + 0.5f) * r.inv_bw);
+                const uint32_t lx = local - ly * r.bw;
+                const int32_t sx = (int32_t)(r.bx0 + lx) * 256 + 128;
+                const int32_t sy = (int32_t)(r.by0 + ly) * 256 + 128;
+                const int32_t e0 = (r.x[1] - r.x[0]) * (sy - r.y[0]) - (r.y[1] - r.y[0]) * (sx - r.x[0]);
+                const int32_t e1 = (r.x[2] - r.x[1]) * (sy - r.y[1]) - (r.y[2] - r.y[1]) * (sx - r.x[1]);
+                const int32_t e2 = (r.x[0] - r.x[2]) * (sy - r.y[2]) - (r.y[0] - r.y[2]) * (sx - r.x[2]);
+                if (e0 >= (int32_t)(r.bias & 1u) && e1 >= (int32_t)((r.bias >> 1) & 1u) &&
+                    e2 >= (int32_t)((r.bias >> 2) & 1u)) {
+                    float z = __fmaf_rn(r.pa, __int2float_rn(sx - r.x[0]),
+                                        __fmaf_rn(r.pb, __int2float_rn(sy - r.y[0]), r.z0));
+                    if (!(z > 0.0f)) z = 0.0f;
+                    if (z > 1.0f) z = 1.0f;
+                    atomicMax(c.depth + (size_t)(r.by0 + ly) * c.w + (r.bx0 + lx),
+                              ((unsigned long long)__float_as_uint(z) << 32) | ((unsigned long long)r.id + 1ull));
+                }
+            }
+            __syncwarp();
         }
-        __syncwarp();
     }
 }
 

@@ -110,13 +110,18 @@ class ViewBuffers:
         dev = torch.device(device)
         levels, floats = pyramid_layout(width, height)
         cam_t = torch.from_numpy(np.frombuffer(C.string_at(C.addressof(cam), C.sizeof(cam)), np.uint8).copy()).to(dev)
+        pyr = torch.zeros(max(1, floats), dtype=torch.float32, device=dev) if pyramid and levels else None
+        if prev_pyramid == "alias":
+            # temporal HiZ in place: the frame reads last frame's pyramid
+            # before its own reduce chain overwrites it
+            prev = pyr
+        else:
+            prev = torch.zeros(max(1, floats), dtype=torch.float32, device=dev) if prev_pyramid and levels else None
         return cls(width=width, height=height, camera=cam_t,
                    depth_id=torch.zeros(width * height, dtype=torch.int64, device=dev),
                    visbuffer=torch.zeros(width * height, dtype=torch.int32, device=dev) if ids else None,
                    color=torch.zeros(width * height, dtype=torch.int32, device=dev) if color else None,
-                   pyramid=torch.zeros(max(1, floats), dtype=torch.float32, device=dev) if pyramid and levels else None,
-                   prev_pyramid=(torch.zeros(max(1, floats), dtype=torch.float32, device=dev)
-                                 if prev_pyramid and levels else None),
+                   pyramid=pyr, prev_pyramid=prev,
                    survivors=torch.zeros(max(1, draw_capacity), dtype=torch.int32, device=dev) if survivors else None,
                    survivor_count=torch.zeros(1, dtype=torch.int32, device=dev) if survivors else None,
                    levels=levels)
@@ -154,6 +159,11 @@ class Graph:
 
     def launch(self, stream=None) -> None:
         abi.check(abi.load().vkgv_graph_launch(self.handle, _stream_handle(stream)), self.renderer.ctx)
+
+    def kernel_count(self) -> int:
+        n = C.c_uint32()
+        abi.check(abi.load().vkgv_graph_kernel_count(self.handle, C.byref(n)), self.renderer.ctx)
+        return int(n.value)
 
     def close(self) -> None:
         if self.handle:
