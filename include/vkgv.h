@@ -232,6 +232,19 @@ int vkgv_clear(vkgv_ctx* ctx, const vkgv_view* view, void* stream);
  * occlusionViewProjection. */
 int vkgv_cull(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view,
               uint32_t flags, uint32_t pass, void* stream);
+/* No counterpart in the reference.  vkgv_cull for callers that cannot
+ * allocate device memory (a frame loop under global-mode stream capture, or
+ * a plugin whose host owns every allocation): no context, no cudaMalloc.
+ * Its scratch (view table, counters, status word, pass-1 reject list) is one
+ * file-scope device array of about 1 MiB that every GPU loading the library
+ * keeps until exit.  Scenes above 262,144 meshlet draws return
+ * VKGV_LIMIT_EXCEEDED.  view->survivors and view->survivor_count are
+ * required.  All calls share the array and leave its contents behind (pass 2
+ * re-tests the rejects of the preceding pass-1 call); calls that overlap on
+ * the GPU race.  The first call on a device looks up the array's device
+ * address, so make it before any stream capture. */
+int vkgv_cull_static(const vkgv_scene* scene, const vkgv_view* view, uint32_t flags,
+                     uint32_t pass, void* stream);
 /* Mesh shader + raster + fragment shader
  * (shaders/visbuffer/visbuffer.mesh.glsl:30-104, visbuffer.frag.glsl:28-39):
  * rasterises draw_list[first .. *draw_count) into view->depth_id with a
