@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--batch-views", type=int, default=256)
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--batched-only", action="store_true",
+                   help="run only the batched leg (for profiling); prints its own JSON line")
     return p.parse_args()
 
 
@@ -152,6 +154,56 @@ def run_reference(args, rank, world):
     }), flush=True)
 
 
+def run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier):
+    """Batched leg: the uneven views rendered in one captured graph launch,
+    steady state (each view reads its own previous pyramid)."""
+    import numpy as np
+    import torch
+
+    from vk_gltf_viewer_gb300 import scene
+    from vk_gltf_viewer_gb300.renderer import ViewBuffers
+
+    bv = []
+    for bcam, w, h in scene.batch_views(args.batch_views):
+        vb = ViewBuffers.allocate(w, h, bcam, host.draw_count, device=f"cuda:{local}", prev_pyramid="alias",
+                                  survivors=False)
+        bv.append(vb)
+    for vb in bv:
+        vb.use_prev = False
+    r.frame(dev, bv, flags)
+    for vb in bv:
+        vb.use_prev = True
+    r.frame(dev, bv, flags)
+    r.set_profiling(True)
+    r.frame(dev, bv, flags)
+    stages = r.stage_times()
+    r.set_profiling(False)
+    bgraph = r.capture(dev, bv, flags)
+    for _ in range(2):
+        bgraph.launch()
+    torch.cuda.synchronize()
+    bsteps = max(2, min(args.steps, 5))
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    b0.record(stream)
+    for _ in range(bsteps):
+        bgraph.launch()
+    b1.record(stream)
+    torch.cuda.synchronize()
+    tb = torch.tensor([b0.elapsed_time(b1) / 1000.0], device=f"cuda:{local}")
+    if pg:
+        pg.all_reduce(tb, op=pg.ReduceOp.MAX)
+    bval = world * bsteps * len(bv) / float(tb.item())
+    out = {"value": bval, "unit": "views/s", "views_per_launch": len(bv), "steps": bsteps,
+           "ms_per_launch": 1000.0 * float(tb.item()) / bsteps, "kernels_per_launch": bgraph.kernel_count(),
+           "mean_pixels_per_view": float(np.mean([vb.width * vb.height for vb in bv])),
+           "stages_ms": stages,
+           "config": f"{len(bv)} poses on a radius-30 sphere around the grid centre, sizes uniform over "
+                     "256^2, 512x384, 1024x576, 1280x720, 1920x1080"}
+    bgraph.close()
+    return out
+
+
 # ------------------------------------------------------------------- ours
 
 def main():
@@ -186,6 +238,13 @@ def main():
     dev = DeviceScene(host, f"cuda:{local}")
     flags = (abi.CULL_FRUSTUM | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID | abi.RESOLVE_TEXTURED
              | abi.WRITE_IDS)
+    stream = torch.cuda.current_stream()
+    if args.batched_only:
+        out = run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "batched": out}), flush=True)
+        r.close()
+        return
     cam = scene.grid_camera(W1080, H1080)
     view = ViewBuffers.allocate(W1080, H1080, cam, host.draw_count, device=f"cuda:{local}", prev_pyramid="alias")
     # first frame without history, then steady state
@@ -290,42 +349,8 @@ def main():
     # ---- batched leg: 256 uneven views in one graph launch
     batched = None
     if not args.no_batched and args.batch_views > 0:
-        bv = []
-        for bcam, w, h in scene.batch_views(args.batch_views):
-            vb = ViewBuffers.allocate(w, h, bcam, host.draw_count, device=f"cuda:{local}", prev_pyramid="alias",
-                                      survivors=False)
-            bv.append(vb)
-        for vb in bv:
-            vb.use_prev = False
-        r.frame(dev, bv, flags)
-        for vb in bv:
-            vb.use_prev = True
-        r.frame(dev, bv, flags)
-        bgraph = r.capture(dev, bv, flags)
-        for _ in range(2):
-            bgraph.launch()
-        torch.cuda.synchronize()
-        bsteps = max(2, min(args.steps, 5))
-        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        barrier()
-        b0.record(stream)
-        for _ in range(bsteps):
-            bgraph.launch()
-        b1.record(stream)
-        torch.cuda.synchronize()
-        tb = torch.tensor([b0.elapsed_time(b1) / 1000.0], device=f"cuda:{local}")
-        if pg:
-            pg.all_reduce(tb, op=pg.ReduceOp.MAX)
-        bval = world * bsteps * len(bv) / float(tb.item())
-        batched = {"value": bval, "unit": "views/s", "views_per_launch": len(bv), "steps": bsteps,
-                   "ms_per_launch": 1000.0 * float(tb.item()) / bsteps,
-                   "kernels_per_launch": bgraph.kernel_count(),
-                   "speedup_vs_single_view": bval / value,
-                   "mean_pixels_per_view": float(np.mean([vb.width * vb.height for vb in bv])),
-                   "config": "256 poses on a radius-30 sphere around the grid centre, sizes uniform over "
-                             "256^2, 512x384, 1024x576, 1280x720, 1920x1080"}
-        bgraph.close()
-        del bv
+        batched = run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier)
+        batched["speedup_vs_single_view"] = batched["value"] / value
 
     # ---- CPU baseline: the oracle on the host cores, bounded sample
     cpu = None

@@ -1,0 +1,56 @@
+"""Parity at the benchmark's full size: the 82M-triangle torus grid at
+1920x1080 with two-pass occlusion culling and the textured resolve, in the
+steady state the benchmark times (previous frame's pyramid), plus a batch of
+uneven views as in the batched leg.  Visibility IDs, depth|id, survivor sets
+and HiZ mips must be bit-exact; RGBA within 1/255."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import binding as ob
+from vk_gltf_viewer_gb300 import abi, scene
+
+from gpu_util import Pair, oracle_flags, rgba_close, u32, u64, view
+
+pytestmark = pytest.mark.gpu
+
+FLAGS = (abi.CULL_FRUSTUM | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID | abi.RESOLVE_TEXTURED
+         | abi.WRITE_IDS)
+
+
+@pytest.fixture(scope="module")
+def full(renderer):
+    return Pair(scene.scene_torus_grid())
+
+
+def test_full_size_frame_bit_exact(renderer, full):
+    w, h = 1920, 1080
+    cam = scene.grid_camera(w, h)
+    first = ob.frame(full.orc, cam, w, h, oracle_flags(FLAGS))
+    exp = ob.frame(full.orc, cam, w, h, oracle_flags(FLAGS), prev_pyramid=first["pyramid"])
+    v = view(full, cam, w, h, prev=first["pyramid"])
+    renderer.frame(full.dev, [v], FLAGS)
+    torch.cuda.synchronize()
+    assert full.host.triangle_count == 81_920_000
+    assert np.array_equal(np.sort(v.survivor_list()), np.sort(exp["survivors"]))
+    assert np.array_equal(u64(v.depth_id), exp["depth_id"])
+    assert np.array_equal(u32(v.visbuffer), exp["ids"])
+    assert np.array_equal(v.pyramid.cpu().numpy()[: exp["pyramid"].size], exp["pyramid"])
+    ok, bad = rgba_close(u32(v.color), exp["rgba"])
+    assert ok, f"{bad} pixels off by more than 1/255"
+    assert renderer.device_status() == (0, 0)
+
+
+def test_full_size_batched_views_bit_exact(renderer, full):
+    """Eight of the 256 batched poses (uneven sizes) in one launch."""
+    views, exps = [], []
+    for cam, w, h in scene.batch_views(8, seed=3):
+        first = ob.frame(full.orc, cam, w, h, oracle_flags(FLAGS))
+        exps.append(ob.frame(full.orc, cam, w, h, oracle_flags(FLAGS), prev_pyramid=first["pyramid"]))
+        views.append(view(full, cam, w, h, prev=first["pyramid"]))
+    renderer.frame(full.dev, views, FLAGS)
+    torch.cuda.synchronize()
+    for v, e in zip(views, exps):
+        assert np.array_equal(u32(v.visbuffer), e["ids"])
+        assert np.array_equal(np.sort(v.survivor_list()), np.sort(e["survivors"]))
+        assert np.array_equal(v.pyramid.cpu().numpy()[: e["pyramid"].size], e["pyramid"])

@@ -18,7 +18,7 @@ using namespace vkgv;
 namespace {
 
 constexpr uint32_t kRing = 4;                 // in-flight frames sharing staging slots
-constexpr uint32_t kCountersPerView = 4;      // see DeviceView::counters
+constexpr uint32_t kCountersPerView = 8;      // see DeviceView::counters
 constexpr uint32_t kGlobalCounters = 8;       // [0] pass-1 big queue, [1] pass-2 big queue
 constexpr uint32_t kDefaultBigCapacity = 1u << 21;
 
@@ -47,6 +47,7 @@ struct vkgv_ctx {
 
     Scratch survivors;  // per view: capacity draw_count
     Scratch rejected;   // per view: capacity draw_count
+    Scratch deferred;   // per view: capacity draw_count
     BigTri* big = nullptr;
     uint32_t big_cap = 0;
     cudaStream_t capture_stream = nullptr;
@@ -174,6 +175,7 @@ struct Prepared {
     SceneArgs S;
     uint32_t max_w = 0, max_h = 0;
     uint64_t max_px = 0;
+    uint32_t hiz_tx = 1, hiz_ty = 1;  // single-pass HiZ grid (max over views)
 };
 
 // Builds the DeviceView table for `views` into `host` (count n).
@@ -184,6 +186,8 @@ int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, 
     const uint32_t D = scene->meshlet_draw_count;
     size_t per_view = std::max<size_t>(D, 1) * sizeof(uint32_t);
     rc = ensure_scratch(ctx, ctx->rejected, per_view * n, "rejected lists");
+    if (rc) return rc;
+    rc = ensure_scratch(ctx, ctx->deferred, per_view * n, "deferred meshlet lists");
     if (rc) return rc;
     bool need_surv = false;
     for (uint32_t i = 0; i < n; ++i) need_surv |= views[i].survivors == 0;
@@ -229,9 +233,16 @@ int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, 
             d.survivor_capacity = D;
         }
         d.rejected = reinterpret_cast<uint32_t*>(ctx->rejected.ptr) + (size_t)i * std::max<uint32_t>(D, 1);
+        d.deferred = reinterpret_cast<uint32_t*>(ctx->deferred.ptr) + (size_t)i * std::max<uint32_t>(D, 1);
         d.counters = ctx->counters + kGlobalCounters + kCountersPerView * i;
         P.max_w = std::max(P.max_w, v.width);
         P.max_h = std::max(P.max_h, v.height);
+        if (v.pyramid.levels) {
+            uint32_t tx = 1, ty = 1;
+            hiz_tiles(v.width, v.height, v.pyramid.levels, &tx, &ty);
+            P.hiz_tx = std::max(P.hiz_tx, tx);
+            P.hiz_ty = std::max(P.hiz_ty, ty);
+        }
         P.max_px = std::max<uint64_t>(P.max_px, (uint64_t)v.width * v.height);
     }
     return VKGV_OK;
@@ -274,24 +285,24 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
     zone(1);
     launch_cull(P.S, dv, n, flags, 1, ctx->status, ctx->sm_count, stream);
     zone(2);
-    RasterLists l1{1, nullptr, nullptr, 0};
+    RasterLists l1{1, nullptr, nullptr, 0, 4};
     launch_raster(P.S, dv, n, l1, ctx->raster, ctx->big, gc + 0, ctx->big_cap, ctx->status, ctx->sm_count, stream,
                   zones ? zones[3] : nullptr);
     zone(4);
     const bool two = (flags & VKGV_CULL_TWO_PASS) && (flags & VKGV_CULL_OCCLUSION);
-    if (two) launch_hiz(dv, n, P.max_w, P.max_h, ctx->sm_count, stream);
+    if (two) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, ctx->status, stream);
     zone(5);
     if (two) launch_cull(P.S, dv, n, flags, 2, ctx->status, ctx->sm_count, stream);
     zone(6);
     if (two) {
-        RasterLists l2{2, nullptr, nullptr, 0};
+        RasterLists l2{2, nullptr, nullptr, 0, 5};
         launch_raster(P.S, dv, n, l2, ctx->raster, ctx->big, gc + 1, ctx->big_cap, ctx->status, ctx->sm_count,
                       stream, zones ? zones[7] : nullptr);
     } else {
         zone(7);
     }
     zone(8);
-    if (flags & VKGV_BUILD_PYRAMID) launch_hiz(dv, n, P.max_w, P.max_h, ctx->sm_count, stream);
+    if (flags & VKGV_BUILD_PYRAMID) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, ctx->status, stream);
     zone(9);
     if (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS))
         launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
@@ -390,6 +401,7 @@ int vkgv_destroy(vkgv_ctx* ctx) {
     if (ctx->big) cudaFree(ctx->big);
     if (ctx->survivors.ptr) cudaFree(ctx->survivors.ptr);
     if (ctx->rejected.ptr) cudaFree(ctx->rejected.ptr);
+    if (ctx->deferred.ptr) cudaFree(ctx->deferred.ptr);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     for (uint32_t i = 0; i <= VKGV_STAGE_COUNT; ++i)
         if (ctx->zone[i]) cudaEventDestroy(ctx->zone[i]);
@@ -528,8 +540,10 @@ int vkgv_raster(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, u
     RasterLists l{0, draw_list ? reinterpret_cast<const uint32_t*>(draw_list) : reinterpret_cast<const uint32_t*>(view->survivors),
                   draw_count ? reinterpret_cast<const uint32_t*>(draw_count)
                              : reinterpret_cast<const uint32_t*>(view->survivor_count),
-                  first};
+                  first, 6};
+    // big-queue counter and the view's deferred-list counter start at zero
     VKGV_CUDA(ctx, cudaMemsetAsync(ctx->counters, 0, sizeof(uint32_t), stream));
+    VKGV_CUDA(ctx, cudaMemsetAsync(ctx->counters + kGlobalCounters + 6, 0, sizeof(uint32_t), stream));
     launch_raster(P.S, dv, 1, l, ctx->raster, ctx->big, ctx->counters, ctx->big_cap, ctx->status, ctx->sm_count,
                   stream);
     rc = check_launch(ctx);
@@ -552,7 +566,7 @@ int vkgv_hiz_reduce(vkgv_ctx* ctx, const vkgv_view* view, void* stream_) {
     if (rc) return rc;
     rc = commit_views(ctx, slot, 1, stream);
     if (rc) return rc;
-    launch_hiz(dv, 1, P.max_w, P.max_h, ctx->sm_count, stream);
+    launch_hiz(dv, 1, P.hiz_tx, P.hiz_ty, ctx->status, stream);
     rc = check_launch(ctx);
     if (rc) return rc;
     return close_slot(ctx, slot, stream);

@@ -44,7 +44,10 @@ struct DeviceView {
     uint32_t* survivors;        // pass-1 survivors at [0, c[0]), pass-2 at [c[0], c[0]+c[2])
     uint32_t* survivor_count;   // user-visible total (written by the finalize step)
     uint32_t* rejected;         // pass-1 occlusion rejects (scratch)
-    uint32_t* counters;         // scratch: [0] pass-1 survivors, [1] rejects, [2] pass-2 survivors
+    uint32_t* deferred;         // meshlets with clipped or large triangles (scratch, capacity = draws)
+    // scratch counters: [0] pass-1 survivors, [1] rejects, [2] pass-2 survivors,
+    // [3] HiZ tiles done, [4..6] deferred meshlets of raster pass 1 / 2 / explicit list
+    uint32_t* counters;
     uint32_t survivor_capacity;
     uint32_t _pad;
 };
@@ -138,6 +141,34 @@ __host__ __device__ __forceinline__ uint64_t mip_offset(uint32_t w0, uint32_t h0
     uint64_t off = 0;
     for (uint32_t k = 0; k < level; ++k) off += (uint64_t)mip_dim(w0, k) * mip_dim(h0, k);
     return off;
+}
+
+// HiZ tiling (single-pass reduce): a CTA owns an 8x8 tile of the highest
+// tiled level (at most level 4) and the matching 2^k-times larger tiles of
+// the levels below it.  Levels with a zero dimension are never tiled.
+constexpr int kHizTileLevels = 4;
+constexpr int kHizTopTile = 8;
+
+__host__ __device__ __forceinline__ int hiz_tile_levels(uint32_t w, uint32_t h, uint32_t levels) {
+    int k = (int)(levels < (uint32_t)kHizTileLevels ? levels : (uint32_t)kHizTileLevels);
+    while (k > 0 && ((w >> k) == 0 || (h >> k) == 0)) --k;
+    return k;
+}
+
+__host__ __device__ __forceinline__ int hiz_tile_edge(int level, int top) { return kHizTopTile << (top - level); }
+
+__host__ __device__ __forceinline__ void hiz_tiles(uint32_t w, uint32_t h, uint32_t levels, uint32_t* tx,
+                                                   uint32_t* ty) {
+    const int top = hiz_tile_levels(w, h, levels);
+    uint32_t nx = 1, ny = 1;
+    for (int j = 1; j <= top; ++j) {
+        const uint32_t t = (uint32_t)hiz_tile_edge(j, top);
+        const uint32_t ax = ((w >> j) + t - 1) / t, ay = ((h >> j) + t - 1) / t;
+        nx = ax > nx ? ax : nx;
+        ny = ay > ny ? ay : ny;
+    }
+    *tx = nx;
+    *ty = ny;
 }
 
 // Texels of one axis of the MIN-reduction LINEAR footprint (pinned rule):

@@ -1,5 +1,5 @@
-// HiZ min-pyramid: the reduce chain of application.cpp:951-1003 running
-// shaders/hiz_reduce.comp.glsl once per level.
+// HiZ min-pyramid: the reduce chain of application.cpp:951-1003 that runs
+// shaders/hiz_reduce.comp.glsl once per level, here in one launch per frame.
 //
 // Level i (1..L) writes mip i-1 at size (W>>i, H>>i) from mip i-2 (the depth
 // image for i = 1): texel p = MIN over the bilinear footprint of the source
@@ -10,62 +10,208 @@
 // reference's bounds test `pos > size` (hiz_reduce.comp.glsl:24) also lets
 // pos == size through, whose image store is out of bounds; only pos < size is
 // written here.
+//
+// Single pass: each CTA owns an 8x8 tile of level 4 and the 16x16, 32x32 and
+// 64x64 tiles of levels 3, 2, 1 above it.  For odd sizes the footprints do
+// not nest, so each CTA computes the hull of its owned tile and the
+// footprint of the level above it (a halo of a few texels, recomputed rather
+// than exchanged), keeping levels 1-3 in shared memory and reading the depth
+// image once.  The last CTA of a view to finish computes the remaining top
+// levels from global memory.
 #include "kernels.cuh"
 
 namespace vkgv {
 
 namespace {
 
-__device__ __forceinline__ float src_at(const unsigned long long* depth_id, const float* src, uint32_t sw,
-                                        int x, int y) {
-    if (depth_id) return u2f((uint32_t)(__ldg(depth_id + (size_t)y * sw + x) >> 32));
-    return __ldg(src + (size_t)y * sw + x);
+constexpr int kCap1 = 80, kCap2 = 40, kCap3 = 20, kCap4 = 12;  // per-axis smem capacity per level
+constexpr int kThreads = 1024;
+// Dynamic shared memory: the tile levels, later reused by the tail as two
+// ping-pong buffers (A, B) when the top tiled mip fits.
+constexpr int kOff2 = kCap1 * kCap1, kOff3 = kOff2 + kCap2 * kCap2, kOff4 = kOff3 + kCap3 * kCap3;
+constexpr int kTailA = 16384, kTailB = 8192;
+constexpr int kSmemFloats = kTailA + kTailB;
+static_assert(kOff4 + kCap4 * kCap4 <= kSmemFloats, "tile levels fit the shared buffer");
+
+struct Range {
+    int lo, hi;  // inclusive; empty when lo > hi
+};
+
+__device__ __forceinline__ Range hull(Range a, Range b) {
+    if (a.lo > a.hi) return b;
+    if (b.lo > b.hi) return a;
+    return Range{min(a.lo, b.lo), max(a.hi, b.hi)};
 }
 
-__global__ void __launch_bounds__(256) k_hiz_level(const DeviceView* __restrict__ views, uint32_t level) {
-    const DeviceView& V = views[blockIdx.z];
-    if (!V.pyr || level > V.pyr_levels) return;
-    const uint32_t px = blockIdx.x * 32 + (threadIdx.x & 31);
-    const uint32_t py = blockIdx.y * 8 + (threadIdx.x >> 5);
-    const uint32_t w0 = V.w >> 1, h0 = V.h >> 1;
-    const uint32_t dw = V.w >> level, dh = V.h >> level;
-    const uint32_t mw = mip_dim(w0, level - 1), mh = mip_dim(h0, level - 1);
-    float* dst = V.pyr + mip_offset(w0, h0, level - 1);
-    if (dw == 0 || dh == 0) {
-        if (px < mw && py < mh) dst[(size_t)py * mw + px] = 0.0f;
-        return;
-    }
-    if (px >= dw || py >= dh) return;
-    const unsigned long long* depth_id = level == 1 ? V.depth_id : nullptr;
-    const float* src = level == 1 ? nullptr : V.pyr + mip_offset(w0, h0, level - 2);
-    const uint32_t sw = level == 1 ? V.w : mip_dim(w0, level - 2);
-    const uint32_t sh = level == 1 ? V.h : mip_dim(h0, level - 2);
-    const float u = fdiv(fadd((float)px, 0.5f), (float)dw);
-    const float v = fdiv(fadd((float)py, 0.5f), (float)dh);
+// Texels of level j (size s_lo) read by texels [r.lo, r.hi] of level j+1
+// (size s_hi); the footprint is monotone in the texel index.
+__device__ __forceinline__ Range footprint_range(Range r, uint32_t s_hi, uint32_t s_lo) {
+    if (r.lo > r.hi) return r;
+    int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+    footprint_axis(fdiv(fadd((float)r.lo, 0.5f), (float)s_hi), s_lo, a0, a1);
+    const int nb = footprint_axis(fdiv(fadd((float)r.hi, 0.5f), (float)s_hi), s_lo, b0, b1);
+    return Range{a0, nb == 2 ? b1 : b0};
+}
+
+__device__ __forceinline__ Range owned(uint32_t tile, uint32_t t, uint32_t size) {
+    const int lo = (int)(tile * t);
+    const int hi = (int)min((tile + 1) * t, size) - 1;
+    return Range{lo, hi};
+}
+
+__device__ __forceinline__ float depth_at(const unsigned long long* d, uint32_t w, int x, int y) {
+    return u2f((uint32_t)(__ldg(d + (size_t)y * w + x) >> 32));
+}
+
+// One texel of level j from a source sampled through `fetch(x, y)`.
+template <class F>
+__device__ __forceinline__ float reduce_texel(int x, int y, uint32_t dw, uint32_t dh, uint32_t sw, uint32_t sh,
+                                              F fetch) {
+    const float u = fdiv(fadd((float)x, 0.5f), (float)dw);
+    const float v = fdiv(fadd((float)y, 0.5f), (float)dh);
     int x0 = 0, x1 = 0, y0 = 0, y1 = 0;
     const int nx = footprint_axis(u, sw, x0, x1);
     const int ny = footprint_axis(v, sh, y0, y1);
-    float r = src_at(depth_id, src, sw, x0, y0);
-    if (nx == 2) r = gmin(r, src_at(depth_id, src, sw, x1, y0));
+    float r = fetch(x0, y0);
+    if (nx == 2) r = gmin(r, fetch(x1, y0));
     if (ny == 2) {
-        r = gmin(r, src_at(depth_id, src, sw, x0, y1));
-        if (nx == 2) r = gmin(r, src_at(depth_id, src, sw, x1, y1));
+        r = gmin(r, fetch(x0, y1));
+        if (nx == 2) r = gmin(r, fetch(x1, y1));
     }
-    dst[(size_t)py * dw + px] = r;
+    return r;
+}
+
+__global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__ views, uint32_t* status) {
+    const DeviceView& V = views[blockIdx.z];
+    if (!V.pyr || V.pyr_levels == 0) return;
+    const uint32_t w = V.w, h = V.h, L = V.pyr_levels;
+    const uint32_t w0 = w >> 1, h0 = h >> 1;
+    const int Kp = hiz_tile_levels(w, h, L);
+    uint32_t ntx = 1, nty = 1;
+    hiz_tiles(w, h, L, &ntx, &nty);
+    const uint32_t bx = blockIdx.x, by = blockIdx.y;
+    if (bx >= ntx || by >= nty) return;
+
+    extern __shared__ float smem[];
+    __shared__ Range rx[5], ry[5];
+    __shared__ int s_bad, s_last;
+    float* lvl[5] = {nullptr, smem, smem + kOff2, smem + kOff3, smem + kOff4};
+    const int cap[5] = {0, kCap1, kCap2, kCap3, kCap4};
+
+    if (threadIdx.x == 0) {
+        // Ranges each level must compute: owned tile, plus the footprint of
+        // the level above (top-down).
+        s_bad = 0;
+        for (int j = Kp; j >= 1; --j) {
+            const uint32_t t = (uint32_t)hiz_tile_edge(j, Kp);
+            Range ox = owned(bx, t, w >> j), oy = owned(by, t, h >> j);
+            if (j < Kp) {
+                ox = hull(ox, footprint_range(rx[j + 1], w >> (j + 1), w >> j));
+                oy = hull(oy, footprint_range(ry[j + 1], h >> (j + 1), h >> j));
+            }
+            rx[j] = ox;
+            ry[j] = oy;
+            if (ox.hi - ox.lo + 1 > cap[j] || oy.hi - oy.lo + 1 > cap[j]) s_bad = 1;
+        }
+    }
+    __syncthreads();
+    if (s_bad) {
+        if (threadIdx.x == 0) report(status, kStatusBadIndex, 0x48495a00u | (uint32_t)Kp);
+    } else {
+        for (int j = 1; j <= Kp; ++j) {
+            const Range X = rx[j], Y = ry[j];
+            const int rw = X.hi - X.lo + 1, rh = Y.hi - Y.lo + 1;
+            if (rw <= 0 || rh <= 0) {
+                __syncthreads();
+                continue;
+            }
+            const uint32_t dw = w >> j, dh = h >> j;
+            const uint32_t t = (uint32_t)hiz_tile_edge(j, Kp);
+            const Range OX = owned(bx, t, dw), OY = owned(by, t, dh);
+            float* dst = V.pyr + mip_offset(w0, h0, (uint32_t)(j - 1));
+            float* here = lvl[j];
+            const float* below = lvl[j - 1];
+            const Range BX = j > 1 ? rx[j - 1] : Range{0, 0};
+            const Range BY = j > 1 ? ry[j - 1] : Range{0, 0};
+            const int bw = BX.hi - BX.lo + 1;
+#pragma unroll 4
+            for (int i = threadIdx.x; i < rw * rh; i += blockDim.x) {
+                const int x = X.lo + i % rw, y = Y.lo + i / rw;
+                float r;
+                if (j == 1) {
+                    r = reduce_texel(x, y, dw, dh, w, h, [&](int sx, int sy) { return depth_at(V.depth_id, w, sx, sy); });
+                } else {
+                    r = reduce_texel(x, y, dw, dh, w >> (j - 1), h >> (j - 1),
+                                     [&](int sx, int sy) { return below[(sy - BY.lo) * bw + (sx - BX.lo)]; });
+                }
+                here[i] = r;
+                if (x >= OX.lo && x <= OX.hi && y >= OY.lo && y <= OY.hi) dst[(size_t)y * dw + x] = r;
+            }
+            __syncthreads();
+        }
+    }
+    // The last CTA of this view finishes levels Kp+1..L.  When the top tiled
+    // mip fits in shared memory the tail works there (ping-pong A/B) and
+    // only writes each level out; otherwise it reads back from global.
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&V.counters[3], 1u) == ntx * nty - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const uint32_t top_w = Kp > 0 ? (w >> Kp) : 0, top_h = Kp > 0 ? (h >> Kp) : 0;
+    const bool in_smem = Kp > 0 && top_w * top_h <= (uint32_t)kTailA;
+    float* cur = smem;
+    float* nxt = smem + kTailA;
+    if (in_smem) {
+        const float* src = V.pyr + mip_offset(w0, h0, (uint32_t)(Kp - 1));
+        for (uint32_t i = threadIdx.x; i < top_w * top_h; i += blockDim.x) cur[i] = __ldcg(src + i);
+        __syncthreads();
+    }
+    for (uint32_t j = (uint32_t)Kp + 1; j <= L; ++j) {
+        const uint32_t dw = w >> j, dh = h >> j;
+        const uint32_t mw = mip_dim(w0, j - 1), mh = mip_dim(h0, j - 1);
+        float* dst = V.pyr + mip_offset(w0, h0, j - 1);
+        if (dw == 0 || dh == 0) {
+            for (uint32_t i = threadIdx.x; i < mw * mh; i += blockDim.x) dst[i] = 0.0f;
+        } else {
+            const uint32_t sw = j == 1 ? w : mip_dim(w0, j - 2), sh = j == 1 ? h : mip_dim(h0, j - 2);
+            const float* src = j == 1 ? nullptr : V.pyr + mip_offset(w0, h0, j - 2);
+            for (uint32_t i = threadIdx.x; i < dw * dh; i += blockDim.x) {
+                const int x = (int)(i % dw), y = (int)(i / dw);
+                float r;
+                if (in_smem)
+                    r = reduce_texel(x, y, dw, dh, sw, sh, [&](int sx, int sy) { return cur[sy * (int)sw + sx]; });
+                else if (j == 1)
+                    r = reduce_texel(x, y, dw, dh, sw, sh, [&](int sx, int sy) { return depth_at(V.depth_id, w, sx, sy); });
+                else
+                    r = reduce_texel(x, y, dw, dh, sw, sh,
+                                     [&](int sx, int sy) { return __ldcg(src + (size_t)sy * sw + sx); });
+                if (in_smem) nxt[i] = r;
+                dst[i] = r;
+            }
+        }
+        __syncthreads();
+        if (in_smem) {
+            float* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+    }
+    if (threadIdx.x == 0) V.counters[3] = 0;  // ready for the next reduce of this view
 }
 
 }  // namespace
 
-void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h, uint32_t sm_count,
+void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t* status,
                 cudaStream_t stream) {
-    (void)sm_count;
-    uint32_t mx = max_w > max_h ? max_w : max_h, L = 0;
-    while ((2u << L) <= mx) ++L;
-    for (uint32_t i = 1; i <= L; ++i) {
-        uint32_t w = mip_dim(max_w >> 1, i - 1), h = mip_dim(max_h >> 1, i - 1);
-        dim3 grid((w + 31) / 32, (h + 7) / 8, nviews);
-        k_hiz_level<<<grid, 256, 0, stream>>>(views, i);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_hiz, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemFloats * (int)sizeof(float));
+        attr_set = true;
     }
+    dim3 grid(tiles_x ? tiles_x : 1, tiles_y ? tiles_y : 1, nviews);
+    k_hiz<<<grid, kThreads, kSmemFloats * sizeof(float), stream>>>(views, status);
 }
 
 }  // namespace vkgv

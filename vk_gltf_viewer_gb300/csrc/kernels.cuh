@@ -10,6 +10,7 @@ struct RasterLists {
     const uint32_t* list;     // explicit list (pass 0)
     const uint32_t* count;    // explicit count (pass 0), device
     uint32_t first;           // explicit start (pass 0)
+    uint32_t deferred_slot;   // DeviceView::counters index of this raster's deferred list (4, 5, 6)
 };
 
 struct RasterConfig {
@@ -26,7 +27,7 @@ void launch_cull(const SceneArgs& S, const DeviceView* views, uint32_t nviews, u
 void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews, const RasterLists& lists,
                    const RasterConfig& cfg, BigTri* big, uint32_t* big_count, uint32_t big_capacity,
                    uint32_t* status, uint32_t sm_count, cudaStream_t stream, cudaEvent_t between = nullptr);
-void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h, uint32_t sm_count,
+void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t* status,
                 cudaStream_t stream);
 void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h,
                     uint32_t flags, cudaStream_t stream);

@@ -263,12 +263,25 @@ constexpr uint8_t kFlagSnapped = 1u << 7;
 // keep every edge-function value of their bbox inside int32.
 constexpr int32_t kSmallExtent = 1 << 14;
 
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 8 * 4 / WARPS) k_raster(RasterParams P) {
+enum TriKind : int { kDrop = 0, kFast = 1, kSlowClip = 2, kSlowSetup = 3 };
+
+#ifndef VKGV_RASTER_WARPS_PER_SM
+#define VKGV_RASTER_WARPS_PER_SM 32
+#endif
+
+// Warp-per-meshlet raster.  The fast instance (SLOW = false) handles every
+// triangle that needs no clipping and fits the cooperative small-triangle
+// path, and appends a meshlet that has any other triangle to the view's
+// deferred list.  The slow instance (SLOW = true) re-runs those meshlets and
+// handles only the remaining triangles (homogeneous clipping, large or
+// off-screen-spanning triangles), so the fast instance calls no function.
+template <int WARPS, bool SLOW>
+__global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER_SM) / WARPS) k_raster(RasterParams P) {
     __shared__ float4 s_clip[WARPS][64];
-    __shared__ int2 s_xy[WARPS][64];
-    __shared__ float s_z[WARPS][64];
-    __shared__ uint8_t s_fl[WARPS][64];
+    // per vertex: {X, Y (28.8), Z bits, flags} read with one 16-byte load
+    __shared__ int4 s_vtx[WARPS][64];
+    // the meshlet's triangle-index bytes (<= 126 triangles)
+    __shared__ uint32_t s_idx[WARPS][96];
     __shared__ TriRec s_tri[WARPS][32];
     __shared__ uint32_t s_end[WARPS][32];
     __shared__ float s_mvp[WARPS][16];
@@ -279,9 +292,14 @@ __global__ void __launch_bounds__(WARPS * 32, 8 * 4 / WARPS) k_raster(RasterPara
     const DeviceView& V = P.views[vi];
     if (threadIdx.x < 16) s_vp[threadIdx.x] = V.cam->view_projection[threadIdx.x];
     __syncthreads();
+    const uint32_t slot = P.lists.deferred_slot;
+    const uint32_t defer_cap = P.S.draw_count;
     const uint32_t* list;
     uint32_t count, first = 0;
-    if (P.lists.pass == 1) {
+    if (SLOW) {
+        list = V.deferred;
+        count = min(V.counters[slot], defer_cap);
+    } else if (P.lists.pass == 1) {
         list = V.survivors;
         count = min(V.counters[0], V.survivor_capacity);
     } else if (P.lists.pass == 2) {
@@ -307,9 +325,9 @@ __global__ void __launch_bounds__(WARPS * 32, 8 * 4 / WARPS) k_raster(RasterPara
     c.chunk = P.chunk;
     c.status = P.status;
     float4* clip = s_clip[warp];
-    int2* sxy = s_xy[warp];
-    float* sz = s_z[warp];
-    uint8_t* sfl = s_fl[warp];
+    int4* svtx = s_vtx[warp];
+    uint32_t* sidx = s_idx[warp];
+    const uint8_t* sidx8 = reinterpret_cast<const uint8_t*>(sidx);
     TriRec* recs = s_tri[warp];
     uint32_t* ends = s_end[warp];
     const uint32_t stride = gridDim.x * WARPS;
@@ -327,7 +345,7 @@ __global__ void __launch_bounds__(WARPS * 32, 8 * 4 / WARPS) k_raster(RasterPara
         }
         const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
         const uint32_t vc = ml->vertex_count, tc = ml->triangle_count;
-        if (vc > 64) {
+        if (vc > VKGV_MAX_VERTICES || tc > VKGV_MAX_PRIMITIVES) {
             if (lane == 0) report(P.status, kStatusBadIndex, d);
             continue;
         }
@@ -365,98 +383,121 @@ __global__ void __launch_bounds__(WARPS * 32, 8 * 4 / WARPS) k_raster(RasterPara
             clip[k] = cv;
             int32_t X = 0, Y = 0;
             float Z = 0.0f;
-            uint8_t fl = (uint8_t)outcode(cv);
+            uint32_t fl = (uint32_t)outcode(cv);
             if (outside_guard(cv)) fl |= kFlagGuard;
             if (snap(cv, c, X, Y, Z)) fl |= kFlagSnapped;
-            sxy[k] = make_int2(X, Y);
-            sz[k] = Z;
-            sfl[k] = fl;
+            svtx[k] = make_int4(X, Y, __float_as_int(Z), (int)fl);
+        }
+        // Triangle-index bytes into shared memory, 32-bit loads when the
+        // block is 4-byte aligned (meshoptimizer pads each block to 4).
+        {
+            const uint32_t nbytes = 3 * tc;
+            if ((reinterpret_cast<uintptr_t>(tri) & 3u) == 0) {
+                const uint32_t* tw = reinterpret_cast<const uint32_t*>(tri);
+                for (uint32_t k = lane; k < (nbytes + 3) / 4; k += 32) sidx[k] = __ldg(tw + k);
+            } else {
+                uint8_t* b = reinterpret_cast<uint8_t*>(sidx);
+                for (uint32_t k = lane; k < nbytes; k += 32) b[k] = __ldg(tri + k);
+            }
         }
         __syncwarp();
+        bool any_slow = false;
         for (uint32_t tbase = 0; tbase < tc; tbase += 32) {
             const uint32_t t = tbase + lane;
             uint32_t area = 0;
             if (t < tc) {
-                const uint32_t i0 = __ldg(tri + 3 * t), i1 = __ldg(tri + 3 * t + 1), i2 = __ldg(tri + 3 * t + 2);
-                bool live = true;
-                if (i0 >= vc || i1 >= vc || i2 >= vc) {
-                    report(P.status, kStatusBadIndex, d);
-                    live = false;
-                }
-                if (live && !double_sided) {
-                    const float4 a = clip[i0], b = clip[i1], cc = clip[i2];
-                    const float det = det3(a.x, a.y, a.w, b.x, b.y, b.w, cc.x, cc.y, cc.w);
-                    live = !(tdet < 0.0f ? det < 0.0f : det > 0.0f);
-                }
+                const uint32_t i0 = sidx8[3 * t], i1 = sidx8[3 * t + 1], i2 = sidx8[3 * t + 2];
                 const uint32_t id = (d << 7) | t;
-                uint8_t f0 = 0, f1 = 0, f2 = 0;
-                if (live) {
-                    f0 = sfl[i0], f1 = sfl[i1], f2 = sfl[i2];
-                    if (f0 & f1 & f2 & 63) live = false;  // outcode reject
-                }
-                if (live && ((f0 | f1 | f2) & (OC_ZLO | OC_ZHI | kFlagGuard))) {
-                    raster_clipped(clip[i0], clip[i1], clip[i2], ((f0 | f1 | f2) & (OC_ZLO | OC_ZHI)) != 0, id, c);
-                    live = false;
-                }
-                if (live && !(f0 & f1 & f2 & kFlagSnapped)) live = false;
-                if (live) {
-                    int2 p0 = sxy[i0], p1 = sxy[i1], p2 = sxy[i2];
-                    float z0 = sz[i0], z1 = sz[i1], z2 = sz[i2];
-                    const int64_t A = (int64_t)(p1.x - p0.x) * (p2.y - p0.y) - (int64_t)(p1.y - p0.y) * (p2.x - p0.x);
-                    const int32_t minx = min(p0.x, min(p1.x, p2.x)), maxx = max(p0.x, max(p1.x, p2.x));
-                    const int32_t miny = min(p0.y, min(p1.y, p2.y)), maxy = max(p0.y, max(p1.y, p2.y));
-                    if (A != 0 && maxx - minx < kSmallExtent && maxy - miny < kSmallExtent) {
-                        int32_t px0 = (minx - 128 + 255) >> 8, px1 = (maxx - 128) >> 8;
-                        int32_t py0 = (miny - 128 + 255) >> 8, py1 = (maxy - 128) >> 8;
-                        px0 = max(px0, 0);
-                        py0 = max(py0, 0);
-                        px1 = min(px1, (int32_t)c.w - 1);
-                        py1 = min(py1, (int32_t)c.h - 1);
-                        if (px0 <= px1 && py0 <= py1) {
-                            const uint32_t bw = (uint32_t)(px1 - px0 + 1), bh = (uint32_t)(py1 - py0 + 1);
-                            if (bw * bh <= c.small_area) {
-                                if (A < 0) {
-                                    const int2 tp = p1;
-                                    p1 = p2;
-                                    p2 = tp;
-                                    const float tz = z1;
-                                    z1 = z2;
-                                    z2 = tz;
-                                }
-                                const int64_t Ap = A < 0 ? -A : A;
-                                TriRec& r = recs[lane];
-                                r.x[0] = p0.x, r.x[1] = p1.x, r.x[2] = p2.x;
-                                r.y[0] = p0.y, r.y[1] = p1.y, r.y[2] = p2.y;
-                                uint8_t bias = 0;
-#pragma unroll
-                                for (int k = 0; k < 3; ++k) {
-                                    const int32_t dx = r.x[(k + 1) % 3] - r.x[k], dy = r.y[(k + 1) % 3] - r.y[k];
-                                    if (!(dy < 0 || (dy == 0 && dx > 0))) bias |= (uint8_t)(1u << k);
-                                }
-                                const float dx1 = __int2float_rn(p1.x - p0.x), dy1 = __int2float_rn(p1.y - p0.y);
-                                const float dx2 = __int2float_rn(p2.x - p0.x), dy2 = __int2float_rn(p2.y - p0.y);
-                                const float af = __ll2float_rn(Ap);
-                                const float dz1 = fsub(z1, z0), dz2 = fsub(z2, z0);
-                                r.z0 = z0;
-                                r.pa = fdiv(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), af);
-                                r.pb = fdiv(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), af);
-                                r.inv_bw = 1.0f / (float)bw;
-                                r.id = id;
-                                r.bx0 = (uint16_t)px0;
-                                r.by0 = (uint16_t)py0;
-                                r.bw = (uint8_t)bw;
-                                r.bh = (uint8_t)bh;
-                                r.bias = bias;
-                                area = bw * bh;
-                            } else {
-                                setup_and_raster(p0.x, p0.y, z0, p1.x, p1.y, z1, p2.x, p2.y, z2, id, c);
+                int kind = kDrop;
+                int4 q0 = make_int4(0, 0, 0, 0), q1 = q0, q2 = q0;
+                int32_t minx = 0, maxx = 0, miny = 0, maxy = 0;
+                int64_t A = 0;
+                if (i0 >= vc || i1 >= vc || i2 >= vc) {
+                    if (!SLOW) report(P.status, kStatusBadIndex, d);
+                } else {
+                    q0 = svtx[i0], q1 = svtx[i1], q2 = svtx[i2];
+                    const uint32_t f0 = (uint32_t)q0.w, f1 = (uint32_t)q1.w, f2 = (uint32_t)q2.w;
+                    // The backface test (visbuffer.mesh.glsl:86-101) and the
+                    // empty-bbox test are both pure filters, so the cheap
+                    // bbox test runs first for triangles that need no clipping.
+                    auto backfacing = [&]() {
+                        if (double_sided) return false;
+                        const float4 a = clip[i0], b = clip[i1], cc = clip[i2];
+                        const float det = det3(a.x, a.y, a.w, b.x, b.y, b.w, cc.x, cc.y, cc.w);
+                        return tdet < 0.0f ? det < 0.0f : det > 0.0f;
+                    };
+                    if (f0 & f1 & f2 & 63) {
+                        kind = kDrop;  // outcode reject
+                    } else if ((f0 | f1 | f2) & (OC_ZLO | OC_ZHI | kFlagGuard)) {
+                        kind = backfacing() ? kDrop : kSlowClip;
+                    } else if (f0 & f1 & f2 & kFlagSnapped) {
+                        minx = min(q0.x, min(q1.x, q2.x)), maxx = max(q0.x, max(q1.x, q2.x));
+                        miny = min(q0.y, min(q1.y, q2.y)), maxy = max(q0.y, max(q1.y, q2.y));
+                        const int32_t qx0 = max((minx - 128 + 255) >> 8, 0), qx1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
+                        const int32_t qy0 = max((miny - 128 + 255) >> 8, 0), qy1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
+                        if (qx0 <= qx1 && qy0 <= qy1 && !backfacing()) {
+                            A = (int64_t)(q1.x - q0.x) * (q2.y - q0.y) - (int64_t)(q1.y - q0.y) * (q2.x - q0.x);
+                            if (A != 0) {
+                                const bool small = maxx - minx < kSmallExtent && maxy - miny < kSmallExtent &&
+                                                   (uint32_t)((qx1 - qx0 + 1) * (qy1 - qy0 + 1)) <= c.small_area;
+                                kind = small ? kFast : kSlowSetup;
                             }
                         }
-                    } else if (A != 0) {
-                        setup_and_raster(p0.x, p0.y, z0, p1.x, p1.y, z1, p2.x, p2.y, z2, id, c);
                     }
                 }
+                if (SLOW) {
+                    if (kind == kSlowClip) {
+                        raster_clipped(clip[i0], clip[i1], clip[i2],
+                                       (((uint32_t)q0.w | (uint32_t)q1.w | (uint32_t)q2.w) & (OC_ZLO | OC_ZHI)) != 0,
+                                       id, c);
+                    } else if (kind == kSlowSetup) {
+                        setup_and_raster(q0.x, q0.y, __int_as_float(q0.z), q1.x, q1.y, __int_as_float(q1.z), q2.x,
+                                         q2.y, __int_as_float(q2.z), id, c);
+                    }
+                } else if (kind == kSlowClip || kind == kSlowSetup) {
+                    any_slow = true;
+                } else if (kind == kFast) {
+                    int2 p0 = make_int2(q0.x, q0.y), p1 = make_int2(q1.x, q1.y), p2 = make_int2(q2.x, q2.y);
+                    float z0 = __int_as_float(q0.z), z1 = __int_as_float(q1.z), z2 = __int_as_float(q2.z);
+                    if (A < 0) {
+                        const int2 tp = p1;
+                        p1 = p2;
+                        p2 = tp;
+                        const float tz = z1;
+                        z1 = z2;
+                        z2 = tz;
+                    }
+                    const int64_t Ap = A < 0 ? -A : A;
+                    const int32_t px0 = max((minx - 128 + 255) >> 8, 0), px1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
+                    const int32_t py0 = max((miny - 128 + 255) >> 8, 0), py1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
+                    const uint32_t bw = (uint32_t)(px1 - px0 + 1), bh = (uint32_t)(py1 - py0 + 1);
+                    TriRec& r = recs[lane];
+                    r.x[0] = p0.x, r.x[1] = p1.x, r.x[2] = p2.x;
+                    r.y[0] = p0.y, r.y[1] = p1.y, r.y[2] = p2.y;
+                    uint8_t bias = 0;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const int32_t dx = r.x[(k + 1) % 3] - r.x[k], dy = r.y[(k + 1) % 3] - r.y[k];
+                        if (!(dy < 0 || (dy == 0 && dx > 0))) bias |= (uint8_t)(1u << k);
+                    }
+                    const float dx1 = __int2float_rn(p1.x - p0.x), dy1 = __int2float_rn(p1.y - p0.y);
+                    const float dx2 = __int2float_rn(p2.x - p0.x), dy2 = __int2float_rn(p2.y - p0.y);
+                    const float af = __ll2float_rn(Ap);
+                    const float dz1 = fsub(z1, z0), dz2 = fsub(z2, z0);
+                    r.z0 = z0;
+                    r.pa = fdiv(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), af);
+                    r.pb = fdiv(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), af);
+                    r.inv_bw = 1.0f / (float)bw;
+                    r.id = id;
+                    r.bx0 = (uint16_t)px0;
+                    r.by0 = (uint16_t)py0;
+                    r.bw = (uint8_t)bw;
+                    r.bh = (uint8_t)bh;
+                    r.bias = bias;
+                    area = bw * bh;
+                }
             }
+            if (SLOW) continue;
             // Warp-cooperative raster of this round's small triangles: an
             // inclusive scan of their bbox areas spreads the pixels evenly.
             uint32_t incl = area;
@@ -489,12 +530,20 @@ __global__ void __launch_bounds__(WARPS * 32, 8 * 4 / WARPS) k_raster(RasterPara
                                         __fmaf_rn(r.pb, __int2float_rn(sy - r.y[0]), r.z0));
                     if (!(z > 0.0f)) z = 0.0f;
                     if (z > 1.0f) z = 1.0f;
-                    atomicMax(c.depth + (size_t)(r.by0 + ly) * c.w + (r.bx0 + lx),
-                              ((unsigned long long)__float_as_uint(z) << 32) | ((unsigned long long)r.id + 1ull));
+                    plot(c.depth + (size_t)(r.by0 + ly) * c.w + (r.bx0 + lx),
+                         ((unsigned long long)__float_as_uint(z) << 32) | ((unsigned long long)r.id + 1ull));
                 }
             }
             __syncwarp();
         }
+        if (!SLOW && __any_sync(0xffffffffu, any_slow) && lane == 0) {
+            const uint32_t k = atomicAdd(&V.counters[slot], 1u);
+            if (k < defer_cap)
+                V.deferred[k] = d;
+            else
+                report(P.status, kStatusListOverflow, d);
+        }
+        __syncwarp();
     }
 }
 
@@ -539,6 +588,12 @@ __global__ void __launch_bounds__(256) k_raster_big(const BigTri* __restrict__ q
     }
 }
 
+template <int WARPS>
+void launch_variant(const RasterParams& P, dim3 grid, cudaStream_t stream) {
+    k_raster<WARPS, false><<<grid, WARPS * 32, 0, stream>>>(P);
+    k_raster<WARPS, true><<<grid, WARPS * 32, 0, stream>>>(P);
+}
+
 }  // namespace
 
 void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews, const RasterLists& lists,
@@ -558,10 +613,10 @@ void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews,
     if (bpv == 0) bpv = 1;
     dim3 grid(bpv, nviews);
     switch (cfg.warps_per_cta) {
-        case 1: k_raster<1><<<grid, 32, 0, stream>>>(P); break;
-        case 2: k_raster<2><<<grid, 64, 0, stream>>>(P); break;
-        case 8: k_raster<8><<<grid, 256, 0, stream>>>(P); break;
-        default: k_raster<4><<<grid, 128, 0, stream>>>(P); break;
+        case 1: launch_variant<1>(P, grid, stream); break;
+        case 2: launch_variant<2>(P, grid, stream); break;
+        case 8: launch_variant<8>(P, grid, stream); break;
+        default: launch_variant<4>(P, grid, stream); break;
     }
     if (between) cudaEventRecord(between, stream);
     k_raster_big<<<sm_count * 8, 256, 0, stream>>>(big, big_count, big_capacity, views);

@@ -19,24 +19,26 @@ namespace vkgv {
 
 namespace {
 
+// fromLinear / toLinear (shaders/srgb.h.glsl:9-23), with the operation
+// order of the oracle so that only powf's last ulp can differ.
 __device__ __forceinline__ float from_linear(float c) {
     const bool cutoff = c < 0.0031308f;
-    const float higher = 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
-    const float lower = c * 12.92f;
+    const float higher = fsub(fmul(1.055f, powf(c, 1.0f / 2.4f)), 0.055f);
+    const float lower = fmul(c, 12.92f);
     return cutoff ? lower : higher;
 }
 
 __device__ __forceinline__ float to_linear(float c) {
     const bool cutoff = c < 0.04045f;
-    const float higher = powf((c + 0.055f) / 1.055f, 2.4f);
-    const float lower = c / 12.92f;
+    const float higher = powf(fdiv(fadd(c, 0.055f), 1.055f), 2.4f);
+    const float lower = fdiv(c, 12.92f);
     return cutoff ? lower : higher;
 }
 
 __device__ __forceinline__ uint32_t unorm8(float c) {
     if (!(c > 0.0f)) return 0;
     if (c > 1.0f) c = 1.0f;
-    return (uint32_t)__float2int_rn(c * 255.0f);
+    return (uint32_t)__float2int_rn(fmul(c, 255.0f));
 }
 
 __device__ __forceinline__ uint32_t pack_rgba(const float lin[4]) {
@@ -44,12 +46,17 @@ __device__ __forceinline__ uint32_t pack_rgba(const float lin[4]) {
            (unorm8(lin[3]) << 24);
 }
 
+__device__ __forceinline__ float lerp(float a, float b, float t) { return fadd(a, fmul(t, fsub(b, a))); }
+
+// Bilinear REPEAT sample, texel centres at +0.5.  Textured shading of a
+// high-frequency texture is very sensitive to the sample position, so every
+// operation follows the oracle's order (no contraction).
 __device__ void sample_texture(const vkgv_texture& t, float u, float v, float out[4]) {
-    const float tx = u * (float)t.width - 0.5f, ty = v * (float)t.height - 0.5f;
+    const float tx = fsub(fmul(u, (float)t.width), 0.5f), ty = fsub(fmul(v, (float)t.height), 0.5f);
     const float fx = floorf(tx), fy = floorf(ty);
-    const float ax = tx - fx, ay = ty - fy;
+    const float ax = fsub(tx, fx), ay = fsub(ty, fy);
     const long long W = t.width, H = t.height;
-    long long x0 = (long long)fx, y0 = (long long)fy;
+    const long long x0 = (long long)fx, y0 = (long long)fy;
     const long long xs[2] = {((x0 % W) + W) % W, (((x0 + 1) % W) + W) % W};
     const long long ys[2] = {((y0 % H) + H) % H, (((y0 + 1) % H) + H) % H};
     float tex[2][2][4];
@@ -60,10 +67,10 @@ __device__ void sample_texture(const vkgv_texture& t, float u, float v, float ou
             const size_t idx = (size_t)ys[j] * t.row_pitch + (size_t)xs[i];
             if (t.format == VKGV_TEXTURE_RGBA8) {
                 const uchar4 p = __ldg(reinterpret_cast<const uchar4*>(t.data) + idx);
-                tex[j][i][0] = (float)p.x / 255.0f;
-                tex[j][i][1] = (float)p.y / 255.0f;
-                tex[j][i][2] = (float)p.z / 255.0f;
-                tex[j][i][3] = (float)p.w / 255.0f;
+                tex[j][i][0] = fdiv((float)p.x, 255.0f);
+                tex[j][i][1] = fdiv((float)p.y, 255.0f);
+                tex[j][i][2] = fdiv((float)p.z, 255.0f);
+                tex[j][i][3] = fdiv((float)p.w, 255.0f);
             } else {
                 const float* p = reinterpret_cast<const float*>(t.data) + 3 * idx;
                 tex[j][i][0] = __ldg(p);
@@ -74,9 +81,9 @@ __device__ void sample_texture(const vkgv_texture& t, float u, float v, float ou
         }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const float top = tex[0][0][k] + ax * (tex[0][1][k] - tex[0][0][k]);
-        const float bot = tex[1][0][k] + ax * (tex[1][1][k] - tex[1][0][k]);
-        out[k] = top + ay * (bot - top);
+        const float top = lerp(tex[0][0][k], tex[0][1][k], ax);
+        const float bot = lerp(tex[1][0][k], tex[1][1][k], ax);
+        out[k] = lerp(top, bot, ay);
     }
 }
 
@@ -105,41 +112,47 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
         vx[k] = verts + vidx[tri[k]];
         m4v(mvp, vx[k]->position[0], vx[k]->position[1], vx[k]->position[2], 1.0f, c[k]);
     }
-    const float nx = (((float)px + 0.5f) / (float)V.w) * 2.0f - 1.0f;
-    const float ny = (((float)py + 0.5f) / (float)V.h) * 2.0f - 1.0f;
+    // Perspective-correct barycentrics: the clip-space weights whose point
+    // projects to the pixel centre are proportional to a x b.
+    const float nx = fsub(fmul(fdiv(fadd((float)px, 0.5f), (float)V.w), 2.0f), 1.0f);
+    const float ny = fsub(fmul(fdiv(fadd((float)py, 0.5f), (float)V.h), 2.0f), 1.0f);
     float a[3], b[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        a[k] = c[k][0] - nx * c[k][3];
-        b[k] = c[k][1] - ny * c[k][3];
+        a[k] = fsub(c[k][0], fmul(nx, c[k][3]));
+        b[k] = fsub(c[k][1], fmul(ny, c[k][3]));
     }
-    float l[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-    const float sum = (l[0] + l[1]) + l[2];
+    float l[3] = {fsub(fmul(a[1], b[2]), fmul(a[2], b[1])), fsub(fmul(a[2], b[0]), fmul(a[0], b[2])),
+                  fsub(fmul(a[0], b[1]), fmul(a[1], b[0]))};
+    const float sum = fadd(fadd(l[0], l[1]), l[2]);
     if (sum != 0.0f) {
-        l[0] /= sum;
-        l[1] /= sum;
-        l[2] /= sum;
+        l[0] = fdiv(l[0], sum);
+        l[1] = fdiv(l[1], sum);
+        l[2] = fdiv(l[2], sum);
     } else {
         l[0] = l[1] = l[2] = 1.0f / 3.0f;
     }
     float col[4], uv[2];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        col[k] = (l[0] * ((float)vx[0]->color[k] / 255.0f) + l[1] * ((float)vx[1]->color[k] / 255.0f)) +
-                 l[2] * ((float)vx[2]->color[k] / 255.0f);
+        col[k] = fadd(fadd(fmul(l[0], fdiv((float)vx[0]->color[k], 255.0f)),
+                           fmul(l[1], fdiv((float)vx[1]->color[k], 255.0f))),
+                      fmul(l[2], fdiv((float)vx[2]->color[k], 255.0f)));
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const float h0 = __half2float(__ushort_as_half(vx[0]->uv[k]));
         const float h1 = __half2float(__ushort_as_half(vx[1]->uv[k]));
         const float h2 = __half2float(__ushort_as_half(vx[2]->uv[k]));
-        uv[k] = (l[0] * h0 + l[1] * h1) + l[2] * h2;
+        uv[k] = fadd(fadd(fmul(l[0], h0), fmul(l[1], h1)), fmul(l[2], h2));
     }
     float sampled[4] = {1.0f, 1.0f, 1.0f, 1.0f};
     if (mat.albedo_index != VKGV_INVALID_HANDLE && mat.albedo_index < S.texture_count) {
+        // transformUv (mesh_common.h.glsl:129-135): rotate, scale, offset
         const float cs = cosf(mat.uv_rotation), sn = sinf(mat.uv_rotation);
-        const float ru = cs * uv[0] + sn * uv[1], rv = -sn * uv[0] + cs * uv[1];
-        const float tu = ru * mat.uv_scale[0] + mat.uv_offset[0];
-        const float tv = rv * mat.uv_scale[1] + mat.uv_offset[1];
+        const float ru = fadd(fmul(cs, uv[0]), fmul(sn, uv[1]));
+        const float rv = fadd(fmul(-sn, uv[0]), fmul(cs, uv[1]));
+        const float tu = fadd(fmul(ru, mat.uv_scale[0]), mat.uv_offset[0]);
+        const float tv = fadd(fmul(rv, mat.uv_scale[1]), mat.uv_offset[1]);
         const vkgv_texture tex = S.textures[mat.albedo_index];
         sample_texture(tex, tu, tv, sampled);
         if (tex.format == VKGV_TEXTURE_RGBA8)
@@ -147,7 +160,7 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
             for (int k = 0; k < 3; ++k) sampled[k] = to_linear(sampled[k]);
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k) out[k] = col[k] * mat.albedo_factor[k] * sampled[k];
+    for (int k = 0; k < 4; ++k) out[k] = fmul(fmul(col[k], mat.albedo_factor[k]), sampled[k]);
 }
 
 template <bool TEXTURED>
@@ -184,7 +197,7 @@ __global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* 
 __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ views, uint32_t* counters,
                                                uint32_t counter_words, uint32_t skip_pixels) {
     const DeviceView& V = views[blockIdx.y];
-    if (blockIdx.x == 0 && threadIdx.x < 4) V.counters[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < 8) V.counters[threadIdx.x] = 0;
     if (blockIdx.x == 0 && blockIdx.y == 0)
         for (uint32_t i = threadIdx.x; i < counter_words; i += blockDim.x) counters[i] = 0;
     if (skip_pixels) return;
