@@ -29,10 +29,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "views/s at 1080p, 82M-tri scene: batched vs single-view CUDA; adjoint ms/view"
 WORKLOAD = ("torus grid: 2048 instances x 40,000 tris = 81.92M tris, 843,776 meshlet draws (<=64 verts/"
-            "<=124 tris), 1920x1080, two-pass frustum+HiZ culling, HiZ pyramid, textured resolve, "
+            "<=124 tris), 1920x1080, two-pass frustum+cone+HiZ culling, HiZ pyramid, textured resolve, "
             "steady state (previous frame's pyramid)")
 W1080, H1080 = 1920, 1080
-FLAGS_NAMES = "CULL_FRUSTUM|CULL_OCCLUSION|CULL_TWO_PASS|BUILD_PYRAMID|RESOLVE_TEXTURED|WRITE_IDS"
+FLAGS_NAMES = "CULL_FRUSTUM|CULL_CONE|CULL_OCCLUSION|CULL_TWO_PASS|BUILD_PYRAMID|RESOLVE_TEXTURED|WRITE_IDS"
 
 
 def parse():
@@ -130,7 +130,8 @@ def run_reference(args, rank, world):
     host = scene.scene_torus_grid()
     cam = scene.grid_camera(W1080, H1080)
     osc = ob.OracleScene(host)
-    flags = ob.CULL_FRUSTUM | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID | ob.RESOLVE_TEXTURED
+    flags = (ob.CULL_FRUSTUM | ob.CULL_CONE | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID
+             | ob.RESOLVE_TEXTURED)
     prev = ob.frame(osc, cam, W1080, H1080, flags)["pyramid"]
     for _ in range(max(0, args.warmup)):
         prev = ob.frame(osc, cam, W1080, H1080, flags, prev_pyramid=prev)["pyramid"]
@@ -236,8 +237,8 @@ def main():
     r = Renderer(local)
     host = scene.scene_torus_grid()
     dev = DeviceScene(host, f"cuda:{local}")
-    flags = (abi.CULL_FRUSTUM | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID | abi.RESOLVE_TEXTURED
-             | abi.WRITE_IDS)
+    flags = (abi.CULL_FRUSTUM | abi.CULL_CONE | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID
+             | abi.RESOLVE_TEXTURED | abi.WRITE_IDS)
     stream = torch.cuda.current_stream()
     if args.batched_only:
         out = run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier)
@@ -283,10 +284,14 @@ def main():
             graph.launch()
             ends[i].record(stream)
         torch.cuda.synchronize()
-        # keep sampling a moment under load for the clock record
-        for _ in range(20):
-            graph.launch()
-        torch.cuda.synchronize()
+        # The timed region is far shorter than the 200 ms sampling period:
+        # keep the same frame running for ~1.5 s so the clock record has
+        # samples under this load.
+        t_load = time.perf_counter()
+        while time.perf_counter() - t_load < 1.5:
+            for _ in range(50):
+                graph.launch()
+            torch.cuda.synchronize()
     per_step = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_local = sum(per_step) / 1000.0
     t = torch.tensor([t_local], device=f"cuda:{local}")
@@ -359,7 +364,8 @@ def main():
         threads = os.cpu_count() or 1
         ob.set_threads(threads)
         osc = ob.OracleScene(host)
-        of = ob.CULL_FRUSTUM | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID | ob.RESOLVE_TEXTURED
+        of = (ob.CULL_FRUSTUM | ob.CULL_CONE | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID
+              | ob.RESOLVE_TEXTURED)
         prev = ob.frame(osc, cam, W1080, H1080, of)["pyramid"]
         n_cpu = 0
         tc0 = time.perf_counter()

@@ -158,7 +158,25 @@ typedef struct vkgv_scene {
     uint64_t texture_table;      /* vkgv_texture[texture_count] or 0      */
     uint32_t meshlet_draw_count;
     uint32_t texture_count;
+    /* Optional normal cones for VKGV_CULL_CONE: a device array of one
+     * device address per primitive, each pointing at that primitive's
+     * vkgv_meshlet_cone[meshlet_count] (0 = no cones for it). */
+    uint64_t cone_table;
+    uint32_t primitive_count;    /* entries of cone_table                 */
+    uint32_t _pad;
 } vkgv_scene;
+
+/* Normal cone of one meshlet in object space (an addition: glsl::Meshlet
+ * has no cone, mesh_common.h.glsl:49-58, and the reference builds meshlets
+ * with coneWeight 0, assets.cpp:323).  Every triangle normal n satisfies
+ * dot(n, axis) >= cutoff and every vertex lies in the sphere (center,
+ * radius).  cutoff <= 0 means the meshlet is never cone-culled.  32 bytes. */
+typedef struct vkgv_meshlet_cone {
+    float center[3];
+    float radius;
+    float axis[3];
+    float cutoff;
+} vkgv_meshlet_cone;
 
 /* One headless view: the camera half of the push constants plus the
  * per-view images of the visbuffer, resolve and HiZ passes. */
@@ -309,6 +327,7 @@ typedef struct vkgv_mesh_info {
     const uint8_t* primitive_indices;
     float aabb_extents[3];
     float aabb_center[3];
+    const vkgv_meshlet_cone* cones;  /* one per meshlet                   */
 } vkgv_mesh_info;
 
 /* Icosahedron subdivided `level` times onto the unit sphere

@@ -29,7 +29,7 @@ BUILD_PYRAMID = 1 << 6
 class OrcPrimitive(C.Structure):
     _fields_ = [("vertex_indices", C.c_void_p), ("primitive_indices", C.c_void_p), ("vertices", C.c_void_p),
                 ("meshlets", C.c_void_p), ("aabb_extents", C.c_float * 3), ("aabb_center", C.c_float * 3),
-                ("meshlet_count", C.c_uint32), ("material_index", C.c_uint32)]
+                ("meshlet_count", C.c_uint32), ("material_index", C.c_uint32), ("cones", C.c_void_p)]
 
 
 class OrcTexture(C.Structure):
@@ -116,6 +116,10 @@ class OracleScene:
             prims[p].aabb_center[:] = [float(x) for x in m.aabb_center]
             prims[p].meshlet_count = m.meshlet_count
             prims[p].material_index = host.prim_materials[p]
+            if m.cones is not None and m.cones.size:
+                cones = np.ascontiguousarray(m.cones)
+                self._keep.append(cones)
+                prims[p].cones = _addr(cones)
         self.prims = prims
         self.draws = np.ascontiguousarray(host.draws, np.uint32)
         self.transforms = np.ascontiguousarray(host.transforms, np.float32)

@@ -212,6 +212,43 @@ int orc_frustum_visible(const float c[3], const float e[3], const float planes[2
     return 1;
 }
 
+/* Eye of a view-projection: the point with clip x = y = w = 0, by Cramer's
+ * rule on rows 0, 1, 3 (pinned like the kernel).  0 when singular. */
+static int eye_from_vp(const float* vp, float e[3]) {
+    const float a0[3] = {vp[0], vp[4], vp[8]}, a1[3] = {vp[1], vp[5], vp[9]}, a2[3] = {vp[3], vp[7], vp[11]};
+    const float b0 = -vp[12], b1 = -vp[13], b2 = -vp[15];
+    float det = det3(a0, a1, a2);
+    if (!(det != 0.0f)) return 0;
+    const float x0[3] = {b0, a0[1], a0[2]}, x1[3] = {b1, a1[1], a1[2]}, x2[3] = {b2, a2[1], a2[2]};
+    const float y0[3] = {a0[0], b0, a0[2]}, y1[3] = {a1[0], b1, a1[2]}, y2[3] = {a2[0], b2, a2[2]};
+    const float z0[3] = {a0[0], a0[1], b0}, z1[3] = {a1[0], a1[1], b1}, z2[3] = {a2[0], a2[1], b2};
+    e[0] = det3(x0, x1, x2) / det;
+    e[1] = det3(y0, y1, y2) / det;
+    e[2] = det3(z0, z1, z2) / det;
+    return 1;
+}
+
+/* Conservative meshlet backface test in object space (the cone-culling
+ * addition): every triangle faces away from the eye by 1e-3 (L + r) when
+ * d*c + sqrt(L^2 - d^2)*s < -(r + 1e-3 (L + r)). */
+static int cone_culled(const orc_cone* cone, const float* M, const float* eye) {
+    const float c = cone->cutoff;
+    if (!(c > 0.0f)) return 0;
+    const float C0[3] = {M[0], M[1], M[2]}, C1[3] = {M[4], M[5], M[6]}, C2[3] = {M[8], M[9], M[10]};
+    const float det = det3(C0, C1, C2);
+    if (!(det != 0.0f)) return 0;
+    const float v[3] = {eye[0] - M[12], eye[1] - M[13], eye[2] - M[14]};
+    const float ox = det3(v, C1, C2) / det, oy = det3(C0, v, C2) / det, oz = det3(C0, C1, v) / det;
+    const float wx = ox - cone->center[0], wy = oy - cone->center[1], wz = oz - cone->center[2];
+    const float L2 = (wx * wx + wy * wy) + wz * wz;
+    const float d = (cone->axis[0] * wx + cone->axis[1] * wy) + cone->axis[2] * wz;
+    const float s = sqrtf(fmaxf(1.0f - c * c, 0.0f));
+    const float perp = sqrtf(fmaxf(L2 - d * d, 0.0f));
+    const float lhs = d * c + perp * s;
+    const float margin = cone->radius + 1e-3f * (sqrtf(L2) + cone->radius);
+    return lhs < -margin;
+}
+
 /* Exact floor(log2(m)) clamped to [0, levels-1] (pinned rule above). */
 static int hiz_level(float m, uint32_t levels) {
     int top = (int)levels - 1;
@@ -227,7 +264,7 @@ static int hiz_level(float m, uint32_t levels) {
  * visible; *occluded is set when the frustum test passed and the occlusion
  * test failed. */
 static int cull_draw(const orc_scene* s, const orc_camera* cam, const orc_pyramid* pyr,
-                     uint32_t flags, uint32_t pass, uint32_t d, int* occluded) {
+                     uint32_t flags, uint32_t pass, uint32_t d, const float* eye, int* occluded) {
     *occluded = 0;
     const orc_draw* dr = &s->draws[d];
     const float* M = s->transforms + 16 * (size_t)dr->transform_index;
@@ -243,6 +280,8 @@ static int cull_draw(const orc_scene* s, const orc_camera* cam, const orc_pyrami
     for (int j = 0; j < 3; ++j)
         we[j] = (fabsf(M[0 * 4 + j]) * e[0] + fabsf(M[1 * 4 + j]) * e[1]) + fabsf(M[2 * 4 + j]) * e[2];
     if ((flags & ORC_CULL_FRUSTUM) && !orc_frustum_visible(wc, we, (const float*)cam->frustum)) return 0;
+    /* cone-culling addition: after the frustum test, before the occlusion test */
+    if (eye && prim->cones && cone_culled(&prim->cones[dr->meshlet_index], M, eye)) return 0;
     if (!(flags & ORC_CULL_OCCLUSION) || !pyr || pyr->levels == 0) return 1;
     /* projectAabb (culling.h.glsl:32-56) */
     static const float corners[8][3] = {{1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, -1},
@@ -282,6 +321,7 @@ typedef struct {
     uint32_t flags, pass;
     const uint32_t* cand;
     uint8_t* verdict; /* 0 culled, 1 visible, 2 occluded */
+    const float* eye; /* NULL: no cone test */
 } cull_ctx;
 
 static void cull_range(void* p, int64_t b, int64_t e, int worker) {
@@ -290,7 +330,7 @@ static void cull_range(void* p, int64_t b, int64_t e, int worker) {
     for (int64_t i = b; i < e; ++i) {
         uint32_t d = c->cand ? c->cand[i] : (uint32_t)i;
         int occ;
-        int vis = cull_draw(c->s, c->cam, c->pyr, c->flags, c->pass, d, &occ);
+        int vis = cull_draw(c->s, c->cam, c->pyr, c->flags, c->pass, d, c->eye, &occ);
         c->verdict[i] = vis ? 1 : (occ ? 2 : 0);
     }
 }
@@ -300,7 +340,9 @@ void orc_cull(const orc_scene* s, const orc_camera* cam, const orc_pyramid* pyr,
               uint32_t* rejected, uint32_t* nrej) {
     uint32_t n = cand ? ncand : s->draw_count;
     uint8_t* verdict = (uint8_t*)malloc(n ? n : 1);
-    cull_ctx c = {s, cam, pyr, flags, pass, cand, verdict};
+    float eye[3];
+    int have_eye = (flags & ORC_CULL_CONE) && eye_from_vp(cam->vp, eye);
+    cull_ctx c = {s, cam, pyr, flags, pass, cand, verdict, have_eye ? eye : NULL};
     orc_parallel_for(n, cull_range, &c);
     uint32_t ns = 0, nr = 0;
     for (uint32_t i = 0; i < n; ++i) {
@@ -498,6 +540,8 @@ static void raster_draw(const orc_scene* s, const orc_camera* cam, uint32_t w, u
     m4m(cam->vp, M, mvp);
     float clip[256][4];
     uint32_t vc = ml->vertex_count;
+    /* mesh-shader output limits (mesh_common.h.glsl:36-37) */
+    if (vc > 64 || ml->triangle_count > 126) return;
     for (uint32_t v = 0; v < vc; ++v) {
         uint32_t vi = prim->vertex_indices[ml->vertex_offset + v];
         const float* p = prim->vertices[vi].position;

@@ -57,6 +57,11 @@ typedef struct orc_camera {
     float frustum[6][4];
 } orc_camera; /* 352 B */
 
+/* Meshlet normal cone (object space) used by the cone-culling addition. */
+typedef struct orc_cone {
+    float center[3], radius, axis[3], cutoff;
+} orc_cone; /* 32 B */
+
 /* A primitive with host pointers in place of the device addresses. */
 typedef struct orc_primitive {
     const uint32_t* vertex_indices;
@@ -65,6 +70,7 @@ typedef struct orc_primitive {
     const orc_meshlet* meshlets;
     float aabb_extents[3], aabb_center[3];
     uint32_t meshlet_count, material_index;
+    const orc_cone* cones; /* NULL: no cone culling for this primitive */
 } orc_primitive;
 
 typedef struct orc_texture {

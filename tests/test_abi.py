@@ -35,7 +35,7 @@ def test_c_layout_matches_ctypes(tmp_path):
         "vkgv_meshlet": abi.Meshlet, "vkgv_vertex": abi.Vertex, "vkgv_meshlet_draw": abi.MeshletDraw,
         "vkgv_primitive": abi.Primitive, "vkgv_material": abi.Material, "vkgv_camera": abi.Camera,
         "vkgv_texture": abi.Texture, "vkgv_pyramid": abi.Pyramid, "vkgv_scene": abi.Scene, "vkgv_view": abi.View,
-        "vkgv_config": abi.Config, "vkgv_mesh_info": abi.MeshInfo,
+        "vkgv_config": abi.Config, "vkgv_mesh_info": abi.MeshInfo, "vkgv_meshlet_cone": abi.MeshletCone,
     }
     lines = []
     for cname, cls in structs.items():

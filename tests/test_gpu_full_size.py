@@ -14,8 +14,8 @@ from gpu_util import Pair, oracle_flags, rgba_close, u32, u64, view
 
 pytestmark = pytest.mark.gpu
 
-FLAGS = (abi.CULL_FRUSTUM | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID | abi.RESOLVE_TEXTURED
-         | abi.WRITE_IDS)
+FLAGS = (abi.CULL_FRUSTUM | abi.CULL_CONE | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID
+         | abi.RESOLVE_TEXTURED | abi.WRITE_IDS)
 
 
 @pytest.fixture(scope="module")

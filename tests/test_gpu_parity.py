@@ -231,3 +231,24 @@ def test_invalid_arguments(renderer, ico):
     assert lib.vkgv_frame(renderer.ctx, C.byref(ico.dev.scene), C.byref(huge), 1, abi.FRAME_REFERENCE, 0) == \
         abi.LIMIT_EXCEEDED
     assert b"8192" in lib.vkgv_last_error(renderer.ctx)
+
+
+@pytest.mark.parametrize("which", ["ico", "grid"])
+def test_cone_cull_matches_oracle_and_keeps_ids(renderer, ico, grid, which):
+    """Meshlet cone culling (an addition) gives the oracle's survivor sets
+    bit-exactly and leaves the visibility IDs unchanged."""
+    pair = ico if which == "ico" else grid
+    w, h = 800, 450
+    centre = (0.0, 0.0, 0.0) if which == "ico" else tuple(scene.grid_centre() * 0.25)
+    radius = 2.8 if which == "ico" else 10.0
+    for cam in orbit_cameras(3, radius, w, h, seed=31, centre=centre, fovy=70.0):
+        base = abi.CULL_FRUSTUM | abi.BUILD_PYRAMID | abi.RESOLVE_FLAT | abi.WRITE_IDS
+        v0, v1 = view(pair, cam, w, h), view(pair, cam, w, h)
+        renderer.frame(pair.dev, [v0], base)
+        renderer.frame(pair.dev, [v1], base | abi.CULL_CONE)
+        torch.cuda.synchronize()
+        exp = ob.frame(pair.orc, cam, w, h, oracle_flags(base | abi.CULL_CONE))
+        assert np.array_equal(np.sort(v1.survivor_list()), np.sort(exp["survivors"]))
+        assert v1.survivor_list().size < v0.survivor_list().size
+        assert np.array_equal(u32(v1.visbuffer), u32(v0.visbuffer))
+        assert np.array_equal(u32(v1.visbuffer), exp["ids"])

@@ -97,7 +97,12 @@ class Pyramid(C.Structure):
 class Scene(C.Structure):
     _fields_ = [("draw_buffer", C.c_uint64), ("transform_buffer", C.c_uint64), ("primitive_buffer", C.c_uint64),
                 ("material_buffer", C.c_uint64), ("texture_table", C.c_uint64),
-                ("meshlet_draw_count", C.c_uint32), ("texture_count", C.c_uint32)]
+                ("meshlet_draw_count", C.c_uint32), ("texture_count", C.c_uint32),
+                ("cone_table", C.c_uint64), ("primitive_count", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class MeshletCone(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("radius", C.c_float), ("axis", C.c_float * 3), ("cutoff", C.c_float)]
 
 
 class View(C.Structure):
@@ -119,7 +124,8 @@ class MeshInfo(C.Structure):
                 ("vertices", C.POINTER(Vertex)), ("positions", C.POINTER(C.c_float)), ("uvs", C.POINTER(C.c_float)),
                 ("indices", C.POINTER(C.c_uint32)), ("meshlets", C.POINTER(Meshlet)),
                 ("vertex_indices", C.POINTER(C.c_uint32)), ("primitive_indices", C.POINTER(C.c_uint8)),
-                ("aabb_extents", C.c_float * 3), ("aabb_center", C.c_float * 3)]
+                ("aabb_extents", C.c_float * 3), ("aabb_center", C.c_float * 3),
+                ("cones", C.POINTER(MeshletCone))]
 
 
 EXPECTED_SIZES = {"Meshlet": 36, "Vertex": 24, "MeshletDraw": 12, "Primitive": 64, "Material": 48, "Camera": 352}

@@ -203,6 +203,9 @@ int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, 
     P.S.textures = reinterpret_cast<const vkgv_texture*>(scene->texture_table);
     P.S.draw_count = D;
     P.S.texture_count = scene->texture_count;
+    P.S.cone_table = reinterpret_cast<const uint64_t*>(scene->cone_table);
+    P.S.primitive_count = scene->cone_table ? scene->primitive_count : 0;
+    P.S._pad = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const vkgv_view& v = views[i];
         rc = validate_view(ctx, v, flags);

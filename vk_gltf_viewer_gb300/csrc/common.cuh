@@ -60,6 +60,9 @@ struct SceneArgs {
     const vkgv_texture* textures;
     uint32_t draw_count;
     uint32_t texture_count;
+    const uint64_t* cone_table;   // per primitive: device address of its cones, or 0
+    uint32_t primitive_count;
+    uint32_t _pad;
 };
 
 // One binned (large) triangle chunk: a sub-rectangle of a snapped triangle.
@@ -130,6 +133,44 @@ __device__ __forceinline__ float det4(const float* m) {
         d[r] = det3(c1[0], c1[1], c1[2], c2[0], c2[1], c2[2], c3[0], c3[1], c3[2]);
     }
     return fsub(fadd(fsub(fmul(m[0], d[0]), fmul(m[1], d[1])), fmul(m[2], d[2])), fmul(m[3], d[3]));
+}
+
+// Eye position of a view-projection (the point where clip x, y and w are 0),
+// by Cramer's rule on rows 0, 1 and 3.  Returns false when singular.
+__device__ __forceinline__ bool eye_from_vp(const float* vp, float e[3]) {
+    const float a0x = vp[0], a0y = vp[4], a0z = vp[8], b0 = -vp[12];
+    const float a1x = vp[1], a1y = vp[5], a1z = vp[9], b1 = -vp[13];
+    const float a2x = vp[3], a2y = vp[7], a2z = vp[11], b2 = -vp[15];
+    const float det = det3(a0x, a0y, a0z, a1x, a1y, a1z, a2x, a2y, a2z);
+    if (!(det != 0.0f)) return false;
+    e[0] = fdiv(det3(b0, a0y, a0z, b1, a1y, a1z, b2, a2y, a2z), det);
+    e[1] = fdiv(det3(a0x, b0, a0z, a1x, b1, a1z, a2x, b2, a2z), det);
+    e[2] = fdiv(det3(a0x, a0y, b0, a1x, a1y, b1, a2x, a2y, b2), det);
+    return true;
+}
+
+// Conservative meshlet backface test in object space: every triangle of
+// the meshlet faces away from the eye by a margin of 1e-3 (L + r) when
+//   d*c + sqrt(L^2 - d^2)*s < -(r + 1e-3 (L + r)),
+// with L = |eye - center|, d = axis . (eye - center), c the cone cutoff and
+// s = sqrt(1 - c^2).  `M` is the instance transform (column-major).
+__device__ __forceinline__ bool cone_culled(const vkgv_meshlet_cone& cone, const float* M, const float* eye) {
+    const float c = cone.cutoff;
+    if (!(c > 0.0f)) return false;
+    const float det = det3(M[0], M[1], M[2], M[4], M[5], M[6], M[8], M[9], M[10]);
+    if (!(det != 0.0f)) return false;
+    const float vx = fsub(eye[0], M[12]), vy = fsub(eye[1], M[13]), vz = fsub(eye[2], M[14]);
+    const float ox = fdiv(det3(vx, vy, vz, M[4], M[5], M[6], M[8], M[9], M[10]), det);
+    const float oy = fdiv(det3(M[0], M[1], M[2], vx, vy, vz, M[8], M[9], M[10]), det);
+    const float oz = fdiv(det3(M[0], M[1], M[2], M[4], M[5], M[6], vx, vy, vz), det);
+    const float wx = fsub(ox, cone.center[0]), wy = fsub(oy, cone.center[1]), wz = fsub(oz, cone.center[2]);
+    const float L2 = fadd(fadd(fmul(wx, wx), fmul(wy, wy)), fmul(wz, wz));
+    const float d = fadd(fadd(fmul(cone.axis[0], wx), fmul(cone.axis[1], wy)), fmul(cone.axis[2], wz));
+    const float s = __fsqrt_rn(fmaxf(fsub(1.0f, fmul(c, c)), 0.0f));
+    const float perp = __fsqrt_rn(fmaxf(fsub(L2, fmul(d, d)), 0.0f));
+    const float lhs = fadd(fmul(d, c), fmul(perp, s));
+    const float margin = fadd(cone.radius, fmul(1e-3f, fadd(__fsqrt_rn(L2), cone.radius)));
+    return lhs < -margin;
 }
 
 __host__ __device__ __forceinline__ uint32_t mip_dim(uint32_t base, uint32_t k) {

@@ -33,7 +33,7 @@ struct CullResult {
     bool occluded;
 };
 
-__device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceView& V, const float* frustum,
+__device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceView& V, const float* frustum, const float* eye,
                                                const float* occl_vp, const float* pyr, uint32_t pw0,
                                                uint32_t ph0, uint32_t plevels, uint32_t flags, uint32_t d,
                                                uint32_t* status) {
@@ -73,6 +73,13 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
             float distance = fsub(fadd(fadd(fmul(p0, wc4[0]), fmul(p1, wc4[1])), fmul(p2, wc4[2])), p3);
             if (-radius > distance) return res;
         }
+    }
+    // Meshlet normal-cone backface test (an addition; conservative with
+    // respect to the per-triangle test of visbuffer.mesh.glsl:86-101).
+    if (eye && S.cone_table && dr.primitive_index < S.primitive_count) {
+        const uint64_t cones = S.cone_table[dr.primitive_index];
+        if (cones && cone_culled(reinterpret_cast<const vkgv_meshlet_cone*>(cones)[dr.meshlet_index], M, eye))
+            return res;
     }
     if (!pyr) {
         res.visible = true;
@@ -152,11 +159,21 @@ __global__ void __launch_bounds__(256) k_cull(SceneArgs S, const DeviceView* __r
     const vkgv_camera* cam = V.cam;
     __shared__ float s_frustum[24];
     __shared__ float s_vp[16];
+    __shared__ float s_eye[3];
+    __shared__ int s_eye_ok;
     if (threadIdx.x < 24) s_frustum[threadIdx.x] = (&cam->frustum[0][0])[threadIdx.x];
     if (threadIdx.x < 16)
         s_vp[threadIdx.x] = pass == 1 ? cam->prev_occlusion_view_projection[threadIdx.x]
                                       : cam->occlusion_view_projection[threadIdx.x];
+    if (threadIdx.x == 32) {
+        // the eye of the raster view-projection, for the cone test
+        float vp[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) vp[k] = cam->view_projection[k];
+        s_eye_ok = (flags & VKGV_CULL_CONE) && S.cone_table && eye_from_vp(vp, s_eye);
+    }
     __syncthreads();
+    const float* eye = s_eye_ok ? s_eye : nullptr;
     const float* pyr = nullptr;
     uint32_t pw0 = 0, ph0 = 0, pl = 0;
     if (flags & VKGV_CULL_OCCLUSION) {
@@ -188,7 +205,7 @@ __global__ void __launch_bounds__(256) k_cull(SceneArgs S, const DeviceView* __r
         if (i < n) {
             d = pass == 1 ? i : V.rejected[i];
             if (d < S.draw_count) {
-                CullResult r = cull_one(S, V, s_frustum, s_vp, pyr, pw0, ph0, pl, flags, d, status);
+                CullResult r = cull_one(S, V, s_frustum, eye, s_vp, pyr, pw0, ph0, pl, flags, d, status);
                 vis = r.visible;
                 occ = r.occluded;
             } else {

@@ -22,6 +22,7 @@ struct vkgv_mesh {
     std::vector<uint32_t> idx;   // 3 per triangle
     std::vector<vkgv_vertex> verts;
     std::vector<vkgv_meshlet> meshlets;
+    std::vector<vkgv_meshlet_cone> cones;
     std::vector<uint32_t> vtx_idx;
     std::vector<uint8_t> prim_idx;
     float aabb_ext[3] = {0, 0, 0};
@@ -281,6 +282,7 @@ extern "C" int vkgv_mesh_displace(vkgv_mesh* m, float amp, uint64_t seed) {
     compute_aabb(*m);
     fill_vertex_stream(*m);
     m->meshlets.clear();
+    m->cones.clear();
     m->vtx_idx.clear();
     m->prim_idx.clear();
     return VKGV_OK;
@@ -387,6 +389,67 @@ extern "C" int vkgv_mesh_set_attributes(vkgv_mesh* m, const float* rgba, const f
 
 // ------------------------------------------------------------ meshletiser
 
+namespace {
+
+// Normal cone of a meshlet (object space), rounded so that it stays a
+// bound in fp32: cutoff rounded down, radius rounded up.  A meshlet with a
+// degenerate triangle or a cone wider than ~87 degrees gets cutoff -1
+// (never culled).
+vkgv_meshlet_cone meshlet_cone(const vkgv_mesh& m, const std::vector<uint32_t>& tris,
+                               const std::vector<uint32_t>& verts, const float* center) {
+    vkgv_meshlet_cone cone{};
+    for (int c = 0; c < 3; ++c) cone.center[c] = center[c];
+    double r2 = 0;
+    for (uint32_t v : verts) {
+        double d2 = 0;
+        for (int c = 0; c < 3; ++c) {
+            double e = double(m.pos[3 * size_t(v) + c]) - double(center[c]);
+            d2 += e * e;
+        }
+        r2 = std::max(r2, d2);
+    }
+    double r = std::sqrt(r2) * (1.0 + 1e-6) + 1e-7;
+    cone.radius = std::nextafter(float(r), INFINITY);
+    cone.cutoff = -1.0f;
+    std::vector<std::array<double, 3>> normals;
+    double sum[3] = {0, 0, 0};
+    for (uint32_t t : tris) {
+        const float* a = &m.pos[3 * size_t(m.idx[3 * t])];
+        const float* b = &m.pos[3 * size_t(m.idx[3 * t + 1])];
+        const float* c = &m.pos[3 * size_t(m.idx[3 * t + 2])];
+        double e1[3], e2[3];
+        for (int k = 0; k < 3; ++k) {
+            e1[k] = double(b[k]) - a[k];
+            e2[k] = double(c[k]) - a[k];
+        }
+        std::array<double, 3> n = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                   e1[0] * e2[1] - e1[1] * e2[0]};
+        double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (!(len > 1e-30)) return cone;  // degenerate triangle: no cone
+        for (double& x : n) x /= len;
+        normals.push_back(n);
+        for (int k = 0; k < 3; ++k) sum[k] += n[k];
+    }
+    double sl = std::sqrt(sum[0] * sum[0] + sum[1] * sum[1] + sum[2] * sum[2]);
+    if (!(sl > 1e-12)) return cone;
+    double axis[3] = {sum[0] / sl, sum[1] / sl, sum[2] / sl};
+    double cmin = 1.0;
+    for (auto& n : normals) cmin = std::min(cmin, n[0] * axis[0] + n[1] * axis[1] + n[2] * axis[2]);
+    if (!(cmin > 0.05)) return cone;
+    for (int k = 0; k < 3; ++k) cone.axis[k] = float(axis[k]);
+    // The stored axis is the rounded one: recompute the bound against it.
+    double cmin_f = 1.0;
+    double fa[3] = {cone.axis[0], cone.axis[1], cone.axis[2]};
+    double fal = std::sqrt(fa[0] * fa[0] + fa[1] * fa[1] + fa[2] * fa[2]);
+    for (auto& n : normals) cmin_f = std::min(cmin_f, (n[0] * fa[0] + n[1] * fa[1] + n[2] * fa[2]) / fal);
+    cmin_f -= 1e-6;
+    if (!(cmin_f > 0.05)) return cone;
+    cone.cutoff = std::nextafter(float(cmin_f), -INFINITY);
+    return cone;
+}
+
+}  // namespace
+
 // Greedy, adjacency-driven meshletiser.  Like meshopt_buildMeshlets with
 // coneWeight 0 (assets.cpp:323-341) it grows one meshlet at a time under the
 // vertex and triangle limits; it prefers the adjacent triangle that adds the
@@ -397,6 +460,7 @@ extern "C" int vkgv_mesh_build_meshlets(vkgv_mesh* m, uint32_t max_v, uint32_t m
     if (!m || max_v < 3 || max_v > 255 || max_t < 1 || max_t > 255) return VKGV_INVALID_ARG;
     const size_t nv = m->pos.size() / 3, nt = m->idx.size() / 3;
     m->meshlets.clear();
+    m->cones.clear();
     m->vtx_idx.clear();
     m->prim_idx.clear();
     // vertex -> triangles adjacency (CSR)
@@ -482,6 +546,7 @@ extern "C" int vkgv_mesh_build_meshlets(vkgv_mesh* m, uint32_t max_v, uint32_t m
             ml.aabb_extents[c] = mx[c] - ctr;
         }
         m->meshlets.push_back(ml);
+        m->cones.push_back(meshlet_cone(*m, mtris, mverts, ml.aabb_center));
         for (uint32_t v : mverts) local[v] = -1;
     }
     return VKGV_OK;
@@ -503,6 +568,7 @@ extern "C" int vkgv_mesh_get_info(const vkgv_mesh* m, vkgv_mesh_info* out) {
     out->meshlets = m->meshlets.empty() ? nullptr : m->meshlets.data();
     out->vertex_indices = m->vtx_idx.empty() ? nullptr : m->vtx_idx.data();
     out->primitive_indices = m->prim_idx.empty() ? nullptr : m->prim_idx.data();
+    out->cones = m->cones.empty() ? nullptr : m->cones.data();
     for (int c = 0; c < 3; ++c) {
         out->aabb_extents[c] = m->aabb_ext[c];
         out->aabb_center[c] = m->aabb_ctr[c];

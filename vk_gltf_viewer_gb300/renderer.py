@@ -70,10 +70,17 @@ class DeviceScene:
             table[i].format = t.format
             table[i].row_pitch = t.width
         self.texture_table = _to_device(np.frombuffer(bytes(table), np.uint8), self.device)
+        # meshlet normal cones (for VKGV_CULL_CONE): one device array per
+        # primitive, addressed through a table of device addresses
+        self.cone_data = [_to_device(m.cones, self.device) if m.cones is not None and m.cones.size else None
+                          for m in host.meshes]
+        cone_ptrs = np.array([_ptr(t) for t in self.cone_data], dtype=np.uint64)
+        self.cone_table = _to_device(cone_ptrs, self.device)
         self.scene = abi.Scene(draw_buffer=_ptr(self.draws), transform_buffer=_ptr(self.transforms),
                                primitive_buffer=_ptr(self.primitives), material_buffer=_ptr(self.materials),
                                texture_table=_ptr(self.texture_table) if host.textures else 0,
-                               meshlet_draw_count=host.draw_count, texture_count=len(host.textures))
+                               meshlet_draw_count=host.draw_count, texture_count=len(host.textures),
+                               cone_table=_ptr(self.cone_table), primitive_count=len(host.meshes))
 
     @property
     def draw_count(self) -> int:

@@ -23,6 +23,9 @@ MESHLET_DTYPE = np.dtype({"names": ["vertex_offset", "triangle_offset", "vertex_
 VERTEX_DTYPE = np.dtype({"names": ["position", "color", "normal", "pad", "uv"],
                          "formats": [("<f4", 3), ("u1", 4), ("u1", 3), "u1", ("<u2", 2)],
                          "offsets": [0, 12, 16, 19, 20], "itemsize": 24})
+CONE_DTYPE = np.dtype({"names": ["center", "radius", "axis", "cutoff"],
+                       "formats": [("<f4", 3), "<f4", ("<f4", 3), "<f4"],
+                       "offsets": [0, 12, 16, 28], "itemsize": 32})
 MATERIAL_DTYPE = np.dtype({"names": ["albedo_factor", "albedo_index", "uv_offset", "uv_scale", "uv_rotation",
                                      "alpha_cutoff", "double_sided"],
                            "formats": [("<f4", 4), "<u4", ("<f4", 2), ("<f4", 2), "<f4", "<f4", "<u4"],
@@ -42,6 +45,7 @@ class Mesh:
     aabb_extents: np.ndarray
     aabb_center: np.ndarray
     position_scale: float = 1.0
+    cones: np.ndarray | None = None  # CONE_DTYPE, one per meshlet
 
     @property
     def meshlet_count(self) -> int:
@@ -82,6 +86,7 @@ def _mesh_from_handle(h, max_vertices: int = 64, max_triangles: int = 124) -> Me
             aabb_extents=np.array(info.aabb_extents[:], np.float32),
             aabb_center=np.array(info.aabb_center[:], np.float32),
             position_scale=float(info.position_scale),
+            cones=_copy(C.cast(info.cones, C.c_void_p).value, info.meshlet_count, CONE_DTYPE),
         )
     finally:
         lib.vkgv_mesh_free(h)
