@@ -305,6 +305,54 @@ int vkgv_graph_destroy(vkgv_graph* graph);
 /* Number of kernel launches one vkgv_graph_launch performs. */
 int vkgv_graph_kernel_count(const vkgv_graph* graph, uint32_t* out_count);
 
+/* ------------------------------------------------ adjoint of the resolve */
+/* An addition with no reference implementation: a differentiable form of
+ * the textured resolve (the commented-out visbuffer.frag.glsl:29-34) over
+ * fp32 parameters.  Shading is linear RGB
+ *     rgb = interp(colour) * albedo * tex(transformUv(interp(uv)))
+ * with perspective-correct barycentrics of the visible triangle and a
+ * bilinear REPEAT fp32 RGB texture.  Visibility comes from the regular cull
+ * and raster kernels (identity node transform) and is recomputed in the
+ * backward pass instead of being stored. */
+typedef struct vkgv_diff_scene {
+    uint64_t meshlet_buffer;          /* vkgv_meshlet[meshlet_count]        */
+    uint64_t vertex_index_buffer;     /* uint32 meshlet vertex indices      */
+    uint64_t primitive_index_buffer;  /* uint8 meshlet-local triplets       */
+    uint64_t positions;               /* float[3 * vertex_count]            */
+    uint64_t colors;                  /* float[3 * vertex_count], linear    */
+    uint64_t uvs;                     /* float[2 * vertex_count]            */
+    uint64_t texture;                 /* float[3 * tex_width * tex_height]  */
+    uint32_t meshlet_count;
+    uint32_t vertex_count;
+    uint32_t tex_width;
+    uint32_t tex_height;
+    float albedo[3];
+    float uv_offset[2];
+    float uv_scale[2];
+    float uv_rotation;
+    uint32_t double_sided;
+    uint32_t _pad;
+} vkgv_diff_scene;
+
+typedef struct vkgv_diff_view {
+    uint64_t camera_buffer;  /* device vkgv_camera                         */
+    uint32_t width, height;
+    uint64_t depth_id;       /* uint64[W*H] visibility scratch, 16-byte aligned */
+    uint64_t rgb;            /* float[3*W*H] shaded output, or 0           */
+    uint64_t target;         /* float[3*W*H] target image (backward)       */
+} vkgv_diff_view;
+
+/* Renders every view's shaded linear RGB into view.rgb. */
+int vkgv_diff_forward(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_diff_view* views,
+                      uint32_t view_count, void* stream);
+/* Loss L = scale * sum over views, pixels and channels of (rgb - target)^2
+ * (empty pixels contribute (0 - target)^2).  Accumulates L into *loss and
+ * dL/dpositions, dL/dcolors, dL/dtexels into the three gradient arrays
+ * (fp32 atomics; zero them first).  Any gradient pointer may be 0. */
+int vkgv_diff_backward(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_diff_view* views,
+                       uint32_t view_count, float scale, uint64_t loss, uint64_t grad_positions,
+                       uint64_t grad_colors, uint64_t grad_texture, void* stream);
+
 /* ---------------------------------------------- host scene producers (A15) */
 /* Replace the glTF import + meshletiser (src/vk_gltf_viewer/assets.cpp:288-430)
  * for procedural scenes, and the camera update (src/vk_gltf_viewer/camera.cpp). */

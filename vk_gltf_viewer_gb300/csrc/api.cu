@@ -48,6 +48,7 @@ struct vkgv_ctx {
     Scratch survivors;  // per view: capacity draw_count
     Scratch rejected;   // per view: capacity draw_count
     Scratch deferred;   // per view: capacity draw_count
+    Scratch diff;       // adjoint: internal raster scene of the differentiable mesh
     BigTri* big = nullptr;
     uint32_t big_cap = 0;
     cudaStream_t capture_stream = nullptr;
@@ -307,10 +308,12 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
     zone(8);
     if (flags & VKGV_BUILD_PYRAMID) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, ctx->status, stream);
     zone(9);
-    if (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS))
-        launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
+    // The resolve also writes the survivor totals; without it a small
+    // finalise kernel does.
+    const bool resolve = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS)) != 0;
+    if (resolve) launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
     zone(10);
-    launch_finalize(dv, n, stream);
+    if (!resolve) launch_finalize(dv, n, stream);
     zone(11);
 }
 
@@ -405,6 +408,7 @@ int vkgv_destroy(vkgv_ctx* ctx) {
     if (ctx->survivors.ptr) cudaFree(ctx->survivors.ptr);
     if (ctx->rejected.ptr) cudaFree(ctx->rejected.ptr);
     if (ctx->deferred.ptr) cudaFree(ctx->deferred.ptr);
+    if (ctx->diff.ptr) cudaFree(ctx->diff.ptr);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     for (uint32_t i = 0; i <= VKGV_STAGE_COUNT; ++i)
         if (ctx->zone[i]) cudaEventDestroy(ctx->zone[i]);
@@ -593,6 +597,126 @@ int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, 
     rc = check_launch(ctx);
     if (rc) return rc;
     return close_slot(ctx, slot, stream);
+}
+
+}  // extern "C"
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// One pass of the adjoint: builds the internal raster scene from the current
+// positions, recomputes visibility (clear, cull without culling tests, since
+// the builder's meshlet bounds do not follow moving vertices, raster) and
+// runs the shading kernel forward or backward.
+int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* views, uint32_t n, bool backward,
+             float scale, uint64_t loss, uint64_t gpos, uint64_t gcol, uint64_t gtex, void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!ds || !views || n == 0) return fail(ctx, VKGV_INVALID_ARG, "adjoint: scene and views are required");
+    if (!ds->meshlet_buffer || !ds->vertex_index_buffer || !ds->primitive_index_buffer || !ds->positions ||
+        !ds->colors || !ds->uvs || !ds->texture || ds->vertex_count == 0 || ds->tex_width == 0 || ds->tex_height == 0)
+        return fail(ctx, VKGV_INVALID_ARG, "adjoint: incomplete scene");
+    if (ds->meshlet_count >= (1u << VKGV_DRAW_INDEX_BITS))
+        return fail(ctx, VKGV_LIMIT_EXCEEDED, "adjoint: meshlet_count must be < 2^25");
+    if (n > 65535u) return fail(ctx, VKGV_LIMIT_EXCEEDED, "at most 65535 views per call");
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    const size_t V = ds->vertex_count, M = ds->meshlet_count;
+    const size_t off_draws = align256(sizeof(vkgv_vertex) * V);
+    const size_t off_xf = off_draws + align256(sizeof(vkgv_meshlet_draw) * std::max<size_t>(M, 1));
+    const size_t off_prim = off_xf + 256, off_mat = off_prim + 256, total = off_mat + 256;
+    int rc = ensure_scratch(ctx, ctx->diff, total, "adjoint scene");
+    if (rc) return rc;
+    char* base = static_cast<char*>(ctx->diff.ptr);
+    DiffSetup S{};
+    S.positions = reinterpret_cast<const float*>(ds->positions);
+    S.vertex_count = ds->vertex_count;
+    S.meshlet_count = ds->meshlet_count;
+    S.meshlets = reinterpret_cast<const vkgv_meshlet*>(ds->meshlet_buffer);
+    S.vertex_indices = reinterpret_cast<const uint32_t*>(ds->vertex_index_buffer);
+    S.tri_indices = reinterpret_cast<const uint8_t*>(ds->primitive_index_buffer);
+    S.double_sided = ds->double_sided;
+    S.vertices = reinterpret_cast<vkgv_vertex*>(base);
+    S.draws = reinterpret_cast<vkgv_meshlet_draw*>(base + off_draws);
+    S.transform = reinterpret_cast<float*>(base + off_xf);
+    S.primitive = reinterpret_cast<vkgv_primitive*>(base + off_prim);
+    S.material = reinterpret_cast<vkgv_material*>(base + off_mat);
+    vkgv_scene scene{};
+    scene.draw_buffer = reinterpret_cast<uint64_t>(S.draws);
+    scene.transform_buffer = reinterpret_cast<uint64_t>(S.transform);
+    scene.primitive_buffer = reinterpret_cast<uint64_t>(S.primitive);
+    scene.material_buffer = reinterpret_cast<uint64_t>(S.material);
+    scene.meshlet_draw_count = ds->meshlet_count;
+    std::vector<vkgv_view> vv(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (backward && !views[i].target) return fail(ctx, VKGV_INVALID_ARG, "adjoint: backward needs a target");
+        vv[i] = vkgv_view{};
+        vv[i].camera_buffer = views[i].camera_buffer;
+        vv[i].width = views[i].width;
+        vv[i].height = views[i].height;
+        vv[i].depth_id = views[i].depth_id;
+    }
+    rc = ensure_views(ctx, n);
+    if (rc) return rc;
+    DeviceView *dv, *hv;
+    int slot = 0;
+    rc = acquire_slot(ctx, &slot, &dv, &hv);
+    if (rc) return rc;
+    Prepared P;
+    rc = build_views(ctx, &scene, vv.data(), n, 0, hv, P);
+    if (rc) return rc;
+    for (uint32_t i = 0; i < n; ++i) {
+        hv[i].diff_rgb = reinterpret_cast<float*>(views[i].rgb);
+        hv[i].diff_target = reinterpret_cast<const float*>(views[i].target);
+    }
+    rc = commit_views(ctx, slot, n, stream);
+    if (rc) return rc;
+    launch_diff_setup(S, stream);
+    launch_clear(dv, n, P.max_px, ctx->counters, kGlobalCounters, ctx->sm_count, stream);
+    launch_cull(P.S, dv, n, 0u, 1, ctx->status, ctx->sm_count, stream);
+    RasterLists l1{1, nullptr, nullptr, 0, 4};
+    launch_raster(P.S, dv, n, l1, ctx->raster, ctx->big, ctx->counters + 0, ctx->big_cap, ctx->status, ctx->sm_count,
+                  stream);
+    DiffArgs A{};
+    A.meshlets = S.meshlets;
+    A.vertex_indices = S.vertex_indices;
+    A.tri_indices = S.tri_indices;
+    A.positions = S.positions;
+    A.colors = reinterpret_cast<const float*>(ds->colors);
+    A.uvs = reinterpret_cast<const float*>(ds->uvs);
+    A.texture = reinterpret_cast<const float*>(ds->texture);
+    A.tex_w = ds->tex_width;
+    A.tex_h = ds->tex_height;
+    for (int k = 0; k < 3; ++k) A.albedo[k] = ds->albedo[k];
+    for (int k = 0; k < 2; ++k) {
+        A.uv_offset[k] = ds->uv_offset[k];
+        A.uv_scale[k] = ds->uv_scale[k];
+    }
+    A.uv_rotation = ds->uv_rotation;
+    A.scale = scale;
+    A.loss = reinterpret_cast<float*>(loss);
+    A.grad_positions = reinterpret_cast<float*>(gpos);
+    A.grad_colors = reinterpret_cast<float*>(gcol);
+    A.grad_texture = reinterpret_cast<float*>(gtex);
+    launch_diff_shade(A, dv, n, P.max_px, backward, stream);
+    rc = check_launch(ctx);
+    if (rc) return rc;
+    return close_slot(ctx, slot, stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int vkgv_diff_forward(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_diff_view* views, uint32_t view_count,
+                      void* stream) {
+    return diff_run(ctx, scene, views, view_count, false, 0.0f, 0, 0, 0, 0, stream);
+}
+
+int vkgv_diff_backward(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_diff_view* views, uint32_t view_count,
+                       float scale, uint64_t loss, uint64_t grad_positions, uint64_t grad_colors,
+                       uint64_t grad_texture, void* stream) {
+    return diff_run(ctx, scene, views, view_count, true, scale, loss, grad_positions, grad_colors, grad_texture,
+                    stream);
 }
 
 int vkgv_graph_capture(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, uint32_t view_count,

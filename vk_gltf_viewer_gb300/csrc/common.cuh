@@ -50,6 +50,8 @@ struct DeviceView {
     uint32_t* counters;
     uint32_t survivor_capacity;
     uint32_t _pad;
+    float* diff_rgb;            // adjoint: shaded linear RGB output (forward)
+    const float* diff_target;   // adjoint: target image (backward)
 };
 
 struct SceneArgs {

@@ -1,0 +1,247 @@
+// Adjoint of the textured resolve (an addition with no reference
+// implementation; the shading formula is the commented-out
+// visbuffer.frag.glsl:29-34 in linear RGB).
+//
+// Forward, per covered pixel of the visibility buffer:
+//   lambda = l / sum(l),  l = a x b,  a_k = x_k - nx w_k,  b_k = y_k - ny w_k
+//   col = sum lambda_k C_k,  uv = sum lambda_k UV_k
+//   uv' = R(rot) uv * scale + offset       (transformUv, mesh_common.h.glsl:129-135)
+//   tex = bilinear REPEAT sample of the fp32 RGB texture at uv'
+//   rgb = col * albedo * tex
+// Backward, with g = dL/drgb = 2 scale (rgb - target): the chain rule through
+// the texture's bilinear weights (texel gradients and d tex / d uv'), the
+// uv transform, the attribute interpolation (colour gradients), the
+// normalisation of lambda, the cross product and the clip transform
+// (position gradients).  Gradients are accumulated with fp32 atomics; the
+// visibility is the one the raster recomputes in the same call.
+#include "kernels.cuh"
+
+namespace vkgv {
+
+namespace {
+
+// Builds the internal raster scene of a differentiable mesh: the vertex
+// stream from the fp32 positions, one draw per meshlet, an identity node
+// transform, one primitive and one material.
+__global__ void k_diff_setup(DiffSetup S) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    for (uint32_t i = tid; i < S.vertex_count; i += stride) {
+        vkgv_vertex v;
+        v.position[0] = S.positions[3 * i];
+        v.position[1] = S.positions[3 * i + 1];
+        v.position[2] = S.positions[3 * i + 2];
+        v.color[0] = v.color[1] = v.color[2] = v.color[3] = 255;
+        v.normal[0] = v.normal[1] = v.normal[2] = 127;
+        v._pad = 0;
+        v.uv[0] = v.uv[1] = 0;
+        S.vertices[i] = v;
+    }
+    for (uint32_t i = tid; i < S.meshlet_count; i += stride) S.draws[i] = vkgv_meshlet_draw{0u, i, 0u};
+    if (tid < 16) S.transform[tid] = (tid % 5 == 0) ? 1.0f : 0.0f;
+    if (tid == 0) {
+        vkgv_primitive pr{};
+        pr.vertex_index_buffer = reinterpret_cast<uint64_t>(S.vertex_indices);
+        pr.primitive_index_buffer = reinterpret_cast<uint64_t>(S.tri_indices);
+        pr.vertex_buffer = reinterpret_cast<uint64_t>(S.vertices);
+        pr.meshlet_buffer = reinterpret_cast<uint64_t>(S.meshlets);
+        pr.meshlet_count = S.meshlet_count;
+        pr.material_index = 0;
+        *S.primitive = pr;
+        vkgv_material mt{};
+        mt.albedo_factor[0] = mt.albedo_factor[1] = mt.albedo_factor[2] = mt.albedo_factor[3] = 1.0f;
+        mt.albedo_index = VKGV_INVALID_HANDLE;
+        mt.uv_scale[0] = mt.uv_scale[1] = 1.0f;
+        mt.double_sided = S.double_sided;
+        *S.material = mt;
+    }
+}
+
+__device__ __forceinline__ int wrap(int i, int n) {
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+template <bool BACKWARD>
+__global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView* __restrict__ views) {
+    const DeviceView& V = views[blockIdx.y];
+    const uint32_t w = V.w, n = V.w * V.h;
+    const vkgv_meshlet* meshlets = A.meshlets;
+    float VP[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) VP[k] = V.cam->view_projection[k];
+    float sn, cs;
+    sincosf(A.uv_rotation, &sn, &cs);
+    float loss_acc = 0.0f;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint32_t lo = (uint32_t)V.depth_id[p];
+        float tgt[3] = {0.0f, 0.0f, 0.0f};
+        if (BACKWARD) {
+            tgt[0] = V.diff_target[3 * p];
+            tgt[1] = V.diff_target[3 * p + 1];
+            tgt[2] = V.diff_target[3 * p + 2];
+        }
+        if (lo == 0) {
+            if (BACKWARD) loss_acc += A.scale * (tgt[0] * tgt[0] + tgt[1] * tgt[1] + tgt[2] * tgt[2]);
+            else if (V.diff_rgb) V.diff_rgb[3 * p] = V.diff_rgb[3 * p + 1] = V.diff_rgb[3 * p + 2] = 0.0f;
+            continue;
+        }
+        const uint32_t id = lo - 1u;
+        const uint32_t m = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
+        const vkgv_meshlet ml = meshlets[m];
+        const uint8_t* tri = A.tri_indices + ml.triangle_offset + 3 * t;
+        uint32_t vi[3];
+        float c[3][4];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            vi[k] = A.vertex_indices[ml.vertex_offset + tri[k]];
+            const float* q = A.positions + 3 * (size_t)vi[k];
+            m4v(VP, q[0], q[1], q[2], 1.0f, c[k]);
+        }
+        const float nx = fsub(fmul(fdiv(fadd((float)(p % w), 0.5f), (float)V.w), 2.0f), 1.0f);
+        const float ny = fsub(fmul(fdiv(fadd((float)(p / w), 0.5f), (float)V.h), 2.0f), 1.0f);
+        float a[3], b[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            a[k] = fsub(c[k][0], fmul(nx, c[k][3]));
+            b[k] = fsub(c[k][1], fmul(ny, c[k][3]));
+        }
+        float l[3] = {fsub(fmul(a[1], b[2]), fmul(a[2], b[1])), fsub(fmul(a[2], b[0]), fmul(a[0], b[2])),
+                      fsub(fmul(a[0], b[1]), fmul(a[1], b[0]))};
+        const float sum = fadd(fadd(l[0], l[1]), l[2]);
+        if (!(sum != 0.0f)) {  // degenerate: shaded as empty, no gradient
+            if (BACKWARD) loss_acc += A.scale * (tgt[0] * tgt[0] + tgt[1] * tgt[1] + tgt[2] * tgt[2]);
+            else if (V.diff_rgb) V.diff_rgb[3 * p] = V.diff_rgb[3 * p + 1] = V.diff_rgb[3 * p + 2] = 0.0f;
+            continue;
+        }
+        float lam[3] = {fdiv(l[0], sum), fdiv(l[1], sum), fdiv(l[2], sum)};
+        float C[3][3], UV[3][2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) C[k][j] = A.colors[3 * (size_t)vi[k] + j];
+            UV[k][0] = A.uvs[2 * (size_t)vi[k]];
+            UV[k][1] = A.uvs[2 * (size_t)vi[k] + 1];
+        }
+        float col[3], uv[2];
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            col[j] = fadd(fadd(fmul(lam[0], C[0][j]), fmul(lam[1], C[1][j])), fmul(lam[2], C[2][j]));
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            uv[j] = fadd(fadd(fmul(lam[0], UV[0][j]), fmul(lam[1], UV[1][j])), fmul(lam[2], UV[2][j]));
+        const float ru = fadd(fmul(cs, uv[0]), fmul(sn, uv[1]));
+        const float rv = fadd(fmul(-sn, uv[0]), fmul(cs, uv[1]));
+        const float tu = fadd(fmul(ru, A.uv_scale[0]), A.uv_offset[0]);
+        const float tv = fadd(fmul(rv, A.uv_scale[1]), A.uv_offset[1]);
+        const float tx = fsub(fmul(tu, (float)A.tex_w), 0.5f), ty = fsub(fmul(tv, (float)A.tex_h), 0.5f);
+        const float fx = floorf(tx), fy = floorf(ty);
+        const float ax = fsub(tx, fx), ay = fsub(ty, fy);
+        const int x0 = wrap((int)fx, (int)A.tex_w), x1 = wrap((int)fx + 1, (int)A.tex_w);
+        const int y0 = wrap((int)fy, (int)A.tex_h), y1 = wrap((int)fy + 1, (int)A.tex_h);
+        const size_t i00 = 3 * ((size_t)y0 * A.tex_w + x0), i01 = 3 * ((size_t)y0 * A.tex_w + x1);
+        const size_t i10 = 3 * ((size_t)y1 * A.tex_w + x0), i11 = 3 * ((size_t)y1 * A.tex_w + x1);
+        float T00[3], T01[3], T10[3], T11[3], tex[3], rgb[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            T00[j] = A.texture[i00 + j];
+            T01[j] = A.texture[i01 + j];
+            T10[j] = A.texture[i10 + j];
+            T11[j] = A.texture[i11 + j];
+            const float top = fadd(T00[j], fmul(ax, fsub(T01[j], T00[j])));
+            const float bot = fadd(T10[j], fmul(ax, fsub(T11[j], T10[j])));
+            tex[j] = fadd(top, fmul(ay, fsub(bot, top)));
+            rgb[j] = fmul(fmul(col[j], A.albedo[j]), tex[j]);
+        }
+        if (!BACKWARD) {
+            if (V.diff_rgb) {
+                V.diff_rgb[3 * p] = rgb[0];
+                V.diff_rgb[3 * p + 1] = rgb[1];
+                V.diff_rgb[3 * p + 2] = rgb[2];
+            }
+            continue;
+        }
+        // ---- backward
+        float g[3], dcol[3], dtex[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float r = rgb[j] - tgt[j];
+            loss_acc += A.scale * r * r;
+            g[j] = 2.0f * A.scale * r;
+            dcol[j] = g[j] * A.albedo[j] * tex[j];
+            dtex[j] = g[j] * col[j] * A.albedo[j];
+        }
+        if (A.grad_texture) {
+            const float w00 = (1.0f - ax) * (1.0f - ay), w01 = ax * (1.0f - ay);
+            const float w10 = (1.0f - ax) * ay, w11 = ax * ay;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                atomicAdd(A.grad_texture + i00 + j, dtex[j] * w00);
+                atomicAdd(A.grad_texture + i01 + j, dtex[j] * w01);
+                atomicAdd(A.grad_texture + i10 + j, dtex[j] * w10);
+                atomicAdd(A.grad_texture + i11 + j, dtex[j] * w11);
+            }
+        }
+        // d tex / d uv' through the bilinear weights
+        float dtu = 0.0f, dtv = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            dtu += dtex[j] * ((1.0f - ay) * (T01[j] - T00[j]) + ay * (T11[j] - T10[j]));
+            dtv += dtex[j] * ((1.0f - ax) * (T10[j] - T00[j]) + ax * (T11[j] - T01[j]));
+        }
+        dtu *= (float)A.tex_w;
+        dtv *= (float)A.tex_h;
+        const float dru = dtu * A.uv_scale[0], drv = dtv * A.uv_scale[1];
+        const float du = cs * dru - sn * drv, dv = sn * dru + cs * drv;
+        float dlam[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            dlam[k] = dcol[0] * C[k][0] + dcol[1] * C[k][1] + dcol[2] * C[k][2] + du * UV[k][0] + dv * UV[k][1];
+            if (A.grad_colors)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) atomicAdd(A.grad_colors + 3 * (size_t)vi[k] + j, dcol[j] * lam[k]);
+        }
+        if (!A.grad_positions) continue;
+        const float dot = lam[0] * dlam[0] + lam[1] * dlam[1] + lam[2] * dlam[2];
+        const float dl[3] = {(dlam[0] - dot) / sum, (dlam[1] - dot) / sum, (dlam[2] - dot) / sum};
+        // l = a x b: dL/da = b x dl, dL/db = dl x a
+        const float da[3] = {b[1] * dl[2] - b[2] * dl[1], b[2] * dl[0] - b[0] * dl[2], b[0] * dl[1] - b[1] * dl[0]};
+        const float db[3] = {dl[1] * a[2] - dl[2] * a[1], dl[2] * a[0] - dl[0] * a[2], dl[0] * a[1] - dl[1] * a[0]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float dx = da[k], dy = db[k], dw = -nx * da[k] - ny * db[k];
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                atomicAdd(A.grad_positions + 3 * (size_t)vi[k] + q,
+                          VP[q * 4 + 0] * dx + VP[q * 4 + 1] * dy + VP[q * 4 + 3] * dw);
+        }
+    }
+    if (BACKWARD && A.loss) {
+        // warp-reduce the loss, one atomic per warp
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(A.loss, loss_acc);
+    }
+}
+
+}  // namespace
+
+void launch_diff_setup(const DiffSetup& S, cudaStream_t stream) {
+    const uint32_t n = S.vertex_count > S.meshlet_count ? S.vertex_count : S.meshlet_count;
+    uint32_t blocks = (n + 255) / 256;
+    blocks = blocks ? (blocks < 4096 ? blocks : 4096) : 1;
+    k_diff_setup<<<blocks, 256, 0, stream>>>(S);
+}
+
+void launch_diff_shade(const DiffArgs& A, const DeviceView* views, uint32_t nviews, uint64_t max_px, bool backward,
+                       cudaStream_t stream) {
+    uint32_t bx = (uint32_t)((max_px + 255) / 256);
+    if (bx > 65535u) bx = 65535u;
+    if (bx == 0) bx = 1;
+    dim3 grid(bx, nviews);
+    if (backward)
+        k_diff_shade<true><<<grid, 256, 0, stream>>>(A, views);
+    else
+        k_diff_shade<false><<<grid, 256, 0, stream>>>(A, views);
+}
+
+}  // namespace vkgv

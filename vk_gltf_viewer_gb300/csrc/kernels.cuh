@@ -33,4 +33,45 @@ void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews
                     uint32_t flags, cudaStream_t stream);
 void launch_finalize(const DeviceView* views, uint32_t nviews, cudaStream_t stream);
 
+// ---- adjoint of the resolve
+struct DiffSetup {
+    const float* positions;
+    uint32_t vertex_count;
+    uint32_t meshlet_count;
+    const vkgv_meshlet* meshlets;
+    const uint32_t* vertex_indices;
+    const uint8_t* tri_indices;
+    uint32_t double_sided;
+    uint32_t _pad;
+    vkgv_vertex* vertices;         // scratch outputs
+    vkgv_meshlet_draw* draws;
+    float* transform;
+    vkgv_primitive* primitive;
+    vkgv_material* material;
+};
+
+struct DiffArgs {
+    const vkgv_meshlet* meshlets;
+    const uint32_t* vertex_indices;
+    const uint8_t* tri_indices;
+    const float* positions;
+    const float* colors;
+    const float* uvs;
+    const float* texture;
+    uint32_t tex_w, tex_h;
+    float albedo[3];
+    float uv_offset[2];
+    float uv_scale[2];
+    float uv_rotation;
+    float scale;
+    float* loss;
+    float* grad_positions;
+    float* grad_colors;
+    float* grad_texture;
+};
+
+void launch_diff_setup(const DiffSetup& S, cudaStream_t stream);
+void launch_diff_shade(const DiffArgs& A, const DeviceView* views, uint32_t nviews, uint64_t max_px, bool backward,
+                       cudaStream_t stream);
+
 }  // namespace vkgv

@@ -547,11 +547,14 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
     }
 }
 
-// Drains the binned rectangles: one CTA per rectangle, 64 x 4 threads.
+// Drains the binned rectangles: one CTA per rectangle, its 256 threads laid
+// out as chunk x (256 / chunk).
 __global__ void __launch_bounds__(256) k_raster_big(const BigTri* __restrict__ q, const uint32_t* count,
-                                                    uint32_t cap, const DeviceView* __restrict__ views) {
+                                                    uint32_t cap, const DeviceView* __restrict__ views,
+                                                    uint32_t chunk) {
     const uint32_t n = min(*count, cap);
-    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
+    const int tx = (int)(threadIdx.x % chunk), ty = (int)(threadIdx.x / chunk);
+    const int rows = (int)(256 / chunk);
     for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
         const BigTri t = q[e];
         const DeviceView& V = views[t.view];
@@ -565,10 +568,10 @@ __global__ void __launch_bounds__(256) k_raster_big(const BigTri* __restrict__ q
             const int32_t dx = t.x[b] - t.x[a], dy = t.y[b] - t.y[a];
             bias[k] = (dy < 0 || (dy == 0 && dx > 0)) ? 0 : 1;
         }
-        for (int py = t.py0 + ty; py <= (int)t.py1; py += 4) {
+        for (int py = t.py0 + ty; py <= (int)t.py1; py += rows) {
             const int32_t sy = py * 256 + 128;
             const float zrow = __fmaf_rn(t.pb, __int2float_rn(sy - t.y[0]), t.z0);
-            for (int px = t.px0 + tx; px <= (int)t.px1; px += 64) {
+            for (int px = t.px0 + tx; px <= (int)t.px1; px += (int)chunk) {
                 const int32_t sx = px * 256 + 128;
                 bool covered = true;
 #pragma unroll
@@ -619,7 +622,8 @@ void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews,
         default: launch_variant<4>(P, grid, stream); break;
     }
     if (between) cudaEventRecord(between, stream);
-    k_raster_big<<<sm_count * 8, 256, 0, stream>>>(big, big_count, big_capacity, views);
+    const uint32_t chunk = cfg.chunk >= 8 && cfg.chunk <= 64 ? cfg.chunk : 32;
+    k_raster_big<<<sm_count * 8, 256, 0, stream>>>(big, big_count, big_capacity, views, chunk);
 }
 
 }  // namespace vkgv

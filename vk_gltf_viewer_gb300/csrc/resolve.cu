@@ -35,6 +35,23 @@ __device__ __forceinline__ float to_linear(float c) {
     return cutoff ? lower : higher;
 }
 
+// The textured resolve is compared within 1/255; its sRGB curves use the
+// hardware exp2/log2 pow (relative error ~1e-6, which can move a channel by
+// one step only at a rounding boundary).
+__device__ __forceinline__ float from_linear_fast(float c) {
+    const bool cutoff = c < 0.0031308f;
+    const float higher = fsub(fmul(1.055f, __powf(c, 1.0f / 2.4f)), 0.055f);
+    const float lower = fmul(c, 12.92f);
+    return cutoff ? lower : higher;
+}
+
+__device__ __forceinline__ float to_linear_fast(float c) {
+    const bool cutoff = c < 0.04045f;
+    const float higher = __powf(fdiv(fadd(c, 0.055f), 1.055f), 2.4f);
+    const float lower = fdiv(c, 12.92f);
+    return cutoff ? lower : higher;
+}
+
 __device__ __forceinline__ uint32_t unorm8(float c) {
     if (!(c > 0.0f)) return 0;
     if (c > 1.0f) c = 1.0f;
@@ -46,7 +63,20 @@ __device__ __forceinline__ uint32_t pack_rgba(const float lin[4]) {
            (unorm8(lin[3]) << 24);
 }
 
+__device__ __forceinline__ uint32_t pack_rgba_fast(const float lin[4]) {
+    return unorm8(from_linear_fast(lin[0])) | (unorm8(from_linear_fast(lin[1])) << 8) |
+           (unorm8(from_linear_fast(lin[2])) << 16) | (unorm8(lin[3]) << 24);
+}
+
 __device__ __forceinline__ float lerp(float a, float b, float t) { return fadd(a, fmul(t, fsub(b, a))); }
+
+// Total survivors of the frame (pass 1 + pass 2) into the caller's counter.
+__device__ __forceinline__ void finalize_view(const DeviceView& V) {
+    if (!V.survivor_count) return;
+    const uint32_t c0 = min(V.counters[0], V.survivor_capacity);
+    const uint32_t c2 = min(V.counters[2], V.survivor_capacity - c0);
+    *V.survivor_count = c0 + c2;
+}
 
 // Bilinear REPEAT sample, texel centres at +0.5.  Textured shading of a
 // high-frequency texture is very sensitive to the sample position, so every
@@ -148,7 +178,8 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
     float sampled[4] = {1.0f, 1.0f, 1.0f, 1.0f};
     if (mat.albedo_index != VKGV_INVALID_HANDLE && mat.albedo_index < S.texture_count) {
         // transformUv (mesh_common.h.glsl:129-135): rotate, scale, offset
-        const float cs = cosf(mat.uv_rotation), sn = sinf(mat.uv_rotation);
+        float sn, cs;
+        sincosf(mat.uv_rotation, &sn, &cs);
         const float ru = fadd(fmul(cs, uv[0]), fmul(sn, uv[1]));
         const float rv = fadd(fmul(-sn, uv[0]), fmul(cs, uv[1]));
         const float tu = fadd(fmul(ru, mat.uv_scale[0]), mat.uv_offset[0]);
@@ -157,7 +188,7 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
         sample_texture(tex, tu, tv, sampled);
         if (tex.format == VKGV_TEXTURE_RGBA8)
 #pragma unroll
-            for (int k = 0; k < 3; ++k) sampled[k] = to_linear(sampled[k]);
+            for (int k = 0; k < 3; ++k) sampled[k] = to_linear_fast(sampled[k]);
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) out[k] = fmul(fmul(col[k], mat.albedo_factor[k]), sampled[k]);
@@ -169,6 +200,7 @@ __global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* 
     const uint32_t w = V.w, n = V.w * V.h;
     uint32_t* ids = (flags & VKGV_WRITE_IDS) ? V.ids : nullptr;
     uint32_t* rgba = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED)) ? V.rgba : nullptr;
+    if (blockIdx.x == 0 && threadIdx.x == 0) finalize_view(V);
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const uint32_t lo = (uint32_t)__ldcs(V.depth_id + p);
         const uint32_t id = lo ? lo - 1u : VKGV_VISBUFFER_CLEAR;
@@ -188,7 +220,7 @@ __global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* 
                 lin[2] = a.z;
                 lin[3] = a.w;
             }
-            out = pack_rgba(lin);
+            out = TEXTURED ? pack_rgba_fast(lin) : pack_rgba(lin);
         }
         __stcs(rgba + p, out);
     }
@@ -214,11 +246,7 @@ __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ vi
 __global__ void k_finalize(const DeviceView* __restrict__ views, uint32_t nviews) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nviews) return;
-    const DeviceView& V = views[v];
-    if (!V.survivor_count) return;
-    const uint32_t c0 = min(V.counters[0], V.survivor_capacity);
-    const uint32_t c2 = min(V.counters[2], V.survivor_capacity - c0);
-    *V.survivor_count = c0 + c2;
+    finalize_view(views[v]);
 }
 
 }  // namespace
