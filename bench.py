@@ -46,6 +46,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batched-only", action="store_true",
                    help="run only the batched leg (for profiling); prints its own JSON line")
+    p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--adjoint-only", action="store_true",
+                   help="run only the adjoint legs (for profiling); prints their own JSON line")
     return p.parse_args()
 
 
@@ -195,14 +198,125 @@ def run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier):
     if pg:
         pg.all_reduce(tb, op=pg.ReduceOp.MAX)
     bval = world * bsteps * len(bv) / float(tb.item())
+    kernels_per_launch = bgraph.kernel_count()
+    bgraph.close()
+
+    # The same poses through the plain single-view path: one captured
+    # single-view frame per pose, replayed back to back on the stream.
+    singles = [r.capture(dev, [vb], flags) for vb in bv]
+    for g in singles:
+        g.launch()
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    s0.record(stream)
+    for _ in range(bsteps):
+        for g in singles:
+            g.launch()
+    s1.record(stream)
+    torch.cuda.synchronize()
+    ts = torch.tensor([s0.elapsed_time(s1) / 1000.0], device=f"cuda:{local}")
+    if pg:
+        pg.all_reduce(ts, op=pg.ReduceOp.MAX)
+    sval = world * bsteps * len(bv) / float(ts.item())
+    for g in singles:
+        g.close()
     out = {"value": bval, "unit": "views/s", "views_per_launch": len(bv), "steps": bsteps,
-           "ms_per_launch": 1000.0 * float(tb.item()) / bsteps, "kernels_per_launch": bgraph.kernel_count(),
+           "single_view_same_poses": {"value": sval, "unit": "views/s",
+                                      "ms_per_pass": 1000.0 * float(ts.item()) / bsteps},
+           "speedup_vs_single_view_same_poses": bval / sval,
+           "ms_per_launch": 1000.0 * float(tb.item()) / bsteps, "kernels_per_launch": kernels_per_launch,
            "mean_pixels_per_view": float(np.mean([vb.width * vb.height for vb in bv])),
            "stages_ms": stages,
            "config": f"{len(bv)} poses on a radius-30 sphere around the grid centre, sizes uniform over "
                      "256^2, 512x384, 1024x576, 1280x720, 1920x1080"}
-    bgraph.close()
     return out
+
+
+def sphere_poses(rng, n, radius=3.0):
+    """n eye points uniform on a sphere, aimed at the origin."""
+    import numpy as np
+    v = rng.normal(size=(n, 3))
+    return radius * v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def run_adjoint_case(r, local, level, displace, tex_size, sizes, seed, steps, warmup, stream):
+    """One adjoint workload: zero + forward + backward (MSE against target
+    renders) over all views in one captured graph; returns ms/view and the
+    device memory the workload holds."""
+    import numpy as np
+    import torch
+
+    from vk_gltf_viewer_gb300 import diff, scene
+
+    dev = torch.device("cuda", local)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    torch.cuda.reset_peak_memory_stats(dev)
+    alloc0 = torch.cuda.memory_allocated(dev)
+    free0, total = torch.cuda.mem_get_info(dev)
+    rng = np.random.default_rng(seed)
+    mesh = scene.icosphere(level, displace=displace, seed=seed)
+    nv = mesh.positions.shape[0]
+    colors = rng.uniform(0, 1, size=(nv, 3)).astype(np.float32)
+    texture = rng.uniform(0, 1, size=(tex_size, tex_size, 3)).astype(np.float32)
+    ds = diff.DiffScene.create(mesh, colors, texture, device=dev)
+    trng = np.random.default_rng(seed + 1000)
+    pos_t = mesh.positions + trng.normal(0, 0.01, size=mesh.positions.shape).astype(np.float32)
+    tex_t = trng.uniform(0, 1, size=texture.shape).astype(np.float32)
+    dt = diff.DiffScene.create(mesh, colors, tex_t, device=dev, positions=pos_t)
+    views, targets, rgb = [], [], []
+    for eye, (w, h) in zip(sphere_poses(rng, len(sizes)), sizes):
+        cam = scene.camera(tuple(eye), (0, 0, 0), scene.safe_up(eye, (0, 0, 0)), 60.0, w / h)
+        views.append(diff.DiffViewBuffers.allocate(w, h, cam, device=dev))
+        targets.append(torch.empty(w * h * 3, device=dev))
+        rgb.append(torch.empty(w * h * 3, device=dev))
+    diff.forward(r, dt, views, targets)
+    gp, gc, gt = torch.empty_like(ds.positions), torch.empty_like(ds.colors), torch.empty_like(ds.texture)
+    loss = torch.zeros(1, device=dev)
+    px = sum(w * h for w, h in sizes)
+    g = diff.capture_step(r, ds, views, rgb_out=rgb, targets=targets, grad_positions=gp, grad_colors=gc,
+                          grad_texture=gt, scale=1.0 / (3 * px), loss=loss)
+    for _ in range(max(3, warmup)):
+        g.launch()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        g.launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    out = {"ms_per_view": ms / len(sizes), "ms_per_step": ms, "views": len(sizes), "pixels_per_step": px,
+           "triangles": mesh.triangle_count, "vertices": nv, "texture": f"{tex_size}x{tex_size} fp32 RGB",
+           "kernels_per_step": g.kernel_count(), "loss": float(loss.item()),
+           "device_bytes_held": int(free0 - free1),
+           "peak_tensor_bytes": int(torch.cuda.max_memory_allocated(dev) - alloc0)}
+    g.close()
+    del ds, dt, views, targets, rgb, gp, gc, gt
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_adjoint(r, local, args, stream):
+    """Adjoint legs: the 64-view 512^2 icosphere-5 case and the batched
+    512-view uneven-resolution icosphere-8 case (one graph per step)."""
+    import numpy as np
+
+    steps = max(3, min(args.steps, 10))
+    c4 = run_adjoint_case(r, local, 5, 0.0, 1024, [(512, 512)] * 64, 41, steps, args.warmup, stream)
+    c4["config"] = ("icosphere level 5 (20,480 tris), per-vertex colours U(0,1), 1024^2 fp32 texture, 64 views "
+                    "512^2 on a radius-3 sphere, MSE vs renders of N(0,0.01^2)-perturbed positions and a "
+                    "separately seeded texture; step = zero + forward + backward in one graph")
+    rng = np.random.default_rng(77)
+    sides = rng.integers(256, 1025, size=512)
+    c5 = run_adjoint_case(r, local, 8, 0.02, 2048, [(int(s), int(s)) for s in sides], 43, max(2, steps // 3),
+                          args.warmup, stream)
+    c5["config"] = ("icosphere level 8 (1,310,720 tris) with seeded normal displacement 0.02, 2048^2 fp32 "
+                    "texture, 512 square views with sides uniform in [256, 1024] on a radius-3 sphere; "
+                    "zero + forward + backward (visibility recomputed) in one graph")
+    return {"c4": c4, "c5": c5}
 
 
 # ------------------------------------------------------------------- ours
@@ -244,6 +358,12 @@ def main():
         out = run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier)
         if rank == 0:
             print(json.dumps({"metric": METRIC, "batched": out}), flush=True)
+        r.close()
+        return
+    if args.adjoint_only:
+        out = run_adjoint(r, local, args, stream)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "adjoint": out}), flush=True)
         r.close()
         return
     cam = scene.grid_camera(W1080, H1080)
@@ -357,6 +477,11 @@ def main():
         batched = run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier)
         batched["speedup_vs_single_view"] = batched["value"] / value
 
+    # ---- adjoint legs (ms/view)
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = run_adjoint(r, local, args, stream)
+
     # ---- CPU baseline: the oracle on the host cores, bounded sample
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -399,6 +524,8 @@ def main():
         }
         if batched:
             out["batched"] = batched
+        if adjoint:
+            out["adjoint"] = adjoint
         print(json.dumps(out), flush=True)
     if pg:
         pg.destroy_process_group()

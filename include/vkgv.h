@@ -305,6 +305,27 @@ int vkgv_graph_destroy(vkgv_graph* graph);
 /* Number of kernel launches one vkgv_graph_launch performs. */
 int vkgv_graph_kernel_count(const vkgv_graph* graph, uint32_t* out_count);
 
+/* ------------------------------------------------------------- autotuner */
+/* An addition with no reference counterpart (the reference's mesh-shader
+ * workgroup sizes are fixed at pipeline creation).  Sweeps raster bin size
+ * {8, 16, 32} x meshlets per CTA {1, 2, 4}: for each candidate a context
+ * built from `base` with those two fields captures this frame as a graph,
+ * launches it once to warm up, then `launches` times between CUDA events on
+ * a private stream.  The candidates render into the caller's views (every
+ * candidate produces the same visibility; the parity tests cover each).
+ * Writes up to entry_capacity entries (in sweep order) and the fastest
+ * configuration into *best. */
+typedef struct vkgv_tune_entry {
+    uint32_t bin_size;
+    uint32_t meshlets_per_cta;
+    float ms_per_launch;
+    uint32_t _pad;
+} vkgv_tune_entry;
+
+int vkgv_autotune(const vkgv_config* base, const vkgv_scene* scene, const vkgv_view* views, uint32_t view_count,
+                  uint32_t flags, uint32_t launches, vkgv_tune_entry* entries, uint32_t entry_capacity,
+                  uint32_t* out_entry_count, vkgv_config* best);
+
 /* ------------------------------------------------ adjoint of the resolve */
 /* An addition with no reference implementation: a differentiable form of
  * the textured resolve (the commented-out visbuffer.frag.glsl:29-34) over
@@ -339,19 +360,36 @@ typedef struct vkgv_diff_view {
     uint32_t width, height;
     uint64_t depth_id;       /* uint64[W*H] visibility scratch, 16-byte aligned */
     uint64_t rgb;            /* float[3*W*H] shaded output, or 0           */
-    uint64_t target;         /* float[3*W*H] target image (backward)       */
+    uint64_t target;         /* float[3*W*H] MSE target (backward), or 0   */
+    uint64_t grad_rgb;       /* float[3*W*H] dL/drgb (backward, used when target is 0) */
 } vkgv_diff_view;
 
 /* Renders every view's shaded linear RGB into view.rgb. */
 int vkgv_diff_forward(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_diff_view* views,
                       uint32_t view_count, void* stream);
-/* Loss L = scale * sum over views, pixels and channels of (rgb - target)^2
- * (empty pixels contribute (0 - target)^2).  Accumulates L into *loss and
- * dL/dpositions, dL/dcolors, dL/dtexels into the three gradient arrays
- * (fp32 atomics; zero them first).  Any gradient pointer may be 0. */
+/* Backward pass.  With view.target: L = scale * sum over views, pixels and
+ * channels of (rgb - target)^2 (empty pixels contribute target^2), which is
+ * accumulated into *loss.  Without a target, view.grad_rgb gives dL/drgb.
+ * Accumulates dL/dpositions, dL/dcolors and dL/dtexels into the three
+ * gradient arrays (fp32 atomics; zero them first); any of them may be 0. */
 int vkgv_diff_backward(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_diff_view* views,
                        uint32_t view_count, float scale, uint64_t loss, uint64_t grad_positions,
                        uint64_t grad_colors, uint64_t grad_texture, void* stream);
+
+/* Passes recorded by vkgv_diff_graph_capture, in this order. */
+enum {
+    VKGV_DIFF_ZERO_GRADS = 1, /* memset loss and the gradient arrays to 0    */
+    VKGV_DIFF_FORWARD = 2,    /* visibility + shading into view.rgb          */
+    VKGV_DIFF_BACKWARD = 4    /* visibility recomputed + gradients           */
+};
+/* Captures the selected passes over these views into one CUDA graph (a
+ * training step: zero, forward, backward), launched with vkgv_graph_launch.
+ * Pointers, sizes, scale and view count are baked in; parameter, camera and
+ * target contents may change between launches. */
+int vkgv_diff_graph_capture(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_diff_view* views,
+                            uint32_t view_count, uint32_t passes, float scale, uint64_t loss,
+                            uint64_t grad_positions, uint64_t grad_colors, uint64_t grad_texture,
+                            vkgv_graph** out_graph);
 
 /* ---------------------------------------------- host scene producers (A15) */
 /* Replace the glTF import + meshletiser (src/vk_gltf_viewer/assets.cpp:288-430)

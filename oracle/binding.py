@@ -229,6 +229,60 @@ def frustum_visible(center, extents, planes) -> bool:
     return bool(load().orc_frustum_visible(_addr(c), _addr(e), _addr(p)))
 
 
+class OrcDiffScene(C.Structure):
+    _fields_ = [("meshlets", C.c_void_p), ("vertex_indices", C.c_void_p), ("tri_indices", C.c_void_p),
+                ("positions", C.c_void_p), ("colors", C.c_void_p), ("uvs", C.c_void_p), ("texture", C.c_void_p),
+                ("tex_w", C.c_uint32), ("tex_h", C.c_uint32), ("albedo", C.c_double * 3),
+                ("uv_offset", C.c_double * 2), ("uv_scale", C.c_double * 2), ("uv_rotation", C.c_double)]
+
+
+def diff_f64(mesh, positions, colors, uvs, texture, vp16, w: int, h: int, ids: np.ndarray,
+             target: np.ndarray | None = None, scale: float = 1.0, albedo=(1.0, 1.0, 1.0), uv_offset=(0.0, 0.0),
+             uv_scale=(1.0, 1.0), uv_rotation: float = 0.0, want_rgb=False, want_grads=False,
+             cells: np.ndarray | None = None):
+    """float64 shading/loss/gradients at fixed visibility `ids` (uint32 per
+    pixel).  Parameters are converted to float64.  Returns (loss, rgb or None,
+    (gpos, gcol, gtex) or None).  `cells`, an int32 array of 2*w*h, receives
+    each pixel's unwrapped bilinear cell (INT32_MIN for empty pixels)."""
+    lib = load()
+    if not hasattr(lib.orc_diff_f64, "_typed"):
+        lib.orc_diff_f64.restype = C.c_double
+        lib.orc_diff_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                     C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.orc_diff_f64._typed = True
+    keep = [np.ascontiguousarray(mesh.meshlets), np.ascontiguousarray(mesh.vertex_indices),
+            np.ascontiguousarray(mesh.primitive_indices), np.ascontiguousarray(positions, np.float64),
+            np.ascontiguousarray(colors, np.float64), np.ascontiguousarray(uvs, np.float64),
+            np.ascontiguousarray(texture, np.float64)]
+    s = OrcDiffScene(meshlets=_addr(keep[0]), vertex_indices=_addr(keep[1]), tri_indices=_addr(keep[2]),
+                     positions=_addr(keep[3]), colors=_addr(keep[4]), uvs=_addr(keep[5]), texture=_addr(keep[6]),
+                     tex_w=int(np.asarray(texture).shape[1]), tex_h=int(np.asarray(texture).shape[0]),
+                     uv_rotation=float(uv_rotation))
+    s.albedo[:] = list(albedo)
+    s.uv_offset[:] = list(uv_offset)
+    s.uv_scale[:] = list(uv_scale)
+    vp = np.ascontiguousarray(vp16, np.float32)
+    ids = np.ascontiguousarray(ids, np.uint32)
+    tgt = None if target is None else np.ascontiguousarray(target, np.float32)
+    rgb = np.zeros(w * h * 3, np.float64) if want_rgb else None
+    grads = None
+    if want_grads:
+        grads = (np.zeros(keep[3].size), np.zeros(keep[4].size), np.zeros(keep[6].size))
+    loss = lib.orc_diff_f64(C.addressof(s), _addr(vp), w, h, _addr(ids), _addr(tgt) if tgt is not None else None,
+                            float(scale), _addr(rgb) if rgb is not None else None,
+                            *(tuple(_addr(g) for g in grads) if grads else (None, None, None)),
+                            _cells_addr(cells, w, h))
+    return float(loss), rgb, grads
+
+
+def _cells_addr(cells, w, h):
+    if cells is None:
+        return None
+    if cells.dtype != np.int32 or cells.size != 2 * w * h or not cells.flags.c_contiguous:
+        raise ValueError("cells must be a contiguous int32 array of 2*w*h")
+    return _addr(cells)
+
+
 def from_linear(c: float) -> float:
     return float(load().orc_from_linear(c))
 

@@ -863,3 +863,138 @@ void orc_frame(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h
     free(rej);
     *nsurv = total;
 }
+
+/* ------------------------------------------------- adjoint (float64) */
+
+static int wrapi(int64_t i, int64_t n) {
+    int64_t r = i % n;
+    return (int)(r < 0 ? r + n : r);
+}
+
+/* Forward shading and its exact derivative in float64 at fixed visibility
+ * (the differentiable form of the commented-out visbuffer.frag.glsl:29-34;
+ * transformUv as mesh_common.h.glsl:129-135). */
+double orc_diff_f64(const orc_diff_scene* s, const float vpf[16], uint32_t w, uint32_t h, const uint32_t* ids,
+                    const float* target, double scale, double* rgb_out, double* gpos, double* gcol, double* gtex,
+                    int32_t* cells) {
+    double vp[16];
+    for (int k = 0; k < 16; ++k) vp[k] = vpf[k];
+    const double cs = cos(s->uv_rotation), sn = sin(s->uv_rotation);
+    double loss = 0.0;
+    for (uint32_t py = 0; py < h; ++py)
+        for (uint32_t px = 0; px < w; ++px) {
+            const size_t p = (size_t)py * w + px;
+            double tg[3] = {0, 0, 0};
+            if (target)
+                for (int j = 0; j < 3; ++j) tg[j] = target[3 * p + j];
+            const uint32_t id = ids[p];
+            double shade[3] = {0, 0, 0};
+            if (cells) cells[2 * p] = cells[2 * p + 1] = INT32_MIN;
+            if (id == 0xFFFFFFFFu) {
+                if (rgb_out)
+                    for (int j = 0; j < 3; ++j) rgb_out[3 * p + j] = 0.0;
+                for (int j = 0; j < 3; ++j) loss += scale * tg[j] * tg[j];
+                continue;
+            }
+            const orc_meshlet* ml = &s->meshlets[id >> 7];
+            const uint8_t* tri = s->tri_indices + ml->triangle_offset + 3 * (id & 127u);
+            uint32_t vi[3];
+            double c[3][4];
+            for (int k = 0; k < 3; ++k) {
+                vi[k] = s->vertex_indices[ml->vertex_offset + tri[k]];
+                const double* q = s->positions + 3 * (size_t)vi[k];
+                for (int r = 0; r < 4; ++r) c[k][r] = vp[0 * 4 + r] * q[0] + vp[1 * 4 + r] * q[1] + vp[2 * 4 + r] * q[2] + vp[3 * 4 + r];
+            }
+            const double nx = ((double)px + 0.5) / (double)w * 2.0 - 1.0;
+            const double ny = ((double)py + 0.5) / (double)h * 2.0 - 1.0;
+            double a[3], b[3];
+            for (int k = 0; k < 3; ++k) {
+                a[k] = c[k][0] - nx * c[k][3];
+                b[k] = c[k][1] - ny * c[k][3];
+            }
+            const double l[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+            const double sum = l[0] + l[1] + l[2];
+            if (sum == 0.0) {
+                if (rgb_out)
+                    for (int j = 0; j < 3; ++j) rgb_out[3 * p + j] = 0.0;
+                for (int j = 0; j < 3; ++j) loss += scale * tg[j] * tg[j];
+                continue;
+            }
+            const double lam[3] = {l[0] / sum, l[1] / sum, l[2] / sum};
+            double col[3], uv[2];
+            for (int j = 0; j < 3; ++j)
+                col[j] = lam[0] * s->colors[3 * (size_t)vi[0] + j] + lam[1] * s->colors[3 * (size_t)vi[1] + j] +
+                         lam[2] * s->colors[3 * (size_t)vi[2] + j];
+            for (int j = 0; j < 2; ++j)
+                uv[j] = lam[0] * s->uvs[2 * (size_t)vi[0] + j] + lam[1] * s->uvs[2 * (size_t)vi[1] + j] +
+                        lam[2] * s->uvs[2 * (size_t)vi[2] + j];
+            const double ru = cs * uv[0] + sn * uv[1], rv = -sn * uv[0] + cs * uv[1];
+            const double tu = ru * s->uv_scale[0] + s->uv_offset[0], tv = rv * s->uv_scale[1] + s->uv_offset[1];
+            const double tx = tu * s->tex_w - 0.5, ty = tv * s->tex_h - 0.5;
+            const double fx = floor(tx), fy = floor(ty);
+            const double ax = tx - fx, ay = ty - fy;
+            if (cells) {
+                cells[2 * p] = (int32_t)fx;
+                cells[2 * p + 1] = (int32_t)fy;
+            }
+            const int x0 = wrapi((int64_t)fx, s->tex_w), x1 = wrapi((int64_t)fx + 1, s->tex_w);
+            const int y0 = wrapi((int64_t)fy, s->tex_h), y1 = wrapi((int64_t)fy + 1, s->tex_h);
+            const size_t i00 = 3 * ((size_t)y0 * s->tex_w + x0), i01 = 3 * ((size_t)y0 * s->tex_w + x1);
+            const size_t i10 = 3 * ((size_t)y1 * s->tex_w + x0), i11 = 3 * ((size_t)y1 * s->tex_w + x1);
+            const double* T = s->texture;
+            double tex[3];
+            for (int j = 0; j < 3; ++j) {
+                const double top = T[i00 + j] + ax * (T[i01 + j] - T[i00 + j]);
+                const double bot = T[i10 + j] + ax * (T[i11 + j] - T[i10 + j]);
+                tex[j] = top + ay * (bot - top);
+                shade[j] = col[j] * s->albedo[j] * tex[j];
+            }
+            if (rgb_out)
+                for (int j = 0; j < 3; ++j) rgb_out[3 * p + j] = shade[j];
+            double g[3], dcol[3], dtex[3];
+            for (int j = 0; j < 3; ++j) {
+                const double r = shade[j] - tg[j];
+                loss += scale * r * r;
+                g[j] = 2.0 * scale * r;
+                dcol[j] = g[j] * s->albedo[j] * tex[j];
+                dtex[j] = g[j] * col[j] * s->albedo[j];
+            }
+            if (gtex) {
+                const double w00 = (1 - ax) * (1 - ay), w01 = ax * (1 - ay), w10 = (1 - ax) * ay, w11 = ax * ay;
+                for (int j = 0; j < 3; ++j) {
+                    gtex[i00 + j] += dtex[j] * w00;
+                    gtex[i01 + j] += dtex[j] * w01;
+                    gtex[i10 + j] += dtex[j] * w10;
+                    gtex[i11 + j] += dtex[j] * w11;
+                }
+            }
+            double dtu = 0, dtv = 0;
+            for (int j = 0; j < 3; ++j) {
+                dtu += dtex[j] * ((1 - ay) * (T[i01 + j] - T[i00 + j]) + ay * (T[i11 + j] - T[i10 + j]));
+                dtv += dtex[j] * ((1 - ax) * (T[i10 + j] - T[i00 + j]) + ax * (T[i11 + j] - T[i01 + j]));
+            }
+            dtu *= s->tex_w;
+            dtv *= s->tex_h;
+            const double dru = dtu * s->uv_scale[0], drv = dtv * s->uv_scale[1];
+            const double du = cs * dru - sn * drv, dv = sn * dru + cs * drv;
+            double dlam[3];
+            for (int k = 0; k < 3; ++k) {
+                dlam[k] = du * s->uvs[2 * (size_t)vi[k]] + dv * s->uvs[2 * (size_t)vi[k] + 1];
+                for (int j = 0; j < 3; ++j) {
+                    dlam[k] += dcol[j] * s->colors[3 * (size_t)vi[k] + j];
+                    if (gcol) gcol[3 * (size_t)vi[k] + j] += dcol[j] * lam[k];
+                }
+            }
+            if (!gpos) continue;
+            const double dot = lam[0] * dlam[0] + lam[1] * dlam[1] + lam[2] * dlam[2];
+            const double dl[3] = {(dlam[0] - dot) / sum, (dlam[1] - dot) / sum, (dlam[2] - dot) / sum};
+            const double da[3] = {b[1] * dl[2] - b[2] * dl[1], b[2] * dl[0] - b[0] * dl[2], b[0] * dl[1] - b[1] * dl[0]};
+            const double db[3] = {dl[1] * a[2] - dl[2] * a[1], dl[2] * a[0] - dl[0] * a[2], dl[0] * a[1] - dl[1] * a[0]};
+            for (int k = 0; k < 3; ++k) {
+                const double dx = da[k], dy = db[k], dw = -nx * da[k] - ny * db[k];
+                for (int q = 0; q < 3; ++q)
+                    gpos[3 * (size_t)vi[k] + q] += vp[q * 4 + 0] * dx + vp[q * 4 + 1] * dy + vp[q * 4 + 3] * dw;
+            }
+        }
+    return loss;
+}

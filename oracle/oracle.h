@@ -135,6 +135,37 @@ void orc_frame(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h
                uint32_t* ids, uint32_t* rgba, float* pyramid_out,
                uint32_t* survivors, uint32_t* nsurv);
 
+/* Adjoint reference in float64 (the differentiable textured resolve, an
+ * addition with no reference implementation).  Parameters are doubles so
+ * that finite differences see the perturbation exactly.  For the visibility
+ * ids of each pixel (0xFFFFFFFF = empty; draw index = meshlet index, identity
+ * node transform):
+ *   rgb = interp(colour) * albedo * bilinearREPEAT(texture, transformUv(interp(uv)))
+ *   L   = scale * sum (rgb - target)^2
+ * Returns L; writes rgb (if non-NULL) and ACCUMULATES the gradients into
+ * gpos / gcol / gtex (each may be NULL). */
+typedef struct orc_diff_scene {
+    const orc_meshlet* meshlets;
+    const uint32_t* vertex_indices;
+    const uint8_t* tri_indices;
+    const double* positions; /* 3 per vertex */
+    const double* colors;    /* 3 per vertex */
+    const double* uvs;       /* 2 per vertex */
+    const double* texture;   /* 3 per texel */
+    uint32_t tex_w, tex_h;
+    double albedo[3], uv_offset[2], uv_scale[2], uv_rotation;
+} orc_diff_scene;
+
+double orc_diff_f64(const orc_diff_scene* s, const float vp[16], uint32_t w, uint32_t h, const uint32_t* ids,
+                    const float* target, double scale, double* rgb, double* gpos, double* gcol, double* gtex,
+                    int32_t* cells);
+/* cells (if non-NULL) receives, per pixel, the unwrapped bilinear cell
+ * (floor(u*W - 0.5), floor(v*H - 0.5)), or INT32_MIN twice for an empty
+ * pixel.  Bilinear filtering is only piecewise smooth: its derivative jumps
+ * where a sample crosses a texel centre, so a finite difference in the
+ * positions is a valid check of the analytic gradient only while no pixel's
+ * cell changes across the stencil. */
+
 /* Single-fragment helpers exported for the known-answer tests. */
 float orc_from_linear(float c);
 float orc_to_linear(float c);

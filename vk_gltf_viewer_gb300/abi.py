@@ -40,6 +40,11 @@ RESOLVE_TEXTURED = 1 << 5
 BUILD_PYRAMID = 1 << 6
 WRITE_IDS = 1 << 7
 SKIP_CLEAR = 1 << 8
+
+# passes of vkgv_diff_graph_capture
+DIFF_ZERO_GRADS = 1
+DIFF_FORWARD = 2
+DIFF_BACKWARD = 4
 FRAME_REFERENCE = CULL_FRUSTUM | CULL_OCCLUSION | RESOLVE_FLAT | BUILD_PYRAMID | WRITE_IDS
 
 STAGE_COUNT = 11
@@ -117,6 +122,11 @@ class Config(C.Structure):
                 ("big_triangle_capacity", C.c_uint32), ("spin_limit", C.c_uint32), ("_reserved", C.c_uint32 * 3)]
 
 
+class TuneEntry(C.Structure):
+    _fields_ = [("bin_size", C.c_uint32), ("meshlets_per_cta", C.c_uint32), ("ms_per_launch", C.c_float),
+                ("_pad", C.c_uint32)]
+
+
 class MeshInfo(C.Structure):
     _fields_ = [("vertex_count", C.c_uint32), ("triangle_count", C.c_uint32), ("meshlet_count", C.c_uint32),
                 ("vertex_index_count", C.c_uint32), ("primitive_index_bytes", C.c_uint32),
@@ -126,6 +136,20 @@ class MeshInfo(C.Structure):
                 ("vertex_indices", C.POINTER(C.c_uint32)), ("primitive_indices", C.POINTER(C.c_uint8)),
                 ("aabb_extents", C.c_float * 3), ("aabb_center", C.c_float * 3),
                 ("cones", C.POINTER(MeshletCone))]
+
+
+class DiffScene(C.Structure):
+    _fields_ = [("meshlet_buffer", C.c_uint64), ("vertex_index_buffer", C.c_uint64),
+                ("primitive_index_buffer", C.c_uint64), ("positions", C.c_uint64), ("colors", C.c_uint64),
+                ("uvs", C.c_uint64), ("texture", C.c_uint64), ("meshlet_count", C.c_uint32),
+                ("vertex_count", C.c_uint32), ("tex_width", C.c_uint32), ("tex_height", C.c_uint32),
+                ("albedo", C.c_float * 3), ("uv_offset", C.c_float * 2), ("uv_scale", C.c_float * 2),
+                ("uv_rotation", C.c_float), ("double_sided", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class DiffView(C.Structure):
+    _fields_ = [("camera_buffer", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("depth_id", C.c_uint64), ("rgb", C.c_uint64), ("target", C.c_uint64), ("grad_rgb", C.c_uint64)]
 
 
 EXPECTED_SIZES = {"Meshlet": 36, "Vertex": 24, "MeshletDraw": 12, "Primitive": 64, "Material": 48, "Camera": 352}
@@ -162,6 +186,13 @@ _PROTOS = {
                                      C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_float]),
     "vkgv_frustum_planes": (C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "vkgv_version": (C.c_char_p, []),
+    "vkgv_diff_forward": (C.c_int, [_P, C.POINTER(DiffScene), C.POINTER(DiffView), _U32, _P]),
+    "vkgv_diff_backward": (C.c_int, [_P, C.POINTER(DiffScene), C.POINTER(DiffView), _U32, C.c_float, _U64, _U64,
+                                     _U64, _U64, _P]),
+    "vkgv_diff_graph_capture": (C.c_int, [_P, C.POINTER(DiffScene), C.POINTER(DiffView), _U32, _U32, C.c_float,
+                                          _U64, _U64, _U64, _U64, C.POINTER(_P)]),
+    "vkgv_autotune": (C.c_int, [C.POINTER(Config), C.POINTER(Scene), C.POINTER(View), _U32, _U32, _U32,
+                                C.POINTER(TuneEntry), _U32, C.POINTER(_U32), C.POINTER(Config)]),
     "vkgv_set_profiling": (C.c_int, [_P, C.c_int32]),
     "vkgv_stage_times": (C.c_int, [_P, C.POINTER(C.c_float), _U32]),
 }

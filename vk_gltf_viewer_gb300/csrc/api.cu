@@ -605,12 +605,18 @@ namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// One pass of the adjoint: builds the internal raster scene from the current
-// positions, recomputes visibility (clear, cull without culling tests, since
-// the builder's meshlet bounds do not follow moving vertices, raster) and
-// runs the shading kernel forward or backward.
-int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* views, uint32_t n, bool backward,
-             float scale, uint64_t loss, uint64_t gpos, uint64_t gcol, uint64_t gtex, void* stream_) {
+// The adjoint's launch plan: the internal raster scene built from the
+// current positions (identity node transform, one draw per meshlet), the
+// per-view device descriptors and the shading arguments.
+struct DiffPlan {
+    DiffSetup S{};
+    DiffArgs A{};
+    Prepared P;
+    std::vector<DeviceView> views;
+};
+
+int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* views, uint32_t n, bool backward,
+                 float scale, uint64_t loss, uint64_t gpos, uint64_t gcol, uint64_t gtex, DiffPlan& D) {
     if (!ctx) return VKGV_INVALID_ARG;
     if (!ds || !views || n == 0) return fail(ctx, VKGV_INVALID_ARG, "adjoint: scene and views are required");
     if (!ds->meshlet_buffer || !ds->vertex_index_buffer || !ds->primitive_index_buffer || !ds->positions ||
@@ -619,7 +625,6 @@ int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* vie
     if (ds->meshlet_count >= (1u << VKGV_DRAW_INDEX_BITS))
         return fail(ctx, VKGV_LIMIT_EXCEEDED, "adjoint: meshlet_count must be < 2^25");
     if (n > 65535u) return fail(ctx, VKGV_LIMIT_EXCEEDED, "at most 65535 views per call");
-    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
     const size_t V = ds->vertex_count, M = ds->meshlet_count;
     const size_t off_draws = align256(sizeof(vkgv_vertex) * V);
     const size_t off_xf = off_draws + align256(sizeof(vkgv_meshlet_draw) * std::max<size_t>(M, 1));
@@ -627,7 +632,7 @@ int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* vie
     int rc = ensure_scratch(ctx, ctx->diff, total, "adjoint scene");
     if (rc) return rc;
     char* base = static_cast<char*>(ctx->diff.ptr);
-    DiffSetup S{};
+    DiffSetup& S = D.S;
     S.positions = reinterpret_cast<const float*>(ds->positions);
     S.vertex_count = ds->vertex_count;
     S.meshlet_count = ds->meshlet_count;
@@ -648,7 +653,8 @@ int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* vie
     scene.meshlet_draw_count = ds->meshlet_count;
     std::vector<vkgv_view> vv(n);
     for (uint32_t i = 0; i < n; ++i) {
-        if (backward && !views[i].target) return fail(ctx, VKGV_INVALID_ARG, "adjoint: backward needs a target");
+        if (backward && !views[i].target && !views[i].grad_rgb)
+            return fail(ctx, VKGV_INVALID_ARG, "adjoint: backward needs a target or grad_rgb per view");
         vv[i] = vkgv_view{};
         vv[i].camera_buffer = views[i].camera_buffer;
         vv[i].width = views[i].width;
@@ -657,26 +663,15 @@ int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* vie
     }
     rc = ensure_views(ctx, n);
     if (rc) return rc;
-    DeviceView *dv, *hv;
-    int slot = 0;
-    rc = acquire_slot(ctx, &slot, &dv, &hv);
-    if (rc) return rc;
-    Prepared P;
-    rc = build_views(ctx, &scene, vv.data(), n, 0, hv, P);
+    D.views.assign(n, DeviceView{});
+    rc = build_views(ctx, &scene, vv.data(), n, 0, D.views.data(), D.P);
     if (rc) return rc;
     for (uint32_t i = 0; i < n; ++i) {
-        hv[i].diff_rgb = reinterpret_cast<float*>(views[i].rgb);
-        hv[i].diff_target = reinterpret_cast<const float*>(views[i].target);
+        D.views[i].diff_rgb = reinterpret_cast<float*>(views[i].rgb);
+        D.views[i].diff_target = reinterpret_cast<const float*>(views[i].target);
+        D.views[i].diff_grad = reinterpret_cast<const float*>(views[i].grad_rgb);
     }
-    rc = commit_views(ctx, slot, n, stream);
-    if (rc) return rc;
-    launch_diff_setup(S, stream);
-    launch_clear(dv, n, P.max_px, ctx->counters, kGlobalCounters, ctx->sm_count, stream);
-    launch_cull(P.S, dv, n, 0u, 1, ctx->status, ctx->sm_count, stream);
-    RasterLists l1{1, nullptr, nullptr, 0, 4};
-    launch_raster(P.S, dv, n, l1, ctx->raster, ctx->big, ctx->counters + 0, ctx->big_cap, ctx->status, ctx->sm_count,
-                  stream);
-    DiffArgs A{};
+    DiffArgs& A = D.A;
     A.meshlets = S.meshlets;
     A.vertex_indices = S.vertex_indices;
     A.tri_indices = S.tri_indices;
@@ -697,7 +692,38 @@ int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* vie
     A.grad_positions = reinterpret_cast<float*>(gpos);
     A.grad_colors = reinterpret_cast<float*>(gcol);
     A.grad_texture = reinterpret_cast<float*>(gtex);
-    launch_diff_shade(A, dv, n, P.max_px, backward, stream);
+    return VKGV_OK;
+}
+
+// One pass of the adjoint over device view descriptors dv: vertex records
+// from the current positions, visibility recomputed (clear, cull without
+// culling tests, since the builder's meshlet bounds do not follow moving
+// vertices, raster), then the shading kernel forward or backward.
+void diff_record(vkgv_ctx* ctx, const DiffPlan& D, const DeviceView* dv, uint32_t n, bool backward,
+                 cudaStream_t stream) {
+    launch_diff_setup(D.S, stream);
+    launch_clear(dv, n, D.P.max_px, ctx->counters, kGlobalCounters, ctx->sm_count, stream);
+    launch_cull(D.P.S, dv, n, 0u, 1, ctx->status, ctx->sm_count, stream);
+    RasterLists l1{1, nullptr, nullptr, 0, 4};
+    launch_raster(D.P.S, dv, n, l1, ctx->raster, ctx->big, ctx->counters + 0, ctx->big_cap, ctx->status,
+                  ctx->sm_count, stream);
+    launch_diff_shade(D.A, dv, n, D.P.max_px, backward, stream);
+}
+
+int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* views, uint32_t n, bool backward,
+             float scale, uint64_t loss, uint64_t gpos, uint64_t gcol, uint64_t gtex, void* stream_) {
+    DiffPlan D;
+    int rc = diff_prepare(ctx, ds, views, n, backward, scale, loss, gpos, gcol, gtex, D);
+    if (rc) return rc;
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    DeviceView *dv, *hv;
+    int slot = 0;
+    rc = acquire_slot(ctx, &slot, &dv, &hv);
+    if (rc) return rc;
+    std::memcpy(hv, D.views.data(), sizeof(DeviceView) * n);
+    rc = commit_views(ctx, slot, n, stream);
+    if (rc) return rc;
+    diff_record(ctx, D, dv, n, backward, stream);
     rc = check_launch(ctx);
     if (rc) return rc;
     return close_slot(ctx, slot, stream);
@@ -717,6 +743,58 @@ int vkgv_diff_backward(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_d
                        uint64_t grad_texture, void* stream) {
     return diff_run(ctx, scene, views, view_count, true, scale, loss, grad_positions, grad_colors, grad_texture,
                     stream);
+}
+
+int vkgv_diff_graph_capture(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const vkgv_diff_view* views,
+                            uint32_t view_count, uint32_t passes, float scale, uint64_t loss, uint64_t grad_positions,
+                            uint64_t grad_colors, uint64_t grad_texture, vkgv_graph** out_graph) {
+    if (!ctx || !out_graph) return VKGV_INVALID_ARG;
+    *out_graph = nullptr;
+    const uint32_t known = VKGV_DIFF_ZERO_GRADS | VKGV_DIFF_FORWARD | VKGV_DIFF_BACKWARD;
+    if (passes == 0 || (passes & ~known)) return fail(ctx, VKGV_INVALID_ARG, "adjoint graph: unknown passes");
+    const bool bwd = (passes & VKGV_DIFF_BACKWARD) != 0;
+    DiffPlan D;
+    int rc = diff_prepare(ctx, scene, views, view_count, bwd, scale, loss, grad_positions, grad_colors,
+                          grad_texture, D);
+    if (rc) return rc;
+    vkgv_graph* g = new (std::nothrow) vkgv_graph();
+    if (!g) return fail(ctx, VKGV_OUT_OF_MEMORY, "graph object");
+    g->ctx = ctx;
+    if (cudaMalloc(&g->d_views, sizeof(DeviceView) * view_count) != cudaSuccess ||
+        cudaMemcpy(g->d_views, D.views.data(), sizeof(DeviceView) * view_count, cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        vkgv_graph_destroy(g);
+        return fail(ctx, VKGV_OUT_OF_MEMORY, "graph view table");
+    }
+    cudaStream_t s = ctx->capture_stream;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        vkgv_graph_destroy(g);
+        return cuda_fail(ctx, e, "cudaStreamBeginCapture");
+    }
+    if (passes & VKGV_DIFF_ZERO_GRADS) {
+        const size_t nv = 3 * size_t(scene->vertex_count);
+        const size_t nt = 3 * size_t(scene->tex_width) * scene->tex_height;
+        if (loss) cudaMemsetAsync(reinterpret_cast<void*>(loss), 0, sizeof(float), s);
+        if (grad_positions) cudaMemsetAsync(reinterpret_cast<void*>(grad_positions), 0, sizeof(float) * nv, s);
+        if (grad_colors) cudaMemsetAsync(reinterpret_cast<void*>(grad_colors), 0, sizeof(float) * nv, s);
+        if (grad_texture) cudaMemsetAsync(reinterpret_cast<void*>(grad_texture), 0, sizeof(float) * nt, s);
+    }
+    if (passes & VKGV_DIFF_FORWARD) diff_record(ctx, D, g->d_views, view_count, false, s);
+    if (bwd) diff_record(ctx, D, g->d_views, view_count, true, s);
+    e = cudaStreamEndCapture(s, &g->graph);
+    if (e != cudaSuccess) {
+        vkgv_graph_destroy(g);
+        return cuda_fail(ctx, e, "cudaStreamEndCapture");
+    }
+    e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+        vkgv_graph_destroy(g);
+        return cuda_fail(ctx, e, "cudaGraphInstantiate");
+    }
+    *out_graph = g;
+    return VKGV_OK;
 }
 
 int vkgv_graph_capture(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, uint32_t view_count,
@@ -794,6 +872,68 @@ int vkgv_graph_destroy(vkgv_graph* g) {
     }
     delete g;
     return VKGV_OK;
+}
+
+int vkgv_autotune(const vkgv_config* base, const vkgv_scene* scene, const vkgv_view* views, uint32_t view_count,
+                  uint32_t flags, uint32_t launches, vkgv_tune_entry* entries, uint32_t entry_capacity,
+                  uint32_t* out_entry_count, vkgv_config* best) {
+    if (!scene || !views || view_count == 0 || launches == 0 || !best) return VKGV_INVALID_ARG;
+    static const uint32_t kBins[] = {8, 16, 32};
+    static const uint32_t kSplits[] = {1, 2, 4};
+    const vkgv_config b = base ? *base : vkgv_config{};
+    if (b.device >= 0 && cudaSetDevice(b.device) != cudaSuccess) return VKGV_CUDA_ERROR;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cudaGetLastError();
+        if (s) cudaStreamDestroy(s);
+        if (e0) cudaEventDestroy(e0);
+        return VKGV_CUDA_ERROR;
+    }
+    int rc = VKGV_OK;
+    uint32_t n = 0;
+    float best_ms = 0.f;
+    for (uint32_t bin : kBins) {
+        for (uint32_t split : kSplits) {
+            vkgv_config c = b;
+            c.bin_size = bin;
+            c.meshlets_per_cta = split;
+            vkgv_ctx* ctx = nullptr;
+            vkgv_graph* g = nullptr;
+            rc = vkgv_create(&c, &ctx);
+            if (rc == VKGV_OK) rc = vkgv_graph_capture(ctx, scene, views, view_count, flags, &g);
+            float ms = 0.f;
+            if (rc == VKGV_OK) rc = vkgv_graph_launch(g, s);
+            if (rc == VKGV_OK && cudaEventRecord(e0, s) != cudaSuccess) rc = VKGV_CUDA_ERROR;
+            for (uint32_t i = 0; rc == VKGV_OK && i < launches; ++i) rc = vkgv_graph_launch(g, s);
+            if (rc == VKGV_OK && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                                  cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+                rc = VKGV_CUDA_ERROR;
+            if (rc == VKGV_OK) {
+                uint32_t code = 0, detail = 0;
+                vkgv_device_status(ctx, &code, &detail);
+                if (code) rc = VKGV_DEVICE_FAULT;
+            }
+            if (g) vkgv_graph_destroy(g);
+            if (ctx) vkgv_destroy(ctx);
+            if (rc != VKGV_OK) break;
+            ms /= float(launches);
+            if (entries && n < entry_capacity) entries[n] = vkgv_tune_entry{bin, split, ms, 0};
+            ++n;
+            if (n == 1 || ms < best_ms) {
+                best_ms = ms;
+                *best = c;
+            }
+        }
+        if (rc != VKGV_OK) break;
+    }
+    cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    if (out_entry_count) *out_entry_count = std::min(n, entry_capacity);
+    return rc;
 }
 
 }  // extern "C"

@@ -51,7 +51,8 @@ struct DeviceView {
     uint32_t survivor_capacity;
     uint32_t _pad;
     float* diff_rgb;            // adjoint: shaded linear RGB output (forward)
-    const float* diff_target;   // adjoint: target image (backward)
+    const float* diff_target;   // adjoint: MSE target image (backward)
+    const float* diff_grad;     // adjoint: dL/drgb (backward, without a target)
 };
 
 struct SceneArgs {

@@ -75,7 +75,8 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const uint32_t lo = (uint32_t)V.depth_id[p];
         float tgt[3] = {0.0f, 0.0f, 0.0f};
-        if (BACKWARD) {
+        const bool mse = V.diff_target != nullptr;
+        if (BACKWARD && mse) {
             tgt[0] = V.diff_target[3 * p];
             tgt[1] = V.diff_target[3 * p + 1];
             tgt[2] = V.diff_target[3 * p + 2];
@@ -164,9 +165,13 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
         float g[3], dcol[3], dtex[3];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const float r = rgb[j] - tgt[j];
-            loss_acc += A.scale * r * r;
-            g[j] = 2.0f * A.scale * r;
+            if (mse) {
+                const float r = rgb[j] - tgt[j];
+                loss_acc += A.scale * r * r;
+                g[j] = 2.0f * A.scale * r;
+            } else {
+                g[j] = V.diff_grad[3 * p + j];
+            }
             dcol[j] = g[j] * A.albedo[j] * tex[j];
             dtex[j] = g[j] * col[j] * A.albedo[j];
         }

@@ -198,6 +198,10 @@ class Renderer:
         ctx = C.c_void_p()
         abi.check(self.lib.vkgv_create(C.byref(cfg), C.byref(ctx)))
         self.ctx = ctx
+        self.device = device
+        self.bin_size = bin_size
+        self.meshlets_per_cta = meshlets_per_cta
+        self.big_capacity = big_capacity
 
     def close(self) -> None:
         if self.ctx:
@@ -253,6 +257,19 @@ class Renderer:
         abi.check(self.lib.vkgv_graph_capture(self.ctx, C.byref(scene.scene), arr, len(views), flags, C.byref(g)),
                   self.ctx)
         return Graph(self, g.value, (scene, views))
+
+    def sweep(self, scene: DeviceScene, views: list[ViewBuffers], flags: int, launches: int = 3):
+        """Native launch-shape sweep (vkgv_autotune) over this workload.
+        Returns ([(bin_size, meshlets_per_cta, ms_per_launch)], best (bin, split))."""
+        arr = self._views(scene, views)
+        base = abi.Config(device=self.device, big_triangle_capacity=self.big_capacity)
+        entries = (abi.TuneEntry * 16)()
+        n = C.c_uint32()
+        best = abi.Config()
+        abi.check(self.lib.vkgv_autotune(C.byref(base), C.byref(scene.scene), arr, len(views), flags, launches,
+                                         entries, 16, C.byref(n), C.byref(best)))
+        table = [(int(e.bin_size), int(e.meshlets_per_cta), float(e.ms_per_launch)) for e in entries[:n.value]]
+        return table, (int(best.bin_size), int(best.meshlets_per_cta))
 
     def set_profiling(self, enable: bool) -> None:
         abi.check(self.lib.vkgv_set_profiling(self.ctx, 1 if enable else 0), self.ctx)
