@@ -163,7 +163,10 @@ typedef struct vkgv_scene {
      * vkgv_meshlet_cone[meshlet_count] (0 = no cones for it). */
     uint64_t cone_table;
     uint32_t primitive_count;    /* entries of cone_table                 */
-    uint32_t _pad;
+    /* Nodes in transform_buffer, or 0.  When given, a frame evaluates each
+     * node's determinant (the winding sign of visbuffer.mesh.glsl:71) once
+     * instead of once per meshlet draw; every transform_index must be below it. */
+    uint32_t transform_count;
 } vkgv_scene;
 
 /* Normal cone of one meshlet in object space (an addition: glsl::Meshlet

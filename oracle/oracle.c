@@ -905,8 +905,10 @@ double orc_diff_f64(const orc_diff_scene* s, const float vpf[16], uint32_t w, ui
                 const double* q = s->positions + 3 * (size_t)vi[k];
                 for (int r = 0; r < 4; ++r) c[k][r] = vp[0 * 4 + r] * q[0] + vp[1 * 4 + r] * q[1] + vp[2 * 4 + r] * q[2] + vp[3 * 4 + r];
             }
-            const double nx = ((double)px + 0.5) / (double)w * 2.0 - 1.0;
-            const double ny = ((double)py + 0.5) / (double)h * 2.0 - 1.0;
+            /* the sample point is the fp32 NDC of the pixel centre (the
+             * point the GPU evaluates), then carried in double */
+            const double nx = (double)(((float)px + 0.5f) / (float)w * 2.0f - 1.0f);
+            const double ny = (double)(((float)py + 0.5f) / (float)h * 2.0f - 1.0f);
             double a[3], b[3];
             for (int k = 0; k < 3; ++k) {
                 a[k] = c[k][0] - nx * c[k][3];

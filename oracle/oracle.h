@@ -142,6 +142,8 @@ void orc_frame(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h
  * node transform):
  *   rgb = interp(colour) * albedo * bilinearREPEAT(texture, transformUv(interp(uv)))
  *   L   = scale * sum (rgb - target)^2
+ * with perspective-correct barycentrics at the pixel centre's fp32 NDC
+ * ((px + 0.5) / w * 2 - 1 in float, the point the GPU evaluates).
  * Returns L; writes rgb (if non-NULL) and ACCUMULATES the gradients into
  * gpos / gcol / gtex (each may be NULL). */
 typedef struct orc_diff_scene {

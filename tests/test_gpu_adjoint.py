@@ -138,10 +138,10 @@ def test_finite_differences_200_params(renderer, su):
     Bilinear filtering has a derivative jump wherever a sample crosses a
     texel centre, so a position is only drawn when no pixel of any view
     changes bilinear cell across its stencil.  Parameters are drawn among
-    those whose float64 gradient is at least 1e-2 of the largest of their
-    kind (about half of each kind): a near-zero gradient is a sum of cancelling per-pixel terms whose
-    fp32 rounding (the forward residual rgb - target is computed in fp32)
-    sets an absolute, not a relative, error floor."""
+    those whose float64 gradient is at least 1e-3 of the largest of their
+    kind (three quarters of each kind or more): a near-zero gradient is a
+    sum of cancelling per-pixel terms whose fp32 rounding sets an absolute,
+    not a relative, error floor."""
     targets = su.render(renderer, su.target_scene)
     su.render(renderer)
     _, gp, gc, gt = gpu_grads(renderer, su, targets)
@@ -165,7 +165,7 @@ def test_finite_differences_200_params(renderer, su):
     for kind, n in (("pos", 60), ("col", 60), ("tex", 80)):
         taken = 0
         mag = np.abs(ref64[kind])
-        for i in rng.permutation(np.nonzero(mag >= 1e-2 * mag.max())[0]):
+        for i in rng.permutation(np.nonzero(mag >= 1e-3 * mag.max())[0]):
             if kind == "pos":
                 (lp, s1), (lm, s2), (lp2, s3), (lm2, s4) = (loss_at(kind, i, s) for s in (h, -h, h / 2, -h / 2))
                 if not (s1 and s2 and s3 and s4):

@@ -103,7 +103,7 @@ class Scene(C.Structure):
     _fields_ = [("draw_buffer", C.c_uint64), ("transform_buffer", C.c_uint64), ("primitive_buffer", C.c_uint64),
                 ("material_buffer", C.c_uint64), ("texture_table", C.c_uint64),
                 ("meshlet_draw_count", C.c_uint32), ("texture_count", C.c_uint32),
-                ("cone_table", C.c_uint64), ("primitive_count", C.c_uint32), ("_pad", C.c_uint32)]
+                ("cone_table", C.c_uint64), ("primitive_count", C.c_uint32), ("transform_count", C.c_uint32)]
 
 
 class MeshletCone(C.Structure):

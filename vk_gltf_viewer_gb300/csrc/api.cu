@@ -19,7 +19,7 @@ namespace {
 
 constexpr uint32_t kRing = 4;                 // in-flight frames sharing staging slots
 constexpr uint32_t kCountersPerView = 8;      // see DeviceView::counters
-constexpr uint32_t kGlobalCounters = 8;       // [0] pass-1 big queue, [1] pass-2 big queue
+constexpr uint32_t kGlobalCounters = 8;       // [0] pass-1 big queue, [1] pass-2 big queue, [6..7] raster work
 constexpr uint32_t kDefaultBigCapacity = 1u << 21;
 
 struct Scratch {
@@ -49,6 +49,8 @@ struct vkgv_ctx {
     Scratch rejected;   // per view: capacity draw_count
     Scratch deferred;   // per view: capacity draw_count
     Scratch diff;       // adjoint: internal raster scene of the differentiable mesh
+    Scratch tdet;       // determinant(M) per node transform (vkgv_scene.transform_count)
+    Scratch mvp;        // view_projection * M per view and node
     BigTri* big = nullptr;
     uint32_t big_cap = 0;
     cudaStream_t capture_stream = nullptr;
@@ -177,6 +179,8 @@ struct Prepared {
     uint32_t max_w = 0, max_h = 0;
     uint64_t max_px = 0;
     uint32_t hiz_tx = 1, hiz_ty = 1;  // single-pass HiZ grid (max over views)
+    float* tdets = nullptr;           // node tables filled by the clear (whole frames only)
+    float* mvps = nullptr;
 };
 
 // Builds the DeviceView table for `views` into `host` (count n).
@@ -206,7 +210,8 @@ int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, 
     P.S.texture_count = scene->texture_count;
     P.S.cone_table = reinterpret_cast<const uint64_t*>(scene->cone_table);
     P.S.primitive_count = scene->cone_table ? scene->primitive_count : 0;
-    P.S._pad = 0;
+    P.S.transform_count = scene->transform_count;
+    P.S.tdets = nullptr;
     for (uint32_t i = 0; i < n; ++i) {
         const vkgv_view& v = views[i];
         rc = validate_view(ctx, v, flags);
@@ -285,12 +290,13 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
     };
     uint32_t* gc = ctx->counters;
     zone(0);
-    launch_clear(dv, n, (flags & VKGV_SKIP_CLEAR) ? 0 : P.max_px, gc, kGlobalCounters, ctx->sm_count, stream);
+    launch_clear(dv, n, (flags & VKGV_SKIP_CLEAR) ? 0 : P.max_px, gc, kGlobalCounters, ctx->sm_count, stream,
+                 P.S.transforms, P.tdets ? P.S.transform_count : 0u, P.tdets, P.mvps);
     zone(1);
     launch_cull(P.S, dv, n, flags, 1, ctx->status, ctx->sm_count, stream);
     zone(2);
     RasterLists l1{1, nullptr, nullptr, 0, 4};
-    launch_raster(P.S, dv, n, l1, ctx->raster, ctx->big, gc + 0, ctx->big_cap, ctx->status, ctx->sm_count, stream,
+    launch_raster(P.S, dv, n, l1, ctx->raster, ctx->big, gc + 0, ctx->big_cap, gc + 6, ctx->status, ctx->sm_count, stream,
                   zones ? zones[3] : nullptr);
     zone(4);
     const bool two = (flags & VKGV_CULL_TWO_PASS) && (flags & VKGV_CULL_OCCLUSION);
@@ -300,7 +306,7 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
     zone(6);
     if (two) {
         RasterLists l2{2, nullptr, nullptr, 0, 5};
-        launch_raster(P.S, dv, n, l2, ctx->raster, ctx->big, gc + 1, ctx->big_cap, ctx->status, ctx->sm_count,
+        launch_raster(P.S, dv, n, l2, ctx->raster, ctx->big, gc + 1, ctx->big_cap, gc + 6, ctx->status, ctx->sm_count,
                       stream, zones ? zones[7] : nullptr);
     } else {
         zone(7);
@@ -320,6 +326,23 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
 int check_launch(vkgv_ctx* ctx) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
+    return VKGV_OK;
+}
+
+// When the scene gives its node count, a whole frame evaluates each node's
+// determinant(M) and each view's view_projection * M once (in the clear
+// kernel) instead of once per meshlet draw (raster) or per pixel (resolve).
+int attach_node_tables(vkgv_ctx* ctx, Prepared& P, DeviceView* host, uint32_t n) {
+    const size_t T = P.S.transform_count;
+    if (T == 0 || P.S.draw_count == 0) return VKGV_OK;
+    int rc = ensure_scratch(ctx, ctx->tdet, sizeof(float) * T, "node determinants");
+    if (rc) return rc;
+    rc = ensure_scratch(ctx, ctx->mvp, sizeof(float) * 16 * T * n, "per-view node matrices");
+    if (rc) return rc;
+    P.tdets = static_cast<float*>(ctx->tdet.ptr);
+    P.mvps = static_cast<float*>(ctx->mvp.ptr);
+    P.S.tdets = P.tdets;
+    for (uint32_t i = 0; i < n; ++i) host[i].mvps = P.mvps + 16 * T * i;
     return VKGV_OK;
 }
 
@@ -450,6 +473,8 @@ int vkgv_frame(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, u
     Prepared P;
     rc = build_views(ctx, scene, views, view_count, flags, hv, P);
     if (rc) return rc;
+    rc = attach_node_tables(ctx, P, hv, view_count);
+    if (rc) return rc;
     rc = commit_views(ctx, slot, view_count, stream);
     if (rc) return rc;
     record_frame(ctx, P, dv, view_count, flags, stream, ctx->profile ? ctx->zone : nullptr);
@@ -551,8 +576,8 @@ int vkgv_raster(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, u
     // big-queue counter and the view's deferred-list counter start at zero
     VKGV_CUDA(ctx, cudaMemsetAsync(ctx->counters, 0, sizeof(uint32_t), stream));
     VKGV_CUDA(ctx, cudaMemsetAsync(ctx->counters + kGlobalCounters + 6, 0, sizeof(uint32_t), stream));
-    launch_raster(P.S, dv, 1, l, ctx->raster, ctx->big, ctx->counters, ctx->big_cap, ctx->status, ctx->sm_count,
-                  stream);
+    launch_raster(P.S, dv, 1, l, ctx->raster, ctx->big, ctx->counters, ctx->big_cap, ctx->counters + 6, ctx->status,
+                  ctx->sm_count, stream);
     rc = check_launch(ctx);
     if (rc) return rc;
     return close_slot(ctx, slot, stream);
@@ -705,7 +730,7 @@ void diff_record(vkgv_ctx* ctx, const DiffPlan& D, const DeviceView* dv, uint32_
     launch_clear(dv, n, D.P.max_px, ctx->counters, kGlobalCounters, ctx->sm_count, stream);
     launch_cull(D.P.S, dv, n, 0u, 1, ctx->status, ctx->sm_count, stream);
     RasterLists l1{1, nullptr, nullptr, 0, 4};
-    launch_raster(D.P.S, dv, n, l1, ctx->raster, ctx->big, ctx->counters + 0, ctx->big_cap, ctx->status,
+    launch_raster(D.P.S, dv, n, l1, ctx->raster, ctx->big, ctx->counters + 0, ctx->big_cap, ctx->counters + 6, ctx->status,
                   ctx->sm_count, stream);
     launch_diff_shade(D.A, dv, n, D.P.max_px, backward, stream);
 }
@@ -809,6 +834,8 @@ int vkgv_graph_capture(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* 
     std::vector<DeviceView> host(view_count);
     Prepared P;
     rc = build_views(ctx, scene, views, view_count, flags, host.data(), P);
+    if (rc) return rc;
+    rc = attach_node_tables(ctx, P, host.data(), view_count);
     if (rc) return rc;
     vkgv_graph* g = new (std::nothrow) vkgv_graph();
     if (!g) return fail(ctx, VKGV_OUT_OF_MEMORY, "graph object");

@@ -53,6 +53,8 @@ struct DeviceView {
     float* diff_rgb;            // adjoint: shaded linear RGB output (forward)
     const float* diff_target;   // adjoint: MSE target image (backward)
     const float* diff_grad;     // adjoint: dL/drgb (backward, without a target)
+    // view_projection * M per node (16 floats each, computed by the clear), or null
+    const float* mvps;
 };
 
 struct SceneArgs {
@@ -65,7 +67,8 @@ struct SceneArgs {
     uint32_t texture_count;
     const uint64_t* cone_table;   // per primitive: device address of its cones, or 0
     uint32_t primitive_count;
-    uint32_t _pad;
+    uint32_t transform_count;
+    const float* tdets;           // determinant(M) per node (computed by the clear), or null
 };
 
 // One binned (large) triangle chunk: a sub-rectangle of a snapped triangle.

@@ -2,7 +2,8 @@
 // implementation; the shading formula is the commented-out
 // visbuffer.frag.glsl:29-34 in linear RGB).
 //
-// Forward, per covered pixel of the visibility buffer:
+// Forward, per covered pixel of the visibility buffer, at the pixel centre
+// (nx, ny) in fp32 NDC:
 //   lambda = l / sum(l),  l = a x b,  a_k = x_k - nx w_k,  b_k = y_k - ny w_k
 //   col = sum lambda_k C_k,  uv = sum lambda_k UV_k
 //   uv' = R(rot) uv * scale + offset       (transformUv, mesh_common.h.glsl:129-135)
@@ -61,6 +62,50 @@ __device__ __forceinline__ int wrap(int i, int n) {
     return i < 0 ? i + n : i;
 }
 
+// Error-free transformations (Dekker / Knuth) for the compensated clip-space
+// setup: x * y = p + e exactly, and x + y = s + e exactly.
+__device__ __forceinline__ void two_prod(float x, float y, float& p, float& e) {
+    p = __fmul_rn(x, y);
+    e = __fmaf_rn(x, y, -p);
+}
+
+__device__ __forceinline__ void two_sum(float x, float y, float& s, float& e) {
+    s = __fadd_rn(x, y);
+    const float bb = __fsub_rn(s, x);
+    e = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bb)), __fsub_rn(y, bb));
+}
+
+// Row j of the column-major M applied to (x, y, z, 1) as an unevaluated sum
+// hi + lo accurate to about twice fp32 precision (the compensated dot
+// product of Ogita, Rump and Oishi, "Accurate sum and dot product", 2005).
+__device__ __forceinline__ void dot_df(const float* M, int j, float x, float y, float z, float& hi, float& lo) {
+    float s = M[12 + j], err = 0.0f, p, e, q;
+    two_prod(M[j], x, p, e);
+    two_sum(s, p, s, q);
+    err = __fadd_rn(err, __fadd_rn(q, e));
+    two_prod(M[4 + j], y, p, e);
+    two_sum(s, p, s, q);
+    err = __fadd_rn(err, __fadd_rn(q, e));
+    two_prod(M[8 + j], z, p, e);
+    two_sum(s, p, s, q);
+    err = __fadd_rn(err, __fadd_rn(q, e));
+    two_sum(s, err, hi, lo);
+}
+
+// a = x - nx w and b = y - ny w of one vertex, each rounded once from an
+// almost exact value.  a and b vanish where the pixel ray passes near the
+// vertex; there the plain fp32 form loses most of its digits to
+// cancellation, and the position gradient (through l = a x b) inherits
+// the loss.
+__device__ __forceinline__ void clip_ab(const float* VP, const float* q, float nx, float ny, float& a, float& b) {
+    float xh, xl, yh, yl, wh, wl;
+    dot_df(VP, 0, q[0], q[1], q[2], xh, xl);
+    dot_df(VP, 1, q[0], q[1], q[2], yh, yl);
+    dot_df(VP, 3, q[0], q[1], q[2], wh, wl);
+    a = __fadd_rn(__fmaf_rn(-nx, wh, xh), __fmaf_rn(-nx, wl, xl));
+    b = __fadd_rn(__fmaf_rn(-ny, wh, yh), __fmaf_rn(-ny, wl, yl));
+}
+
 template <bool BACKWARD>
 __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView* __restrict__ views) {
     const DeviceView& V = views[blockIdx.y];
@@ -90,21 +135,15 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
         const uint32_t m = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
         const vkgv_meshlet ml = meshlets[m];
         const uint8_t* tri = A.tri_indices + ml.triangle_offset + 3 * t;
-        uint32_t vi[3];
-        float c[3][4];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            vi[k] = A.vertex_indices[ml.vertex_offset + tri[k]];
-            const float* q = A.positions + 3 * (size_t)vi[k];
-            m4v(VP, q[0], q[1], q[2], 1.0f, c[k]);
-        }
+        // The sample point is the fp32 NDC of the pixel centre.
         const float nx = fsub(fmul(fdiv(fadd((float)(p % w), 0.5f), (float)V.w), 2.0f), 1.0f);
         const float ny = fsub(fmul(fdiv(fadd((float)(p / w), 0.5f), (float)V.h), 2.0f), 1.0f);
+        uint32_t vi[3];
         float a[3], b[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            a[k] = fsub(c[k][0], fmul(nx, c[k][3]));
-            b[k] = fsub(c[k][1], fmul(ny, c[k][3]));
+            vi[k] = A.vertex_indices[ml.vertex_offset + tri[k]];
+            clip_ab(VP, A.positions + 3 * (size_t)vi[k], nx, ny, a[k], b[k]);
         }
         float l[3] = {fsub(fmul(a[1], b[2]), fmul(a[2], b[1])), fsub(fmul(a[2], b[0]), fmul(a[0], b[2])),
                       fsub(fmul(a[0], b[1]), fmul(a[1], b[0]))};

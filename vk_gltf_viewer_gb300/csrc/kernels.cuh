@@ -20,13 +20,20 @@ struct RasterConfig {
     uint32_t blocks_per_view;
 };
 
+// Also evaluates, when transform_count > 0, determinant(M) of
+// transforms[0, transform_count) into tdets and each view's
+// view_projection * M into mvps[view][node].
 void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels, uint32_t* counters,
-                  uint32_t counter_words, uint32_t sm_count, cudaStream_t stream);
+                  uint32_t counter_words, uint32_t sm_count, cudaStream_t stream, const float* transforms = nullptr,
+                  uint32_t transform_count = 0, float* tdets = nullptr, float* mvps = nullptr);
 void launch_cull(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t flags, uint32_t pass,
                  uint32_t* status, uint32_t sm_count, cudaStream_t stream);
+// work: two counters that are zero between launches (each launch returns
+// them to zero).
 void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews, const RasterLists& lists,
                    const RasterConfig& cfg, BigTri* big, uint32_t* big_count, uint32_t big_capacity,
-                   uint32_t* status, uint32_t sm_count, cudaStream_t stream, cudaEvent_t between = nullptr);
+                   uint32_t* work, uint32_t* status, uint32_t sm_count, cudaStream_t stream,
+                   cudaEvent_t between = nullptr);
 void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t* status,
                 cudaStream_t stream);
 void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h,

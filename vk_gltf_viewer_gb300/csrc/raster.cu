@@ -232,9 +232,14 @@ __device__ __noinline__ void raster_clipped(float4 v0, float4 v1, float4 v2, boo
         setup_and_raster(X[0], Y[0], Z[0], X[k], Y[k], Z[k], X[k + 1], Y[k + 1], Z[k + 1], id, c);
 }
 
+// Views per raster launch (the launcher splits larger batches).
+constexpr uint32_t kRasterMaxViews = 1024;
+
 struct RasterParams {
     SceneArgs S;
-    const DeviceView* views;
+    const DeviceView* views;  // this launch's views
+    uint32_t nviews;          // <= kRasterMaxViews
+    uint32_t view_base;       // index of views[0] in the frame's view table
     RasterLists lists;
     BigTri* big;
     uint32_t* big_count;
@@ -242,7 +247,33 @@ struct RasterParams {
     uint32_t small_area;
     uint32_t chunk;
     uint32_t* status;
+    uint32_t* work;           // [0] items taken, [1] warps done (zero between launches)
 };
+
+// The meshlet list a raster instance draws for one view: pass-1 or pass-2
+// survivors, the view's deferred meshlets (slow instance), or an explicit
+// list; items are list[first, first + count).
+template <bool SLOW>
+__device__ __forceinline__ void view_work(const RasterParams& P, const DeviceView& V, const uint32_t*& list,
+                                          uint32_t& count, uint32_t& first) {
+    first = 0;
+    if (SLOW) {
+        list = V.deferred;
+        count = min(V.counters[P.lists.deferred_slot], P.S.draw_count);
+    } else if (P.lists.pass == 1) {
+        list = V.survivors;
+        count = min(V.counters[0], V.survivor_capacity);
+    } else if (P.lists.pass == 2) {
+        const uint32_t c0 = min(V.counters[0], V.survivor_capacity);
+        list = V.survivors + c0;
+        count = min(V.counters[2], V.survivor_capacity - c0);
+    } else {
+        list = P.lists.list;
+        const uint32_t n = *P.lists.count;
+        first = P.lists.first;
+        count = n > first ? n - first : 0u;
+    }
+}
 
 // Setup record of one small triangle, shared by the warp while it
 // rasterises all small triangles of a round cooperatively.
@@ -269,6 +300,157 @@ enum TriKind : int { kDrop = 0, kFast = 1, kSlowClip = 2, kSlowSetup = 3 };
 #define VKGV_RASTER_WARPS_PER_SM 32
 #endif
 
+// Small triangles whose clamped bbox has at most this many pixels are
+// rasterised by their own lane; larger small ones by the whole warp.
+constexpr uint32_t kLaneArea = 4;
+
+struct TriClass {
+    int4 q0, q1, q2;  // snapped vertex records {X, Y, Z bits, flags}
+};
+
+// Sorts one meshlet triangle into drop / fast / slow-clip / slow-setup.  The
+// backface test (visbuffer.mesh.glsl:86-101) and the empty-bbox test are
+// both pure filters, so the cheap bbox test runs first for triangles that
+// need no clipping.  kFast: snapped, inside the guard band, front-facing,
+// non-zero area, a pixel centre in its bbox, bbox within small_area pixels
+// and edge values within int32.
+template <bool SLOW>
+__device__ __forceinline__ int classify(uint32_t i0, uint32_t i1, uint32_t i2, uint32_t vc, const int4* svtx,
+                                        const float4* clip, bool double_sided, float tdet, const RasterCtx& c,
+                                        uint32_t d, TriClass& k) {
+    if (i0 >= vc || i1 >= vc || i2 >= vc) {
+        if (!SLOW) report(c.status, kStatusBadIndex, d);
+        return kDrop;
+    }
+    k.q0 = svtx[i0];
+    k.q1 = svtx[i1];
+    k.q2 = svtx[i2];
+    const uint32_t f0 = (uint32_t)k.q0.w, f1 = (uint32_t)k.q1.w, f2 = (uint32_t)k.q2.w;
+    auto backfacing = [&]() {
+        if (double_sided) return false;
+        const float4 a = clip[i0], b = clip[i1], cc = clip[i2];
+        const float det = det3(a.x, a.y, a.w, b.x, b.y, b.w, cc.x, cc.y, cc.w);
+        return tdet < 0.0f ? det < 0.0f : det > 0.0f;
+    };
+    if (f0 & f1 & f2 & 63) return kDrop;  // outcode reject
+    if ((f0 | f1 | f2) & (OC_ZLO | OC_ZHI | kFlagGuard)) return backfacing() ? kDrop : kSlowClip;
+    if (!(f0 & f1 & f2 & kFlagSnapped)) return kDrop;
+    const int4 &q0 = k.q0, &q1 = k.q1, &q2 = k.q2;
+    const int32_t minx = min(q0.x, min(q1.x, q2.x)), maxx = max(q0.x, max(q1.x, q2.x));
+    const int32_t miny = min(q0.y, min(q1.y, q2.y)), maxy = max(q0.y, max(q1.y, q2.y));
+    const int32_t qx0 = max((minx - 128 + 255) >> 8, 0), qx1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
+    const int32_t qy0 = max((miny - 128 + 255) >> 8, 0), qy1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
+    if (qx0 > qx1 || qy0 > qy1 || backfacing()) return kDrop;
+    const int64_t A = (int64_t)(q1.x - q0.x) * (q2.y - q0.y) - (int64_t)(q1.y - q0.y) * (q2.x - q0.x);
+    if (A == 0) return kDrop;
+    const bool small = maxx - minx < kSmallExtent && maxy - miny < kSmallExtent &&
+                       (uint32_t)((qx1 - qx0 + 1) * (qy1 - qy0 + 1)) <= c.small_area;
+    return small ? kFast : kSlowSetup;
+}
+
+// One sample of a small triangle: int32 edge functions (the extent bound of
+// kFast keeps them exact), top-left bias, plane depth clamped to [0, 1].
+__device__ __forceinline__ void small_sample(const int32_t* x, const int32_t* y, uint32_t bias, float z0, float pa,
+                                             float pb, int32_t px, int32_t py, unsigned long long lo,
+                                             const RasterCtx& c) {
+    const int32_t sx = px * 256 + 128, sy = py * 256 + 128;
+    const int32_t e0 = (x[1] - x[0]) * (sy - y[0]) - (y[1] - y[0]) * (sx - x[0]);
+    const int32_t e1 = (x[2] - x[1]) * (sy - y[1]) - (y[2] - y[1]) * (sx - x[1]);
+    const int32_t e2 = (x[0] - x[2]) * (sy - y[2]) - (y[0] - y[2]) * (sx - x[2]);
+    if (e0 >= (int32_t)(bias & 1u) && e1 >= (int32_t)((bias >> 1) & 1u) && e2 >= (int32_t)((bias >> 2) & 1u)) {
+        float z = __fmaf_rn(pa, __int2float_rn(sx - x[0]), __fmaf_rn(pb, __int2float_rn(sy - y[0]), z0));
+        if (!(z > 0.0f)) z = 0.0f;
+        if (z > 1.0f) z = 1.0f;
+        plot(c.depth + (size_t)py * c.w + px, ((unsigned long long)__float_as_uint(z) << 32) | lo);
+    }
+}
+
+// Setup and raster of up to 32 compacted kFast triangles, one per lane (ct =
+// meshlet-local triangle index, 0xffffffff = none).  A triangle whose
+// clamped bbox has at most kLaneArea pixels is rasterised by its own lane;
+// the larger ones are spread over the warp by an inclusive scan of their
+// bbox areas.
+__device__ __forceinline__ void raster_small(uint32_t ct, const uint8_t* sidx8, const int4* svtx, uint32_t d,
+                                             const RasterCtx& c, TriRec* recs, uint32_t* ends, int lane) {
+    uint32_t coop_area = 0;
+    if (ct != 0xffffffffu) {
+        const int4 q0 = svtx[sidx8[3 * ct]], q1 = svtx[sidx8[3 * ct + 1]], q2 = svtx[sidx8[3 * ct + 2]];
+        const int64_t A = (int64_t)(q1.x - q0.x) * (q2.y - q0.y) - (int64_t)(q1.y - q0.y) * (q2.x - q0.x);
+        int32_t x[3] = {q0.x, q1.x, q2.x}, y[3] = {q0.y, q1.y, q2.y};
+        float z0 = __int_as_float(q0.z), z1 = __int_as_float(q1.z), z2 = __int_as_float(q2.z);
+        if (A < 0) {  // orient to positive area
+            x[1] = q2.x, y[1] = q2.y, x[2] = q1.x, y[2] = q1.y;
+            z1 = __int_as_float(q2.z), z2 = __int_as_float(q1.z);
+        }
+        const int64_t Ap = A < 0 ? -A : A;
+        const int32_t minx = min(x[0], min(x[1], x[2])), maxx = max(x[0], max(x[1], x[2]));
+        const int32_t miny = min(y[0], min(y[1], y[2])), maxy = max(y[0], max(y[1], y[2]));
+        const int32_t px0 = max((minx - 128 + 255) >> 8, 0), px1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
+        const int32_t py0 = max((miny - 128 + 255) >> 8, 0), py1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
+        const uint32_t bw = (uint32_t)(px1 - px0 + 1), bh = (uint32_t)(py1 - py0 + 1);
+        uint32_t bias = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int32_t dx = x[(k + 1) % 3] - x[k], dy = y[(k + 1) % 3] - y[k];
+            if (!(dy < 0 || (dy == 0 && dx > 0))) bias |= 1u << k;
+        }
+        const float dx1 = __int2float_rn(x[1] - x[0]), dy1 = __int2float_rn(y[1] - y[0]);
+        const float dx2 = __int2float_rn(x[2] - x[0]), dy2 = __int2float_rn(y[2] - y[0]);
+        const float af = __ll2float_rn(Ap);
+        const float dz1 = fsub(z1, z0), dz2 = fsub(z2, z0);
+        const float pa = fdiv(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), af);
+        const float pb = fdiv(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), af);
+        const uint32_t id = (d << 7) | ct;
+        if (bw * bh <= kLaneArea) {
+            const unsigned long long lo = (unsigned long long)id + 1ull;
+            for (uint32_t ly = 0; ly < bh; ++ly)
+                for (uint32_t lx = 0; lx < bw; ++lx)
+                    small_sample(x, y, bias, z0, pa, pb, px0 + (int32_t)lx, py0 + (int32_t)ly, lo, c);
+        } else {
+            TriRec& r = recs[lane];
+            r.x[0] = x[0], r.x[1] = x[1], r.x[2] = x[2];
+            r.y[0] = y[0], r.y[1] = y[1], r.y[2] = y[2];
+            r.z0 = z0;
+            r.pa = pa;
+            r.pb = pb;
+            r.inv_bw = 1.0f / (float)bw;
+            r.id = id;
+            r.bx0 = (uint16_t)px0;
+            r.by0 = (uint16_t)py0;
+            r.bw = (uint8_t)bw;
+            r.bh = (uint8_t)bh;
+            r.bias = (uint8_t)bias;
+            coop_area = bw * bh;
+        }
+    }
+    if (__ballot_sync(0xffffffffu, coop_area != 0) == 0) return;
+    // Warp-cooperative raster: an inclusive scan of the bbox areas spreads
+    // the pixels of the larger small triangles evenly over the lanes.
+    uint32_t incl = coop_area;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    ends[lane] = incl;
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    for (uint32_t p = lane; p < total; p += 32) {
+        // smallest j with ends[j] > p
+        uint32_t j = 0;
+#pragma unroll
+        for (uint32_t step = 16; step > 0; step >>= 1)
+            if (ends[j + step - 1] <= p) j += step;
+        const TriRec& r = recs[j];
+        const uint32_t local = p - (ends[j] - (uint32_t)r.bw * r.bh);
+        const uint32_t ly = (uint32_t)(((float)local + 0.5f) * r.inv_bw);
+        const uint32_t lx = local - ly * r.bw;
+        small_sample(r.x, r.y, r.bias, r.z0, r.pa, r.pb, (int32_t)(r.bx0 + lx), (int32_t)(r.by0 + ly),
+                     (unsigned long long)r.id + 1ull, c);
+    }
+    __syncwarp();
+}
+
 // Warp-per-meshlet raster.  The fast instance (SLOW = false) handles every
 // triangle that needs no clipping and fits the cooperative small-triangle
 // path, and appends a meshlet that has any other triangle to the view's
@@ -283,267 +465,244 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
     // the meshlet's triangle-index bytes (<= 126 triangles)
     __shared__ uint32_t s_idx[WARPS][96];
     __shared__ TriRec s_tri[WARPS][32];
+    // ring of compacted kFast triangle indices (fast instance)
+    __shared__ uint8_t s_ring[WARPS][64];
     __shared__ uint32_t s_end[WARPS][32];
     __shared__ float s_mvp[WARPS][16];
     __shared__ float s_tdet[WARPS];
-    __shared__ float s_vp[16];
+    __shared__ float s_vp[WARPS][16];
+    // exclusive prefix of the views' work counts: view v owns the global
+    // work items [s_pre[v], s_pre[v + 1])
+    __shared__ uint32_t s_pre[kRasterMaxViews + 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t vi = blockIdx.y;
-    const DeviceView& V = P.views[vi];
-    if (threadIdx.x < 16) s_vp[threadIdx.x] = V.cam->view_projection[threadIdx.x];
+    const uint32_t nv = P.nviews;
+    for (uint32_t v = threadIdx.x; v < nv; v += blockDim.x) {
+        const uint32_t* l;
+        uint32_t n, f;
+        view_work<SLOW>(P, P.views[v], l, n, f);
+        s_pre[v + 1] = n;
+    }
+    if (threadIdx.x == 0) s_pre[0] = 0;
     __syncthreads();
+    if (warp == 0) {
+        // inclusive scan of s_pre[1..nv]: lane-contiguous segments, then a
+        // warp scan of the segment sums
+        const uint32_t seg = (nv + 31) / 32, b = 1 + lane * seg, e = min(b + seg, nv + 1);
+        uint32_t sum = 0;
+        for (uint32_t i = b; i < e; ++i) sum += s_pre[i];
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        uint32_t run = incl - sum;
+        for (uint32_t i = b; i < e; ++i) {
+            run += s_pre[i];
+            s_pre[i] = run;
+        }
+    }
+    __syncthreads();
+    const uint32_t total = s_pre[nv];
     const uint32_t slot = P.lists.deferred_slot;
     const uint32_t defer_cap = P.S.draw_count;
-    const uint32_t* list;
-    uint32_t count, first = 0;
-    if (SLOW) {
-        list = V.deferred;
-        count = min(V.counters[slot], defer_cap);
-    } else if (P.lists.pass == 1) {
-        list = V.survivors;
-        count = min(V.counters[0], V.survivor_capacity);
-    } else if (P.lists.pass == 2) {
-        const uint32_t c0 = min(V.counters[0], V.survivor_capacity);
-        list = V.survivors + c0;
-        count = min(V.counters[2], V.survivor_capacity - c0);
-    } else {
-        list = P.lists.list;
-        count = *P.lists.count;
-        first = P.lists.first;
-    }
-    RasterCtx c;
-    c.depth = V.depth_id;
-    c.w = V.w;
-    c.h = V.h;
-    c.hw = 0.5f * (float)V.w;
-    c.hh = 0.5f * (float)V.h;
-    c.view = vi;
-    c.big = P.big;
-    c.big_count = P.big_count;
-    c.big_cap = P.big_cap;
-    c.small_area = P.small_area;
-    c.chunk = P.chunk;
-    c.status = P.status;
     float4* clip = s_clip[warp];
     int4* svtx = s_vtx[warp];
     uint32_t* sidx = s_idx[warp];
     const uint8_t* sidx8 = reinterpret_cast<const uint8_t*>(sidx);
     TriRec* recs = s_tri[warp];
     uint32_t* ends = s_end[warp];
-    const uint32_t stride = gridDim.x * WARPS;
-    for (uint32_t s = first + blockIdx.x * WARPS + warp; s < count; s += stride) {
-        const uint32_t d = list[s];
-        if (d >= P.S.draw_count) {
-            if (lane == 0) report(P.status, kStatusBadIndex, d);
-            continue;
+    // Warps take runs of `grab` consecutive work items from one counter, so
+    // views are drawn roughly in order (their depth buffers stay in L2) and
+    // no warp idles while work is left.
+    const uint32_t warps_total = gridDim.x * WARPS;
+    const uint32_t grab = max(1u, min(16u, total / (warps_total * 8u)));
+    uint32_t cur_v = 0xffffffffu;
+    const DeviceView* Vp = P.views;
+    const uint32_t* list = nullptr;
+    uint32_t first = 0;
+    // the warp's raster context lives in shared memory (fewer live registers)
+    __shared__ RasterCtx s_ctx[WARPS];
+    RasterCtx& c = s_ctx[warp];
+    if (lane == 0) {
+        c.big = P.big;
+        c.big_count = P.big_count;
+        c.big_cap = P.big_cap;
+        c.small_area = P.small_area;
+        c.chunk = P.chunk;
+        c.status = P.status;
+    }
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(P.work, grab);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        const uint32_t stop = min(base + grab, total);
+        // the view holding `base`: the last v with s_pre[v] <= base
+        uint32_t v = 0, hi = nv;
+        while (v + 1 < hi) {
+            const uint32_t mid = (v + hi) >> 1;
+            if (s_pre[mid] <= base) v = mid;
+            else hi = mid;
         }
-        const vkgv_meshlet_draw dr = P.S.draws[d];
-        const vkgv_primitive* prim = &P.S.prims[dr.primitive_index];
-        if (dr.meshlet_index >= prim->meshlet_count) {
-            if (lane == 0) report(P.status, kStatusBadIndex, d);
-            continue;
-        }
-        const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
-        const uint32_t vc = ml->vertex_count, tc = ml->triangle_count;
-        if (vc > VKGV_MAX_VERTICES || tc > VKGV_MAX_PRIMITIVES) {
-            if (lane == 0) report(P.status, kStatusBadIndex, d);
-            continue;
-        }
-        const uint32_t* vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
-        const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset;
-        const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
-        const bool double_sided = P.S.mats[prim->material_index].double_sided != 0;
-        // mvp = VP * M, one element per lane (lanes 0-15); lane 16 takes the
-        // sign source determinant(M) of visbuffer.mesh.glsl:71.
-        const float* Mg = P.S.transforms + 16 * (size_t)dr.transform_index;
-        if (lane < 16) {
-            const int cc = lane >> 2, j = lane & 3;
-            const float4 mc = __ldg(reinterpret_cast<const float4*>(Mg) + cc);
-            s_mvp[warp][lane] = fadd(fadd(fadd(fmul(s_vp[0 * 4 + j], mc.x), fmul(s_vp[1 * 4 + j], mc.y)),
-                                          fmul(s_vp[2 * 4 + j], mc.z)),
-                                     fmul(s_vp[3 * 4 + j], mc.w));
-        } else if (lane == 16) {
-            float M[16];
-#pragma unroll
-            for (int q = 0; q < 16; ++q) M[q] = __ldg(Mg + q);
-            s_tdet[warp] = det4(M);
-        }
-        __syncwarp();
-        const float tdet = s_tdet[warp];
-        const float* mvp = s_mvp[warp];
-        // Vertex stage: clip position, outcode, guard flag and the 28.8 snap,
-        // each computed once per meshlet vertex.
-        for (uint32_t k = lane; k < vc; k += 32) {
-            const vkgv_vertex* vx = verts + __ldg(vidx + k);
-            const float2 xy = __ldg(reinterpret_cast<const float2*>(vx->position));
-            const float zz = __ldg(&vx->position[2]);
-            float r[4];
-            m4v(mvp, xy.x, xy.y, zz, 1.0f, r);
-            const float4 cv = make_float4(r[0], r[1], r[2], r[3]);
-            clip[k] = cv;
-            int32_t X = 0, Y = 0;
-            float Z = 0.0f;
-            uint32_t fl = (uint32_t)outcode(cv);
-            if (outside_guard(cv)) fl |= kFlagGuard;
-            if (snap(cv, c, X, Y, Z)) fl |= kFlagSnapped;
-            svtx[k] = make_int4(X, Y, __float_as_int(Z), (int)fl);
-        }
-        // Triangle-index bytes into shared memory, 32-bit loads when the
-        // block is 4-byte aligned (meshoptimizer pads each block to 4).
-        {
-            const uint32_t nbytes = 3 * tc;
-            if ((reinterpret_cast<uintptr_t>(tri) & 3u) == 0) {
-                const uint32_t* tw = reinterpret_cast<const uint32_t*>(tri);
-                for (uint32_t k = lane; k < (nbytes + 3) / 4; k += 32) sidx[k] = __ldg(tw + k);
-            } else {
-                uint8_t* b = reinterpret_cast<uint8_t*>(sidx);
-                for (uint32_t k = lane; k < nbytes; k += 32) b[k] = __ldg(tri + k);
-            }
-        }
-        __syncwarp();
-        bool any_slow = false;
-        for (uint32_t tbase = 0; tbase < tc; tbase += 32) {
-            const uint32_t t = tbase + lane;
-            uint32_t area = 0;
-            if (t < tc) {
-                const uint32_t i0 = sidx8[3 * t], i1 = sidx8[3 * t + 1], i2 = sidx8[3 * t + 2];
-                const uint32_t id = (d << 7) | t;
-                int kind = kDrop;
-                int4 q0 = make_int4(0, 0, 0, 0), q1 = q0, q2 = q0;
-                int32_t minx = 0, maxx = 0, miny = 0, maxy = 0;
-                int64_t A = 0;
-                if (i0 >= vc || i1 >= vc || i2 >= vc) {
-                    if (!SLOW) report(P.status, kStatusBadIndex, d);
-                } else {
-                    q0 = svtx[i0], q1 = svtx[i1], q2 = svtx[i2];
-                    const uint32_t f0 = (uint32_t)q0.w, f1 = (uint32_t)q1.w, f2 = (uint32_t)q2.w;
-                    // The backface test (visbuffer.mesh.glsl:86-101) and the
-                    // empty-bbox test are both pure filters, so the cheap
-                    // bbox test runs first for triangles that need no clipping.
-                    auto backfacing = [&]() {
-                        if (double_sided) return false;
-                        const float4 a = clip[i0], b = clip[i1], cc = clip[i2];
-                        const float det = det3(a.x, a.y, a.w, b.x, b.y, b.w, cc.x, cc.y, cc.w);
-                        return tdet < 0.0f ? det < 0.0f : det > 0.0f;
-                    };
-                    if (f0 & f1 & f2 & 63) {
-                        kind = kDrop;  // outcode reject
-                    } else if ((f0 | f1 | f2) & (OC_ZLO | OC_ZHI | kFlagGuard)) {
-                        kind = backfacing() ? kDrop : kSlowClip;
-                    } else if (f0 & f1 & f2 & kFlagSnapped) {
-                        minx = min(q0.x, min(q1.x, q2.x)), maxx = max(q0.x, max(q1.x, q2.x));
-                        miny = min(q0.y, min(q1.y, q2.y)), maxy = max(q0.y, max(q1.y, q2.y));
-                        const int32_t qx0 = max((minx - 128 + 255) >> 8, 0), qx1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
-                        const int32_t qy0 = max((miny - 128 + 255) >> 8, 0), qy1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
-                        if (qx0 <= qx1 && qy0 <= qy1 && !backfacing()) {
-                            A = (int64_t)(q1.x - q0.x) * (q2.y - q0.y) - (int64_t)(q1.y - q0.y) * (q2.x - q0.x);
-                            if (A != 0) {
-                                const bool small = maxx - minx < kSmallExtent && maxy - miny < kSmallExtent &&
-                                                   (uint32_t)((qx1 - qx0 + 1) * (qy1 - qy0 + 1)) <= c.small_area;
-                                kind = small ? kFast : kSlowSetup;
-                            }
-                        }
-                    }
+        for (uint32_t g = base; g < stop; ++g) {
+            while (g >= s_pre[v + 1]) ++v;
+            if (v != cur_v) {
+                cur_v = v;
+                Vp = P.views + v;
+                uint32_t n;
+                view_work<SLOW>(P, *Vp, list, n, first);
+                __syncwarp();
+                if (lane == 0) {
+                    c.depth = Vp->depth_id;
+                    c.w = Vp->w;
+                    c.h = Vp->h;
+                    c.hw = 0.5f * (float)Vp->w;
+                    c.hh = 0.5f * (float)Vp->h;
+                    c.view = P.view_base + v;
                 }
-                if (SLOW) {
+                if (lane < 16) s_vp[warp][lane] = Vp->cam->view_projection[lane];
+                __syncwarp();
+            }
+            const DeviceView& V = *Vp;
+            const uint32_t d = list[first + (g - s_pre[v])];
+            if (d >= P.S.draw_count) {
+                if (lane == 0) report(P.status, kStatusBadIndex, d);
+                continue;
+            }
+            const vkgv_meshlet_draw dr = P.S.draws[d];
+            const vkgv_primitive* prim = &P.S.prims[dr.primitive_index];
+            if (dr.meshlet_index >= prim->meshlet_count) {
+                if (lane == 0) report(P.status, kStatusBadIndex, d);
+                continue;
+            }
+            const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
+            const uint32_t vc = ml->vertex_count, tc = ml->triangle_count;
+            if (vc > VKGV_MAX_VERTICES || tc > VKGV_MAX_PRIMITIVES) {
+                if (lane == 0) report(P.status, kStatusBadIndex, d);
+                continue;
+            }
+            const uint32_t* vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
+            const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset;
+            const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
+            const bool double_sided = P.S.mats[prim->material_index].double_sided != 0;
+            // mvp = VP * M, one element per lane (lanes 0-15); lane 16 takes the
+            // sign source determinant(M) of visbuffer.mesh.glsl:71.
+            const float* Mg = P.S.transforms + 16 * (size_t)dr.transform_index;
+            const bool have_tdet = P.S.tdets != nullptr && dr.transform_index < P.S.transform_count;
+            if (lane < 16 && V.mvps && dr.transform_index < P.S.transform_count) {
+                s_mvp[warp][lane] = __ldg(V.mvps + 16 * (size_t)dr.transform_index + lane);
+            } else if (lane < 16) {
+                const int cc = lane >> 2, j = lane & 3;
+                const float4 mc = __ldg(reinterpret_cast<const float4*>(Mg) + cc);
+                s_mvp[warp][lane] = fadd(fadd(fadd(fmul(s_vp[warp][0 * 4 + j], mc.x), fmul(s_vp[warp][1 * 4 + j], mc.y)),
+                                              fmul(s_vp[warp][2 * 4 + j], mc.z)),
+                                         fmul(s_vp[warp][3 * 4 + j], mc.w));
+            } else if (lane == 16 && have_tdet) {
+                s_tdet[warp] = P.S.tdets[dr.transform_index];
+            } else if (lane == 16) {
+                float M[16];
+    #pragma unroll
+                for (int q = 0; q < 16; ++q) M[q] = __ldg(Mg + q);
+                s_tdet[warp] = det4(M);
+            }
+            __syncwarp();
+            const float tdet = s_tdet[warp];
+            const float* mvp = s_mvp[warp];
+            // Vertex stage: clip position, outcode, guard flag and the 28.8 snap,
+            // each computed once per meshlet vertex.
+            for (uint32_t k = lane; k < vc; k += 32) {
+                const vkgv_vertex* vx = verts + __ldg(vidx + k);
+                const float2 xy = __ldg(reinterpret_cast<const float2*>(vx->position));
+                const float zz = __ldg(&vx->position[2]);
+                float r[4];
+                m4v(mvp, xy.x, xy.y, zz, 1.0f, r);
+                const float4 cv = make_float4(r[0], r[1], r[2], r[3]);
+                clip[k] = cv;
+                int32_t X = 0, Y = 0;
+                float Z = 0.0f;
+                uint32_t fl = (uint32_t)outcode(cv);
+                if (outside_guard(cv)) fl |= kFlagGuard;
+                if (snap(cv, c, X, Y, Z)) fl |= kFlagSnapped;
+                svtx[k] = make_int4(X, Y, __float_as_int(Z), (int)fl);
+            }
+            // Triangle-index bytes into shared memory, 32-bit loads when the
+            // block is 4-byte aligned (meshoptimizer pads each block to 4).
+            {
+                const uint32_t nbytes = 3 * tc;
+                if ((reinterpret_cast<uintptr_t>(tri) & 3u) == 0) {
+                    const uint32_t* tw = reinterpret_cast<const uint32_t*>(tri);
+                    for (uint32_t k = lane; k < (nbytes + 3) / 4; k += 32) sidx[k] = __ldg(tw + k);
+                } else {
+                    uint8_t* b = reinterpret_cast<uint8_t*>(sidx);
+                    for (uint32_t k = lane; k < nbytes; k += 32) b[k] = __ldg(tri + k);
+                }
+            }
+            __syncwarp();
+            bool any_slow = false;
+            if constexpr (SLOW) {
+                // Deferred meshlet: only the triangles the fast instance skipped.
+                for (uint32_t t = lane; t < tc; t += 32) {
+                    TriClass k;
+                    const uint32_t i0 = sidx8[3 * t], i1 = sidx8[3 * t + 1], i2 = sidx8[3 * t + 2];
+                    const int kind = classify<true>(i0, i1, i2, vc, svtx, clip, double_sided, tdet, c, d, k);
                     if (kind == kSlowClip) {
                         raster_clipped(clip[i0], clip[i1], clip[i2],
-                                       (((uint32_t)q0.w | (uint32_t)q1.w | (uint32_t)q2.w) & (OC_ZLO | OC_ZHI)) != 0,
-                                       id, c);
+                                       (((uint32_t)k.q0.w | (uint32_t)k.q1.w | (uint32_t)k.q2.w) & (OC_ZLO | OC_ZHI)) != 0,
+                                       (d << 7) | t, c);
                     } else if (kind == kSlowSetup) {
-                        setup_and_raster(q0.x, q0.y, __int_as_float(q0.z), q1.x, q1.y, __int_as_float(q1.z), q2.x,
-                                         q2.y, __int_as_float(q2.z), id, c);
+                        setup_and_raster(k.q0.x, k.q0.y, __int_as_float(k.q0.z), k.q1.x, k.q1.y, __int_as_float(k.q1.z),
+                                         k.q2.x, k.q2.y, __int_as_float(k.q2.z), (d << 7) | t, c);
                     }
-                } else if (kind == kSlowClip || kind == kSlowSetup) {
-                    any_slow = true;
-                } else if (kind == kFast) {
-                    int2 p0 = make_int2(q0.x, q0.y), p1 = make_int2(q1.x, q1.y), p2 = make_int2(q2.x, q2.y);
-                    float z0 = __int_as_float(q0.z), z1 = __int_as_float(q1.z), z2 = __int_as_float(q2.z);
-                    if (A < 0) {
-                        const int2 tp = p1;
-                        p1 = p2;
-                        p2 = tp;
-                        const float tz = z1;
-                        z1 = z2;
-                        z2 = tz;
+                }
+            } else {
+                // Classify 32 triangles per round; the ones that reach the small
+                // raster are compacted into a ring so that setup and raster run
+                // on full warps (about a quarter of the triangles of a dense
+                // meshlet have a sample in their bounding box).
+                uint8_t* ring = s_ring[warp];
+                uint32_t head = 0, pending = 0;
+                for (uint32_t tbase = 0; tbase < tc; tbase += 32) {
+                    const uint32_t t = tbase + lane;
+                    int kind = kDrop;
+                    if (t < tc) {
+                        TriClass k;
+                        kind = classify<false>(sidx8[3 * t], sidx8[3 * t + 1], sidx8[3 * t + 2], vc, svtx, clip,
+                                               double_sided, tdet, c, d, k);
                     }
-                    const int64_t Ap = A < 0 ? -A : A;
-                    const int32_t px0 = max((minx - 128 + 255) >> 8, 0), px1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
-                    const int32_t py0 = max((miny - 128 + 255) >> 8, 0), py1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
-                    const uint32_t bw = (uint32_t)(px1 - px0 + 1), bh = (uint32_t)(py1 - py0 + 1);
-                    TriRec& r = recs[lane];
-                    r.x[0] = p0.x, r.x[1] = p1.x, r.x[2] = p2.x;
-                    r.y[0] = p0.y, r.y[1] = p1.y, r.y[2] = p2.y;
-                    uint8_t bias = 0;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const int32_t dx = r.x[(k + 1) % 3] - r.x[k], dy = r.y[(k + 1) % 3] - r.y[k];
-                        if (!(dy < 0 || (dy == 0 && dx > 0))) bias |= (uint8_t)(1u << k);
+                    any_slow |= kind == kSlowClip || kind == kSlowSetup;
+                    const uint32_t fm = __ballot_sync(0xffffffffu, kind == kFast);
+                    if (kind == kFast) ring[(head + pending + __popc(fm & ((1u << lane) - 1u))) & 63u] = (uint8_t)t;
+                    pending += __popc(fm);
+                    const bool last = tbase + 32 >= tc;
+                    while (pending >= 32 || (last && pending > 0)) {
+                        __syncwarp();
+                        const uint32_t n = min(pending, 32u);
+                        const uint32_t ct = lane < n ? ring[(head + lane) & 63u] : 0xffffffffu;
+                        __syncwarp();
+                        raster_small(ct, sidx8, svtx, d, c, recs, ends, lane);
+                        head = (head + n) & 63u;
+                        pending -= n;
                     }
-                    const float dx1 = __int2float_rn(p1.x - p0.x), dy1 = __int2float_rn(p1.y - p0.y);
-                    const float dx2 = __int2float_rn(p2.x - p0.x), dy2 = __int2float_rn(p2.y - p0.y);
-                    const float af = __ll2float_rn(Ap);
-                    const float dz1 = fsub(z1, z0), dz2 = fsub(z2, z0);
-                    r.z0 = z0;
-                    r.pa = fdiv(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), af);
-                    r.pb = fdiv(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), af);
-                    r.inv_bw = 1.0f / (float)bw;
-                    r.id = id;
-                    r.bx0 = (uint16_t)px0;
-                    r.by0 = (uint16_t)py0;
-                    r.bw = (uint8_t)bw;
-                    r.bh = (uint8_t)bh;
-                    r.bias = bias;
-                    area = bw * bh;
                 }
             }
-            if (SLOW) continue;
-            // Warp-cooperative raster of this round's small triangles: an
-            // inclusive scan of their bbox areas spreads the pixels evenly.
-            uint32_t incl = area;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += v;
-            }
-            ends[lane] = incl;
-            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-            __syncwarp();
-            for (uint32_t p = lane; p < total; p += 32) {
-                // smallest j with ends[j] > p
-                uint32_t j = 0;
-#pragma unroll
-                for (uint32_t step = 16; step > 0; step >>= 1)
-                    if (ends[j + step - 1] <= p) j += step;
-                const TriRec& r = recs[j];
-                const uint32_t local = p - (ends[j] - (uint32_t)r.bw * r.bh);
-                const uint32_t ly = (uint32_t)(((float)local + 0.5f) * r.inv_bw);
-                const uint32_t lx = local - ly * r.bw;
-                const int32_t sx = (int32_t)(r.bx0 + lx) * 256 + 128;
-                const int32_t sy = (int32_t)(r.by0 + ly) * 256 + 128;
-                const int32_t e0 = (r.x[1] - r.x[0]) * (sy - r.y[0]) - (r.y[1] - r.y[0]) * (sx - r.x[0]);
-                const int32_t e1 = (r.x[2] - r.x[1]) * (sy - r.y[1]) - (r.y[2] - r.y[1]) * (sx - r.x[1]);
-                const int32_t e2 = (r.x[0] - r.x[2]) * (sy - r.y[2]) - (r.y[0] - r.y[2]) * (sx - r.x[2]);
-                if (e0 >= (int32_t)(r.bias & 1u) && e1 >= (int32_t)((r.bias >> 1) & 1u) &&
-                    e2 >= (int32_t)((r.bias >> 2) & 1u)) {
-                    float z = __fmaf_rn(r.pa, __int2float_rn(sx - r.x[0]),
-                                        __fmaf_rn(r.pb, __int2float_rn(sy - r.y[0]), r.z0));
-                    if (!(z > 0.0f)) z = 0.0f;
-                    if (z > 1.0f) z = 1.0f;
-                    plot(c.depth + (size_t)(r.by0 + ly) * c.w + (r.bx0 + lx),
-                         ((unsigned long long)__float_as_uint(z) << 32) | ((unsigned long long)r.id + 1ull));
-                }
+            if (!SLOW && __any_sync(0xffffffffu, any_slow) && lane == 0) {
+                const uint32_t k = atomicAdd(&V.counters[slot], 1u);
+                if (k < defer_cap)
+                    V.deferred[k] = d;
+                else
+                    report(P.status, kStatusListOverflow, d);
             }
             __syncwarp();
         }
-        if (!SLOW && __any_sync(0xffffffffu, any_slow) && lane == 0) {
-            const uint32_t k = atomicAdd(&V.counters[slot], 1u);
-            if (k < defer_cap)
-                V.deferred[k] = d;
-            else
-                report(P.status, kStatusListOverflow, d);
+    }
+    // The last warp to finish resets the work counters for the next launch.
+    if (lane == 0) {
+        __threadfence();
+        if (atomicAdd(P.work + 1, 1u) == warps_total - 1) {
+            P.work[0] = 0;
+            P.work[1] = 0;
         }
-        __syncwarp();
     }
 }
 
@@ -591,20 +750,23 @@ __global__ void __launch_bounds__(256) k_raster_big(const BigTri* __restrict__ q
     }
 }
 
+// One wave of CTAs: every warp stays resident and takes work until none is
+// left.
 template <int WARPS>
-void launch_variant(const RasterParams& P, dim3 grid, cudaStream_t stream) {
-    k_raster<WARPS, false><<<grid, WARPS * 32, 0, stream>>>(P);
-    k_raster<WARPS, true><<<grid, WARPS * 32, 0, stream>>>(P);
+void launch_variant(const RasterParams& P, uint32_t sm_count, uint32_t blocks_override, cudaStream_t stream) {
+    const uint32_t fast = blocks_override ? blocks_override : sm_count * (VKGV_RASTER_WARPS_PER_SM / WARPS);
+    const uint32_t slow = blocks_override ? blocks_override : sm_count * (16 / WARPS > 0 ? 16 / WARPS : 1);
+    k_raster<WARPS, false><<<fast, WARPS * 32, 0, stream>>>(P);
+    k_raster<WARPS, true><<<slow, WARPS * 32, 0, stream>>>(P);
 }
 
 }  // namespace
 
 void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews, const RasterLists& lists,
                    const RasterConfig& cfg, BigTri* big, uint32_t* big_count, uint32_t big_capacity,
-                   uint32_t* status, uint32_t sm_count, cudaStream_t stream, cudaEvent_t between) {
+                   uint32_t* work, uint32_t* status, uint32_t sm_count, cudaStream_t stream, cudaEvent_t between) {
     RasterParams P;
     P.S = S;
-    P.views = views;
     P.lists = lists;
     P.big = big;
     P.big_count = big_count;
@@ -612,14 +774,17 @@ void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews,
     P.small_area = cfg.small_area;
     P.chunk = cfg.chunk;
     P.status = status;
-    uint32_t bpv = cfg.blocks_per_view ? cfg.blocks_per_view : (sm_count * 16 + nviews - 1) / nviews;
-    if (bpv == 0) bpv = 1;
-    dim3 grid(bpv, nviews);
-    switch (cfg.warps_per_cta) {
-        case 1: launch_variant<1>(P, grid, stream); break;
-        case 2: launch_variant<2>(P, grid, stream); break;
-        case 8: launch_variant<8>(P, grid, stream); break;
-        default: launch_variant<4>(P, grid, stream); break;
+    P.work = work;
+    for (uint32_t v0 = 0; v0 < nviews; v0 += kRasterMaxViews) {
+        P.views = views + v0;
+        P.nviews = nviews - v0 < kRasterMaxViews ? nviews - v0 : kRasterMaxViews;
+        P.view_base = v0;
+        switch (cfg.warps_per_cta) {
+            case 1: launch_variant<1>(P, sm_count, cfg.blocks_per_view, stream); break;
+            case 2: launch_variant<2>(P, sm_count, cfg.blocks_per_view, stream); break;
+            case 8: launch_variant<8>(P, sm_count, cfg.blocks_per_view, stream); break;
+            default: launch_variant<4>(P, sm_count, cfg.blocks_per_view, stream); break;
+        }
     }
     if (between) cudaEventRecord(between, stream);
     const uint32_t chunk = cfg.chunk >= 8 && cfg.chunk <= 64 ? cfg.chunk : 32;

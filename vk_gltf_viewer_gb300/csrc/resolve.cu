@@ -81,7 +81,7 @@ __device__ __forceinline__ void finalize_view(const DeviceView& V) {
 // Bilinear REPEAT sample, texel centres at +0.5.  Textured shading of a
 // high-frequency texture is very sensitive to the sample position, so every
 // operation follows the oracle's order (no contraction).
-__device__ void sample_texture(const vkgv_texture& t, float u, float v, float out[4]) {
+__device__ void sample_texture(const vkgv_texture& t, float u, float v, const float* unorm, float out[4]) {
     const float tx = fsub(fmul(u, (float)t.width), 0.5f), ty = fsub(fmul(v, (float)t.height), 0.5f);
     const float fx = floorf(tx), fy = floorf(ty);
     const float ax = fsub(tx, fx), ay = fsub(ty, fy);
@@ -97,10 +97,10 @@ __device__ void sample_texture(const vkgv_texture& t, float u, float v, float ou
             const size_t idx = (size_t)ys[j] * t.row_pitch + (size_t)xs[i];
             if (t.format == VKGV_TEXTURE_RGBA8) {
                 const uchar4 p = __ldg(reinterpret_cast<const uchar4*>(t.data) + idx);
-                tex[j][i][0] = fdiv((float)p.x, 255.0f);
-                tex[j][i][1] = fdiv((float)p.y, 255.0f);
-                tex[j][i][2] = fdiv((float)p.z, 255.0f);
-                tex[j][i][3] = fdiv((float)p.w, 255.0f);
+                tex[j][i][0] = unorm[p.x];
+                tex[j][i][1] = unorm[p.y];
+                tex[j][i][2] = unorm[p.z];
+                tex[j][i][3] = unorm[p.w];
             } else {
                 const float* p = reinterpret_cast<const float*>(t.data) + 3 * idx;
                 tex[j][i][0] = __ldg(p);
@@ -117,21 +117,32 @@ __device__ void sample_texture(const vkgv_texture& t, float u, float v, float ou
     }
 }
 
+// unorm[i] = i / 255 (correctly rounded), a per-block table in shared memory.
 __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32_t px, uint32_t py, uint32_t id,
-                                 float out[4]) {
+                                 const float* unorm, float out[4]) {
     const uint32_t d = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
     const vkgv_meshlet_draw dr = S.draws[d];
     const vkgv_primitive* prim = &S.prims[dr.primitive_index];
     const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
     const vkgv_material& mat = S.mats[prim->material_index];
-    const float* Mp = S.transforms + 16 * (size_t)dr.transform_index;
-    float M[16], VP[16], mvp[16];
+    float mvp[16];
+    if (V.mvps && dr.transform_index < S.transform_count) {
+        const float4* q = reinterpret_cast<const float4*>(V.mvps + 16 * (size_t)dr.transform_index);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-        M[k] = __ldg(Mp + k);
-        VP[k] = V.cam->view_projection[k];
+        for (int k = 0; k < 4; ++k) {
+            const float4 c = __ldg(q + k);
+            mvp[4 * k] = c.x, mvp[4 * k + 1] = c.y, mvp[4 * k + 2] = c.z, mvp[4 * k + 3] = c.w;
+        }
+    } else {
+        const float* Mp = S.transforms + 16 * (size_t)dr.transform_index;
+        float M[16], VP[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            M[k] = __ldg(Mp + k);
+            VP[k] = V.cam->view_projection[k];
+        }
+        m4m(VP, M, mvp);
     }
-    m4m(VP, M, mvp);
     const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset + 3 * t;
     const uint32_t* vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
     const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
@@ -165,9 +176,8 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
     float col[4], uv[2];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        col[k] = fadd(fadd(fmul(l[0], fdiv((float)vx[0]->color[k], 255.0f)),
-                           fmul(l[1], fdiv((float)vx[1]->color[k], 255.0f))),
-                      fmul(l[2], fdiv((float)vx[2]->color[k], 255.0f)));
+        col[k] = fadd(fadd(fmul(l[0], unorm[vx[0]->color[k]]), fmul(l[1], unorm[vx[1]->color[k]])),
+                      fmul(l[2], unorm[vx[2]->color[k]]));
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const float h0 = __half2float(__ushort_as_half(vx[0]->uv[k]));
@@ -185,7 +195,7 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
         const float tu = fadd(fmul(ru, mat.uv_scale[0]), mat.uv_offset[0]);
         const float tv = fadd(fmul(rv, mat.uv_scale[1]), mat.uv_offset[1]);
         const vkgv_texture tex = S.textures[mat.albedo_index];
-        sample_texture(tex, tu, tv, sampled);
+        sample_texture(tex, tu, tv, unorm, sampled);
         if (tex.format == VKGV_TEXTURE_RGBA8)
 #pragma unroll
             for (int k = 0; k < 3; ++k) sampled[k] = to_linear_fast(sampled[k]);
@@ -197,6 +207,11 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
 template <bool TEXTURED>
 __global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
     const DeviceView& V = views[blockIdx.y];
+    __shared__ float s_unorm[256];
+    if (TEXTURED) {
+        s_unorm[threadIdx.x] = fdiv((float)threadIdx.x, 255.0f);  // blockDim.x == 256
+        __syncthreads();
+    }
     const uint32_t w = V.w, n = V.w * V.h;
     uint32_t* ids = (flags & VKGV_WRITE_IDS) ? V.ids : nullptr;
     uint32_t* rgba = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED)) ? V.rgba : nullptr;
@@ -210,7 +225,7 @@ __global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* 
         if (id != VKGV_VISBUFFER_CLEAR) {
             float lin[4];
             if (TEXTURED) {
-                resolve_textured(S, V, p % w, p / w, id, lin);
+                resolve_textured(S, V, p % w, p / w, id, s_unorm, lin);
             } else {
                 const vkgv_meshlet_draw dr = S.draws[id >> VKGV_TRIANGLE_BITS];
                 const vkgv_material& mat = S.mats[S.prims[dr.primitive_index].material_index];
@@ -227,8 +242,30 @@ __global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* 
 }
 
 __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ views, uint32_t* counters,
-                                               uint32_t counter_words, uint32_t skip_pixels) {
+                                               uint32_t counter_words, uint32_t skip_pixels,
+                                               const float* __restrict__ transforms, uint32_t transform_count,
+                                               float* __restrict__ tdets, float* __restrict__ mvps) {
     const DeviceView& V = views[blockIdx.y];
+    if (transform_count) {
+        __shared__ float s_vp[16];
+        if (threadIdx.x < 16) s_vp[threadIdx.x] = V.cam->view_projection[threadIdx.x];
+        __syncthreads();
+        float* out = mvps + (size_t)blockIdx.y * transform_count * 16;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < transform_count; i += gridDim.x * blockDim.x) {
+            float M[16], r[16];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float4 q = __ldg(reinterpret_cast<const float4*>(transforms + 16 * (size_t)i) + k);
+                M[4 * k] = q.x, M[4 * k + 1] = q.y, M[4 * k + 2] = q.z, M[4 * k + 3] = q.w;
+            }
+            if (blockIdx.y == 0) tdets[i] = det4(M);
+            m4m(s_vp, M, r);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                reinterpret_cast<float4*>(out + 16 * (size_t)i)[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2],
+                                                                                  r[4 * k + 3]);
+        }
+    }
     if (blockIdx.x == 0 && threadIdx.x < 8) V.counters[threadIdx.x] = 0;
     if (blockIdx.x == 0 && blockIdx.y == 0)
         for (uint32_t i = threadIdx.x; i < counter_words; i += blockDim.x) counters[i] = 0;
@@ -264,14 +301,17 @@ void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews
 }
 
 void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels, uint32_t* counters,
-                  uint32_t counter_words, uint32_t sm_count, cudaStream_t stream) {
+                  uint32_t counter_words, uint32_t sm_count, cudaStream_t stream, const float* transforms,
+                  uint32_t transform_count, float* tdets, float* mvps) {
     const bool skip = max_pixels == 0;
     uint64_t want = (max_pixels / 2 + 255) / 256;
     uint32_t cap = (sm_count * 16 + nviews - 1) / nviews;
     if (cap < 1) cap = 1;
     uint32_t bx = skip ? 1u : (uint32_t)(want < cap ? (want ? want : 1) : cap);
     dim3 grid(bx, nviews);
-    k_clear<<<grid, 256, 0, stream>>>(views, counters, counter_words, skip ? 1u : 0u);
+    if (!tdets || !mvps) transform_count = 0;
+    k_clear<<<grid, 256, 0, stream>>>(views, counters, counter_words, skip ? 1u : 0u, transforms, transform_count,
+                                      tdets, mvps);
 }
 
 void launch_finalize(const DeviceView* views, uint32_t nviews, cudaStream_t stream) {

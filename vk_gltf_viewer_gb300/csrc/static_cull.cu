@@ -122,7 +122,8 @@ extern "C" int vkgv_cull_static(const vkgv_scene* scene, const vkgv_view* view, 
     S.texture_count = scene->texture_count;
     S.cone_table = reinterpret_cast<const uint64_t*>(scene->cone_table);
     S.primitive_count = scene->cone_table ? scene->primitive_count : 0;
-    S._pad = 0;
+    S.transform_count = scene->transform_count;
+    S.tdets = nullptr;
 
     DeviceView v{};
     v.cam = reinterpret_cast<const vkgv_camera*>(view->camera_buffer);

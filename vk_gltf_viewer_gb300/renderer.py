@@ -80,7 +80,8 @@ class DeviceScene:
                                primitive_buffer=_ptr(self.primitives), material_buffer=_ptr(self.materials),
                                texture_table=_ptr(self.texture_table) if host.textures else 0,
                                meshlet_draw_count=host.draw_count, texture_count=len(host.textures),
-                               cone_table=_ptr(self.cone_table), primitive_count=len(host.meshes))
+                               cone_table=_ptr(self.cone_table), primitive_count=len(host.meshes),
+                               transform_count=int(host.transforms.shape[0]))
 
     @property
     def draw_count(self) -> int:
