@@ -63,15 +63,26 @@ __device__ __forceinline__ float depth_at(const unsigned long long* d, uint32_t 
     return u2f((uint32_t)(__ldg(d + (size_t)y * w + x) >> 32));
 }
 
+// Footprint along one axis of texel x of a level of size d in its source of
+// size s.  When s == 2d the sample point (x + 0.5) / d * s - 0.5 lies within
+// about (2x + 1) * 2^-22 of 2x + 0.5 (sizes <= 8192), so both weights are
+// non-zero and the footprint is exactly {2x, 2x + 1}: no division needed.
+__device__ __forceinline__ int axis_footprint(int x, uint32_t d, uint32_t s, int& i0, int& i1) {
+    if (s == 2 * d) {
+        i0 = 2 * x;
+        i1 = 2 * x + 1;
+        return 2;
+    }
+    return footprint_axis(fdiv(fadd((float)x, 0.5f), (float)d), s, i0, i1);
+}
+
 // One texel of level j from a source sampled through `fetch(x, y)`.
 template <class F>
 __device__ __forceinline__ float reduce_texel(int x, int y, uint32_t dw, uint32_t dh, uint32_t sw, uint32_t sh,
                                               F fetch) {
-    const float u = fdiv(fadd((float)x, 0.5f), (float)dw);
-    const float v = fdiv(fadd((float)y, 0.5f), (float)dh);
     int x0 = 0, x1 = 0, y0 = 0, y1 = 0;
-    const int nx = footprint_axis(u, sw, x0, x1);
-    const int ny = footprint_axis(v, sh, y0, y1);
+    const int nx = axis_footprint(x, dw, sw, x0, x1);
+    const int ny = axis_footprint(y, dh, sh, y0, y1);
     float r = fetch(x0, y0);
     if (nx == 2) r = gmin(r, fetch(x1, y0));
     if (ny == 2) {
@@ -138,7 +149,16 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
             for (int i = threadIdx.x; i < rw * rh; i += blockDim.x) {
                 const int x = X.lo + i % rw, y = Y.lo + i / rw;
                 float r;
-                if (j == 1) {
+                if (j == 1 && w == 2 * dw && h == 2 * dh) {
+                    // 2x2 block of the depth image: one 16-byte load per row
+                    // (depth_id is 16-byte aligned and w is even)
+                    const ulonglong2* q =
+                        reinterpret_cast<const ulonglong2*>(V.depth_id + (size_t)(2 * y) * w + 2 * x);
+                    const ulonglong2 a = __ldg(q), b = __ldg(q + (w >> 1));
+                    r = gmin(gmin(gmin(u2f((uint32_t)(a.x >> 32)), u2f((uint32_t)(a.y >> 32))),
+                                  u2f((uint32_t)(b.x >> 32))),
+                             u2f((uint32_t)(b.y >> 32)));
+                } else if (j == 1) {
                     r = reduce_texel(x, y, dw, dh, w, h, [&](int sx, int sy) { return depth_at(V.depth_id, w, sx, sy); });
                 } else {
                     r = reduce_texel(x, y, dw, dh, w >> (j - 1), h >> (j - 1),

@@ -532,11 +532,14 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
         c.chunk = P.chunk;
         c.status = P.status;
     }
+    // the next run is requested while the current one is drawn, so the
+    // atomic's round trip is off the critical path
+    uint32_t next = 0;
+    if (lane == 0) next = atomicAdd(P.work, grab);
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(P.work, grab);
-        base = __shfl_sync(0xffffffffu, base, 0);
+        const uint32_t base = __shfl_sync(0xffffffffu, next, 0);
         if (base >= total) break;
+        if (lane == 0) next = atomicAdd(P.work, grab);
         const uint32_t stop = min(base + grab, total);
         // the view holding `base`: the last v with s_pre[v] <= base
         uint32_t v = 0, hi = nv;

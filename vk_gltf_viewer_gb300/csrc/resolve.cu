@@ -78,6 +78,15 @@ __device__ __forceinline__ void finalize_view(const DeviceView& V) {
     *V.survivor_count = c0 + c2;
 }
 
+// REPEAT addressing: the non-negative remainder of i by n (n >= 1), with a
+// mask for power-of-two sizes and 32-bit arithmetic where i fits.
+__device__ __forceinline__ uint32_t wrap_texel(long long i, uint32_t n) {
+    if ((n & (n - 1)) == 0) return (uint32_t)(i & (long long)(n - 1));
+    if (i >= 0 && i < 0x7fffffffll) return (uint32_t)i % n;
+    const long long r = i % (long long)n;
+    return (uint32_t)(r < 0 ? r + n : r);
+}
+
 // Bilinear REPEAT sample, texel centres at +0.5.  Textured shading of a
 // high-frequency texture is very sensitive to the sample position, so every
 // operation follows the oracle's order (no contraction).
@@ -85,10 +94,9 @@ __device__ void sample_texture(const vkgv_texture& t, float u, float v, const fl
     const float tx = fsub(fmul(u, (float)t.width), 0.5f), ty = fsub(fmul(v, (float)t.height), 0.5f);
     const float fx = floorf(tx), fy = floorf(ty);
     const float ax = fsub(tx, fx), ay = fsub(ty, fy);
-    const long long W = t.width, H = t.height;
     const long long x0 = (long long)fx, y0 = (long long)fy;
-    const long long xs[2] = {((x0 % W) + W) % W, (((x0 + 1) % W) + W) % W};
-    const long long ys[2] = {((y0 % H) + H) % H, (((y0 + 1) % H) + H) % H};
+    const uint32_t xs[2] = {wrap_texel(x0, t.width), wrap_texel(x0 + 1, t.width)};
+    const uint32_t ys[2] = {wrap_texel(y0, t.height), wrap_texel(y0 + 1, t.height)};
     float tex[2][2][4];
 #pragma unroll
     for (int j = 0; j < 2; ++j)
