@@ -250,7 +250,9 @@ int vkgv_clear(vkgv_ctx* ctx, const vkgv_view* view, void* stream);
  * surviving draw indices to view->survivors.  pass 1 tests against
  * view->prev_pyramid with prevOcclusionViewProjection; pass 2 re-tests the
  * pass-1 occlusion rejects against view->pyramid with
- * occlusionViewProjection. */
+ * occlusionViewProjection (only the occlusion test: the rejects already
+ * passed the frustum and cone tests of pass 1, whose camera fields
+ * (frustum, view_projection) must not change in between). */
 int vkgv_cull(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view,
               uint32_t flags, uint32_t pass, void* stream);
 /* No counterpart in the reference.  vkgv_cull for callers that cannot

@@ -36,7 +36,7 @@ struct CullResult {
 __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceView& V, const float* frustum, const float* eye,
                                                const float* occl_vp, const float* pyr, uint32_t pw0,
                                                uint32_t ph0, uint32_t plevels, uint32_t flags, uint32_t d,
-                                               uint32_t* status) {
+                                               bool retest, uint32_t* status) {
     CullResult res{false, false};
     const vkgv_meshlet_draw dr = S.draws[d];
     const vkgv_primitive* prim = &S.prims[dr.primitive_index];
@@ -64,8 +64,10 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
 #pragma unroll
     for (int j = 0; j < 3; ++j)
         we[j] = fadd(fadd(fmul(fabsf(M[0 * 4 + j]), e0), fmul(fabsf(M[1 * 4 + j]), e1)), fmul(fabsf(M[2 * 4 + j]), e2));
-    // isAabbInFrustum (culling.h.glsl:8-19)
-    if (flags & VKGV_CULL_FRUSTUM) {
+    // isAabbInFrustum (culling.h.glsl:8-19).  A pass-2 candidate passed the
+    // frustum and cone tests in pass 1 with the same planes and eye, and
+    // would pass them again bit for bit, so only its occlusion is re-tested.
+    if ((flags & VKGV_CULL_FRUSTUM) && !retest) {
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
             const float p0 = frustum[4 * i], p1 = frustum[4 * i + 1], p2 = frustum[4 * i + 2], p3 = frustum[4 * i + 3];
@@ -76,7 +78,7 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
     }
     // Meshlet normal-cone backface test (an addition; conservative with
     // respect to the per-triangle test of visbuffer.mesh.glsl:86-101).
-    if (eye && S.cone_table && dr.primitive_index < S.primitive_count) {
+    if (!retest && eye && S.cone_table && dr.primitive_index < S.primitive_count) {
         const uint64_t cones = S.cone_table[dr.primitive_index];
         if (cones && cone_culled(reinterpret_cast<const vkgv_meshlet_cone*>(cones)[dr.meshlet_index], M, eye))
             return res;
@@ -205,7 +207,7 @@ __global__ void __launch_bounds__(256) k_cull(SceneArgs S, const DeviceView* __r
         if (i < n) {
             d = pass == 1 ? i : V.rejected[i];
             if (d < S.draw_count) {
-                CullResult r = cull_one(S, V, s_frustum, eye, s_vp, pyr, pw0, ph0, pl, flags, d, status);
+                CullResult r = cull_one(S, V, s_frustum, eye, s_vp, pyr, pw0, ph0, pl, flags, d, pass == 2, status);
                 vis = r.visible;
                 occ = r.occluded;
             } else {

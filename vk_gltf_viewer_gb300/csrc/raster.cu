@@ -613,13 +613,34 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
             const float tdet = s_tdet[warp];
             const float* mvp = s_mvp[warp];
             // Vertex stage: clip position, outcode, guard flag and the 28.8 snap,
-            // each computed once per meshlet vertex.
-            for (uint32_t k = lane; k < vc; k += 32) {
-                const vkgv_vertex* vx = verts + __ldg(vidx + k);
-                const float2 xy = __ldg(reinterpret_cast<const float2*>(vx->position));
-                const float zz = __ldg(&vx->position[2]);
+            // each computed once per meshlet vertex (two per lane).  All global
+            // loads of the stage, and the triangle-index words (32-bit loads
+            // when the block is 4-byte aligned, as meshoptimizer pads each
+            // block to 4), are issued before any of the math.
+            const uint32_t nbytes = 3 * tc, nwords = (nbytes + 3) / 4;  // <= 95 words
+            const bool tri_words = (reinterpret_cast<uintptr_t>(tri) & 3u) == 0;
+            uint32_t tw[3] = {0u, 0u, 0u};
+            if (tri_words) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    if (lane + 32u * q < nwords) tw[q] = __ldg(reinterpret_cast<const uint32_t*>(tri) + lane + 32 * q);
+            }
+            const bool h0 = (uint32_t)lane < vc, h1 = (uint32_t)lane + 32u < vc;
+            const vkgv_vertex* vx0 = verts + (h0 ? __ldg(vidx + lane) : 0u);
+            const vkgv_vertex* vx1 = verts + (h1 ? __ldg(vidx + lane + 32) : 0u);
+            float2 xy0 = make_float2(0.0f, 0.0f), xy1 = xy0;
+            float zz0 = 0.0f, zz1 = 0.0f;
+            if (h0) {
+                xy0 = __ldg(reinterpret_cast<const float2*>(vx0->position));
+                zz0 = __ldg(&vx0->position[2]);
+            }
+            if (h1) {
+                xy1 = __ldg(reinterpret_cast<const float2*>(vx1->position));
+                zz1 = __ldg(&vx1->position[2]);
+            }
+            auto vertex = [&](uint32_t k, float px, float py, float pz) {
                 float r[4];
-                m4v(mvp, xy.x, xy.y, zz, 1.0f, r);
+                m4v(mvp, px, py, pz, 1.0f, r);
                 const float4 cv = make_float4(r[0], r[1], r[2], r[3]);
                 clip[k] = cv;
                 int32_t X = 0, Y = 0;
@@ -628,18 +649,16 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
                 if (outside_guard(cv)) fl |= kFlagGuard;
                 if (snap(cv, c, X, Y, Z)) fl |= kFlagSnapped;
                 svtx[k] = make_int4(X, Y, __float_as_int(Z), (int)fl);
-            }
-            // Triangle-index bytes into shared memory, 32-bit loads when the
-            // block is 4-byte aligned (meshoptimizer pads each block to 4).
-            {
-                const uint32_t nbytes = 3 * tc;
-                if ((reinterpret_cast<uintptr_t>(tri) & 3u) == 0) {
-                    const uint32_t* tw = reinterpret_cast<const uint32_t*>(tri);
-                    for (uint32_t k = lane; k < (nbytes + 3) / 4; k += 32) sidx[k] = __ldg(tw + k);
-                } else {
-                    uint8_t* b = reinterpret_cast<uint8_t*>(sidx);
-                    for (uint32_t k = lane; k < nbytes; k += 32) b[k] = __ldg(tri + k);
-                }
+            };
+            if (h0) vertex(lane, xy0.x, xy0.y, zz0);
+            if (h1) vertex(lane + 32, xy1.x, xy1.y, zz1);
+            if (tri_words) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    if (lane + 32u * q < nwords) sidx[lane + 32 * q] = tw[q];
+            } else {
+                uint8_t* b = reinterpret_cast<uint8_t*>(sidx);
+                for (uint32_t k = lane; k < nbytes; k += 32) b[k] = __ldg(tri + k);
             }
             __syncwarp();
             bool any_slow = false;
