@@ -47,6 +47,7 @@ __device__ __forceinline__ Range hull(Range a, Range b) {
 // (size s_hi); the footprint is monotone in the texel index.
 __device__ __forceinline__ Range footprint_range(Range r, uint32_t s_hi, uint32_t s_lo) {
     if (r.lo > r.hi) return r;
+    if (s_lo == 2 * s_hi) return Range{2 * r.lo, 2 * r.hi + 1};  // exact halving (see axis_footprint)
     int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
     footprint_axis(fdiv(fadd((float)r.lo, 0.5f), (float)s_hi), s_lo, a0, a1);
     const int nb = footprint_axis(fdiv(fadd((float)r.hi, 0.5f), (float)s_hi), s_lo, b0, b1);
@@ -109,20 +110,21 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
     float* lvl[5] = {nullptr, smem, smem + kOff2, smem + kOff3, smem + kOff4};
     const int cap[5] = {0, kCap1, kCap2, kCap3, kCap4};
 
-    if (threadIdx.x == 0) {
-        // Ranges each level must compute: owned tile, plus the footprint of
-        // the level above (top-down).
-        s_bad = 0;
+    if (threadIdx.x == 0) s_bad = 0;
+    __syncthreads();
+    if (threadIdx.x == 0 || threadIdx.x == 32) {
+        // Ranges each level must compute along one axis (x by thread 0, y
+        // by thread 32): the owned tile, plus the footprint of the level
+        // above (top-down).
+        const bool ax = threadIdx.x == 0;
+        const uint32_t full = ax ? w : h, b = ax ? bx : by;
+        Range* rr = ax ? rx : ry;
         for (int j = Kp; j >= 1; --j) {
             const uint32_t t = (uint32_t)hiz_tile_edge(j, Kp);
-            Range ox = owned(bx, t, w >> j), oy = owned(by, t, h >> j);
-            if (j < Kp) {
-                ox = hull(ox, footprint_range(rx[j + 1], w >> (j + 1), w >> j));
-                oy = hull(oy, footprint_range(ry[j + 1], h >> (j + 1), h >> j));
-            }
-            rx[j] = ox;
-            ry[j] = oy;
-            if (ox.hi - ox.lo + 1 > cap[j] || oy.hi - oy.lo + 1 > cap[j]) s_bad = 1;
+            Range o = owned(b, t, full >> j);
+            if (j < Kp) o = hull(o, footprint_range(rr[j + 1], full >> (j + 1), full >> j));
+            rr[j] = o;
+            if (o.hi - o.lo + 1 > cap[j]) s_bad = 1;
         }
     }
     __syncthreads();

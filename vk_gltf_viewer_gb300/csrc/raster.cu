@@ -728,15 +728,14 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
     }
 }
 
-// Drains the binned rectangles: one CTA per rectangle, its 256 threads laid
-// out as chunk x (256 / chunk).
+// Drains the binned rectangles: one warp per rectangle, its pixels spread
+// over the lanes in row-major order (eight rectangles in flight per CTA).
 __global__ void __launch_bounds__(256) k_raster_big(const BigTri* __restrict__ q, const uint32_t* count,
-                                                    uint32_t cap, const DeviceView* __restrict__ views,
-                                                    uint32_t chunk) {
+                                                    uint32_t cap, const DeviceView* __restrict__ views) {
     const uint32_t n = min(*count, cap);
-    const int tx = (int)(threadIdx.x % chunk), ty = (int)(threadIdx.x / chunk);
-    const int rows = (int)(256 / chunk);
-    for (uint32_t e = blockIdx.x; e < n; e += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < n; e += warps) {
         const BigTri t = q[e];
         const DeviceView& V = views[t.view];
         unsigned long long* depth = V.depth_id;
@@ -749,25 +748,27 @@ __global__ void __launch_bounds__(256) k_raster_big(const BigTri* __restrict__ q
             const int32_t dx = t.x[b] - t.x[a], dy = t.y[b] - t.y[a];
             bias[k] = (dy < 0 || (dy == 0 && dx > 0)) ? 0 : 1;
         }
-        for (int py = t.py0 + ty; py <= (int)t.py1; py += rows) {
-            const int32_t sy = py * 256 + 128;
-            const float zrow = __fmaf_rn(t.pb, __int2float_rn(sy - t.y[0]), t.z0);
-            for (int px = t.px0 + tx; px <= (int)t.px1; px += (int)chunk) {
-                const int32_t sx = px * 256 + 128;
-                bool covered = true;
+        const uint32_t bw = (uint32_t)t.px1 - t.px0 + 1u, area = bw * ((uint32_t)t.py1 - t.py0 + 1u);
+        // floor((i + 0.5) / bw) from the float reciprocal is exact here: the
+        // quotient stays at least 0.5 / bw from an integer and i < 4096.
+        const float inv_bw = 1.0f / (float)bw;
+        for (uint32_t i = lane; i < area; i += 32) {
+            const uint32_t ly = (uint32_t)(((float)i + 0.5f) * inv_bw);
+            const int px = (int)(t.px0 + (i - ly * bw)), py = (int)(t.py0 + ly);
+            const int32_t sx = px * 256 + 128, sy = py * 256 + 128;
+            bool covered = true;
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const int a = k, b = (k + 1) % 3;
-                    const int64_t ev = (int64_t)(t.x[b] - t.x[a]) * (sy - t.y[a]) -
-                                       (int64_t)(t.y[b] - t.y[a]) * (sx - t.x[a]);
-                    covered = covered && ev >= bias[k];
-                }
-                if (!covered) continue;
-                float z = __fmaf_rn(t.pa, __int2float_rn(sx - t.x[0]), zrow);
-                if (!(z > 0.0f)) z = 0.0f;
-                if (z > 1.0f) z = 1.0f;
-                plot(depth + (size_t)py * w + px, ((unsigned long long)__float_as_uint(z) << 32) | lo);
+            for (int k = 0; k < 3; ++k) {
+                const int a = k, b = (k + 1) % 3;
+                const int64_t ev = (int64_t)(t.x[b] - t.x[a]) * (sy - t.y[a]) -
+                                   (int64_t)(t.y[b] - t.y[a]) * (sx - t.x[a]);
+                covered = covered && ev >= bias[k];
             }
+            if (!covered) continue;
+            float z = __fmaf_rn(t.pa, __int2float_rn(sx - t.x[0]), __fmaf_rn(t.pb, __int2float_rn(sy - t.y[0]), t.z0));
+            if (!(z > 0.0f)) z = 0.0f;
+            if (z > 1.0f) z = 1.0f;
+            plot(depth + (size_t)py * w + px, ((unsigned long long)__float_as_uint(z) << 32) | lo);
         }
     }
 }
@@ -809,8 +810,7 @@ void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews,
         }
     }
     if (between) cudaEventRecord(between, stream);
-    const uint32_t chunk = cfg.chunk >= 8 && cfg.chunk <= 64 ? cfg.chunk : 32;
-    k_raster_big<<<sm_count * 8, 256, 0, stream>>>(big, big_count, big_capacity, views, chunk);
+    k_raster_big<<<sm_count * 8, 256, 0, stream>>>(big, big_count, big_capacity, views);
 }
 
 }  // namespace vkgv

@@ -196,8 +196,9 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
     float sampled[4] = {1.0f, 1.0f, 1.0f, 1.0f};
     if (mat.albedo_index != VKGV_INVALID_HANDLE && mat.albedo_index < S.texture_count) {
         // transformUv (mesh_common.h.glsl:129-135): rotate, scale, offset
-        float sn, cs;
-        sincosf(mat.uv_rotation, &sn, &cs);
+        // sincos(+-0) = (+-0, 1) exactly; skip the reduction for unrotated UVs
+        float sn = mat.uv_rotation, cs = 1.0f;
+        if (mat.uv_rotation != 0.0f) sincosf(mat.uv_rotation, &sn, &cs);
         const float ru = fadd(fmul(cs, uv[0]), fmul(sn, uv[1]));
         const float rv = fadd(fmul(-sn, uv[0]), fmul(cs, uv[1]));
         const float tu = fadd(fmul(ru, mat.uv_scale[0]), mat.uv_offset[0]);
