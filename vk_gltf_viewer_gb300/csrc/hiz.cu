@@ -31,6 +31,7 @@ constexpr int kThreads = 1024;
 constexpr int kOff2 = kCap1 * kCap1, kOff3 = kOff2 + kCap2 * kCap2, kOff4 = kOff3 + kCap3 * kCap3;
 constexpr int kTailA = 16384, kTailB = 8192;
 constexpr int kSmemFloats = kTailA + kTailB;
+constexpr int kTailAxis = 1024;  // largest tail level edge with per-axis footprint tables
 static_assert(kOff4 + kCap4 * kCap4 <= kSmemFloats, "tile levels fit the shared buffer");
 
 struct Range {
@@ -147,20 +148,44 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
             const Range BX = j > 1 ? rx[j - 1] : Range{0, 0};
             const Range BY = j > 1 ? ry[j - 1] : Range{0, 0};
             const int bw = BX.hi - BX.lo + 1;
+            if (j == 1 && w == 2 * dw && h == 2 * dh) {
+                // Level 1 over the depth image, 2x2 blocks with one 16-byte
+                // load per row (depth_id is 16-byte aligned and w is even).
+                // Batches of four texels per thread: all eight loads are in
+                // flight before the first minimum.
+                for (int i0 = threadIdx.x; i0 < rw * rh; i0 += 4 * kThreads) {
+                    uint32_t d[4][4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int i = i0 + k * kThreads;
+                        if (i < rw * rh) {
+                            const int x = X.lo + i % rw, y = Y.lo + i / rw;
+                            const ulonglong2* q =
+                                reinterpret_cast<const ulonglong2*>(V.depth_id + (size_t)(2 * y) * w + 2 * x);
+                            const ulonglong2 a = __ldg(q), b = __ldg(q + (w >> 1));
+                            d[k][0] = (uint32_t)(a.x >> 32), d[k][1] = (uint32_t)(a.y >> 32);
+                            d[k][2] = (uint32_t)(b.x >> 32), d[k][3] = (uint32_t)(b.y >> 32);
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int i = i0 + k * kThreads;
+                        if (i < rw * rh) {
+                            const int x = X.lo + i % rw, y = Y.lo + i / rw;
+                            const float r = gmin(gmin(gmin(u2f(d[k][0]), u2f(d[k][1])), u2f(d[k][2])), u2f(d[k][3]));
+                            here[i] = r;
+                            if (x >= OX.lo && x <= OX.hi && y >= OY.lo && y <= OY.hi) dst[(size_t)y * dw + x] = r;
+                        }
+                    }
+                }
+                __syncthreads();
+                continue;
+            }
 #pragma unroll 4
             for (int i = threadIdx.x; i < rw * rh; i += blockDim.x) {
                 const int x = X.lo + i % rw, y = Y.lo + i / rw;
                 float r;
-                if (j == 1 && w == 2 * dw && h == 2 * dh) {
-                    // 2x2 block of the depth image: one 16-byte load per row
-                    // (depth_id is 16-byte aligned and w is even)
-                    const ulonglong2* q =
-                        reinterpret_cast<const ulonglong2*>(V.depth_id + (size_t)(2 * y) * w + 2 * x);
-                    const ulonglong2 a = __ldg(q), b = __ldg(q + (w >> 1));
-                    r = gmin(gmin(gmin(u2f((uint32_t)(a.x >> 32)), u2f((uint32_t)(a.y >> 32))),
-                                  u2f((uint32_t)(b.x >> 32))),
-                             u2f((uint32_t)(b.y >> 32)));
-                } else if (j == 1) {
+                if (j == 1) {
                     r = reduce_texel(x, y, dw, dh, w, h, [&](int sx, int sy) { return depth_at(V.depth_id, w, sx, sy); });
                 } else {
                     r = reduce_texel(x, y, dw, dh, w >> (j - 1), h >> (j - 1),
@@ -190,12 +215,44 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
         for (uint32_t i = threadIdx.x; i < top_w * top_h; i += blockDim.x) cur[i] = __ldcg(src + i);
         __syncthreads();
     }
+    // per-axis footprints of the current tail level: x0 | x1 << 14 | n << 28
+    __shared__ uint32_t s_fx[kTailAxis], s_fy[kTailAxis];
+    const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
     for (uint32_t j = (uint32_t)Kp + 1; j <= L; ++j) {
         const uint32_t dw = w >> j, dh = h >> j;
         const uint32_t mw = mip_dim(w0, j - 1), mh = mip_dim(h0, j - 1);
         float* dst = V.pyr + mip_offset(w0, h0, j - 1);
         if (dw == 0 || dh == 0) {
             for (uint32_t i = threadIdx.x; i < mw * mh; i += blockDim.x) dst[i] = 0.0f;
+        } else if (in_smem && dw <= (uint32_t)kTailAxis && dh <= (uint32_t)kTailAxis) {
+            // One footprint per column and per row (dw + dh of them instead
+            // of two per texel), then warps take rows and lanes columns.
+            const uint32_t sw = mip_dim(w0, j - 2), sh = mip_dim(h0, j - 2);
+            for (uint32_t i = threadIdx.x; i < dw + dh; i += blockDim.x) {
+                int a = 0, b = 0;
+                const bool isx = i < dw;
+                const int n = isx ? axis_footprint((int)i, dw, sw, a, b) : axis_footprint((int)(i - dw), dh, sh, a, b);
+                const uint32_t packed = (uint32_t)a | ((uint32_t)b << 14) | ((uint32_t)n << 28);
+                if (isx) s_fx[i] = packed;
+                else s_fy[i - dw] = packed;
+            }
+            __syncthreads();
+            for (uint32_t y = (uint32_t)warp; y < dh; y += kThreads / 32) {
+                const uint32_t fy = s_fy[y];
+                const int y0 = (int)(fy & 0x3fffu), y1 = (int)((fy >> 14) & 0x3fffu), ny = (int)(fy >> 28);
+                for (uint32_t x = (uint32_t)lane; x < dw; x += 32) {
+                    const uint32_t fx = s_fx[x];
+                    const int x0 = (int)(fx & 0x3fffu), x1 = (int)((fx >> 14) & 0x3fffu), nx = (int)(fx >> 28);
+                    float r = cur[y0 * (int)sw + x0];
+                    if (nx == 2) r = gmin(r, cur[y0 * (int)sw + x1]);
+                    if (ny == 2) {
+                        r = gmin(r, cur[y1 * (int)sw + x0]);
+                        if (nx == 2) r = gmin(r, cur[y1 * (int)sw + x1]);
+                    }
+                    nxt[y * dw + x] = r;
+                    dst[y * dw + x] = r;
+                }
+            }
         } else {
             const uint32_t sw = j == 1 ? w : mip_dim(w0, j - 2), sh = j == 1 ? h : mip_dim(h0, j - 2);
             const float* src = j == 1 ? nullptr : V.pyr + mip_offset(w0, h0, j - 2);
