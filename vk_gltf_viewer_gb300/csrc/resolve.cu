@@ -37,7 +37,8 @@ __device__ __forceinline__ float to_linear(float c) {
 
 // The textured resolve is compared within 1/255; its sRGB curves use the
 // hardware exp2/log2 pow (relative error ~1e-6, which can move a channel by
-// one step only at a rounding boundary).
+// one step only at a rounding boundary) and multiply by the reciprocals of
+// 1.055 and 12.92 (one ulp from the quotients) on the filtered colour.
 __device__ __forceinline__ float from_linear_fast(float c) {
     const bool cutoff = c < 0.0031308f;
     const float higher = fsub(fmul(1.055f, __powf(c, 1.0f / 2.4f)), 0.055f);
@@ -47,8 +48,8 @@ __device__ __forceinline__ float from_linear_fast(float c) {
 
 __device__ __forceinline__ float to_linear_fast(float c) {
     const bool cutoff = c < 0.04045f;
-    const float higher = __powf(fdiv(fadd(c, 0.055f), 1.055f), 2.4f);
-    const float lower = fdiv(c, 12.92f);
+    const float higher = __powf(fmul(fadd(c, 0.055f), 1.0f / 1.055f), 2.4f);
+    const float lower = fmul(c, 1.0f / 12.92f);
     return cutoff ? lower : higher;
 }
 
