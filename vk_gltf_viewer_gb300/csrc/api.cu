@@ -49,6 +49,7 @@ struct vkgv_ctx {
     Scratch rejected;   // per view: capacity draw_count
     Scratch deferred;   // per view: capacity draw_count
     Scratch diff;       // adjoint: internal raster scene of the differentiable mesh
+    Scratch diff_acc;   // adjoint: float4 gradient accumulators (positions, colours, texels)
     Scratch tdet;       // determinant(M) per node transform (vkgv_scene.transform_count)
     Scratch mvp;        // view_projection * M per view and node
     BigTri* big = nullptr;
@@ -638,6 +639,7 @@ struct DiffPlan {
     DiffArgs A{};
     Prepared P;
     std::vector<DeviceView> views;
+    size_t acc_bytes = 0;  // float4 accumulators to zero before a backward pass
 };
 
 int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* views, uint32_t n, bool backward,
@@ -717,6 +719,19 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
     A.grad_positions = reinterpret_cast<float*>(gpos);
     A.grad_colors = reinterpret_cast<float*>(gcol);
     A.grad_texture = reinterpret_cast<float*>(gtex);
+    A.vertex_count = ds->vertex_count;
+    if (backward) {
+        const size_t nv = gpos ? V : 0, nc = gcol ? V : 0, nt = gtex ? (size_t)ds->tex_width * ds->tex_height : 0;
+        D.acc_bytes = sizeof(float4) * (nv + nc + nt);
+        if (D.acc_bytes) {
+            rc = ensure_scratch(ctx, ctx->diff_acc, D.acc_bytes, "adjoint accumulators");
+            if (rc) return rc;
+            float4* acc = static_cast<float4*>(ctx->diff_acc.ptr);
+            A.acc_pos = gpos ? acc : nullptr;
+            A.acc_col = gcol ? acc + nv : nullptr;
+            A.acc_tex = gtex ? acc + nv + nc : nullptr;
+        }
+    }
     return VKGV_OK;
 }
 
@@ -732,7 +747,9 @@ void diff_record(vkgv_ctx* ctx, const DiffPlan& D, const DeviceView* dv, uint32_
     RasterLists l1{1, nullptr, nullptr, 0, 4};
     launch_raster(D.P.S, dv, n, l1, ctx->raster, ctx->big, ctx->counters + 0, ctx->big_cap, ctx->counters + 6, ctx->status,
                   ctx->sm_count, stream);
+    if (backward && D.acc_bytes) cudaMemsetAsync(ctx->diff_acc.ptr, 0, D.acc_bytes, stream);
     launch_diff_shade(D.A, dv, n, D.P.max_px, backward, stream);
+    if (backward) launch_diff_scatter(D.A, stream);
 }
 
 int diff_run(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* views, uint32_t n, bool backward,

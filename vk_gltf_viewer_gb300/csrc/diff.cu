@@ -143,7 +143,17 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             vi[k] = A.vertex_indices[ml.vertex_offset + tri[k]];
-            clip_ab(VP, A.positions + 3 * (size_t)vi[k], nx, ny, a[k], b[k]);
+            const float* q = A.positions + 3 * (size_t)vi[k];
+            if (BACKWARD) {
+                clip_ab(VP, q, nx, ny, a[k], b[k]);
+            } else {
+                // the forward image needs fp32 accuracy only (no cancellation
+                // reaches a gradient)
+                float c[4];
+                m4v(VP, q[0], q[1], q[2], 1.0f, c);
+                a[k] = fsub(c[0], fmul(nx, c[3]));
+                b[k] = fsub(c[1], fmul(ny, c[3]));
+            }
         }
         float l[3] = {fsub(fmul(a[1], b[2]), fmul(a[2], b[1])), fsub(fmul(a[2], b[0]), fmul(a[0], b[2])),
                       fsub(fmul(a[0], b[1]), fmul(a[1], b[0]))};
@@ -214,16 +224,13 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
             dcol[j] = g[j] * A.albedo[j] * tex[j];
             dtex[j] = g[j] * col[j] * A.albedo[j];
         }
-        if (A.grad_texture) {
+        if (A.acc_tex) {
             const float w00 = (1.0f - ax) * (1.0f - ay), w01 = ax * (1.0f - ay);
             const float w10 = (1.0f - ax) * ay, w11 = ax * ay;
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                atomicAdd(A.grad_texture + i00 + j, dtex[j] * w00);
-                atomicAdd(A.grad_texture + i01 + j, dtex[j] * w01);
-                atomicAdd(A.grad_texture + i10 + j, dtex[j] * w10);
-                atomicAdd(A.grad_texture + i11 + j, dtex[j] * w11);
-            }
+            atomicAdd(A.acc_tex + i00 / 3, make_float4(dtex[0] * w00, dtex[1] * w00, dtex[2] * w00, 0.0f));
+            atomicAdd(A.acc_tex + i01 / 3, make_float4(dtex[0] * w01, dtex[1] * w01, dtex[2] * w01, 0.0f));
+            atomicAdd(A.acc_tex + i10 / 3, make_float4(dtex[0] * w10, dtex[1] * w10, dtex[2] * w10, 0.0f));
+            atomicAdd(A.acc_tex + i11 / 3, make_float4(dtex[0] * w11, dtex[1] * w11, dtex[2] * w11, 0.0f));
         }
         // d tex / d uv' through the bilinear weights
         float dtu = 0.0f, dtv = 0.0f;
@@ -240,11 +247,10 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             dlam[k] = dcol[0] * C[k][0] + dcol[1] * C[k][1] + dcol[2] * C[k][2] + du * UV[k][0] + dv * UV[k][1];
-            if (A.grad_colors)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) atomicAdd(A.grad_colors + 3 * (size_t)vi[k] + j, dcol[j] * lam[k]);
+            if (A.acc_col)
+                atomicAdd(A.acc_col + vi[k], make_float4(dcol[0] * lam[k], dcol[1] * lam[k], dcol[2] * lam[k], 0.0f));
         }
-        if (!A.grad_positions) continue;
+        if (!A.acc_pos) continue;
         const float dot = lam[0] * dlam[0] + lam[1] * dlam[1] + lam[2] * dlam[2];
         const float dl[3] = {(dlam[0] - dot) / sum, (dlam[1] - dot) / sum, (dlam[2] - dot) / sum};
         // l = a x b: dL/da = b x dl, dL/db = dl x a
@@ -253,10 +259,9 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const float dx = da[k], dy = db[k], dw = -nx * da[k] - ny * db[k];
-#pragma unroll
-            for (int q = 0; q < 3; ++q)
-                atomicAdd(A.grad_positions + 3 * (size_t)vi[k] + q,
-                          VP[q * 4 + 0] * dx + VP[q * 4 + 1] * dy + VP[q * 4 + 3] * dw);
+            atomicAdd(A.acc_pos + vi[k], make_float4(VP[0] * dx + VP[1] * dy + VP[3] * dw,
+                                                     VP[4] * dx + VP[5] * dy + VP[7] * dw,
+                                                     VP[8] * dx + VP[9] * dy + VP[11] * dw, 0.0f));
         }
     }
     if (BACKWARD && A.loss) {
@@ -267,6 +272,23 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
     }
 }
 
+// grad[3 i + j] += acc[i].{x, y, z}
+__global__ void k_diff_scatter(const float4* __restrict__ acc, float* __restrict__ grad, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 a = acc[i];
+        grad[3 * (size_t)i] += a.x;
+        grad[3 * (size_t)i + 1] += a.y;
+        grad[3 * (size_t)i + 2] += a.z;
+    }
+}
+
+void scatter(const float4* acc, float* grad, uint32_t n, cudaStream_t stream) {
+    if (!acc || !grad || n == 0) return;
+    uint32_t blocks = (n + 255) / 256;
+    blocks = blocks < 8192 ? blocks : 8192;
+    k_diff_scatter<<<blocks, 256, 0, stream>>>(acc, grad, n);
+}
+
 }  // namespace
 
 void launch_diff_setup(const DiffSetup& S, cudaStream_t stream) {
@@ -274,6 +296,12 @@ void launch_diff_setup(const DiffSetup& S, cudaStream_t stream) {
     uint32_t blocks = (n + 255) / 256;
     blocks = blocks ? (blocks < 4096 ? blocks : 4096) : 1;
     k_diff_setup<<<blocks, 256, 0, stream>>>(S);
+}
+
+void launch_diff_scatter(const DiffArgs& A, cudaStream_t stream) {
+    scatter(A.acc_pos, A.grad_positions, A.vertex_count, stream);
+    scatter(A.acc_col, A.grad_colors, A.vertex_count, stream);
+    scatter(A.acc_tex, A.grad_texture, A.tex_w * A.tex_h, stream);
 }
 
 void launch_diff_shade(const DiffArgs& A, const DeviceView* views, uint32_t nviews, uint64_t max_px, bool backward,

@@ -75,10 +75,20 @@ struct DiffArgs {
     float* grad_positions;
     float* grad_colors;
     float* grad_texture;
+    // per-vertex / per-texel float4 accumulators (one vector atomic per
+    // vertex or texel instead of three), added into the three arrays above
+    // by launch_diff_scatter; null where the gradient is not requested
+    float4* acc_pos;
+    float4* acc_col;
+    float4* acc_tex;
+    uint32_t vertex_count;
+    uint32_t _pad;
 };
 
 void launch_diff_setup(const DiffSetup& S, cudaStream_t stream);
 void launch_diff_shade(const DiffArgs& A, const DeviceView* views, uint32_t nviews, uint64_t max_px, bool backward,
                        cudaStream_t stream);
+// Adds the float4 accumulators of A into the caller's gradient arrays.
+void launch_diff_scatter(const DiffArgs& A, cudaStream_t stream);
 
 }  // namespace vkgv
