@@ -655,7 +655,9 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
     const size_t V = ds->vertex_count, M = ds->meshlet_count;
     const size_t off_draws = align256(sizeof(vkgv_vertex) * V);
     const size_t off_xf = off_draws + align256(sizeof(vkgv_meshlet_draw) * std::max<size_t>(M, 1));
-    const size_t off_prim = off_xf + 256, off_mat = off_prim + 256, total = off_mat + 256;
+    const size_t off_prim = off_xf + 256, off_mat = off_prim + 256, off_vpack = off_mat + 256;
+    const size_t off_tri = off_vpack + align256(2 * sizeof(float4) * V);
+    const size_t total = off_tri + align256(sizeof(uint4) * (std::max<size_t>(M, 1) << VKGV_TRIANGLE_BITS));
     int rc = ensure_scratch(ctx, ctx->diff, total, "adjoint scene");
     if (rc) return rc;
     char* base = static_cast<char*>(ctx->diff.ptr);
@@ -672,6 +674,10 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
     S.transform = reinterpret_cast<float*>(base + off_xf);
     S.primitive = reinterpret_cast<vkgv_primitive*>(base + off_prim);
     S.material = reinterpret_cast<vkgv_material*>(base + off_mat);
+    S.colors = reinterpret_cast<const float*>(ds->colors);
+    S.uvs = reinterpret_cast<const float*>(ds->uvs);
+    S.vpack = reinterpret_cast<float4*>(base + off_vpack);
+    S.tri_verts = reinterpret_cast<uint4*>(base + off_tri);
     vkgv_scene scene{};
     scene.draw_buffer = reinterpret_cast<uint64_t>(S.draws);
     scene.transform_buffer = reinterpret_cast<uint64_t>(S.transform);
@@ -720,6 +726,8 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
     A.grad_colors = reinterpret_cast<float*>(gcol);
     A.grad_texture = reinterpret_cast<float*>(gtex);
     A.vertex_count = ds->vertex_count;
+    A.vpack = S.vpack;
+    A.tri_verts = S.tri_verts;
     if (backward) {
         const size_t nv = gpos ? V : 0, nc = gcol ? V : 0, nt = gtex ? (size_t)ds->tex_width * ds->tex_height : 0;
         D.acc_bytes = sizeof(float4) * (nv + nc + nt);

@@ -36,6 +36,20 @@ __global__ void k_diff_setup(DiffSetup S) {
         v._pad = 0;
         v.uv[0] = v.uv[1] = 0;
         S.vertices[i] = v;
+        const float* c = S.colors + 3 * (size_t)i;
+        const float* t = S.uvs + 2 * (size_t)i;
+        S.vpack[2 * (size_t)i] = make_float4(v.position[0], v.position[1], v.position[2], c[0]);
+        S.vpack[2 * (size_t)i + 1] = make_float4(c[1], c[2], t[0], t[1]);
+    }
+    // the three vertex indices of every visibility id, so that a pixel
+    // reaches its vertices in one dependent load
+    for (uint32_t j = tid; j < (S.meshlet_count << VKGV_TRIANGLE_BITS); j += stride) {
+        const uint32_t m = j >> VKGV_TRIANGLE_BITS, t = j & ((1u << VKGV_TRIANGLE_BITS) - 1u);
+        const vkgv_meshlet ml = S.meshlets[m];
+        if (t >= ml.triangle_count) continue;
+        const uint8_t* tri = S.tri_indices + ml.triangle_offset + 3 * t;
+        const uint32_t* vidx = S.vertex_indices + ml.vertex_offset;
+        S.tri_verts[j] = make_uint4(vidx[tri[0]], vidx[tri[1]], vidx[tri[2]], 0u);
     }
     for (uint32_t i = tid; i < S.meshlet_count; i += stride) S.draws[i] = vkgv_meshlet_draw{0u, i, 0u};
     if (tid < 16) S.transform[tid] = (tid % 5 == 0) ? 1.0f : 0.0f;
@@ -110,7 +124,6 @@ template <bool BACKWARD>
 __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView* __restrict__ views) {
     const DeviceView& V = views[blockIdx.y];
     const uint32_t w = V.w, n = V.w * V.h;
-    const vkgv_meshlet* meshlets = A.meshlets;
     float VP[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) VP[k] = V.cam->view_projection[k];
@@ -131,19 +144,21 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
             else if (V.diff_rgb) V.diff_rgb[3 * p] = V.diff_rgb[3 * p + 1] = V.diff_rgb[3 * p + 2] = 0.0f;
             continue;
         }
-        const uint32_t id = lo - 1u;
-        const uint32_t m = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
-        const vkgv_meshlet ml = meshlets[m];
-        const uint8_t* tri = A.tri_indices + ml.triangle_offset + 3 * t;
+        const uint4 tvi = A.tri_verts[lo - 1u];
         // The sample point is the fp32 NDC of the pixel centre.
         const float nx = fsub(fmul(fdiv(fadd((float)(p % w), 0.5f), (float)V.w), 2.0f), 1.0f);
         const float ny = fsub(fmul(fdiv(fadd((float)(p / w), 0.5f), (float)V.h), 2.0f), 1.0f);
-        uint32_t vi[3];
+        const uint32_t vi[3] = {tvi.x, tvi.y, tvi.z};
+        float4 P0[3], P1[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            P0[k] = A.vpack[2 * (size_t)vi[k]];
+            P1[k] = A.vpack[2 * (size_t)vi[k] + 1];
+        }
         float a[3], b[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            vi[k] = A.vertex_indices[ml.vertex_offset + tri[k]];
-            const float* q = A.positions + 3 * (size_t)vi[k];
+            const float q[3] = {P0[k].x, P0[k].y, P0[k].z};
             if (BACKWARD) {
                 clip_ab(VP, q, nx, ny, a[k], b[k]);
             } else {
@@ -167,10 +182,8 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
         float C[3][3], UV[3][2];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-#pragma unroll
-            for (int j = 0; j < 3; ++j) C[k][j] = A.colors[3 * (size_t)vi[k] + j];
-            UV[k][0] = A.uvs[2 * (size_t)vi[k]];
-            UV[k][1] = A.uvs[2 * (size_t)vi[k] + 1];
+            C[k][0] = P0[k].w, C[k][1] = P1[k].x, C[k][2] = P1[k].y;
+            UV[k][0] = P1[k].z, UV[k][1] = P1[k].w;
         }
         float col[3], uv[2];
 #pragma unroll

@@ -55,6 +55,10 @@ struct DiffSetup {
     float* transform;
     vkgv_primitive* primitive;
     vkgv_material* material;
+    const float* colors;           // shading inputs packed for the shade kernel
+    const float* uvs;
+    float4* vpack;                 // per vertex: (x, y, z, r), (g, b, u, v)
+    uint4* tri_verts;              // per visibility id (meshlet << 7 | triangle): its 3 vertex indices
 };
 
 struct DiffArgs {
@@ -83,6 +87,8 @@ struct DiffArgs {
     float4* acc_tex;
     uint32_t vertex_count;
     uint32_t _pad;
+    const float4* vpack;           // from DiffSetup
+    const uint4* tri_verts;
 };
 
 void launch_diff_setup(const DiffSetup& S, cudaStream_t stream);
