@@ -303,6 +303,11 @@ enum TriKind : int { kDrop = 0, kFast = 1, kSlowClip = 2, kSlowSetup = 3 };
 // Small triangles whose clamped bbox has at most this many pixels are
 // rasterised by their own lane; larger small ones by the whole warp.
 constexpr uint32_t kLaneArea = 4;
+// Small triangles above this bbox area are queued for k_raster_big.
+#ifndef VKGV_RASTER_QUEUE_AREA
+#define VKGV_RASTER_QUEUE_AREA 16
+#endif
+constexpr uint32_t kQueueArea = VKGV_RASTER_QUEUE_AREA;
 
 struct TriClass {
     int4 q0, q1, q2;  // snapped vertex records {X, Y, Z bits, flags}
@@ -421,6 +426,37 @@ __device__ __forceinline__ void raster_small(uint32_t ct, const uint8_t* sidx8, 
             r.bh = (uint8_t)bh;
             r.bias = (uint8_t)bias;
             coop_area = bw * bh;
+        }
+    }
+    // Triangles whose bbox exceeds kQueueArea pixels go to the
+    // binned-rectangle queue (one rectangle each), drained by k_raster_big
+    // with a warp per rectangle: a meshlet of larger triangles then no
+    // longer holds one warp for all of its pixels.  The rest, and anything
+    // the full queue refuses, take the warp-cooperative raster below.
+    const unsigned mm = __ballot_sync(0xffffffffu, coop_area > kQueueArea);
+    if (mm) {
+        const int leader = __ffs(mm) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(c.big_count, (uint32_t)__popc(mm));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (coop_area > kQueueArea) {
+            const uint32_t slot = base + (uint32_t)__popc(mm & ((1u << lane) - 1u));
+            if (slot < c.big_cap) {
+                const TriRec& r = recs[lane];
+                BigTri t;
+                t.x[0] = r.x[0], t.x[1] = r.x[1], t.x[2] = r.x[2];
+                t.y[0] = r.y[0], t.y[1] = r.y[1], t.y[2] = r.y[2];
+                t.z0 = r.z0, t.pa = r.pa, t.pb = r.pb;
+                t.id = r.id;
+                t.px0 = r.bx0, t.py0 = r.by0;
+                t.px1 = (uint16_t)(r.bx0 + r.bw - 1), t.py1 = (uint16_t)(r.by0 + r.bh - 1);
+                t.view = c.view;
+                t._pad = 0;
+                c.big[slot] = t;
+                coop_area = 0;
+            } else {
+                report(c.status, kStatusQueueOverflow, slot);
+            }
         }
     }
     if (__ballot_sync(0xffffffffu, coop_area != 0) == 0) return;
