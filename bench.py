@@ -547,7 +547,8 @@ def main():
             "e2e": {"value": e2e_value, "unit": "views/s", "h2d_bytes_per_step": 352,
                     "d2h_bytes_per_step": W1080 * H1080 * 4,
                     "note": "camera H2D + frame + RGBA8 D2H per step; the D2H of step i overlaps step i+1 "
-                            "(two colour images, copy stream)"},
+                            "(two colour images, copy stream); a continuous loop, so no L2 flush between "
+                            "steps (the device-only value flushes L2 before every step)"},
             "gpu_launches": kernels_per_frame * args.steps,
             "autotune": {"bin_size": tune1["bin_size"], "meshlets_per_cta": tune1["meshlets_per_cta"],
                          "cached": tune1["cached"], "table": tune1["table"]},
