@@ -252,3 +252,50 @@ def test_cone_cull_matches_oracle_and_keeps_ids(renderer, ico, grid, which):
         assert v1.survivor_list().size < v0.survivor_list().size
         assert np.array_equal(u32(v1.visbuffer), u32(v0.visbuffer))
         assert np.array_equal(u32(v1.visbuffer), exp["ids"])
+
+
+def test_node_tables_do_not_change_the_frame(renderer, grid):
+    """A scene that gives transform_count (per-frame determinant and
+    view-projection x model tables) renders the same bits as one that does
+    not (per-meshlet and per-pixel evaluation)."""
+    flags = (abi.CULL_FRUSTUM | abi.CULL_CONE | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID
+             | abi.RESOLVE_TEXTURED | abi.WRITE_IDS)
+    w, h = 640, 360
+    cam = scene.grid_camera(w, h)
+    outs = []
+    for count in (grid.host.transforms.shape[0], 0):
+        grid.dev.scene.transform_count = count
+        try:
+            v = view(grid, cam, w, h)
+            renderer.frame(grid.dev, [v], flags)
+            torch.cuda.synchronize()
+            outs.append((u64(v.depth_id).copy(), u32(v.visbuffer).copy(), u32(v.color).copy(),
+                         v.pyramid.cpu().numpy().copy()))
+        finally:
+            grid.dev.scene.transform_count = grid.host.transforms.shape[0]
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+
+
+def test_full_rectangle_queue_falls_back_in_place(grid):
+    """With a one-entry binned-rectangle queue every queued triangle takes the
+    in-kernel fallback (warp-cooperative or inline raster); the frame still
+    matches the oracle bit for bit, and the overflow is reported."""
+    from vk_gltf_viewer_gb300.renderer import Renderer
+
+    r = Renderer(0, big_capacity=1)
+    try:
+        flags = abi.CULL_FRUSTUM | abi.BUILD_PYRAMID | abi.RESOLVE_FLAT | abi.WRITE_IDS
+        w, h = 1280, 720
+        # close to the first tori: many triangles above 16 bbox pixels
+        cam = scene.camera((1.25, 1.25, -1.5), (1.25, 1.25, 3.0), (0.0, 1.0, 0.0), 90.0, w / h)
+        v = view(grid, cam, w, h)
+        r.frame(grid.dev, [v], flags)
+        torch.cuda.synchronize()
+        exp = ob.frame(grid.orc, cam, w, h, oracle_flags(flags))
+        assert np.array_equal(u64(v.depth_id), exp["depth_id"])
+        assert np.array_equal(u32(v.visbuffer), exp["ids"])
+        code, _ = r.device_status()
+        assert code == 2  # queue overflow, handled in place
+    finally:
+        r.close()
