@@ -246,6 +246,16 @@ __device__ __forceinline__ int footprint_axis(float u, uint32_t size, int& i0, i
     return n;
 }
 
+// Programmatic dependent launch.  A frame's kernels are launched with the
+// programmatic-stream-serialisation attribute: each one first lets its
+// successor's CTAs be scheduled (they become resident as this grid drains)
+// and then waits for its predecessor grid to complete and flush, before it
+// reads anything.  Without the attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Device status word: records the first violation (code, detail).
 __device__ __forceinline__ void report(uint32_t* status, uint32_t code, uint32_t detail) {
     if (status && atomicCAS(status, 0u, code) == 0u) status[1] = detail;

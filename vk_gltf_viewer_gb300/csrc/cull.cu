@@ -157,6 +157,7 @@ __device__ __forceinline__ void warp_append(bool flag, uint32_t value, uint32_t*
 //         survivors[counters[0] + ...] via counters[2].
 __global__ void __launch_bounds__(256) k_cull(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags,
                                               uint32_t pass, uint32_t* status) {
+    pdl_begin();
     const DeviceView& V = views[blockIdx.y];
     const vkgv_camera* cam = V.cam;
     __shared__ float s_frustum[24];
@@ -232,7 +233,7 @@ void launch_cull(const SceneArgs& S, const DeviceView* views, uint32_t nviews, u
     if (per_view > 65535u) per_view = 65535u;
     if (per_view == 0) per_view = 1;
     dim3 grid(per_view, nviews);
-    k_cull<<<grid, threads, 0, stream>>>(S, views, flags, pass, status);
+    launch_pdl(k_cull, grid, dim3(threads), 0, stream, S, views, flags, pass, status);
 }
 
 }  // namespace vkgv

@@ -95,6 +95,7 @@ __device__ __forceinline__ float reduce_texel(int x, int y, uint32_t dw, uint32_
 }
 
 __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__ views, uint32_t* status) {
+    pdl_begin();
     const DeviceView& V = views[blockIdx.z];
     if (!V.pyr || V.pyr_levels == 0) return;
     const uint32_t w = V.w, h = V.h, L = V.pyr_levels;
@@ -290,7 +291,7 @@ void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint
         attr_set = true;
     }
     dim3 grid(tiles_x ? tiles_x : 1, tiles_y ? tiles_y : 1, nviews);
-    k_hiz<<<grid, kThreads, kSmemFloats * sizeof(float), stream>>>(views, status);
+    launch_pdl(k_hiz, grid, dim3(kThreads), kSmemFloats * sizeof(float), stream, views, status);
 }
 
 }  // namespace vkgv

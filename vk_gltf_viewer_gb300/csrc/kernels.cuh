@@ -1,9 +1,29 @@
 // Kernel launchers shared between the translation units of libvkgv.
 #pragma once
 
+#include <utility>
+
 #include "common.cuh"
 
 namespace vkgv {
+
+// Launches a frame kernel with programmatic stream serialisation (the
+// kernel calls pdl_begin() before touching its predecessor's results).
+template <typename... Params, typename... Args>
+inline void launch_pdl(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 struct RasterLists {
     uint32_t pass;            // 1, 2, or 0 for an explicit list

@@ -495,6 +495,7 @@ __device__ __forceinline__ void raster_small(uint32_t ct, const uint8_t* sidx8, 
 // off-screen-spanning triangles), so the fast instance calls no function.
 template <int WARPS, bool SLOW>
 __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER_SM) / WARPS) k_raster(RasterParams P) {
+    pdl_begin();
     __shared__ float4 s_clip[WARPS][64];
     // per vertex: {X, Y (28.8), Z bits, flags} read with one 16-byte load
     __shared__ int4 s_vtx[WARPS][64];
@@ -768,6 +769,7 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
 // over the lanes in row-major order (eight rectangles in flight per CTA).
 __global__ void __launch_bounds__(256) k_raster_big(const BigTri* __restrict__ q, const uint32_t* count,
                                                     uint32_t cap, const DeviceView* __restrict__ views) {
+    pdl_begin();
     const uint32_t n = min(*count, cap);
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
@@ -815,8 +817,8 @@ template <int WARPS>
 void launch_variant(const RasterParams& P, uint32_t sm_count, uint32_t blocks_override, cudaStream_t stream) {
     const uint32_t fast = blocks_override ? blocks_override : sm_count * (VKGV_RASTER_WARPS_PER_SM / WARPS);
     const uint32_t slow = blocks_override ? blocks_override : sm_count * (16 / WARPS > 0 ? 16 / WARPS : 1);
-    k_raster<WARPS, false><<<fast, WARPS * 32, 0, stream>>>(P);
-    k_raster<WARPS, true><<<slow, WARPS * 32, 0, stream>>>(P);
+    launch_pdl(k_raster<WARPS, false>, dim3(fast), dim3(WARPS * 32), 0, stream, P);
+    launch_pdl(k_raster<WARPS, true>, dim3(slow), dim3(WARPS * 32), 0, stream, P);
 }
 
 }  // namespace
@@ -846,7 +848,8 @@ void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews,
         }
     }
     if (between) cudaEventRecord(between, stream);
-    k_raster_big<<<sm_count * 8, 256, 0, stream>>>(big, big_count, big_capacity, views);
+    launch_pdl(k_raster_big, dim3(sm_count * 8), dim3(256), 0, stream, (const BigTri*)big, (const uint32_t*)big_count,
+               big_capacity, views);
 }
 
 }  // namespace vkgv

@@ -216,6 +216,7 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
 
 template <bool TEXTURED>
 __global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
+    pdl_begin();
     const DeviceView& V = views[blockIdx.y];
     __shared__ float s_unorm[256];
     if (TEXTURED) {
@@ -255,6 +256,7 @@ __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ vi
                                                uint32_t counter_words, uint32_t skip_pixels,
                                                const float* __restrict__ transforms, uint32_t transform_count,
                                                float* __restrict__ tdets, float* __restrict__ mvps) {
+    pdl_begin();
     const DeviceView& V = views[blockIdx.y];
     if (transform_count) {
         __shared__ float s_vp[16];
@@ -291,6 +293,7 @@ __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ vi
 }
 
 __global__ void k_finalize(const DeviceView* __restrict__ views, uint32_t nviews) {
+    pdl_begin();
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nviews) return;
     finalize_view(views[v]);
@@ -305,9 +308,9 @@ void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews
     if (bx > 65535u) bx = 65535u;
     dim3 grid(bx, nviews);
     if (flags & VKGV_RESOLVE_TEXTURED)
-        k_resolve<true><<<grid, 256, 0, stream>>>(S, views, flags);
+        launch_pdl(k_resolve<true>, grid, dim3(256), 0, stream, S, views, flags);
     else
-        k_resolve<false><<<grid, 256, 0, stream>>>(S, views, flags);
+        launch_pdl(k_resolve<false>, grid, dim3(256), 0, stream, S, views, flags);
 }
 
 void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels, uint32_t* counters,
@@ -320,12 +323,12 @@ void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels,
     uint32_t bx = skip ? 1u : (uint32_t)(want < cap ? (want ? want : 1) : cap);
     dim3 grid(bx, nviews);
     if (!tdets || !mvps) transform_count = 0;
-    k_clear<<<grid, 256, 0, stream>>>(views, counters, counter_words, skip ? 1u : 0u, transforms, transform_count,
-                                      tdets, mvps);
+    launch_pdl(k_clear, grid, dim3(256), 0, stream, views, counters, counter_words, skip ? 1u : 0u, transforms,
+               transform_count, tdets, mvps);
 }
 
 void launch_finalize(const DeviceView* views, uint32_t nviews, cudaStream_t stream) {
-    k_finalize<<<(nviews + 127) / 128, 128, 0, stream>>>(views, nviews);
+    launch_pdl(k_finalize, dim3((nviews + 127) / 128), dim3(128), 0, stream, views, nviews);
 }
 
 }  // namespace vkgv
