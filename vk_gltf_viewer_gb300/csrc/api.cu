@@ -55,6 +55,9 @@ struct vkgv_ctx {
     BigTri* big = nullptr;
     uint32_t big_cap = 0;
     cudaStream_t capture_stream = nullptr;
+    // the final HiZ reduce runs beside the resolve (both only read depth_id)
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     // Buffers replaced by a larger allocation stay alive until destroy, since
     // a captured graph may still point at them.
     std::vector<void*> retired_dev;
@@ -313,12 +316,24 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
         zone(7);
     }
     zone(8);
-    if (flags & VKGV_BUILD_PYRAMID) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, ctx->status, stream);
-    zone(9);
     // The resolve also writes the survivor totals; without it a small
     // finalise kernel does.
     const bool resolve = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS)) != 0;
-    if (resolve) launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
+    const bool pyramid = (flags & VKGV_BUILD_PYRAMID) != 0;
+    if (pyramid && resolve && !zones) {
+        // the pyramid reduce and the resolve both only read the final
+        // depth_id: the reduce runs on a side stream beside the resolve
+        cudaEventRecord(ctx->fork_ev, stream);
+        cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0);
+        launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, ctx->status, ctx->side_stream);
+        cudaEventRecord(ctx->join_ev, ctx->side_stream);
+        launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
+        cudaStreamWaitEvent(stream, ctx->join_ev, 0);
+    } else {
+        if (pyramid) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, ctx->status, stream);
+        zone(9);
+        if (resolve) launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
+    }
     zone(10);
     if (!resolve) launch_finalize(dv, n, stream);
     zone(11);
@@ -401,7 +416,10 @@ int vkgv_create(const vkgv_config* config, vkgv_ctx** out_ctx) {
     bool ok = cudaMalloc(&ctx->status, 2 * sizeof(uint32_t)) == cudaSuccess &&
               cudaMemset(ctx->status, 0, 2 * sizeof(uint32_t)) == cudaSuccess &&
               cudaMalloc(&ctx->big, sizeof(BigTri) * (size_t)ctx->big_cap) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking) == cudaSuccess;
+              cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming) == cudaSuccess;
     for (uint32_t i = 0; ok && i < kRing; ++i)
         ok = cudaEventCreateWithFlags(&ctx->ring_ev[i], cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
@@ -433,7 +451,13 @@ int vkgv_destroy(vkgv_ctx* ctx) {
     if (ctx->rejected.ptr) cudaFree(ctx->rejected.ptr);
     if (ctx->deferred.ptr) cudaFree(ctx->deferred.ptr);
     if (ctx->diff.ptr) cudaFree(ctx->diff.ptr);
+    if (ctx->diff_acc.ptr) cudaFree(ctx->diff_acc.ptr);
+    if (ctx->tdet.ptr) cudaFree(ctx->tdet.ptr);
+    if (ctx->mvp.ptr) cudaFree(ctx->mvp.ptr);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+    if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
     for (uint32_t i = 0; i <= VKGV_STAGE_COUNT; ++i)
         if (ctx->zone[i]) cudaEventDestroy(ctx->zone[i]);
     for (void* p : ctx->retired_dev) cudaFree(p);
