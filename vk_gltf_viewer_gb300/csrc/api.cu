@@ -293,9 +293,10 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
         if (zones) cudaEventRecord(zones[i], stream);
     };
     uint32_t* gc = ctx->counters;
+    const uint32_t T = P.tdets ? P.S.transform_count : 0u;
     zone(0);
     launch_clear(dv, n, (flags & VKGV_SKIP_CLEAR) ? 0 : P.max_px, gc, kGlobalCounters, ctx->sm_count, stream,
-                 P.S.transforms, P.tdets ? P.S.transform_count : 0u, P.tdets, P.mvps);
+                 P.S.transforms, T, P.tdets, P.mvps);
     zone(1);
     launch_cull(P.S, dv, n, flags, 1, ctx->status, ctx->sm_count, stream);
     zone(2);

@@ -40,9 +40,10 @@ struct RasterConfig {
     uint32_t blocks_per_view;
 };
 
-// Also evaluates, when transform_count > 0, determinant(M) of
-// transforms[0, transform_count) into tdets and each view's
-// view_projection * M into mvps[view][node].
+// Zeroes the views' depth_id (unless max_pixels is 0) and, when counters is
+// not null, the global and per-view counters.  Also evaluates, when
+// transform_count > 0, determinant(M) of transforms[0, transform_count) into
+// tdets and each view's view_projection * M into mvps[view][node].
 void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels, uint32_t* counters,
                   uint32_t counter_words, uint32_t sm_count, cudaStream_t stream, const float* transforms = nullptr,
                   uint32_t transform_count = 0, float* tdets = nullptr, float* mvps = nullptr);

@@ -278,9 +278,11 @@ __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ vi
                                                                                   r[4 * k + 3]);
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x < 8) V.counters[threadIdx.x] = 0;
-    if (blockIdx.x == 0 && blockIdx.y == 0)
-        for (uint32_t i = threadIdx.x; i < counter_words; i += blockDim.x) counters[i] = 0;
+    if (counters) {
+        if (blockIdx.x == 0 && threadIdx.x < 8) V.counters[threadIdx.x] = 0;
+        if (blockIdx.x == 0 && blockIdx.y == 0)
+            for (uint32_t i = threadIdx.x; i < counter_words; i += blockDim.x) counters[i] = 0;
+    }
     if (skip_pixels) return;
     const uint32_t n = V.w * V.h;
     // 16-byte stores of two pixels; depth_id allocations are 16-byte aligned
