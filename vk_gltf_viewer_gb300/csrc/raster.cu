@@ -571,8 +571,10 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
     }
     // the next run is requested while the current one is drawn, so the
     // atomic's round trip is off the critical path
-    uint32_t next = 0;
-    if (lane == 0) next = atomicAdd(P.work, grab);
+    // Warps beyond the first `total` have nothing to take (each of the
+    // first `total` grabs returns a distinct item), so they skip the counter.
+    uint32_t next = 0xffffffffu;
+    if (lane == 0 && blockIdx.x * WARPS + warp < total) next = atomicAdd(P.work, grab);
     for (;;) {
         const uint32_t base = __shfl_sync(0xffffffffu, next, 0);
         if (base >= total) break;
@@ -755,10 +757,11 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
             __syncwarp();
         }
     }
-    // The last warp to finish resets the work counters for the next launch.
-    if (lane == 0) {
+    // The last CTA to finish resets the work counters for the next launch.
+    __syncthreads();
+    if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(P.work + 1, 1u) == warps_total - 1) {
+        if (atomicAdd(P.work + 1, 1u) == gridDim.x - 1) {
             P.work[0] = 0;
             P.work[1] = 0;
         }
