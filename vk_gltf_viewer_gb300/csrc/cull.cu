@@ -155,7 +155,7 @@ __device__ __forceinline__ void warp_append(bool flag, uint32_t value, uint32_t*
 //         occlusion rejects -> rejected.
 // pass 2: candidates are rejected[0, counters[1]); survivors are appended at
 //         survivors[counters[0] + ...] via counters[2].
-__global__ void __launch_bounds__(256) k_cull(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags,
+__global__ void __launch_bounds__(256, 5) k_cull(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags,
                                               uint32_t pass, uint32_t* status) {
     pdl_begin();
     const DeviceView& V = views[blockIdx.y];
