@@ -215,7 +215,7 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
 }
 
 template <bool TEXTURED>
-__global__ void __launch_bounds__(256) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
+__global__ void __launch_bounds__(256, 6) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
     pdl_begin();
     const DeviceView& V = views[blockIdx.y];
     __shared__ float s_unorm[256];
