@@ -357,7 +357,10 @@ typedef struct vkgv_diff_scene {
     float uv_scale[2];
     float uv_rotation;
     uint32_t double_sided;
-    uint32_t _pad;
+    /* Meshlet normal-cone culling of the visibility passes (cones rebuilt
+     * from the current positions; the visibility is unchanged):
+     * 0 = automatic (on for large batches), 1 = always, 2 = never. */
+    uint32_t cone_mode;
 } vkgv_diff_scene;
 
 typedef struct vkgv_diff_view {

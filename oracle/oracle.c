@@ -280,8 +280,11 @@ static int cull_draw(const orc_scene* s, const orc_camera* cam, const orc_pyrami
     for (int j = 0; j < 3; ++j)
         we[j] = (fabsf(M[0 * 4 + j]) * e[0] + fabsf(M[1 * 4 + j]) * e[1]) + fabsf(M[2 * 4 + j]) * e[2];
     if ((flags & ORC_CULL_FRUSTUM) && !orc_frustum_visible(wc, we, (const float*)cam->frustum)) return 0;
-    /* cone-culling addition: after the frustum test, before the occlusion test */
-    if (eye && prim->cones && cone_culled(&prim->cones[dr->meshlet_index], M, eye)) return 0;
+    /* cone-culling addition: after the frustum test, before the occlusion
+     * test; a double-sided material has no backface test to mirror */
+    if (eye && prim->cones && !s->materials[prim->material_index].double_sided &&
+        cone_culled(&prim->cones[dr->meshlet_index], M, eye))
+        return 0;
     if (!(flags & ORC_CULL_OCCLUSION) || !pyr || pyr->levels == 0) return 1;
     /* projectAabb (culling.h.glsl:32-56) */
     static const float corners[8][3] = {{1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, -1},

@@ -78,6 +78,34 @@ def test_visibility_is_the_raster_of_the_oracle(renderer, su):
         assert np.array_equal(su.ids_of(v), exp)
 
 
+def _moved(mesh, pos):
+    """The mesh with new vertex positions (same meshlets, no cones)."""
+    import dataclasses
+    verts = mesh.vertices.copy()
+    verts["position"] = pos
+    return dataclasses.replace(mesh, vertices=verts, positions=pos, cones=None)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_cone_culled_passes_keep_the_visibility(renderer, su, mode):
+    """The visibility passes with meshlet normal cones rebuilt from the
+    current positions (forced on) or without them (forced off) give the
+    oracle's unculled raster, at the stored and at perturbed positions."""
+    rng = np.random.default_rng(17)
+    for pos in (su.mesh.positions, su.mesh.positions + rng.normal(0, 0.02, size=su.mesh.positions.shape)):
+        pos = np.ascontiguousarray(pos, np.float32)
+        mesh = _moved(su.mesh, pos)
+        host = scene.HostScene(meshes=[mesh], prim_materials=[1],
+                               materials=np.concatenate([scene.default_material(), scene.make_material()]),
+                               transforms=scene.to_column_major(np.eye(4))[None, :].copy(), node_meshes=[[0]])
+        osc = ob.OracleScene(host)
+        sc = diff.DiffScene.create(su.mesh, su.colors, su.texture, positions=pos, cone_mode=mode)
+        su.render(renderer, sc)
+        for v, cam in zip(su.views, su.cams):
+            assert np.array_equal(su.ids_of(v), ob.frame(osc, cam, W, H, 0)["ids"])
+    su._ids = None
+
+
 def test_forward_matches_float64(renderer, su):
     rgb = su.render(renderer)
     for v, cam, out in zip(su.views, su.cams, rgb):

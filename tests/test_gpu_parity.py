@@ -299,3 +299,27 @@ def test_full_rectangle_queue_falls_back_in_place(grid):
         assert code == 2  # queue overflow, handled in place
     finally:
         r.close()
+
+
+def test_cone_cull_skips_double_sided_materials(renderer):
+    """A double-sided material has no backface test, so the cone test must
+    not cull its meshlets: with CULL_CONE the survivors equal those without
+    it (and the oracle's), and so do the IDs, back faces included."""
+    mesh = scene.icosphere(4)
+    mats = np.concatenate([scene.default_material(), scene.make_material((0.8, 0.5, 0.3, 1.0), double_sided=True)])
+    host = scene.HostScene(meshes=[mesh], prim_materials=[1], materials=mats,
+                           transforms=scene.to_column_major(np.eye(4))[None, :].copy(), node_meshes=[[0]])
+    pair = Pair(host)
+    w, h = 640, 360
+    # the eye inside the sphere sees back faces of every meshlet
+    for cam in [scene.camera((0.1, 0.2, 0.3), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0), 90.0, w / h),
+                scene.camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, w / h)]:
+        base = abi.CULL_FRUSTUM | abi.RESOLVE_FLAT | abi.WRITE_IDS
+        v0, v1 = view(pair, cam, w, h), view(pair, cam, w, h)
+        renderer.frame(pair.dev, [v0], base)
+        renderer.frame(pair.dev, [v1], base | abi.CULL_CONE)
+        torch.cuda.synchronize()
+        exp = ob.frame(pair.orc, cam, w, h, oracle_flags(base | abi.CULL_CONE))
+        assert np.array_equal(np.sort(v1.survivor_list()), np.sort(v0.survivor_list()))
+        assert np.array_equal(np.sort(v1.survivor_list()), np.sort(exp["survivors"]))
+        assert np.array_equal(u32(v1.visbuffer), exp["ids"])

@@ -144,7 +144,7 @@ class DiffScene(C.Structure):
                 ("uvs", C.c_uint64), ("texture", C.c_uint64), ("meshlet_count", C.c_uint32),
                 ("vertex_count", C.c_uint32), ("tex_width", C.c_uint32), ("tex_height", C.c_uint32),
                 ("albedo", C.c_float * 3), ("uv_offset", C.c_float * 2), ("uv_scale", C.c_float * 2),
-                ("uv_rotation", C.c_float), ("double_sided", C.c_uint32), ("_pad", C.c_uint32)]
+                ("uv_rotation", C.c_float), ("double_sided", C.c_uint32), ("cone_mode", C.c_uint32)]
 
 
 class DiffView(C.Structure):

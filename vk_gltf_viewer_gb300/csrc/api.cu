@@ -665,6 +665,7 @@ struct DiffPlan {
     Prepared P;
     std::vector<DeviceView> views;
     size_t acc_bytes = 0;  // float4 accumulators to zero before a backward pass
+    uint32_t cone_mode = 0;
 };
 
 int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view* views, uint32_t n, bool backward,
@@ -674,6 +675,7 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
     if (!ds->meshlet_buffer || !ds->vertex_index_buffer || !ds->primitive_index_buffer || !ds->positions ||
         !ds->colors || !ds->uvs || !ds->texture || ds->vertex_count == 0 || ds->tex_width == 0 || ds->tex_height == 0)
         return fail(ctx, VKGV_INVALID_ARG, "adjoint: incomplete scene");
+    if (ds->cone_mode > 2) return fail(ctx, VKGV_INVALID_ARG, "adjoint: cone_mode must be 0, 1 or 2");
     if (ds->meshlet_count >= (1u << VKGV_DRAW_INDEX_BITS))
         return fail(ctx, VKGV_LIMIT_EXCEEDED, "adjoint: meshlet_count must be < 2^25");
     if (n > 65535u) return fail(ctx, VKGV_LIMIT_EXCEEDED, "at most 65535 views per call");
@@ -682,7 +684,9 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
     const size_t off_xf = off_draws + align256(sizeof(vkgv_meshlet_draw) * std::max<size_t>(M, 1));
     const size_t off_prim = off_xf + 256, off_mat = off_prim + 256, off_vpack = off_mat + 256;
     const size_t off_tri = off_vpack + align256(2 * sizeof(float4) * V);
-    const size_t total = off_tri + align256(sizeof(uint4) * (std::max<size_t>(M, 1) << VKGV_TRIANGLE_BITS));
+    const size_t off_cones = off_tri + align256(sizeof(uint4) * (std::max<size_t>(M, 1) << VKGV_TRIANGLE_BITS));
+    const size_t off_cone_table = off_cones + align256(sizeof(vkgv_meshlet_cone) * std::max<size_t>(M, 1));
+    const size_t total = off_cone_table + 256;
     int rc = ensure_scratch(ctx, ctx->diff, total, "adjoint scene");
     if (rc) return rc;
     char* base = static_cast<char*>(ctx->diff.ptr);
@@ -703,12 +707,17 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
     S.uvs = reinterpret_cast<const float*>(ds->uvs);
     S.vpack = reinterpret_cast<float4*>(base + off_vpack);
     S.tri_verts = reinterpret_cast<uint4*>(base + off_tri);
+    S.cones = reinterpret_cast<vkgv_meshlet_cone*>(base + off_cones);
+    S.cone_table = reinterpret_cast<uint64_t*>(base + off_cone_table);
     vkgv_scene scene{};
     scene.draw_buffer = reinterpret_cast<uint64_t>(S.draws);
     scene.transform_buffer = reinterpret_cast<uint64_t>(S.transform);
     scene.primitive_buffer = reinterpret_cast<uint64_t>(S.primitive);
     scene.material_buffer = reinterpret_cast<uint64_t>(S.material);
     scene.meshlet_draw_count = ds->meshlet_count;
+    // normal cones rebuilt from the current positions on every pass
+    scene.cone_table = reinterpret_cast<uint64_t>(S.cone_table);
+    scene.primitive_count = 1;
     std::vector<vkgv_view> vv(n);
     for (uint32_t i = 0; i < n; ++i) {
         if (backward && !views[i].target && !views[i].grad_rgb)
@@ -750,6 +759,7 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
     A.grad_positions = reinterpret_cast<float*>(gpos);
     A.grad_colors = reinterpret_cast<float*>(gcol);
     A.grad_texture = reinterpret_cast<float*>(gtex);
+    D.cone_mode = ds->cone_mode;
     A.vertex_count = ds->vertex_count;
     A.vpack = S.vpack;
     A.tri_verts = S.tri_verts;
@@ -769,14 +779,20 @@ int diff_prepare(vkgv_ctx* ctx, const vkgv_diff_scene* ds, const vkgv_diff_view*
 }
 
 // One pass of the adjoint over device view descriptors dv: vertex records
-// from the current positions, visibility recomputed (clear, cull without
-// culling tests, since the builder's meshlet bounds do not follow moving
-// vertices, raster), then the shading kernel forward or backward.
+// and meshlet normal cones from the current positions, visibility
+// recomputed (clear, cone-only cull: the builder's meshlet bounds do not
+// follow moving vertices, raster), then the shading kernel forward or
+// backward.
 void diff_record(vkgv_ctx* ctx, const DiffPlan& D, const DeviceView* dv, uint32_t n, bool backward,
                  cudaStream_t stream) {
     launch_diff_setup(D.S, stream);
+    // The cone pass has a fixed cost of a few tens of microseconds; it pays
+    // once the pass rasterises enough meshlet-views (measured: 220 meshlets
+    // x 64 views ran 5% slower with it, 14k x 512 ran 13% faster).
+    const bool cones = D.cone_mode == 1 || (D.cone_mode == 0 && (uint64_t)D.S.meshlet_count * n >= (1ull << 20));
+    if (cones) launch_diff_cones(D.S, stream);
     launch_clear(dv, n, D.P.max_px, ctx->counters, kGlobalCounters, ctx->sm_count, stream);
-    launch_cull(D.P.S, dv, n, 0u, 1, ctx->status, ctx->sm_count, stream);
+    launch_cull(D.P.S, dv, n, cones ? (uint32_t)VKGV_CULL_CONE : 0u, 1, ctx->status, ctx->sm_count, stream);
     RasterLists l1{1, nullptr, nullptr, 0, 4};
     launch_raster(D.P.S, dv, n, l1, ctx->raster, ctx->big, ctx->counters + 0, ctx->big_cap, ctx->counters + 6, ctx->status,
                   ctx->sm_count, stream);

@@ -77,8 +77,10 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
         }
     }
     // Meshlet normal-cone backface test (an addition; conservative with
-    // respect to the per-triangle test of visbuffer.mesh.glsl:86-101).
-    if (!retest && eye && S.cone_table && dr.primitive_index < S.primitive_count) {
+    // respect to the per-triangle test of visbuffer.mesh.glsl:86-101, which
+    // a double-sided material skips).
+    if (!retest && eye && S.cone_table && dr.primitive_index < S.primitive_count &&
+        !S.mats[prim->material_index].double_sided) {
         const uint64_t cones = S.cone_table[dr.primitive_index];
         if (cones && cone_culled(reinterpret_cast<const vkgv_meshlet_cone*>(cones)[dr.meshlet_index], M, eye))
             return res;

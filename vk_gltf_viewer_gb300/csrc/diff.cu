@@ -68,6 +68,121 @@ __global__ void k_diff_setup(DiffSetup S) {
         mt.uv_scale[0] = mt.uv_scale[1] = 1.0f;
         mt.double_sided = S.double_sided;
         *S.material = mt;
+        *S.cone_table = reinterpret_cast<uint64_t>(S.cones);
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Unit normal of triangle t of a meshlet in double; false when degenerate.
+__device__ __forceinline__ bool tri_normal(const DiffSetup& S, const uint32_t* vidx, const uint8_t* tri, uint32_t t,
+                                           double n[3]) {
+    const float* a = S.positions + 3 * (size_t)vidx[tri[3 * t]];
+    const float* b = S.positions + 3 * (size_t)vidx[tri[3 * t + 1]];
+    const float* c = S.positions + 3 * (size_t)vidx[tri[3 * t + 2]];
+    double e1[3], e2[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        e1[k] = (double)b[k] - (double)a[k];
+        e2[k] = (double)c[k] - (double)a[k];
+    }
+    n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    const double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(len > 1e-30)) return false;
+    n[0] /= len, n[1] /= len, n[2] /= len;
+    return true;
+}
+
+// One warp per meshlet: a normal cone that bounds every triangle normal of
+// the meshlet at its current positions (the construction of the scene
+// builder: double-precision normals, axis = normalised mean, cutoff = the
+// smallest cosine against the rounded float axis less 1e-6, rounded down;
+// centre = the AABB centre, radius rounded up), or cutoff -1 (no culling)
+// for a degenerate triangle or a spread of normals beyond cos > 0.05.
+__global__ void k_diff_cones(DiffSetup S) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < S.meshlet_count; m += warps) {
+        const vkgv_meshlet ml = S.meshlets[m];
+        const uint32_t vc = min((uint32_t)ml.vertex_count, (uint32_t)VKGV_MAX_VERTICES);
+        const uint32_t tc = min((uint32_t)ml.triangle_count, (uint32_t)VKGV_MAX_PRIMITIVES);
+        const uint32_t* vidx = S.vertex_indices + ml.vertex_offset;
+        const uint8_t* tri = S.tri_indices + ml.triangle_offset;
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t k = lane; k < vc; k += 32) {
+            const float* p = S.positions + 3 * (size_t)vidx[k];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) lo[c] = fmin(lo[c], (double)p[c]), hi[c] = fmax(hi[c], (double)p[c]);
+        }
+        float center[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = warp_min(lo[c]);
+            hi[c] = -warp_min(-hi[c]);
+            center[c] = (float)(0.5 * (lo[c] + hi[c]));
+        }
+        double r2 = 0.0;
+        for (uint32_t k = lane; k < vc; k += 32) {
+            const float* p = S.positions + 3 * (size_t)vidx[k];
+            double d2 = 0.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const double e = (double)p[c] - (double)center[c];
+                d2 += e * e;
+            }
+            r2 = fmax(r2, d2);
+        }
+        r2 = -warp_min(-r2);
+        vkgv_meshlet_cone cone;
+        cone.center[0] = center[0], cone.center[1] = center[1], cone.center[2] = center[2];
+        cone.radius = nextafterf((float)(sqrt(r2) * (1.0 + 1e-6) + 1e-7), INFINITY);
+        cone.axis[0] = cone.axis[1] = cone.axis[2] = 0.0f;
+        cone.cutoff = -1.0f;
+        double sum[3] = {0.0, 0.0, 0.0};
+        bool degenerate = false;
+        for (uint32_t t = lane; t < tc; t += 32) {
+            double n[3];
+            if (!tri_normal(S, vidx, tri, t, n)) {
+                degenerate = true;
+            } else {
+                sum[0] += n[0], sum[1] += n[1], sum[2] += n[2];
+            }
+        }
+        degenerate = __any_sync(0xffffffffu, degenerate);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sum[c] = warp_sum(sum[c]);
+        const double sl = sqrt(sum[0] * sum[0] + sum[1] * sum[1] + sum[2] * sum[2]);
+        if (!degenerate && sl > 1e-12) {
+            const double axis[3] = {sum[0] / sl, sum[1] / sl, sum[2] / sl};
+            const float fa[3] = {(float)axis[0], (float)axis[1], (float)axis[2]};
+            const double fal = sqrt((double)fa[0] * fa[0] + (double)fa[1] * fa[1] + (double)fa[2] * fa[2]);
+            double cmin = 1.0, cmin_f = 1.0;
+            for (uint32_t t = lane; t < tc; t += 32) {
+                double n[3];
+                tri_normal(S, vidx, tri, t, n);
+                cmin = fmin(cmin, n[0] * axis[0] + n[1] * axis[1] + n[2] * axis[2]);
+                cmin_f = fmin(cmin_f, (n[0] * fa[0] + n[1] * fa[1] + n[2] * fa[2]) / fal);
+            }
+            cmin = warp_min(cmin);
+            cmin_f = warp_min(cmin_f) - 1e-6;
+            if (cmin > 0.05 && cmin_f > 0.05) {
+                cone.axis[0] = fa[0], cone.axis[1] = fa[1], cone.axis[2] = fa[2];
+                cone.cutoff = nextafterf((float)cmin_f, -INFINITY);
+            }
+        }
+        if (lane == 0) S.cones[m] = cone;
     }
 }
 
@@ -309,6 +424,12 @@ void launch_diff_setup(const DiffSetup& S, cudaStream_t stream) {
     uint32_t blocks = (n + 255) / 256;
     blocks = blocks ? (blocks < 4096 ? blocks : 4096) : 1;
     k_diff_setup<<<blocks, 256, 0, stream>>>(S);
+}
+
+void launch_diff_cones(const DiffSetup& S, cudaStream_t stream) {
+    uint32_t blocks = (S.meshlet_count * 32 + 255) / 256;
+    blocks = blocks ? (blocks < 8192 ? blocks : 8192) : 1;
+    k_diff_cones<<<blocks, 256, 0, stream>>>(S);
 }
 
 void launch_diff_scatter(const DiffArgs& A, cudaStream_t stream) {

@@ -80,6 +80,8 @@ struct DiffSetup {
     const float* uvs;
     float4* vpack;                 // per vertex: (x, y, z, r), (g, b, u, v)
     uint4* tri_verts;              // per visibility id (meshlet << 7 | triangle): its 3 vertex indices
+    vkgv_meshlet_cone* cones;      // per meshlet, from the current positions
+    uint64_t* cone_table;          // one entry: the address of cones
 };
 
 struct DiffArgs {
@@ -113,6 +115,8 @@ struct DiffArgs {
 };
 
 void launch_diff_setup(const DiffSetup& S, cudaStream_t stream);
+// Conservative normal cones of every meshlet from the current positions.
+void launch_diff_cones(const DiffSetup& S, cudaStream_t stream);
 void launch_diff_shade(const DiffArgs& A, const DeviceView* views, uint32_t nviews, uint64_t max_px, bool backward,
                        cudaStream_t stream);
 // Adds the float4 accumulators of A into the caller's gradient arrays.

@@ -34,6 +34,7 @@ class DiffScene:
     uv_scale: tuple = (1.0, 1.0)
     uv_rotation: float = 0.0
     double_sided: bool = False
+    cone_mode: int = 0  # meshlet cone culling: 0 automatic, 1 always, 2 never
 
     @classmethod
     def create(cls, mesh: Mesh, colors: np.ndarray, texture: np.ndarray, device="cuda",
@@ -71,6 +72,7 @@ class DiffScene:
         s.uv_scale[:] = list(self.uv_scale)
         s.uv_rotation = float(self.uv_rotation)
         s.double_sided = 1 if self.double_sided else 0
+        s.cone_mode = int(self.cone_mode)
         return s
 
 
