@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--batched-only", action="store_true",
                    help="run only the batched leg (for profiling); prints its own JSON line")
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-motion", action="store_true", help="skip the motion-vector frame")
     p.add_argument("--adjoint-only", action="store_true",
                    help="run only the adjoint legs (for profiling); prints their own JSON line")
     return p.parse_args()
@@ -471,6 +472,37 @@ def main():
     if pg:
         pg.all_reduce(te, op=pg.ReduceOp.MAX)
     e2e_value = world * args.steps / float(te.item())
+
+    # ---- the same frame with the motion-vector image as well (the
+    # reference's visibility pass writes it every frame), seen from a camera
+    # that moved 0.1 units since the previous frame; L2 flushed between steps
+    motion = None
+    if not args.no_motion:
+        mflags = flags | abi.WRITE_MOTION
+        view_m = ViewBuffers.allocate(W1080, H1080, scene.grid_camera(W1080, H1080, moved=0.1), host.draw_count,
+                                      device=f"cuda:{local}", prev_pyramid="alias", motion=True)
+        view_m.use_prev = False
+        rs.frame(dev, [view_m], mflags)
+        view_m.use_prev = True
+        for _ in range(2):
+            rs.frame(dev, [view_m], mflags)
+        gm = rs.capture(dev, [view_m], mflags)
+        for _ in range(max(3, args.warmup)):
+            gm.launch()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            starts[i].record(stream)
+            gm.launch()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        ms_m = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+        mv = view_m.motion_vectors()
+        motion = {"value": 1000.0 / ms_m, "unit": "views/s", "ms_per_view": ms_m,
+                  "flags": FLAGS_NAMES + "|WRITE_MOTION", "time_vs_plain": ms_m / ms_per_step,
+                  "mean_abs_motion": float(np.abs(mv).mean()), "camera": "grid camera, moved 0.1 along +x"}
+        gm.close()
+        del view_m
     graph.close()
     rs.close()
 
@@ -565,6 +597,8 @@ def main():
             out["batched"] = batched
         if adjoint:
             out["adjoint"] = adjoint
+        if motion:
+            out["motion"] = motion
         print(json.dumps(out), flush=True)
     if pg:
         pg.destroy_process_group()

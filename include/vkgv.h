@@ -196,6 +196,10 @@ typedef struct vkgv_view {
     uint64_t survivor_count;     /* uint32 counter, or 0                     */
     uint32_t survivor_capacity;
     uint32_t _pad;
+    /* uint32[W*H] motion vectors as two IEEE binary16 (x in the low half),
+     * the visibility pass's second attachment (R16G16_SFLOAT,
+     * application.cpp:250-270), written with VKGV_WRITE_MOTION, or 0 */
+    uint64_t motion;
 } vkgv_view;
 
 /* ------------------------------------------------------------ frame flags */
@@ -209,6 +213,7 @@ enum vkgv_frame_flags {
     VKGV_BUILD_PYRAMID = 1u << 6,       /* HiZ reduce chain into view.pyramid        */
     VKGV_WRITE_IDS = 1u << 7,           /* write the uint32 visbuffer image          */
     VKGV_SKIP_CLEAR = 1u << 8,          /* depth_id already cleared by the caller    */
+    VKGV_WRITE_MOTION = 1u << 9,        /* motion vectors of the visible fragments (visbuffer.frag.glsl:38) */
     /* The reference frame: application.cpp:764-1003. */
     VKGV_FRAME_REFERENCE = (1u << 0) | (1u << 1) | (1u << 4) | (1u << 6) | (1u << 7)
 };
@@ -281,7 +286,9 @@ int vkgv_raster(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view,
 int vkgv_hiz_reduce(vkgv_ctx* ctx, const vkgv_view* view, void* stream);
 /* Resolve (shaders/visbuffer/visbuffer_resolve.comp.glsl:17-41): writes
  * view->color (and view->visbuffer with VKGV_WRITE_IDS).  flags selects
- * VKGV_RESOLVE_FLAT or VKGV_RESOLVE_TEXTURED. */
+ * VKGV_RESOLVE_FLAT or VKGV_RESOLVE_TEXTURED; VKGV_WRITE_MOTION also writes
+ * view->motion, the visible fragments' motion vectors
+ * (visbuffer.frag.glsl:38), from the camera's prev_view_projection. */
 int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view,
                  uint32_t flags, void* stream);
 

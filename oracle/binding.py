@@ -77,6 +77,9 @@ def load() -> C.CDLL:
         lib.orc_hiz.argtypes = [P, U32, U32, P]
         lib.orc_resolve.argtypes = [P, P, U32, U32, P, U32, P, P]
         lib.orc_frame.argtypes = [P, P, U32, U32, P, U32, P, P, P, P, P, P]
+        lib.orc_motion.argtypes = [P, P, U32, U32, P, P]
+        lib.orc_half_rn.restype = C.c_uint16
+        lib.orc_half_rn.argtypes = [C.c_float]
         lib.orc_from_linear.restype = C.c_float
         lib.orc_from_linear.argtypes = [C.c_float]
         lib.orc_to_linear.restype = C.c_float
@@ -189,6 +192,22 @@ def resolve(os_: OracleScene, cam, w: int, h: int, depth_id: np.ndarray, texture
     load().orc_resolve(os_.ptr, C.addressof(cam), w, h, _addr(np.ascontiguousarray(depth_id, np.uint64)),
                        1 if textured else 0, _addr(ids), _addr(rgba))
     return ids, rgba
+
+
+def motion(os_: OracleScene, cam, w: int, h: int, depth_id: np.ndarray) -> np.ndarray:
+    """Motion vectors of the visible fragments of a finished depth_id image:
+    uint32[w*h], two binary16 per pixel (x low), 0 where nothing was drawn."""
+    depth = np.ascontiguousarray(depth_id, np.uint64).reshape(-1)
+    if depth.size != w * h:
+        raise ValueError(f"depth_id has {depth.size} pixels, expected {w * h}")
+    out = np.zeros(w * h, np.uint32)
+    load().orc_motion(os_.ptr, C.addressof(cam), w, h, _addr(depth), _addr(out))
+    return out
+
+
+def half_rn(v: float) -> int:
+    """binary32 -> binary16 bits, round to nearest even."""
+    return int(load().orc_half_rn(v))
 
 
 def frame(os_: OracleScene, cam, w: int, h: int, flags: int, prev_pyramid: np.ndarray | None = None):

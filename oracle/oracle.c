@@ -732,49 +732,70 @@ static void sample_texture(const orc_texture* t, float u, float v, float out[4])
     }
 }
 
-/* Textured resolve of one pixel (extension): perspective-correct
- * barycentrics of (drawIndex, triangle), vertex colour, transformUv
- * (mesh_common.h.glsl:129-135), albedo texture through toLinear, as in the
- * commented-out visbuffer.frag.glsl:29-34. */
-static void resolve_textured_px(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h, uint32_t px,
-                                uint32_t py, uint32_t id, float out[4]) {
+/* The visible fragment of a pixel: the triangle (drawIndex, triangle) of its
+ * id, its vertices in clip space (position of visbuffer.mesh.glsl:57-63) and
+ * the perspective-correct barycentrics of the pixel centre. */
+typedef struct {
+    const orc_vertex* vx[3];
+    const orc_material* mat;
+    const float* M;
+    float c[3][4];
+    float l[3];
+} orc_frag;
+
+static void frag_setup(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h, uint32_t px, uint32_t py,
+                       uint32_t id, orc_frag* f) {
     uint32_t d = id >> 7, t = id & 127u;
     const orc_draw* dr = &s->draws[d];
     const orc_primitive* prim = &s->primitives[dr->primitive_index];
     const orc_meshlet* ml = &prim->meshlets[dr->meshlet_index];
-    const orc_material* mat = &s->materials[prim->material_index];
-    const float* M = s->transforms + 16 * (size_t)dr->transform_index;
+    f->mat = &s->materials[prim->material_index];
+    f->M = s->transforms + 16 * (size_t)dr->transform_index;
     float mvp[16];
-    m4m(cam->vp, M, mvp);
+    m4m(cam->vp, f->M, mvp);
     const uint8_t* tri = prim->primitive_indices + ml->triangle_offset + 3 * t;
-    const orc_vertex* vx[3];
-    float c[3][4];
     for (int k = 0; k < 3; ++k) {
-        vx[k] = &prim->vertices[prim->vertex_indices[ml->vertex_offset + tri[k]]];
-        float p4[4] = {vx[k]->position[0], vx[k]->position[1], vx[k]->position[2], 1.0f};
-        m4v(mvp, p4, c[k]);
+        f->vx[k] = &prim->vertices[prim->vertex_indices[ml->vertex_offset + tri[k]]];
+        float p4[4] = {f->vx[k]->position[0], f->vx[k]->position[1], f->vx[k]->position[2], 1.0f};
+        m4v(mvp, p4, f->c[k]);
     }
+    /* clip-space weights whose point projects to the pixel centre ~ a x b */
     float nx = (((float)px + 0.5f) / (float)w) * 2.0f - 1.0f;
     float ny = (((float)py + 0.5f) / (float)h) * 2.0f - 1.0f;
     float a[3], b[3];
     for (int k = 0; k < 3; ++k) {
-        a[k] = c[k][0] - nx * c[k][3];
-        b[k] = c[k][1] - ny * c[k][3];
+        a[k] = f->c[k][0] - nx * f->c[k][3];
+        b[k] = f->c[k][1] - ny * f->c[k][3];
     }
-    float l[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    float* l = f->l;
+    l[0] = a[1] * b[2] - a[2] * b[1];
+    l[1] = a[2] * b[0] - a[0] * b[2];
+    l[2] = a[0] * b[1] - a[1] * b[0];
     float sum = (l[0] + l[1]) + l[2];
     if (sum != 0.0f) {
         for (int k = 0; k < 3; ++k) l[k] = l[k] / sum;
     } else {
         l[0] = l[1] = l[2] = 1.0f / 3.0f;
     }
+}
+
+static float interp3(const float l[3], float v0, float v1, float v2) { return (l[0] * v0 + l[1] * v1) + l[2] * v2; }
+
+/* Textured resolve of one pixel (extension): vertex colour, transformUv
+ * (mesh_common.h.glsl:129-135), albedo texture through toLinear, as in the
+ * commented-out visbuffer.frag.glsl:29-34. */
+static void resolve_textured_px(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h, uint32_t px,
+                                uint32_t py, uint32_t id, float out[4]) {
+    orc_frag f;
+    frag_setup(s, cam, w, h, px, py, id, &f);
+    const orc_material* mat = f.mat;
+    const float* l = f.l;
     float col[4], uv[2];
     for (int k = 0; k < 4; ++k)
-        col[k] = ((l[0] * ((float)vx[0]->color[k] / 255.0f) + l[1] * ((float)vx[1]->color[k] / 255.0f)) +
-                  l[2] * ((float)vx[2]->color[k] / 255.0f));
+        col[k] = interp3(l, (float)f.vx[0]->color[k] / 255.0f, (float)f.vx[1]->color[k] / 255.0f,
+                         (float)f.vx[2]->color[k] / 255.0f);
     for (int k = 0; k < 2; ++k)
-        uv[k] = (l[0] * half_to_float(vx[0]->uv[k]) + l[1] * half_to_float(vx[1]->uv[k])) +
-                l[2] * half_to_float(vx[2]->uv[k]);
+        uv[k] = interp3(l, half_to_float(f.vx[0]->uv[k]), half_to_float(f.vx[1]->uv[k]), half_to_float(f.vx[2]->uv[k]));
     float sampled[4] = {1.0f, 1.0f, 1.0f, 1.0f};
     if (mat->albedo_index != 0xFFFFFFFFu && mat->albedo_index < s->texture_count) {
         float cs = cosf(mat->uv_rotation), sn = sinf(mat->uv_rotation);
@@ -787,6 +808,83 @@ static void resolve_textured_px(const orc_scene* s, const orc_camera* cam, uint3
             for (int k = 0; k < 3; ++k) sampled[k] = orc_to_linear(sampled[k]);
     }
     for (int k = 0; k < 4; ++k) out[k] = col[k] * mat->albedo_factor[k] * sampled[k];
+}
+
+/* IEEE 754 binary32 -> binary16, round to nearest, ties to even; overflow
+ * rounds to infinity, NaN becomes the quiet NaN 0x7E00 with its sign. */
+uint16_t orc_half_rn(float v) {
+    uint32_t x = f2u(v);
+    uint32_t sign = (x >> 16) & 0x8000u, ax = x & 0x7FFFFFFFu;
+    if (ax > 0x7F800000u) return (uint16_t)(sign | 0x7E00u);
+    if (ax >= 0x477FF000u) return (uint16_t)(sign | 0x7C00u); /* >= 65520: past the last tie */
+    if (ax < 0x38800000u) {                                    /* below 2^-14: subnormal half */
+        if (ax <= 0x33000000u) return (uint16_t)sign;         /* <= 2^-25 rounds to zero (tie to even) */
+        uint32_t e = ax >> 23, m = (ax & 0x7FFFFFu) | 0x800000u;
+        uint32_t shift = 126u - e; /* value / 2^-24 = m >> shift, shift in [14, 24] */
+        uint32_t q = m >> shift, rem = m & ((1u << shift) - 1u), halfway = 1u << (shift - 1u);
+        if (rem > halfway || (rem == halfway && (q & 1u))) ++q;
+        return (uint16_t)(sign | q);
+    }
+    uint32_t r = ax - 0x38000000u; /* rebias the exponent from 127 to 15 */
+    uint32_t q = r >> 13, rem = r & 0x1FFFu;
+    if (rem > 0x1000u || (rem == 0x1000u && (q & 1u))) ++q; /* a carry moves into the exponent */
+    return (uint16_t)(sign | q);
+}
+
+/* Motion vectors (visbuffer.frag.glsl:38) from the varyings position and
+ * prevPosition (visbuffer.mesh.glsl:44-64): viewProjection * M * vertex and
+ * prevViewProjection * M * vertex with the node's current transform M (the
+ * reference has no previous-frame transforms), interpolated with the
+ * fragment's barycentrics, then
+ *   mv = (prev.xy / prev.w * 0.5 - 0.5) - (pos.xy / pos.w * 0.5 - 0.5)
+ * stored as two binary16 (R16G16_SFLOAT, application.cpp:250-270), x in the
+ * low half; the attachment is cleared to 0 (application.cpp:786-797). */
+static uint32_t motion_px(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h, uint32_t px,
+                          uint32_t py, uint32_t id) {
+    orc_frag f;
+    frag_setup(s, cam, w, h, px, py, id, &f);
+    float pmvp[16], p[3][4];
+    m4m(cam->prev_vp, f.M, pmvp);
+    for (int k = 0; k < 3; ++k) {
+        float p4[4] = {f.vx[k]->position[0], f.vx[k]->position[1], f.vx[k]->position[2], 1.0f};
+        m4v(pmvp, p4, p[k]);
+    }
+    float cw = interp3(f.l, f.c[0][3], f.c[1][3], f.c[2][3]);
+    float pw = interp3(f.l, p[0][3], p[1][3], p[2][3]);
+    uint32_t out = 0;
+    for (int j = 0; j < 2; ++j) {
+        float cj = interp3(f.l, f.c[0][j], f.c[1][j], f.c[2][j]);
+        float pj = interp3(f.l, p[0][j], p[1][j], p[2][j]);
+        float cur = (cj / cw) * 0.5f - 0.5f;
+        float prev = (pj / pw) * 0.5f - 0.5f;
+        out |= (uint32_t)orc_half_rn(prev - cur) << (16 * j);
+    }
+    return out;
+}
+
+typedef struct {
+    const orc_scene* s;
+    const orc_camera* cam;
+    uint32_t w, h;
+    const uint64_t* depth_id;
+    uint32_t* motion;
+} motion_ctx;
+
+static void motion_rows(void* p, int64_t b, int64_t e, int worker) {
+    (void)worker;
+    motion_ctx* c = (motion_ctx*)p;
+    for (int64_t y = b; y < e; ++y)
+        for (uint32_t x = 0; x < c->w; ++x) {
+            size_t i = (size_t)y * c->w + x;
+            uint32_t lo = (uint32_t)c->depth_id[i];
+            c->motion[i] = lo ? motion_px(c->s, c->cam, c->w, c->h, x, (uint32_t)y, lo - 1u) : 0u;
+        }
+}
+
+void orc_motion(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h, const uint64_t* depth_id,
+                uint32_t* motion) {
+    motion_ctx c = {s, cam, w, h, depth_id, motion};
+    orc_parallel_for(h, motion_rows, &c);
 }
 
 typedef struct {

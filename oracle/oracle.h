@@ -129,6 +129,14 @@ void orc_hiz(const uint64_t* depth_id, uint32_t w, uint32_t h, float* pyramid);
 void orc_resolve(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h,
                  const uint64_t* depth_id, uint32_t textured, uint32_t* ids, uint32_t* rgba);
 
+/* Motion vectors of the visible fragments (visbuffer.frag.glsl:38): two
+ * binary16 per pixel, x in the low half, 0 where nothing was drawn. */
+void orc_motion(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h, const uint64_t* depth_id,
+                uint32_t* motion);
+/* binary32 -> binary16, round to nearest even (the conversion of the motion
+ * attachment's stores). */
+uint16_t orc_half_rn(float v);
+
 /* A whole frame with the same pass structure as vkgv_frame. */
 void orc_frame(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h,
                const orc_pyramid* prev, uint32_t flags, uint64_t* depth_id,

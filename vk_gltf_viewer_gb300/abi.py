@@ -40,6 +40,7 @@ RESOLVE_TEXTURED = 1 << 5
 BUILD_PYRAMID = 1 << 6
 WRITE_IDS = 1 << 7
 SKIP_CLEAR = 1 << 8
+WRITE_MOTION = 1 << 9
 
 # passes of vkgv_diff_graph_capture
 DIFF_ZERO_GRADS = 1
@@ -114,7 +115,8 @@ class View(C.Structure):
     _fields_ = [("camera_buffer", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("prev_pyramid", Pyramid), ("pyramid", Pyramid), ("depth_id", C.c_uint64),
                 ("visbuffer", C.c_uint64), ("color", C.c_uint64), ("survivors", C.c_uint64),
-                ("survivor_count", C.c_uint64), ("survivor_capacity", C.c_uint32), ("_pad", C.c_uint32)]
+                ("survivor_count", C.c_uint64), ("survivor_capacity", C.c_uint32), ("_pad", C.c_uint32),
+                ("motion", C.c_uint64)]
 
 
 class Config(C.Structure):

@@ -171,6 +171,8 @@ int validate_view(vkgv_ctx* ctx, const vkgv_view& v, uint32_t flags) {
         return fail(ctx, VKGV_INVALID_ARG, "resolve requested without a color image");
     if ((flags & VKGV_WRITE_IDS) && !v.visbuffer)
         return fail(ctx, VKGV_INVALID_ARG, "VKGV_WRITE_IDS without a visbuffer image");
+    if ((flags & VKGV_WRITE_MOTION) && !v.motion)
+        return fail(ctx, VKGV_INVALID_ARG, "VKGV_WRITE_MOTION without a motion image");
     if ((flags & VKGV_RESOLVE_FLAT) && (flags & VKGV_RESOLVE_TEXTURED))
         return fail(ctx, VKGV_INVALID_ARG, "choose one of VKGV_RESOLVE_FLAT and VKGV_RESOLVE_TEXTURED");
     if (v.survivors && !v.survivor_count)
@@ -236,6 +238,7 @@ int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, 
         d.depth_id = reinterpret_cast<unsigned long long*>(v.depth_id);
         d.ids = reinterpret_cast<uint32_t*>(v.visbuffer);
         d.rgba = reinterpret_cast<uint32_t*>(v.color);
+        d.motion = (flags & VKGV_WRITE_MOTION) ? reinterpret_cast<uint32_t*>(v.motion) : nullptr;
         if (v.survivors) {
             d.survivors = reinterpret_cast<uint32_t*>(v.survivors);
             d.survivor_count = reinterpret_cast<uint32_t*>(v.survivor_count);
@@ -319,7 +322,7 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
     zone(8);
     // The resolve also writes the survivor totals; without it a small
     // finalise kernel does.
-    const bool resolve = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS)) != 0;
+    const bool resolve = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS | VKGV_WRITE_MOTION)) != 0;
     const bool pyramid = (flags & VKGV_BUILD_PYRAMID) != 0;
     if (pyramid && resolve && !zones) {
         // the pyramid reduce and the resolve both only read the final
@@ -349,17 +352,23 @@ int check_launch(vkgv_ctx* ctx) {
 // When the scene gives its node count, a whole frame evaluates each node's
 // determinant(M) and each view's view_projection * M once (in the clear
 // kernel) instead of once per meshlet draw (raster) or per pixel (resolve).
-int attach_node_tables(vkgv_ctx* ctx, Prepared& P, DeviceView* host, uint32_t n) {
+// Motion-vector frames add prev_view_projection * M after each view's table.
+int attach_node_tables(vkgv_ctx* ctx, Prepared& P, DeviceView* host, uint32_t n, uint32_t flags) {
     const size_t T = P.S.transform_count;
     if (T == 0 || P.S.draw_count == 0) return VKGV_OK;
+    const bool motion = (flags & VKGV_WRITE_MOTION) != 0;
+    const size_t stride = (motion ? 32 : 16) * T;
     int rc = ensure_scratch(ctx, ctx->tdet, sizeof(float) * T, "node determinants");
     if (rc) return rc;
-    rc = ensure_scratch(ctx, ctx->mvp, sizeof(float) * 16 * T * n, "per-view node matrices");
+    rc = ensure_scratch(ctx, ctx->mvp, sizeof(float) * stride * n, "per-view node matrices");
     if (rc) return rc;
     P.tdets = static_cast<float*>(ctx->tdet.ptr);
     P.mvps = static_cast<float*>(ctx->mvp.ptr);
     P.S.tdets = P.tdets;
-    for (uint32_t i = 0; i < n; ++i) host[i].mvps = P.mvps + 16 * T * i;
+    for (uint32_t i = 0; i < n; ++i) {
+        host[i].mvps = P.mvps + stride * i;
+        host[i].prev_mvps = motion ? P.mvps + stride * i + 16 * T : nullptr;
+    }
     return VKGV_OK;
 }
 
@@ -499,7 +508,7 @@ int vkgv_frame(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, u
     Prepared P;
     rc = build_views(ctx, scene, views, view_count, flags, hv, P);
     if (rc) return rc;
-    rc = attach_node_tables(ctx, P, hv, view_count);
+    rc = attach_node_tables(ctx, P, hv, view_count, flags);
     if (rc) return rc;
     rc = commit_views(ctx, slot, view_count, stream);
     if (rc) return rc;
@@ -564,9 +573,10 @@ int vkgv_cull(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, uin
     int rc = acquire_slot(ctx, &slot, &dv, &hv);
     if (rc) return rc;
     Prepared P;
-    rc = build_views(ctx, scene, view, 1, flags & ~(VKGV_BUILD_PYRAMID | VKGV_RESOLVE_FLAT |
-                                                        VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS),
-                         hv, P);
+    rc = build_views(ctx, scene, view, 1,
+                     flags & ~(VKGV_BUILD_PYRAMID | VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS |
+                               VKGV_WRITE_MOTION),
+                     hv, P);
     if (rc) return rc;
     rc = commit_views(ctx, slot, 1, stream);
     if (rc) return rc;
@@ -639,8 +649,8 @@ int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, 
     int rc = acquire_slot(ctx, &slot, &dv, &hv);
     if (rc) return rc;
     Prepared P;
-    rc = build_views(ctx, scene, view, 1, flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS),
-                         hv, P);
+    rc = build_views(ctx, scene, view, 1,
+                     flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED | VKGV_WRITE_IDS | VKGV_WRITE_MOTION), hv, P);
     if (rc) return rc;
     rc = commit_views(ctx, slot, 1, stream);
     if (rc) return rc;
@@ -901,7 +911,7 @@ int vkgv_graph_capture(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* 
     Prepared P;
     rc = build_views(ctx, scene, views, view_count, flags, host.data(), P);
     if (rc) return rc;
-    rc = attach_node_tables(ctx, P, host.data(), view_count);
+    rc = attach_node_tables(ctx, P, host.data(), view_count, flags);
     if (rc) return rc;
     vkgv_graph* g = new (std::nothrow) vkgv_graph();
     if (!g) return fail(ctx, VKGV_OUT_OF_MEMORY, "graph object");

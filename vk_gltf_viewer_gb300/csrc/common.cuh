@@ -55,6 +55,9 @@ struct DeviceView {
     const float* diff_grad;     // adjoint: dL/drgb (backward, without a target)
     // view_projection * M per node (16 floats each, computed by the clear), or null
     const float* mvps;
+    // prev_view_projection * M per node (motion-vector frames only), or null
+    const float* prev_mvps;
+    uint32_t* motion;           // two binary16 per pixel (x low), or null
 };
 
 struct SceneArgs {

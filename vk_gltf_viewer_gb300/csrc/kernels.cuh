@@ -43,7 +43,9 @@ struct RasterConfig {
 // Zeroes the views' depth_id (unless max_pixels is 0) and, when counters is
 // not null, the global and per-view counters.  Also evaluates, when
 // transform_count > 0, determinant(M) of transforms[0, transform_count) into
-// tdets and each view's view_projection * M into mvps[view][node].
+// tdets and each view's view_projection * M into its DeviceView::mvps table
+// (and prev_view_projection * M into DeviceView::prev_mvps where that is set);
+// mvps is the tables' allocation, null to skip them.
 void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels, uint32_t* counters,
                   uint32_t counter_words, uint32_t sm_count, cudaStream_t stream, const float* transforms = nullptr,
                   uint32_t transform_count = 0, float* tdets = nullptr, float* mvps = nullptr);

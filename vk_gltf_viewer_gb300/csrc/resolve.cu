@@ -126,41 +126,59 @@ __device__ void sample_texture(const vkgv_texture& t, float u, float v, const fl
     }
 }
 
-// unorm[i] = i / 255 (correctly rounded), a per-block table in shared memory.
-__device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32_t px, uint32_t py, uint32_t id,
-                                 const float* unorm, float out[4]) {
-    const uint32_t d = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
-    const vkgv_meshlet_draw dr = S.draws[d];
-    const vkgv_primitive* prim = &S.prims[dr.primitive_index];
-    const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
-    const vkgv_material& mat = S.mats[prim->material_index];
-    float mvp[16];
-    if (V.mvps && dr.transform_index < S.transform_count) {
-        const float4* q = reinterpret_cast<const float4*>(V.mvps + 16 * (size_t)dr.transform_index);
+// The visible fragment of one pixel: its triangle's three vertices in clip
+// space and the perspective-correct barycentrics of the pixel centre.
+struct Frag {
+    const vkgv_vertex* vx[3];
+    const vkgv_material* mat;
+    uint32_t transform_index;
+    float c[3][4];
+    float l[3];
+};
+
+// Loads a 4x4 node-table matrix (16-byte aligned rows of the table).
+__device__ __forceinline__ void load_m4(const float* src, float m[16]) {
+    const float4* q = reinterpret_cast<const float4*>(src);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float4 c = __ldg(q + k);
-            mvp[4 * k] = c.x, mvp[4 * k + 1] = c.y, mvp[4 * k + 2] = c.z, mvp[4 * k + 3] = c.w;
-        }
+    for (int k = 0; k < 4; ++k) {
+        const float4 c = __ldg(q + k);
+        m[4 * k] = c.x, m[4 * k + 1] = c.y, m[4 * k + 2] = c.z, m[4 * k + 3] = c.w;
+    }
+}
+
+// vp * transforms[node], from the per-view node table when the frame has one.
+__device__ __forceinline__ void node_mvp(const SceneArgs& S, const float* table, const float* vp, uint32_t node,
+                                         float mvp[16]) {
+    if (table && node < S.transform_count) {
+        load_m4(table + 16 * (size_t)node, mvp);
     } else {
-        const float* Mp = S.transforms + 16 * (size_t)dr.transform_index;
+        const float* Mp = S.transforms + 16 * (size_t)node;
         float M[16], VP[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
             M[k] = __ldg(Mp + k);
-            VP[k] = V.cam->view_projection[k];
+            VP[k] = vp[k];
         }
         m4m(VP, M, mvp);
     }
+}
+
+__device__ void frag_setup(const SceneArgs& S, const DeviceView& V, uint32_t px, uint32_t py, uint32_t id, Frag& f) {
+    const uint32_t d = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
+    const vkgv_meshlet_draw dr = S.draws[d];
+    const vkgv_primitive* prim = &S.prims[dr.primitive_index];
+    const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
+    f.mat = &S.mats[prim->material_index];
+    f.transform_index = dr.transform_index;
+    float mvp[16];
+    node_mvp(S, V.mvps, V.cam->view_projection, dr.transform_index, mvp);
     const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset + 3 * t;
     const uint32_t* vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
     const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
-    float c[3][4];
-    const vkgv_vertex* vx[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        vx[k] = verts + vidx[tri[k]];
-        m4v(mvp, vx[k]->position[0], vx[k]->position[1], vx[k]->position[2], 1.0f, c[k]);
+        f.vx[k] = verts + vidx[tri[k]];
+        m4v(mvp, f.vx[k]->position[0], f.vx[k]->position[1], f.vx[k]->position[2], 1.0f, f.c[k]);
     }
     // Perspective-correct barycentrics: the clip-space weights whose point
     // projects to the pixel centre are proportional to a x b.
@@ -169,31 +187,38 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
     float a[3], b[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        a[k] = fsub(c[k][0], fmul(nx, c[k][3]));
-        b[k] = fsub(c[k][1], fmul(ny, c[k][3]));
+        a[k] = fsub(f.c[k][0], fmul(nx, f.c[k][3]));
+        b[k] = fsub(f.c[k][1], fmul(ny, f.c[k][3]));
     }
-    float l[3] = {fsub(fmul(a[1], b[2]), fmul(a[2], b[1])), fsub(fmul(a[2], b[0]), fmul(a[0], b[2])),
-                  fsub(fmul(a[0], b[1]), fmul(a[1], b[0]))};
-    const float sum = fadd(fadd(l[0], l[1]), l[2]);
+    f.l[0] = fsub(fmul(a[1], b[2]), fmul(a[2], b[1]));
+    f.l[1] = fsub(fmul(a[2], b[0]), fmul(a[0], b[2]));
+    f.l[2] = fsub(fmul(a[0], b[1]), fmul(a[1], b[0]));
+    const float sum = fadd(fadd(f.l[0], f.l[1]), f.l[2]);
     if (sum != 0.0f) {
-        l[0] = fdiv(l[0], sum);
-        l[1] = fdiv(l[1], sum);
-        l[2] = fdiv(l[2], sum);
+        f.l[0] = fdiv(f.l[0], sum);
+        f.l[1] = fdiv(f.l[1], sum);
+        f.l[2] = fdiv(f.l[2], sum);
     } else {
-        l[0] = l[1] = l[2] = 1.0f / 3.0f;
+        f.l[0] = f.l[1] = f.l[2] = 1.0f / 3.0f;
     }
+}
+
+__device__ __forceinline__ float interp3(const float l[3], float v0, float v1, float v2) {
+    return fadd(fadd(fmul(l[0], v0), fmul(l[1], v1)), fmul(l[2], v2));
+}
+
+// unorm[i] = i / 255 (correctly rounded), a per-block table in shared memory.
+__device__ void shade_textured(const SceneArgs& S, const Frag& f, const float* unorm, float out[4]) {
+    const vkgv_material& mat = *f.mat;
     float col[4], uv[2];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        col[k] = fadd(fadd(fmul(l[0], unorm[vx[0]->color[k]]), fmul(l[1], unorm[vx[1]->color[k]])),
-                      fmul(l[2], unorm[vx[2]->color[k]]));
+        col[k] = interp3(f.l, unorm[f.vx[0]->color[k]], unorm[f.vx[1]->color[k]], unorm[f.vx[2]->color[k]]);
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const float h0 = __half2float(__ushort_as_half(vx[0]->uv[k]));
-        const float h1 = __half2float(__ushort_as_half(vx[1]->uv[k]));
-        const float h2 = __half2float(__ushort_as_half(vx[2]->uv[k]));
-        uv[k] = fadd(fadd(fmul(l[0], h0), fmul(l[1], h1)), fmul(l[2], h2));
-    }
+    for (int k = 0; k < 2; ++k)
+        uv[k] = interp3(f.l, __half2float(__ushort_as_half(f.vx[0]->uv[k])),
+                        __half2float(__ushort_as_half(f.vx[1]->uv[k])),
+                        __half2float(__ushort_as_half(f.vx[2]->uv[k])));
     float sampled[4] = {1.0f, 1.0f, 1.0f, 1.0f};
     if (mat.albedo_index != VKGV_INVALID_HANDLE && mat.albedo_index < S.texture_count) {
         // transformUv (mesh_common.h.glsl:129-135): rotate, scale, offset
@@ -214,8 +239,38 @@ __device__ void resolve_textured(const SceneArgs& S, const DeviceView& V, uint32
     for (int k = 0; k < 4; ++k) out[k] = fmul(fmul(col[k], mat.albedo_factor[k]), sampled[k]);
 }
 
-template <bool TEXTURED>
-__global__ void __launch_bounds__(256, 6) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
+// Motion vector of the visible fragment (visbuffer.frag.glsl:38, with the
+// mesh shader's position / prevPosition varyings of visbuffer.mesh.glsl:44-64):
+//   position     = viewProjection     * M * vertex, interpolated
+//   prevPosition = prevViewProjection * M * vertex, interpolated
+//   motion = (prev.xy / prev.w * 0.5 - 0.5) - (pos.xy / pos.w * 0.5 - 0.5)
+// M is the node's current transform for both (the reference has no
+// previous-frame transforms).  Written as two RN binary16, x in the low half.
+__device__ uint32_t motion_vector(const SceneArgs& S, const DeviceView& V, const Frag& f) {
+    float pmvp[16];
+    node_mvp(S, V.prev_mvps, V.cam->prev_view_projection, f.transform_index, pmvp);
+    float p[3][4];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        m4v(pmvp, f.vx[k]->position[0], f.vx[k]->position[1], f.vx[k]->position[2], 1.0f, p[k]);
+    const float cw = interp3(f.l, f.c[0][3], f.c[1][3], f.c[2][3]);
+    const float pw = interp3(f.l, p[0][3], p[1][3], p[2][3]);
+    uint32_t out = 0;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const float cj = interp3(f.l, f.c[0][j], f.c[1][j], f.c[2][j]);
+        const float pj = interp3(f.l, p[0][j], p[1][j], p[2][j]);
+        const float cur = fsub(fmul(fdiv(cj, cw), 0.5f), 0.5f);
+        const float prev = fsub(fmul(fdiv(pj, pw), 0.5f), 0.5f);
+        out |= (uint32_t)__half_as_ushort(__float2half_rn(fsub(prev, cur))) << (16 * j);
+    }
+    return out;
+}
+
+// Six CTAs per SM hold the colour-only variants without spills; the motion
+// variants keep the previous-frame clip positions live as well.
+template <bool TEXTURED, bool MOTION>
+__global__ void __launch_bounds__(256, MOTION ? 4 : 6) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
     pdl_begin();
     const DeviceView& V = views[blockIdx.y];
     __shared__ float s_unorm[256];
@@ -226,43 +281,55 @@ __global__ void __launch_bounds__(256, 6) k_resolve(SceneArgs S, const DeviceVie
     const uint32_t w = V.w, n = V.w * V.h;
     uint32_t* ids = (flags & VKGV_WRITE_IDS) ? V.ids : nullptr;
     uint32_t* rgba = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED)) ? V.rgba : nullptr;
+    uint32_t* motion = MOTION ? V.motion : nullptr;
     if (blockIdx.x == 0 && threadIdx.x == 0) finalize_view(V);
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const uint32_t lo = (uint32_t)__ldcs(V.depth_id + p);
         const uint32_t id = lo ? lo - 1u : VKGV_VISBUFFER_CLEAR;
         if (ids) __stcs(ids + p, id);
-        if (!rgba) continue;
-        uint32_t out = 0;
+        if (!rgba && !MOTION) continue;
+        uint32_t out = 0, mv = 0;
         if (id != VKGV_VISBUFFER_CLEAR) {
             float lin[4];
-            if (TEXTURED) {
-                resolve_textured(S, V, p % w, p / w, id, s_unorm, lin);
+            if (TEXTURED || MOTION) {
+                Frag f;
+                frag_setup(S, V, p % w, p / w, id, f);
+                if (MOTION) mv = motion_vector(S, V, f);
+                if (TEXTURED) {
+                    shade_textured(S, f, s_unorm, lin);
+                } else {
+                    const float4 a = *reinterpret_cast<const float4*>(f.mat->albedo_factor);
+                    lin[0] = a.x, lin[1] = a.y, lin[2] = a.z, lin[3] = a.w;
+                }
             } else {
                 const vkgv_meshlet_draw dr = S.draws[id >> VKGV_TRIANGLE_BITS];
                 const vkgv_material& mat = S.mats[S.prims[dr.primitive_index].material_index];
                 const float4 a = *reinterpret_cast<const float4*>(mat.albedo_factor);
-                lin[0] = a.x;
-                lin[1] = a.y;
-                lin[2] = a.z;
-                lin[3] = a.w;
+                lin[0] = a.x, lin[1] = a.y, lin[2] = a.z, lin[3] = a.w;
             }
-            out = TEXTURED ? pack_rgba_fast(lin) : pack_rgba(lin);
+            if (rgba) out = TEXTURED ? pack_rgba_fast(lin) : pack_rgba(lin);
         }
-        __stcs(rgba + p, out);
+        if (rgba) __stcs(rgba + p, out);
+        if (MOTION) __stcs(motion + p, mv);
     }
 }
 
 __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ views, uint32_t* counters,
                                                uint32_t counter_words, uint32_t skip_pixels,
                                                const float* __restrict__ transforms, uint32_t transform_count,
-                                               float* __restrict__ tdets, float* __restrict__ mvps) {
+                                               float* __restrict__ tdets) {
     pdl_begin();
     const DeviceView& V = views[blockIdx.y];
     if (transform_count) {
-        __shared__ float s_vp[16];
-        if (threadIdx.x < 16) s_vp[threadIdx.x] = V.cam->view_projection[threadIdx.x];
+        // the view's node tables: view_projection * M, and for motion-vector
+        // frames prev_view_projection * M
+        __shared__ float s_vp[2][16];
+        if (threadIdx.x < 16) s_vp[0][threadIdx.x] = V.cam->view_projection[threadIdx.x];
+        if (threadIdx.x >= 32 && threadIdx.x < 48)
+            s_vp[1][threadIdx.x - 32] = V.cam->prev_view_projection[threadIdx.x - 32];
         __syncthreads();
-        float* out = mvps + (size_t)blockIdx.y * transform_count * 16;
+        float* out = const_cast<float*>(V.mvps);
+        float* prev = const_cast<float*>(V.prev_mvps);
         for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < transform_count; i += gridDim.x * blockDim.x) {
             float M[16], r[16];
 #pragma unroll
@@ -271,11 +338,18 @@ __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ vi
                 M[4 * k] = q.x, M[4 * k + 1] = q.y, M[4 * k + 2] = q.z, M[4 * k + 3] = q.w;
             }
             if (blockIdx.y == 0) tdets[i] = det4(M);
-            m4m(s_vp, M, r);
+            m4m(s_vp[0], M, r);
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 reinterpret_cast<float4*>(out + 16 * (size_t)i)[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2],
                                                                                   r[4 * k + 3]);
+            if (prev) {
+                m4m(s_vp[1], M, r);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    reinterpret_cast<float4*>(prev + 16 * (size_t)i)[k] =
+                        make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+            }
         }
     }
     if (counters) {
@@ -309,10 +383,15 @@ void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews
     uint32_t bx = (uint32_t)((px + 255) / 256);
     if (bx > 65535u) bx = 65535u;
     dim3 grid(bx, nviews);
-    if (flags & VKGV_RESOLVE_TEXTURED)
-        launch_pdl(k_resolve<true>, grid, dim3(256), 0, stream, S, views, flags);
+    const bool tex = (flags & VKGV_RESOLVE_TEXTURED) != 0, mv = (flags & VKGV_WRITE_MOTION) != 0;
+    if (tex && mv)
+        launch_pdl(k_resolve<true, true>, grid, dim3(256), 0, stream, S, views, flags);
+    else if (tex)
+        launch_pdl(k_resolve<true, false>, grid, dim3(256), 0, stream, S, views, flags);
+    else if (mv)
+        launch_pdl(k_resolve<false, true>, grid, dim3(256), 0, stream, S, views, flags);
     else
-        launch_pdl(k_resolve<false>, grid, dim3(256), 0, stream, S, views, flags);
+        launch_pdl(k_resolve<false, false>, grid, dim3(256), 0, stream, S, views, flags);
 }
 
 void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels, uint32_t* counters,
@@ -326,7 +405,7 @@ void launch_clear(const DeviceView* views, uint32_t nviews, uint64_t max_pixels,
     dim3 grid(bx, nviews);
     if (!tdets || !mvps) transform_count = 0;
     launch_pdl(k_clear, grid, dim3(256), 0, stream, views, counters, counter_words, skip ? 1u : 0u, transforms,
-               transform_count, tdets, mvps);
+               transform_count, tdets);
 }
 
 void launch_finalize(const DeviceView* views, uint32_t nviews, cudaStream_t stream) {

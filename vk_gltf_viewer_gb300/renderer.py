@@ -97,7 +97,8 @@ def pyramid_layout(w: int, h: int) -> tuple[int, int]:
 @dataclass
 class ViewBuffers:
     """Per-view device images: camera, depth|id, visbuffer, colour, pyramids,
-    survivor list."""
+    survivor list and, optionally, the motion-vector image (two binary16 per
+    pixel, x in the low half)."""
     width: int
     height: int
     camera: torch.Tensor
@@ -110,11 +111,12 @@ class ViewBuffers:
     survivor_count: torch.Tensor | None
     levels: int
     use_prev: bool = True
+    motion: torch.Tensor | None = None
 
     @classmethod
     def allocate(cls, width: int, height: int, cam: abi.Camera, draw_capacity: int, device="cuda",
                  ids: bool = True, color: bool = True, pyramid: bool = True, prev_pyramid: bool = False,
-                 survivors: bool = True) -> "ViewBuffers":
+                 survivors: bool = True, motion: bool = False) -> "ViewBuffers":
         dev = torch.device(device)
         levels, floats = pyramid_layout(width, height)
         cam_t = torch.from_numpy(np.frombuffer(C.string_at(C.addressof(cam), C.sizeof(cam)), np.uint8).copy()).to(dev)
@@ -132,7 +134,8 @@ class ViewBuffers:
                    pyramid=pyr, prev_pyramid=prev,
                    survivors=torch.zeros(max(1, draw_capacity), dtype=torch.int32, device=dev) if survivors else None,
                    survivor_count=torch.zeros(1, dtype=torch.int32, device=dev) if survivors else None,
-                   levels=levels)
+                   levels=levels,
+                   motion=torch.zeros(width * height, dtype=torch.int32, device=dev) if motion else None)
 
     def set_camera(self, cam: abi.Camera) -> None:
         src = torch.from_numpy(np.frombuffer(C.string_at(C.addressof(cam), C.sizeof(cam)), np.uint8).copy())
@@ -149,10 +152,16 @@ class ViewBuffers:
         v.depth_id = _ptr(self.depth_id)
         v.visbuffer = _ptr(self.visbuffer)
         v.color = _ptr(self.color)
+        v.motion = _ptr(self.motion)
         v.survivors = _ptr(self.survivors)
         v.survivor_count = _ptr(self.survivor_count)
         v.survivor_capacity = 0 if self.survivors is None else int(self.survivors.numel())
         return v
+
+    def motion_vectors(self) -> np.ndarray:
+        """The motion image as float32 (H, W, 2)."""
+        mv = self.motion.cpu().numpy().view(np.float16).astype(np.float32)
+        return mv.reshape(self.height, self.width, 2)
 
     def survivor_list(self) -> np.ndarray:
         n = int(self.survivor_count.item())

@@ -298,12 +298,17 @@ def camera_bytes(cam: abi.Camera) -> np.ndarray:
     return np.frombuffer(C.string_at(C.addressof(cam), C.sizeof(cam)), np.uint8).copy()
 
 
-def grid_camera(width: int = 1920, height: int = 1080, fovy_deg: float = 75.0) -> abi.Camera:
-    """Camera inside the torus grid looking down its long (+x) axis."""
+def grid_camera(width: int = 1920, height: int = 1080, fovy_deg: float = 75.0, moved: float = 0.0) -> abi.Camera:
+    """Camera inside the torus grid looking down its long (+x) axis.  With
+    `moved`, the previous frame's camera stood that far behind (-x)."""
     gx, gz, gy = GRID
     eye = (0.5 * SPACING * 0.5, (gy / 2 - 0.5) * SPACING, (gz / 2 - 0.5) * SPACING)
     target = (eye[0] + 10.0, eye[1], eye[2])
-    return camera(eye, target, (0.0, 1.0, 0.0), fovy_deg, width / height)
+    prev = None
+    if moved:
+        prev = camera((eye[0] - moved, eye[1], eye[2]), (target[0] - moved, target[1], target[2]), (0.0, 1.0, 0.0),
+                      fovy_deg, width / height)
+    return camera(eye, target, (0.0, 1.0, 0.0), fovy_deg, width / height, prev=prev)
 
 
 BATCH_SIZES = [(256, 256), (512, 384), (1024, 576), (1280, 720), (1920, 1080)]
