@@ -406,6 +406,99 @@ int vkgv_diff_graph_capture(vkgv_ctx* ctx, const vkgv_diff_scene* scene, const v
                             uint64_t grad_positions, uint64_t grad_colors, uint64_t grad_texture,
                             vkgv_graph** out_graph);
 
+/* ------------------------------------------------------------------ world */
+/* The node tree, its animations and the per-frame buffers built from it
+ * (src/vk_gltf_viewer/world.cpp:187-345, include/vk_gltf_viewer/assets.hpp:51-113):
+ * World::updateTransformBuffer becomes vkgv_world_update_transforms and
+ * World::rebuildDrawBuffer vkgv_world_build_draws, both on the device.  The
+ * tree is walked depth-first from the roots as World::iterateNode does; every
+ * visit of a node with a mesh takes the next transform index, and its
+ * primitives' meshlets append MeshletDraw records in that order. */
+
+/* A glTF node after DecomposeNodeMatrices (fastgltf::TRS). */
+typedef struct vkgv_node {
+    float translation[3];
+    float rotation[4];      /* quaternion x, y, z, w */
+    float scale[3];
+    uint32_t mesh_index;    /* VKGV_INVALID_HANDLE: no mesh */
+    uint32_t first_child;   /* children at vkgv_world_desc.children[first_child, +child_count) */
+    uint32_t child_count;
+} vkgv_node; /* 52 B */
+
+enum vkgv_anim_path {
+    VKGV_PATH_TRANSLATION = 1,
+    VKGV_PATH_ROTATION = 2,
+    VKGV_PATH_SCALE = 3,
+    VKGV_PATH_WEIGHTS = 4   /* accepted and ignored, as the reference does */
+};
+
+enum vkgv_anim_interpolation {
+    VKGV_INTERP_LINEAR = 0,
+    VKGV_INTERP_STEP = 1,
+    VKGV_INTERP_CUBICSPLINE = 2
+};
+
+/* An animation sampler (assets.hpp:37-47): keyframe times and outputs, host
+ * arrays copied to the device by vkgv_world_create. */
+typedef struct vkgv_anim_sampler {
+    const float* input;      /* input_count times, ascending */
+    const float* output;     /* output_count * components floats */
+    uint32_t input_count;
+    uint32_t output_count;   /* input_count, or 3 * input_count for CUBICSPLINE */
+    uint32_t interpolation;  /* vkgv_anim_interpolation */
+    uint32_t components;     /* 3 (translation, scale) or 4 (rotation) */
+} vkgv_anim_sampler;
+
+/* A channel; channels apply in array order (the reference's animation by
+ * animation, channel by channel), a later one overriding an earlier one. */
+typedef struct vkgv_anim_channel {
+    uint32_t sampler;        /* index into vkgv_world_desc.samplers */
+    uint32_t node;           /* VKGV_INVALID_HANDLE: no target */
+    uint32_t path;           /* vkgv_anim_path */
+    uint32_t _pad;
+} vkgv_anim_channel;
+
+/* Host arrays describing one world (World::addAsset's merged tables). */
+typedef struct vkgv_world_desc {
+    const vkgv_node* nodes;
+    uint32_t node_count;
+    uint32_t child_count;
+    const uint32_t* children;
+    const uint32_t* roots;              /* scenes[0].nodeIndices */
+    uint32_t root_count;
+    uint32_t mesh_count;
+    const uint32_t* mesh_offsets;       /* mesh_count + 1 offsets into mesh_primitives */
+    const uint32_t* mesh_primitives;    /* Mesh::primitiveIndices, concatenated */
+    const uint32_t* primitive_meshlet_counts; /* PrimitiveBuffers::meshletCount */
+    uint32_t primitive_count;
+    uint32_t sampler_count;
+    const vkgv_anim_sampler* samplers;
+    const vkgv_anim_channel* channels;
+    uint32_t channel_count;
+    uint32_t _pad;
+} vkgv_world_desc;
+
+#define VKGV_MAX_NODE_DEPTH 64u
+
+typedef struct vkgv_world vkgv_world;
+/* Validates the tables, walks the tree once on the host (the draw and
+ * transform order never changes afterwards, as world.cpp:236-238 assumes)
+ * and uploads the plan and the keyframes.  A path deeper than
+ * VKGV_MAX_NODE_DEPTH (or a cycle) is VKGV_LIMIT_EXCEEDED. */
+int vkgv_world_create(vkgv_ctx* ctx, const vkgv_world_desc* desc, vkgv_world** out_world);
+int vkgv_world_destroy(vkgv_world* world);
+/* Transform slots (mesh-node visits) and MeshletDraw records of the world. */
+int vkgv_world_info(const vkgv_world* world, uint32_t* out_transform_count, uint64_t* out_draw_count);
+/* World::updateTransformBuffer at animationTime: samples every channel,
+ * composes parent * T * R * S down the tree and writes one column-major
+ * mat4 per transform slot into transform_buffer (device float[16 * T]). */
+int vkgv_world_update_transforms(vkgv_ctx* ctx, vkgv_world* world, float animation_time,
+                                 uint64_t transform_buffer, void* stream);
+/* World::rebuildDrawBuffer: writes the MeshletDraw list on the device into
+ * draw_buffer (16-byte aligned, capacity >= the draw count). */
+int vkgv_world_build_draws(vkgv_ctx* ctx, vkgv_world* world, uint64_t draw_buffer, uint64_t capacity,
+                           void* stream);
+
 /* ---------------------------------------------- host scene producers (A15) */
 /* Replace the glTF import + meshletiser (src/vk_gltf_viewer/assets.cpp:288-430)
  * for procedural scenes, and the camera update (src/vk_gltf_viewer/camera.cpp). */

@@ -47,6 +47,20 @@ class OrcPyramid(C.Structure):
     _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("levels", C.c_uint32)]
 
 
+class OrcWorld(C.Structure):
+    _fields_ = [("nodes", C.c_void_p), ("node_count", C.c_uint32), ("child_count", C.c_uint32),
+                ("children", C.c_void_p), ("roots", C.c_void_p), ("root_count", C.c_uint32),
+                ("mesh_count", C.c_uint32), ("mesh_offsets", C.c_void_p), ("mesh_primitives", C.c_void_p),
+                ("primitive_meshlet_counts", C.c_void_p), ("primitive_count", C.c_uint32),
+                ("sampler_count", C.c_uint32), ("samplers", C.c_void_p), ("channels", C.c_void_p),
+                ("channel_count", C.c_uint32), ("pad_", C.c_uint32)]
+
+
+class OrcAnimSampler(C.Structure):
+    _fields_ = [("input", C.c_void_p), ("output", C.c_void_p), ("input_count", C.c_uint32),
+                ("output_count", C.c_uint32), ("interpolation", C.c_uint32), ("components", C.c_uint32)]
+
+
 _lib = None
 
 
@@ -78,6 +92,17 @@ def load() -> C.CDLL:
         lib.orc_resolve.argtypes = [P, P, U32, U32, P, U32, P, P]
         lib.orc_frame.argtypes = [P, P, U32, U32, P, U32, P, P, P, P, P, P]
         lib.orc_motion.argtypes = [P, P, U32, U32, P, P]
+        lib.orc_world_transforms.restype = C.c_int64
+        lib.orc_world_transforms.argtypes = [P, C.c_float, P, U32]
+        lib.orc_world_draws.restype = C.c_int64
+        lib.orc_world_draws.argtypes = [P, P, C.c_uint64]
+        lib.orc_anim_sample.argtypes = [P, C.c_float, U32, P]
+        lib.orc_slerp.argtypes = [P, P, C.c_float, P]
+        lib.orc_trs_matrix.argtypes = [P, P, P, P]
+        lib.orc_sin_series.restype = C.c_float
+        lib.orc_sin_series.argtypes = [C.c_float]
+        lib.orc_asin_series.restype = C.c_float
+        lib.orc_asin_series.argtypes = [C.c_float]
         lib.orc_half_rn.restype = C.c_uint16
         lib.orc_half_rn.argtypes = [C.c_float]
         lib.orc_from_linear.restype = C.c_float
@@ -308,3 +333,71 @@ def from_linear(c: float) -> float:
 
 def unorm8(c: float) -> int:
     return int(load().orc_unorm8(c))
+
+
+# ------------------------------------------------------------------ world
+
+def _orc_world(host) -> OrcWorld:
+    """The oracle's orc_world over a HostWorld's arrays (same layout as the
+    library's vkgv_world_desc)."""
+    return OrcWorld(**host.desc_fields())
+
+
+def world_transforms(host, animation_time: float) -> np.ndarray:
+    """World::updateTransformBuffer: (T, 16) float32, column-major."""
+    lib = load()
+    w = _orc_world(host)
+    n = lib.orc_world_transforms(C.addressof(w), animation_time, None, 0)
+    if n < 0:
+        raise ValueError("node tree deeper than 64")
+    out = np.zeros((max(1, n), 16), np.float32)
+    lib.orc_world_transforms(C.addressof(w), animation_time, _addr(out), n)
+    return out[:n]
+
+
+def world_draws(host) -> np.ndarray:
+    """World::rebuildDrawBuffer: (D, 3) uint32 {primitive, meshlet, transform}."""
+    lib = load()
+    w = _orc_world(host)
+    n = lib.orc_world_draws(C.addressof(w), None, 0)
+    if n < 0:
+        raise ValueError("node tree deeper than 64")
+    out = np.zeros((max(1, n), 3), np.uint32)
+    lib.orc_world_draws(C.addressof(w), _addr(out), n)
+    return out[:n]
+
+
+def anim_sample(times: np.ndarray, values: np.ndarray, interpolation: int, t: float, path: int) -> np.ndarray:
+    """AnimationSampler::sample of one sampler (values: (output_count, components))."""
+    times = np.ascontiguousarray(times, np.float32)
+    values = np.ascontiguousarray(values, np.float32)
+    s = OrcAnimSampler(times.ctypes.data, values.ctypes.data, times.size, values.shape[0], interpolation,
+                       values.shape[1])
+    out = np.zeros(4, np.float32)
+    load().orc_anim_sample(C.addressof(s), t, path, _addr(out))
+    return out[: values.shape[1]]
+
+
+def slerp(a, b, t: float) -> np.ndarray:
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    out = np.zeros(4, np.float32)
+    load().orc_slerp(_addr(a), _addr(b), t, _addr(out))
+    return out
+
+
+def trs_matrix(t, q, s) -> np.ndarray:
+    t = np.ascontiguousarray(t, np.float32)
+    q = np.ascontiguousarray(q, np.float32)
+    s = np.ascontiguousarray(s, np.float32)
+    out = np.zeros(16, np.float32)
+    load().orc_trs_matrix(_addr(t), _addr(q), _addr(s), _addr(out))
+    return out
+
+
+def sin_series(x: float) -> float:
+    return float(load().orc_sin_series(x))
+
+
+def asin_series(z: float) -> float:
+    return float(load().orc_asin_series(z))

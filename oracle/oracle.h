@@ -176,6 +176,57 @@ double orc_diff_f64(const orc_diff_scene* s, const float vp[16], uint32_t w, uin
  * positions is a valid check of the analytic gradient only while no pixel's
  * cell changes across the stencil. */
 
+/* ------------------------------------------------------------ world.c */
+/* Node tree, animations and the per-frame transform / draw lists
+ * (world.cpp:187-345, assets.hpp:51-113); the same layouts as the library's
+ * vkgv_world_desc. */
+typedef struct orc_node {
+    float translation[3], rotation[4], scale[3]; /* rotation x, y, z, w */
+    uint32_t mesh_index, first_child, child_count;
+} orc_node; /* 52 B */
+
+enum { ORC_PATH_TRANSLATION = 1, ORC_PATH_ROTATION = 2, ORC_PATH_SCALE = 3, ORC_PATH_WEIGHTS = 4 };
+enum { ORC_INTERP_LINEAR = 0, ORC_INTERP_STEP = 1, ORC_INTERP_CUBICSPLINE = 2 };
+
+typedef struct orc_anim_sampler {
+    const float* input;
+    const float* output;
+    uint32_t input_count, output_count, interpolation, components;
+} orc_anim_sampler;
+
+typedef struct orc_anim_channel {
+    uint32_t sampler, node, path, pad_;
+} orc_anim_channel;
+
+typedef struct orc_world {
+    const orc_node* nodes;
+    uint32_t node_count, child_count;
+    const uint32_t* children;
+    const uint32_t* roots;
+    uint32_t root_count, mesh_count;
+    const uint32_t* mesh_offsets;
+    const uint32_t* mesh_primitives;
+    const uint32_t* primitive_meshlet_counts;
+    uint32_t primitive_count, sampler_count;
+    const orc_anim_sampler* samplers;
+    const orc_anim_channel* channels;
+    uint32_t channel_count, pad_;
+} orc_world;
+
+/* World::updateTransformBuffer at animation_time: one column-major mat4 per
+ * node with a mesh, in depth-first order.  Returns the count (-1 for a path
+ * deeper than 64 nodes); writes at most `capacity` matrices. */
+int64_t orc_world_transforms(const orc_world* w, float animation_time, float* transforms, uint32_t capacity);
+/* World::rebuildDrawBuffer: MeshletDraw {primitive, meshlet, transform} as
+ * three words each.  Returns the count (-1 as above). */
+int64_t orc_world_draws(const orc_world* w, uint32_t* draws, uint64_t capacity);
+/* The pinned pieces, exported for the CPU tests. */
+void orc_anim_sample(const orc_anim_sampler* s, float time, uint32_t path, float out[4]);
+void orc_slerp(const float a[4], const float b[4], float t, float out[4]);
+void orc_trs_matrix(const float t[3], const float q[4], const float s[3], float m[16]);
+float orc_sin_series(float x);
+float orc_asin_series(float z);
+
 /* Single-fragment helpers exported for the known-answer tests. */
 float orc_from_linear(float c);
 float orc_to_linear(float c);

@@ -36,6 +36,8 @@ def test_c_layout_matches_ctypes(tmp_path):
         "vkgv_primitive": abi.Primitive, "vkgv_material": abi.Material, "vkgv_camera": abi.Camera,
         "vkgv_texture": abi.Texture, "vkgv_pyramid": abi.Pyramid, "vkgv_scene": abi.Scene, "vkgv_view": abi.View,
         "vkgv_config": abi.Config, "vkgv_mesh_info": abi.MeshInfo, "vkgv_meshlet_cone": abi.MeshletCone,
+        "vkgv_node": abi.Node, "vkgv_anim_sampler": abi.AnimSampler, "vkgv_anim_channel": abi.AnimChannel,
+        "vkgv_world_desc": abi.WorldDesc,
     }
     lines = []
     for cname, cls in structs.items():
@@ -70,13 +72,14 @@ def test_oracle_layouts_match(built):
     from oracle import binding  # noqa: F401  (built fixture compiled it)
     src = abi.ROOT / "oracle" / "oracle.h"
     probe = abi.ROOT / "oracle" / "_build" / "probe_sizes.c"
-    probe.write_text('#include <stdio.h>\n#include "oracle.h"\nint main(void){printf("%zu %zu %zu %zu %zu\\n",'
+    probe.write_text('#include <stdio.h>\n#include "oracle.h"\nint main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",'
                      'sizeof(orc_meshlet), sizeof(orc_vertex), sizeof(orc_draw), sizeof(orc_material),'
-                     'sizeof(orc_camera));return 0;}\n')
+                     'sizeof(orc_camera), sizeof(orc_node), sizeof(orc_anim_sampler), sizeof(orc_anim_channel),'
+                     'sizeof(orc_world));return 0;}\n')
     exe = probe.with_suffix("")
     subprocess.run(["gcc", "-I", str(src.parent), str(probe), "-o", str(exe)], check=True)
     sizes = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()))
-    assert sizes == [36, 24, 12, 48, 352]
+    assert sizes == [36, 24, 12, 48, 352, 52, 32, 16, 96]
 
 
 def test_pyramid_layout_host_helper(built):

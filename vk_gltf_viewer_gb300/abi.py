@@ -154,7 +154,35 @@ class DiffView(C.Structure):
                 ("depth_id", C.c_uint64), ("rgb", C.c_uint64), ("target", C.c_uint64), ("grad_rgb", C.c_uint64)]
 
 
-EXPECTED_SIZES = {"Meshlet": 36, "Vertex": 24, "MeshletDraw": 12, "Primitive": 64, "Material": 48, "Camera": 352}
+class Node(C.Structure):
+    _fields_ = [("translation", C.c_float * 3), ("rotation", C.c_float * 4), ("scale", C.c_float * 3),
+                ("mesh_index", C.c_uint32), ("first_child", C.c_uint32), ("child_count", C.c_uint32)]
+
+
+class AnimSampler(C.Structure):
+    _fields_ = [("input", C.c_void_p), ("output", C.c_void_p), ("input_count", C.c_uint32),
+                ("output_count", C.c_uint32), ("interpolation", C.c_uint32), ("components", C.c_uint32)]
+
+
+class AnimChannel(C.Structure):
+    _fields_ = [("sampler", C.c_uint32), ("node", C.c_uint32), ("path", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class WorldDesc(C.Structure):
+    _fields_ = [("nodes", C.c_void_p), ("node_count", C.c_uint32), ("child_count", C.c_uint32),
+                ("children", C.c_void_p), ("roots", C.c_void_p), ("root_count", C.c_uint32),
+                ("mesh_count", C.c_uint32), ("mesh_offsets", C.c_void_p), ("mesh_primitives", C.c_void_p),
+                ("primitive_meshlet_counts", C.c_void_p), ("primitive_count", C.c_uint32),
+                ("sampler_count", C.c_uint32), ("samplers", C.c_void_p), ("channels", C.c_void_p),
+                ("channel_count", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+PATH_TRANSLATION, PATH_ROTATION, PATH_SCALE, PATH_WEIGHTS = 1, 2, 3, 4
+INTERP_LINEAR, INTERP_STEP, INTERP_CUBICSPLINE = 0, 1, 2
+MAX_NODE_DEPTH = 64
+
+EXPECTED_SIZES = {"Meshlet": 36, "Vertex": 24, "MeshletDraw": 12, "Primitive": 64, "Material": 48, "Camera": 352,
+                  "Node": 52, "AnimSampler": 32, "AnimChannel": 16, "WorldDesc": 96}
 
 _P = C.c_void_p
 _U32 = C.c_uint32
@@ -195,6 +223,11 @@ _PROTOS = {
                                           _U64, _U64, _U64, _U64, C.POINTER(_P)]),
     "vkgv_autotune": (C.c_int, [C.POINTER(Config), C.POINTER(Scene), C.POINTER(View), _U32, _U32, _U32,
                                 C.POINTER(TuneEntry), _U32, C.POINTER(_U32), C.POINTER(Config)]),
+    "vkgv_world_create": (C.c_int, [_P, C.POINTER(WorldDesc), C.POINTER(_P)]),
+    "vkgv_world_destroy": (C.c_int, [_P]),
+    "vkgv_world_info": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U64)]),
+    "vkgv_world_update_transforms": (C.c_int, [_P, _P, C.c_float, _U64, _P]),
+    "vkgv_world_build_draws": (C.c_int, [_P, _P, _U64, _U64, _P]),
     "vkgv_set_profiling": (C.c_int, [_P, C.c_int32]),
     "vkgv_stage_times": (C.c_int, [_P, C.POINTER(C.c_float), _U32]),
 }

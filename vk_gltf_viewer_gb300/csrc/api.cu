@@ -75,6 +75,15 @@ struct vkgv_graph {
     cudaGraphExec_t exec = nullptr;
 };
 
+// A planned node tree: every table in one device allocation.  Updates of one
+// world are issued on one stream at a time (they share the local-matrix
+// scratch).
+struct vkgv_world {
+    void* block = nullptr;
+    WorldArgs args{};
+    uint64_t draw_count = 0;
+};
+
 namespace {
 
 int fail(vkgv_ctx* ctx, int code, const std::string& msg) {
@@ -658,6 +667,119 @@ int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, 
     rc = check_launch(ctx);
     if (rc) return rc;
     return close_slot(ctx, slot, stream);
+}
+
+
+int vkgv_world_create(vkgv_ctx* ctx, const vkgv_world_desc* desc, vkgv_world** out_world) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!desc || !out_world) return fail(ctx, VKGV_INVALID_ARG, "desc and out_world must be non-NULL");
+    *out_world = nullptr;
+    WorldPlan P;
+    std::string err;
+    int rc = plan_world(*desc, P, err);
+    if (rc) return fail(ctx, rc, err);
+    // one allocation, each table 16-byte aligned
+    size_t off = 0;
+    auto place = [&](size_t bytes) {
+        const size_t at = off;
+        off += (bytes + 15) & ~size_t(15);
+        return at;
+    };
+    const size_t o_rest = place(sizeof(float) * P.rest.size());
+    const size_t o_coff = place(sizeof(uint32_t) * P.chan_offsets.size());
+    const size_t o_chans = place(sizeof(uint2) * P.chans.size());
+    const size_t o_samp = place(sizeof(WorldSampler) * P.samplers.size());
+    const size_t o_keys = place(sizeof(float) * P.keys.size());
+    const size_t o_local = place(sizeof(float) * 16 * (size_t)P.node_count);
+    const size_t o_choff = place(sizeof(uint32_t) * P.chain_offsets.size());
+    const size_t o_chain = place(sizeof(uint32_t) * P.chain_nodes.size());
+    const size_t o_sfirst = place(sizeof(uint32_t) * P.seg_first.size());
+    const size_t o_sinfo = place(sizeof(uint2) * P.seg_info.size());
+    const size_t o_tiles = place(sizeof(uint32_t) * P.tile_seg.size());
+    vkgv_world* w = new (std::nothrow) vkgv_world();
+    if (!w) return fail(ctx, VKGV_OUT_OF_MEMORY, "world allocation failed");
+    if (cudaMalloc(&w->block, std::max<size_t>(off, 16)) != cudaSuccess) {
+        cudaGetLastError();
+        delete w;
+        return fail(ctx, VKGV_OUT_OF_MEMORY, "world device tables");
+    }
+    char* b = static_cast<char*>(w->block);
+    auto put = [&](size_t at, const void* src, size_t bytes) {
+        return bytes ? cudaMemcpy(b + at, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+    };
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = put(o_rest, P.rest.data(), sizeof(float) * P.rest.size());
+    if (e == cudaSuccess) e = put(o_coff, P.chan_offsets.data(), sizeof(uint32_t) * P.chan_offsets.size());
+    if (e == cudaSuccess) e = put(o_chans, P.chans.data(), sizeof(uint2) * P.chans.size());
+    if (e == cudaSuccess) e = put(o_samp, P.samplers.data(), sizeof(WorldSampler) * P.samplers.size());
+    if (e == cudaSuccess) e = put(o_keys, P.keys.data(), sizeof(float) * P.keys.size());
+    if (e == cudaSuccess) e = put(o_choff, P.chain_offsets.data(), sizeof(uint32_t) * P.chain_offsets.size());
+    if (e == cudaSuccess) e = put(o_chain, P.chain_nodes.data(), sizeof(uint32_t) * P.chain_nodes.size());
+    if (e == cudaSuccess) e = put(o_sfirst, P.seg_first.data(), sizeof(uint32_t) * P.seg_first.size());
+    if (e == cudaSuccess) e = put(o_sinfo, P.seg_info.data(), sizeof(uint2) * P.seg_info.size());
+    if (e == cudaSuccess) e = put(o_tiles, P.tile_seg.data(), sizeof(uint32_t) * P.tile_seg.size());
+    if (e != cudaSuccess) {
+        cudaFree(w->block);
+        delete w;
+        return cuda_fail(ctx, e, "world upload");
+    }
+    WorldArgs& A = w->args;
+    A.rest = reinterpret_cast<const float*>(b + o_rest);
+    A.chan_offsets = reinterpret_cast<const uint32_t*>(b + o_coff);
+    A.chans = reinterpret_cast<const uint2*>(b + o_chans);
+    A.samplers = reinterpret_cast<const WorldSampler*>(b + o_samp);
+    A.keys = reinterpret_cast<const float*>(b + o_keys);
+    A.local = reinterpret_cast<float*>(b + o_local);
+    A.chain_offsets = reinterpret_cast<const uint32_t*>(b + o_choff);
+    A.chain_nodes = reinterpret_cast<const uint32_t*>(b + o_chain);
+    A.seg_first = reinterpret_cast<const uint32_t*>(b + o_sfirst);
+    A.seg_info = reinterpret_cast<const uint2*>(b + o_sinfo);
+    A.tile_seg = reinterpret_cast<const uint32_t*>(b + o_tiles);
+    A.tile_count = (uint32_t)P.tile_seg.size();
+    A.node_count = P.node_count;
+    A.slot_count = P.slot_count;
+    A.seg_count = P.seg_count;
+    A.draw_count = (uint32_t)P.draw_count;
+    w->draw_count = P.draw_count;
+    *out_world = w;
+    return VKGV_OK;
+}
+
+int vkgv_world_destroy(vkgv_world* world) {
+    if (!world) return VKGV_INVALID_ARG;
+    if (world->block) cudaFree(world->block);
+    delete world;
+    return VKGV_OK;
+}
+
+int vkgv_world_info(const vkgv_world* world, uint32_t* out_transform_count, uint64_t* out_draw_count) {
+    if (!world) return VKGV_INVALID_ARG;
+    if (out_transform_count) *out_transform_count = world->args.slot_count;
+    if (out_draw_count) *out_draw_count = world->draw_count;
+    return VKGV_OK;
+}
+
+int vkgv_world_update_transforms(vkgv_ctx* ctx, vkgv_world* world, float animation_time, uint64_t transform_buffer,
+                                 void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!world) return fail(ctx, VKGV_INVALID_ARG, "world is NULL");
+    if (world->args.slot_count && (!transform_buffer || !aligned16(transform_buffer)))
+        return fail(ctx, VKGV_INVALID_ARG, "transform_buffer must be 16-byte aligned");
+    launch_world_transforms(world->args, animation_time, reinterpret_cast<float*>(transform_buffer),
+                            reinterpret_cast<cudaStream_t>(stream_));
+    return check_launch(ctx);
+}
+
+int vkgv_world_build_draws(vkgv_ctx* ctx, vkgv_world* world, uint64_t draw_buffer, uint64_t capacity,
+                           void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (!world) return fail(ctx, VKGV_INVALID_ARG, "world is NULL");
+    if (capacity < world->draw_count) return fail(ctx, VKGV_LIMIT_EXCEEDED, "draw buffer capacity below the draw count");
+    if (world->draw_count && (!draw_buffer || !aligned16(draw_buffer)))
+        return fail(ctx, VKGV_INVALID_ARG, "draw_buffer must be 16-byte aligned");
+    launch_world_draws(world->args, reinterpret_cast<uint32_t*>(draw_buffer), ctx->sm_count,
+                       reinterpret_cast<cudaStream_t>(stream_));
+    return check_launch(ctx);
 }
 
 }  // extern "C"

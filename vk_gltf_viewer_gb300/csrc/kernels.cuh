@@ -1,7 +1,9 @@
 // Kernel launchers shared between the translation units of libvkgv.
 #pragma once
 
+#include <string>
 #include <utility>
+#include <vector>
 
 #include "common.cuh"
 
@@ -123,5 +125,59 @@ void launch_diff_shade(const DiffArgs& A, const DeviceView* views, uint32_t nvie
                        cudaStream_t stream);
 // Adds the float4 accumulators of A into the caller's gradient arrays.
 void launch_diff_scatter(const DiffArgs& A, cudaStream_t stream);
+
+// ------------------------------------------------------------------ world
+// Device copy of a vkgv_anim_sampler: offsets (in floats) into the pooled
+// keyframe array.
+struct WorldSampler {
+    uint32_t input, output;
+    uint32_t input_count, output_count;
+    uint32_t interpolation, components;
+};
+
+// The node tree's per-frame plan on the device (built once by plan_world).
+struct WorldArgs {
+    const float* rest;              // 10 floats per node: translation, rotation (x, y, z, w), scale
+    const uint32_t* chan_offsets;   // node_count + 1: the node's channels in chans
+    const uint2* chans;             // {sampler, path} in application order
+    const WorldSampler* samplers;
+    const float* keys;              // pooled keyframe times and outputs
+    float* local;                   // scratch: T * R * S per node (16 floats)
+    const uint32_t* chain_offsets;  // slot_count + 1: the slot's path in chain_nodes
+    const uint32_t* chain_nodes;    // root .. node of every transform slot
+    const uint32_t* seg_first;      // seg_count + 1: first draw of each (primitive, slot) segment
+    const uint2* seg_info;          // {primitive, slot} per segment
+    const uint32_t* tile_seg;       // segment of the first draw of every tile of kWorldTile draws
+    uint32_t node_count;
+    uint32_t slot_count;
+    uint32_t seg_count;
+    uint32_t draw_count;
+    uint32_t tile_count;
+};
+
+constexpr uint32_t kWorldTile = 1024;    // draws per k_world_draws block
+constexpr uint32_t kWorldThreads = 256;  // threads per k_world_draws block
+
+// Host tables of the plan (uploaded into one device allocation).
+struct WorldPlan {
+    std::vector<float> rest;
+    std::vector<uint32_t> chan_offsets;
+    std::vector<uint2> chans;
+    std::vector<WorldSampler> samplers;
+    std::vector<float> keys;
+    std::vector<uint32_t> chain_offsets, chain_nodes;
+    std::vector<uint32_t> seg_first;
+    std::vector<uint2> seg_info;
+    std::vector<uint32_t> tile_seg;
+    uint32_t node_count = 0, slot_count = 0, seg_count = 0;
+    uint64_t draw_count = 0;
+};
+
+// Validates a world description and walks its tree; returns a vkgv_status.
+int plan_world(const vkgv_world_desc& desc, WorldPlan& plan, std::string& err);
+// k_world_local + k_world_chain: transforms[16 * slot] at `time`.
+void launch_world_transforms(const WorldArgs& W, float time, float* transforms, cudaStream_t stream);
+// k_world_draws: the MeshletDraw list as 3 words per draw.
+void launch_world_draws(const WorldArgs& W, uint32_t* draws, uint32_t sm_count, cudaStream_t stream);
 
 }  // namespace vkgv

@@ -132,8 +132,8 @@ struct Frag {
     const vkgv_vertex* vx[3];
     const vkgv_material* mat;
     uint32_t transform_index;
-    float c[3][4];
     float l[3];
+    float pos[3];  // the interpolated clip position x, y, w (motion vectors only)
 };
 
 // Loads a 4x4 node-table matrix (16-byte aligned rows of the table).
@@ -146,23 +146,40 @@ __device__ __forceinline__ void load_m4(const float* src, float m[16]) {
     }
 }
 
+// vp * transforms[node] without a node table (the stage entry points); kept
+// out of line so that its registers do not weigh on the table path.
+__device__ __noinline__ void direct_mvp(const float* __restrict__ transforms, const float* vp, uint32_t node,
+                                        float mvp[16]) {
+    const float* Mp = transforms + 16 * (size_t)node;
+    float M[16], VP[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        M[k] = __ldg(Mp + k);
+        VP[k] = vp[k];
+    }
+    m4m(VP, M, mvp);
+}
+
 // vp * transforms[node], from the per-view node table when the frame has one.
+// The out-of-line product writes a separate array, so that `mvp` itself
+// stays in registers on the table path.
 __device__ __forceinline__ void node_mvp(const SceneArgs& S, const float* table, const float* vp, uint32_t node,
                                          float mvp[16]) {
     if (table && node < S.transform_count) {
         load_m4(table + 16 * (size_t)node, mvp);
     } else {
-        const float* Mp = S.transforms + 16 * (size_t)node;
-        float M[16], VP[16];
+        float fb[16];
+        direct_mvp(S.transforms, vp, node, fb);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            M[k] = __ldg(Mp + k);
-            VP[k] = vp[k];
-        }
-        m4m(VP, M, mvp);
+        for (int k = 0; k < 16; ++k) mvp[k] = fb[k];
     }
 }
 
+__device__ __forceinline__ float interp3(const float l[3], float v0, float v1, float v2) {
+    return fadd(fadd(fmul(l[0], v0), fmul(l[1], v1)), fmul(l[2], v2));
+}
+
+template <bool MOTION>
 __device__ void frag_setup(const SceneArgs& S, const DeviceView& V, uint32_t px, uint32_t py, uint32_t id, Frag& f) {
     const uint32_t d = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
     const vkgv_meshlet_draw dr = S.draws[d];
@@ -175,10 +192,11 @@ __device__ void frag_setup(const SceneArgs& S, const DeviceView& V, uint32_t px,
     const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset + 3 * t;
     const uint32_t* vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
     const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
+    float c[3][4];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         f.vx[k] = verts + vidx[tri[k]];
-        m4v(mvp, f.vx[k]->position[0], f.vx[k]->position[1], f.vx[k]->position[2], 1.0f, f.c[k]);
+        m4v(mvp, f.vx[k]->position[0], f.vx[k]->position[1], f.vx[k]->position[2], 1.0f, c[k]);
     }
     // Perspective-correct barycentrics: the clip-space weights whose point
     // projects to the pixel centre are proportional to a x b.
@@ -187,8 +205,8 @@ __device__ void frag_setup(const SceneArgs& S, const DeviceView& V, uint32_t px,
     float a[3], b[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        a[k] = fsub(f.c[k][0], fmul(nx, f.c[k][3]));
-        b[k] = fsub(f.c[k][1], fmul(ny, f.c[k][3]));
+        a[k] = fsub(c[k][0], fmul(nx, c[k][3]));
+        b[k] = fsub(c[k][1], fmul(ny, c[k][3]));
     }
     f.l[0] = fsub(fmul(a[1], b[2]), fmul(a[2], b[1]));
     f.l[1] = fsub(fmul(a[2], b[0]), fmul(a[0], b[2]));
@@ -201,10 +219,11 @@ __device__ void frag_setup(const SceneArgs& S, const DeviceView& V, uint32_t px,
     } else {
         f.l[0] = f.l[1] = f.l[2] = 1.0f / 3.0f;
     }
-}
-
-__device__ __forceinline__ float interp3(const float l[3], float v0, float v1, float v2) {
-    return fadd(fadd(fmul(l[0], v0), fmul(l[1], v1)), fmul(l[2], v2));
+    if (MOTION) {
+        f.pos[0] = interp3(f.l, c[0][0], c[1][0], c[2][0]);
+        f.pos[1] = interp3(f.l, c[0][1], c[1][1], c[2][1]);
+        f.pos[2] = interp3(f.l, c[0][3], c[1][3], c[2][3]);
+    }
 }
 
 // unorm[i] = i / 255 (correctly rounded), a per-block table in shared memory.
@@ -246,31 +265,49 @@ __device__ void shade_textured(const SceneArgs& S, const Frag& f, const float* u
 //   motion = (prev.xy / prev.w * 0.5 - 0.5) - (pos.xy / pos.w * 0.5 - 0.5)
 // M is the node's current transform for both (the reference has no
 // previous-frame transforms).  Written as two RN binary16, x in the low half.
+// Only the x, y and w rows of prevViewProjection * M are needed; each
+// vertex's previous clip position is folded into the interpolation sums
+// ((l0 p0 + l1 p1) + l2 p2) as it is computed, which keeps the variant small
+// enough for six CTAs per SM.
 __device__ uint32_t motion_vector(const SceneArgs& S, const DeviceView& V, const Frag& f) {
-    float pmvp[16];
-    node_mvp(S, V.prev_mvps, V.cam->prev_view_projection, f.transform_index, pmvp);
-    float p[3][4];
+    float rx[4], ry[4], rw[4];  // rows x, y, w of prev_view_projection * M (per column)
+    if (V.prev_mvps && f.transform_index < S.transform_count) {
+        const float4* q = reinterpret_cast<const float4*>(V.prev_mvps + 16 * (size_t)f.transform_index);
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-        m4v(pmvp, f.vx[k]->position[0], f.vx[k]->position[1], f.vx[k]->position[2], 1.0f, p[k]);
-    const float cw = interp3(f.l, f.c[0][3], f.c[1][3], f.c[2][3]);
-    const float pw = interp3(f.l, p[0][3], p[1][3], p[2][3]);
-    uint32_t out = 0;
+        for (int c = 0; c < 4; ++c) {
+            const float4 col = __ldg(q + c);
+            rx[c] = col.x, ry[c] = col.y, rw[c] = col.w;
+        }
+    } else {
+        float pm[16];
+        node_mvp(S, nullptr, V.cam->prev_view_projection, f.transform_index, pm);
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-        const float cj = interp3(f.l, f.c[0][j], f.c[1][j], f.c[2][j]);
-        const float pj = interp3(f.l, p[0][j], p[1][j], p[2][j]);
-        const float cur = fsub(fmul(fdiv(cj, cw), 0.5f), 0.5f);
-        const float prev = fsub(fmul(fdiv(pj, pw), 0.5f), 0.5f);
-        out |= (uint32_t)__half_as_ushort(__float2half_rn(fsub(prev, cur))) << (16 * j);
+        for (int c = 0; c < 4; ++c) rx[c] = pm[4 * c], ry[c] = pm[4 * c + 1], rw[c] = pm[4 * c + 3];
     }
-    return out;
+    float px = 0.0f, py = 0.0f, pw = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float x = f.vx[k]->position[0], y = f.vx[k]->position[1], z = f.vx[k]->position[2];
+        // m4v's order: ((m0 x + m1 y) + m2 z) + m3
+        const float cx = fadd(fadd(fadd(fmul(rx[0], x), fmul(rx[1], y)), fmul(rx[2], z)), fmul(rx[3], 1.0f));
+        const float cy = fadd(fadd(fadd(fmul(ry[0], x), fmul(ry[1], y)), fmul(ry[2], z)), fmul(ry[3], 1.0f));
+        const float cw = fadd(fadd(fadd(fmul(rw[0], x), fmul(rw[1], y)), fmul(rw[2], z)), fmul(rw[3], 1.0f));
+        if (k == 0) {
+            px = fmul(f.l[0], cx), py = fmul(f.l[0], cy), pw = fmul(f.l[0], cw);
+        } else {
+            px = fadd(px, fmul(f.l[k], cx)), py = fadd(py, fmul(f.l[k], cy)), pw = fadd(pw, fmul(f.l[k], cw));
+        }
+    }
+    const float cur_x = fsub(fmul(fdiv(f.pos[0], f.pos[2]), 0.5f), 0.5f);
+    const float cur_y = fsub(fmul(fdiv(f.pos[1], f.pos[2]), 0.5f), 0.5f);
+    const float prev_x = fsub(fmul(fdiv(px, pw), 0.5f), 0.5f);
+    const float prev_y = fsub(fmul(fdiv(py, pw), 0.5f), 0.5f);
+    return (uint32_t)__half_as_ushort(__float2half_rn(fsub(prev_x, cur_x))) |
+           ((uint32_t)__half_as_ushort(__float2half_rn(fsub(prev_y, cur_y))) << 16);
 }
 
-// Six CTAs per SM hold the colour-only variants without spills; the motion
-// variants keep the previous-frame clip positions live as well.
 template <bool TEXTURED, bool MOTION>
-__global__ void __launch_bounds__(256, MOTION ? 4 : 6) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
+__global__ void __launch_bounds__(256, 6) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
     pdl_begin();
     const DeviceView& V = views[blockIdx.y];
     __shared__ float s_unorm[256];
@@ -293,7 +330,7 @@ __global__ void __launch_bounds__(256, MOTION ? 4 : 6) k_resolve(SceneArgs S, co
             float lin[4];
             if (TEXTURED || MOTION) {
                 Frag f;
-                frag_setup(S, V, p % w, p / w, id, f);
+                frag_setup<MOTION>(S, V, p % w, p / w, id, f);
                 if (MOTION) mv = motion_vector(S, V, f);
                 if (TEXTURED) {
                     shade_textured(S, f, s_unorm, lin);
