@@ -367,6 +367,23 @@ def run_world(r, host, local, args, stream, peak):
         "gpu_launches_per_update": 2, "gpu_launches_per_draw_build": 1,
         "device_status": list(status),
     }
+    # the same scene as a .glb (1 primitive, 2,057 nodes, 1,098 channels)
+    # read back through the importer: parse, accessors, meshlets, node tree
+    import tempfile
+
+    from vk_gltf_viewer_gb300 import gltf
+    from vk_gltf_viewer_gb300.gltf_export import write_world
+    with tempfile.TemporaryDirectory() as tmp:
+        path = write_world(Path(tmp) / "grid.glb", [mesh], wh)
+        loads = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            ih, iw = gltf.load(path)
+            loads.append(1000.0 * (time.perf_counter() - t0))
+        out["gltf_import"] = {"ms": statistics.median(loads), "bytes": path.stat().st_size,
+                              "draws": int(ih.draws.shape[0]), "nodes": int(iw.nodes.size),
+                              "note": "host: JSON + GLB parse, accessors, meshlets of the 40k-triangle torus, "
+                                      "node tree, samplers, host draw list"}
     if not args.no_cpu_baseline:
         from oracle import binding as ob
         n_t = n_d = 0

@@ -446,7 +446,7 @@ typedef struct vkgv_anim_sampler {
     uint32_t input_count;
     uint32_t output_count;   /* input_count, or 3 * input_count for CUBICSPLINE */
     uint32_t interpolation;  /* vkgv_anim_interpolation */
-    uint32_t components;     /* 3 (translation, scale) or 4 (rotation) */
+    uint32_t components;     /* 3 (translation, scale), 4 (rotation), 1 (weights, unused) */
 } vkgv_anim_sampler;
 
 /* A channel; channels apply in array order (the reference's animation by
@@ -498,6 +498,56 @@ int vkgv_world_update_transforms(vkgv_ctx* ctx, vkgv_world* world, float animati
  * draw_buffer (16-byte aligned, capacity >= the draw count). */
 int vkgv_world_build_draws(vkgv_ctx* ctx, vkgv_world* world, uint64_t draw_buffer, uint64_t capacity,
                            void* stream);
+
+/* ------------------------------------------------------------ glTF import */
+/* A glTF 2.0 asset (.glb, or .gltf with external or base64 data: buffers)
+ * read into the renderer's layout, as src/vk_gltf_viewer/assets.cpp:288-552
+ * and World::addAsset (world.cpp:9-80) do with fastgltf: POSITION (float or
+ * KHR_mesh_quantization integers), indices (generated when absent), meshlets
+ * of 64 vertices / 124 triangles, material index + 1 (0 = the default
+ * material), baseColorFactor, alphaCutoff, doubleSided, node matrices
+ * decomposed into TRS, the first scene's root nodes, and every animation's
+ * samplers and channels.  COLOR_0 and TEXCOORD_0 are kept when present.
+ * EXT_meshopt_compression is refused (VKGV_INVALID_ARG with a message). */
+typedef struct vkgv_gltf vkgv_gltf;
+
+/* Also store baseColorTexture's texture index and its KHR_texture_transform
+ * in the materials (the reference leaves albedoIndex invalid,
+ * assets.cpp:510-514, and loads no images). */
+#define VKGV_GLTF_TEXTURE_REFERENCES 1u
+
+typedef struct vkgv_gltf_info {
+    uint32_t primitive_count;
+    uint32_t material_count;   /* glTF materials + 1 */
+    uint32_t mesh_count;
+    uint32_t node_count;
+    uint32_t root_count;
+    uint32_t sampler_count;
+    uint32_t channel_count;
+    uint32_t texture_count;
+    uint32_t image_count;
+    uint32_t _pad;
+} vkgv_gltf_info;
+
+typedef struct vkgv_gltf_primitive {
+    struct vkgv_mesh* mesh;    /* meshletised streams, owned by the asset */
+    uint32_t material_index;   /* glTF material + 1, 0 = default (assets.cpp:290-293) */
+    uint32_t mesh_index;       /* the glTF mesh it belongs to */
+    uint32_t meshlet_count;
+    uint32_t _pad;
+} vkgv_gltf_primitive;
+
+/* On failure returns a status and writes a message into error (if given). */
+int vkgv_gltf_load(const char* path, uint32_t flags, vkgv_gltf** out_asset, char* error,
+                   uint32_t error_capacity);
+int vkgv_gltf_get_info(const vkgv_gltf* asset, vkgv_gltf_info* out);
+int vkgv_gltf_get_primitive(const vkgv_gltf* asset, uint32_t index, vkgv_gltf_primitive* out);
+/* Copies material_count materials (index 0 = the glTF default). */
+int vkgv_gltf_get_materials(const vkgv_gltf* asset, vkgv_material* out, uint32_t capacity);
+/* The node tree, meshes and animations as a vkgv_world_desc whose arrays
+ * live until vkgv_gltf_free. */
+int vkgv_gltf_get_world(const vkgv_gltf* asset, vkgv_world_desc* out);
+void vkgv_gltf_free(vkgv_gltf* asset);
 
 /* ---------------------------------------------- host scene producers (A15) */
 /* Replace the glTF import + meshletiser (src/vk_gltf_viewer/assets.cpp:288-430)

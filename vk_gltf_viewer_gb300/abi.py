@@ -177,12 +177,26 @@ class WorldDesc(C.Structure):
                 ("channel_count", C.c_uint32), ("_pad", C.c_uint32)]
 
 
+class GltfInfo(C.Structure):
+    _fields_ = [("primitive_count", C.c_uint32), ("material_count", C.c_uint32), ("mesh_count", C.c_uint32),
+                ("node_count", C.c_uint32), ("root_count", C.c_uint32), ("sampler_count", C.c_uint32),
+                ("channel_count", C.c_uint32), ("texture_count", C.c_uint32), ("image_count", C.c_uint32),
+                ("_pad", C.c_uint32)]
+
+
+class GltfPrimitive(C.Structure):
+    _fields_ = [("mesh", C.c_void_p), ("material_index", C.c_uint32), ("mesh_index", C.c_uint32),
+                ("meshlet_count", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+GLTF_TEXTURE_REFERENCES = 1
 PATH_TRANSLATION, PATH_ROTATION, PATH_SCALE, PATH_WEIGHTS = 1, 2, 3, 4
 INTERP_LINEAR, INTERP_STEP, INTERP_CUBICSPLINE = 0, 1, 2
 MAX_NODE_DEPTH = 64
 
 EXPECTED_SIZES = {"Meshlet": 36, "Vertex": 24, "MeshletDraw": 12, "Primitive": 64, "Material": 48, "Camera": 352,
-                  "Node": 52, "AnimSampler": 32, "AnimChannel": 16, "WorldDesc": 96}
+                  "Node": 52, "AnimSampler": 32, "AnimChannel": 16, "WorldDesc": 96,
+                  "GltfInfo": 40, "GltfPrimitive": 24}
 
 _P = C.c_void_p
 _U32 = C.c_uint32
@@ -228,6 +242,12 @@ _PROTOS = {
     "vkgv_world_info": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U64)]),
     "vkgv_world_update_transforms": (C.c_int, [_P, _P, C.c_float, _U64, _P]),
     "vkgv_world_build_draws": (C.c_int, [_P, _P, _U64, _U64, _P]),
+    "vkgv_gltf_load": (C.c_int, [C.c_char_p, _U32, C.POINTER(_P), C.c_char_p, _U32]),
+    "vkgv_gltf_get_info": (C.c_int, [_P, C.POINTER(GltfInfo)]),
+    "vkgv_gltf_get_primitive": (C.c_int, [_P, _U32, C.POINTER(GltfPrimitive)]),
+    "vkgv_gltf_get_materials": (C.c_int, [_P, _P, _U32]),
+    "vkgv_gltf_get_world": (C.c_int, [_P, C.POINTER(WorldDesc)]),
+    "vkgv_gltf_free": (None, [_P]),
     "vkgv_set_profiling": (C.c_int, [_P, C.c_int32]),
     "vkgv_stage_times": (C.c_int, [_P, C.POINTER(C.c_float), _U32]),
 }

@@ -314,7 +314,7 @@ int plan_world(const vkgv_world_desc& D, WorldPlan& P, std::string& err) {
         const vkgv_anim_sampler& s = D.samplers[i];
         if (s.input_count == 0 || !s.input || !s.output) return bad("sampler without keyframes");
         if (s.interpolation > VKGV_INTERP_CUBICSPLINE) return bad("unknown interpolation");
-        if (s.components != 3 && s.components != 4) return bad("sampler components must be 3 or 4");
+        if (s.components < 1 || s.components > 4) return bad("sampler components must be 1 to 4");
         const uint64_t want = (uint64_t)s.input_count * (s.interpolation == VKGV_INTERP_CUBICSPLINE ? 3u : 1u);
         if (s.output_count != want) return bad("sampler output_count does not match its keyframes");
         const uint64_t total = P.keys.size() + s.input_count + (uint64_t)s.output_count * s.components;

@@ -64,12 +64,15 @@ def _copy(ptr, n: int, dtype) -> np.ndarray:
     return np.frombuffer(raw, dtype=dtype, count=n).copy()
 
 
-def _mesh_from_handle(h, max_vertices: int = 64, max_triangles: int = 124) -> Mesh:
+def _mesh_from_handle(h, max_vertices: int = 64, max_triangles: int = 124, owned: bool = True) -> Mesh:
+    """Copies a mesh handle's streams out.  An owned handle is meshletised
+    here and freed; a borrowed one (an imported asset's) is read as is."""
     lib = abi.load()
     if not h:
         raise abi.VkgvError(abi.INVALID_ARG, "mesh producer failed")
     try:
-        abi.check(lib.vkgv_mesh_build_meshlets(h, max_vertices, max_triangles))
+        if owned:
+            abi.check(lib.vkgv_mesh_build_meshlets(h, max_vertices, max_triangles))
         info = abi.MeshInfo()
         abi.check(lib.vkgv_mesh_get_info(h, C.byref(info)))
         nv, nt = info.vertex_count, info.triangle_count
@@ -89,7 +92,8 @@ def _mesh_from_handle(h, max_vertices: int = 64, max_triangles: int = 124) -> Me
             cones=_copy(C.cast(info.cones, C.c_void_p).value, info.meshlet_count, CONE_DTYPE),
         )
     finally:
-        lib.vkgv_mesh_free(h)
+        if owned:
+            lib.vkgv_mesh_free(h)
 
 
 def icosphere(level: int, displace: float = 0.0, seed: int = 0, rgba: np.ndarray | None = None) -> Mesh:

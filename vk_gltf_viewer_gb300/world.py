@@ -84,6 +84,39 @@ class HostWorld:
     def desc(self) -> abi.WorldDesc:
         return abi.WorldDesc(**self.desc_fields())
 
+    def visits(self) -> list[int]:
+        """Nodes with a mesh in depth-first order from the roots: entry i is
+        the node of transform slot i (World::iterateNode)."""
+        out = []
+        stack = [int(r) for r in self.roots[::-1]]
+        depth_stack = [0] * len(stack)
+        while stack:
+            n, d = stack.pop(), depth_stack.pop()
+            if d >= abi.MAX_NODE_DEPTH:
+                raise ValueError("node tree deeper than 64 (or cyclic)")
+            node = self.nodes[n]
+            if node["mesh_index"] != abi.INVALID_HANDLE:
+                out.append(n)
+            f, c = int(node["first_child"]), int(node["child_count"])
+            kids = [int(x) for x in self.children[f:f + c][::-1]]
+            stack.extend(kids)
+            depth_stack.extend([d + 1] * len(kids))
+        return out
+
+    def draw_list(self) -> np.ndarray:
+        """World::rebuildDrawBuffer on the host: (D, 3) uint32 {primitive,
+        meshlet, transform} (the device builds the same list)."""
+        parts = []
+        for slot, n in enumerate(self.visits()):
+            m = int(self.nodes[n]["mesh_index"])
+            for p in self.mesh_primitives[m]:
+                k = int(self.primitive_meshlet_counts[p])
+                if k:
+                    d = np.empty((k, 3), np.uint32)
+                    d[:, 0], d[:, 1], d[:, 2] = p, np.arange(k, dtype=np.uint32), slot
+                    parts.append(d)
+        return np.ascontiguousarray(np.concatenate(parts)) if parts else np.zeros((0, 3), np.uint32)
+
     @property
     def meshlet_draw_count(self) -> int:
         """Draw count by a host walk of the tree (the plan's own count is
