@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-motion", action="store_true", help="skip the motion-vector frame")
     p.add_argument("--no-world", action="store_true", help="skip the node-tree transform and draw-list leg")
+    p.add_argument("--world-only", action="store_true",
+                   help="run only the node-tree transform and draw-list leg (for profiling); prints its own JSON line")
     p.add_argument("--adjoint-only", action="store_true",
                    help="run only the adjoint legs (for profiling); prints their own JSON line")
     return p.parse_args()
@@ -463,6 +465,14 @@ def main():
         out = run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier)
         if rank == 0:
             print(json.dumps({"metric": METRIC, "batched": out}), flush=True)
+        r.close()
+        return
+    if args.world_only:
+        peaks_path = ROOT / "MEASURED_PEAKS.json"
+        peak = float(json.loads(peaks_path.read_text())["hbm_gbs"]) if peaks_path.exists() else 6800.0
+        out = run_world(r, host, local, args, stream, peak)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "world": out}), flush=True)
         r.close()
         return
     if args.adjoint_only:
