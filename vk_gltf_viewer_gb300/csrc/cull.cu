@@ -14,9 +14,10 @@ namespace vkgv {
 
 namespace {
 
-// Pass-1 corner table of projectAabb (shaders/culling.h.glsl:32-41).
-__constant__ float kCorners[8][3] = {{1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, -1},
-                                     {1, -1, 1},  {1, 1, 1},  {-1, -1, 1}, {-1, 1, 1}};
+// Corner table of projectAabb (shaders/culling.h.glsl:32-41) as sign bits,
+// three per corner (x, y, z; 1 for -1): (1,-1,-1), (1,1,-1), (-1,1,-1),
+// (-1,-1,-1), (1,-1,1), (1,1,1), (-1,-1,1), (-1,1,1).
+constexpr uint32_t kCornerSigns = 0x2c2f66;
 
 // Exact floor(log2(m)) clamped to [0, levels-1]; m <= 0 or NaN -> 0,
 // +inf -> levels-1.
@@ -89,15 +90,36 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
         res.visible = true;
         return res;
     }
-    // projectAabb (culling.h.glsl:44-56)
+    // projectAabb (culling.h.glsl:44-56).  Corner i is (wc +- we) per axis
+    // (the table's +-1 factors are exact), so each row j of occl_vp * corner,
+    // ((m0j x + m1j y) + m2j z) + m3j, is assembled from the two values of
+    // m0j x, m1j y and m2j z: the same rounded operations as transforming
+    // each corner, with the shared products and partial sums formed once.
+    const float ax[2] = {fadd(we[0], wc4[0]), fadd(-we[0], wc4[0])};
+    const float ay[2] = {fadd(we[1], wc4[1]), fadd(-we[1], wc4[1])};
+    const float az[2] = {fadd(we[2], wc4[2]), fadd(-we[2], wc4[2])};
+    float rows[4][2][2][2];  // [j][x sign][y sign][z sign]
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float mx[2] = {fmul(occl_vp[0 * 4 + j], ax[0]), fmul(occl_vp[0 * 4 + j], ax[1])};
+        const float my[2] = {fmul(occl_vp[1 * 4 + j], ay[0]), fmul(occl_vp[1 * 4 + j], ay[1])};
+        const float mz[2] = {fmul(occl_vp[2 * 4 + j], az[0]), fmul(occl_vp[2 * 4 + j], az[1])};
+        const float m3 = fmul(occl_vp[3 * 4 + j], 1.0f);
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                const float xy = fadd(mx[a], my[b]);
+#pragma unroll
+                for (int c = 0; c < 2; ++c) rows[j][a][b][c] = fadd(fadd(xy, mz[c]), m3);
+            }
+    }
     float mn0 = 1.0f, mn1 = 1.0f, mn2 = 1.0f, mx0 = -1.0f, mx1 = -1.0f, mx2 = -1.0f;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        float px = fadd(fmul(kCorners[i][0], we[0]), wc4[0]);
-        float py = fadd(fmul(kCorners[i][1], we[1]), wc4[1]);
-        float pz = fadd(fmul(kCorners[i][2], we[2]), wc4[2]);
-        float clip[4];
-        m4v(occl_vp, px, py, pz, 1.0f, clip);
+        const uint32_t sg = (kCornerSigns >> (3 * i)) & 7u;
+        const int a = (int)(sg & 1u), b = (int)((sg >> 1) & 1u), c = (int)(sg >> 2);
+        const float clip[4] = {rows[0][a][b][c], rows[1][a][b][c], rows[2][a][b][c], rows[3][a][b][c]};
         float ndx = gclamp(fdiv(clip[0], clip[3]), -1.0f, 1.0f);
         float ndy = gclamp(fdiv(clip[1], clip[3]), -1.0f, 1.0f);
         float qx = fadd(fmul(ndx, 0.5f), 0.5f), qy = fadd(fmul(ndy, 0.5f), 0.5f);
