@@ -361,12 +361,14 @@ int check_launch(vkgv_ctx* ctx) {
 // When the scene gives its node count, a whole frame evaluates each node's
 // determinant(M) and each view's view_projection * M once (in the clear
 // kernel) instead of once per meshlet draw (raster) or per pixel (resolve).
-// Motion-vector frames add prev_view_projection * M after each view's table.
+// Motion-vector frames add prev_view_projection * M after each view's table,
+// cone-culled frames the eye in each node's object space (4 floats).
 int attach_node_tables(vkgv_ctx* ctx, Prepared& P, DeviceView* host, uint32_t n, uint32_t flags) {
     const size_t T = P.S.transform_count;
     if (T == 0 || P.S.draw_count == 0) return VKGV_OK;
     const bool motion = (flags & VKGV_WRITE_MOTION) != 0;
-    const size_t stride = (motion ? 32 : 16) * T;
+    const bool eyes = (flags & VKGV_CULL_CONE) && P.S.cone_table;
+    const size_t stride = ((motion ? 32 : 16) + (eyes ? 4 : 0)) * T;
     int rc = ensure_scratch(ctx, ctx->tdet, sizeof(float) * T, "node determinants");
     if (rc) return rc;
     rc = ensure_scratch(ctx, ctx->mvp, sizeof(float) * stride * n, "per-view node matrices");
@@ -377,6 +379,7 @@ int attach_node_tables(vkgv_ctx* ctx, Prepared& P, DeviceView* host, uint32_t n,
     for (uint32_t i = 0; i < n; ++i) {
         host[i].mvps = P.mvps + stride * i;
         host[i].prev_mvps = motion ? P.mvps + stride * i + 16 * T : nullptr;
+        host[i].eyes = eyes ? reinterpret_cast<const float4*>(P.mvps + stride * i + (motion ? 32 : 16) * T) : nullptr;
     }
     return VKGV_OK;
 }

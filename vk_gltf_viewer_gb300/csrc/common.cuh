@@ -58,6 +58,9 @@ struct DeviceView {
     // prev_view_projection * M per node (motion-vector frames only), or null
     const float* prev_mvps;
     uint32_t* motion;           // two binary16 per pixel (x low), or null
+    // per node: the raster eye in the node's object space and 1 (0 for a
+    // singular transform or no eye), for the cone test; filled by the clear
+    const float4* eyes;
 };
 
 struct SceneArgs {
@@ -163,15 +166,23 @@ __device__ __forceinline__ bool eye_from_vp(const float* vp, float e[3]) {
 //   d*c + sqrt(L^2 - d^2)*s < -(r + 1e-3 (L + r)),
 // with L = |eye - center|, d = axis . (eye - center), c the cone cutoff and
 // s = sqrt(1 - c^2).  `M` is the instance transform (column-major).
-__device__ __forceinline__ bool cone_culled(const vkgv_meshlet_cone& cone, const float* M, const float* eye) {
-    const float c = cone.cutoff;
-    if (!(c > 0.0f)) return false;
+// The eye in the object space of instance transform M (Cramer's rule on
+// the upper 3x3); false when that is singular.  It depends on the node and
+// the view only, so whole frames take it from a per-view node table.
+__device__ __forceinline__ bool object_eye(const float* M, const float* eye, float o[3]) {
     const float det = det3(M[0], M[1], M[2], M[4], M[5], M[6], M[8], M[9], M[10]);
     if (!(det != 0.0f)) return false;
     const float vx = fsub(eye[0], M[12]), vy = fsub(eye[1], M[13]), vz = fsub(eye[2], M[14]);
-    const float ox = fdiv(det3(vx, vy, vz, M[4], M[5], M[6], M[8], M[9], M[10]), det);
-    const float oy = fdiv(det3(M[0], M[1], M[2], vx, vy, vz, M[8], M[9], M[10]), det);
-    const float oz = fdiv(det3(M[0], M[1], M[2], M[4], M[5], M[6], vx, vy, vz), det);
+    o[0] = fdiv(det3(vx, vy, vz, M[4], M[5], M[6], M[8], M[9], M[10]), det);
+    o[1] = fdiv(det3(M[0], M[1], M[2], vx, vy, vz, M[8], M[9], M[10]), det);
+    o[2] = fdiv(det3(M[0], M[1], M[2], M[4], M[5], M[6], vx, vy, vz), det);
+    return true;
+}
+
+// The test itself for an object-space eye (ox, oy, oz).
+__device__ __forceinline__ bool cone_culled_at(const vkgv_meshlet_cone& cone, float ox, float oy, float oz) {
+    const float c = cone.cutoff;
+    if (!(c > 0.0f)) return false;
     const float wx = fsub(ox, cone.center[0]), wy = fsub(oy, cone.center[1]), wz = fsub(oz, cone.center[2]);
     const float L2 = fadd(fadd(fmul(wx, wx), fmul(wy, wy)), fmul(wz, wz));
     const float d = fadd(fadd(fmul(cone.axis[0], wx), fmul(cone.axis[1], wy)), fmul(cone.axis[2], wz));
@@ -180,6 +191,13 @@ __device__ __forceinline__ bool cone_culled(const vkgv_meshlet_cone& cone, const
     const float lhs = fadd(fmul(d, c), fmul(perp, s));
     const float margin = fadd(cone.radius, fmul(1e-3f, fadd(__fsqrt_rn(L2), cone.radius)));
     return lhs < -margin;
+}
+
+__device__ __forceinline__ bool cone_culled(const vkgv_meshlet_cone& cone, const float* M, const float* eye) {
+    if (!(cone.cutoff > 0.0f)) return false;
+    float o[3];
+    if (!object_eye(M, eye, o)) return false;
+    return cone_culled_at(cone, o[0], o[1], o[2]);
 }
 
 __host__ __device__ __forceinline__ uint32_t mip_dim(uint32_t base, uint32_t k) {

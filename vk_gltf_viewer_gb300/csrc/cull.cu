@@ -83,8 +83,17 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
     if (!retest && eye && S.cone_table && dr.primitive_index < S.primitive_count &&
         !S.mats[prim->material_index].double_sided) {
         const uint64_t cones = S.cone_table[dr.primitive_index];
-        if (cones && cone_culled(reinterpret_cast<const vkgv_meshlet_cone*>(cones)[dr.meshlet_index], M, eye))
-            return res;
+        if (cones) {
+            const vkgv_meshlet_cone& cone = reinterpret_cast<const vkgv_meshlet_cone*>(cones)[dr.meshlet_index];
+            bool culled;
+            if (V.eyes && dr.transform_index < S.transform_count) {
+                const float4 o = __ldg(V.eyes + dr.transform_index);
+                culled = o.w != 0.0f && cone_culled_at(cone, o.x, o.y, o.z);
+            } else {
+                culled = cone_culled(cone, M, eye);
+            }
+            if (culled) return res;
+        }
     }
     if (!pyr) {
         res.visible = true;

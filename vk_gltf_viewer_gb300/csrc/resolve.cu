@@ -358,15 +358,25 @@ __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ vi
     pdl_begin();
     const DeviceView& V = views[blockIdx.y];
     if (transform_count) {
-        // the view's node tables: view_projection * M, and for motion-vector
-        // frames prev_view_projection * M
+        // the view's node tables: view_projection * M, for motion-vector
+        // frames prev_view_projection * M, and for cone-culled frames the
+        // raster eye in each node's object space
         __shared__ float s_vp[2][16];
+        __shared__ float s_eye[3];
+        __shared__ int s_eye_ok;
         if (threadIdx.x < 16) s_vp[0][threadIdx.x] = V.cam->view_projection[threadIdx.x];
         if (threadIdx.x >= 32 && threadIdx.x < 48)
             s_vp[1][threadIdx.x - 32] = V.cam->prev_view_projection[threadIdx.x - 32];
+        if (threadIdx.x == 64 && V.eyes) {
+            float vp[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) vp[k] = V.cam->view_projection[k];
+            s_eye_ok = eye_from_vp(vp, s_eye);
+        }
         __syncthreads();
         float* out = const_cast<float*>(V.mvps);
         float* prev = const_cast<float*>(V.prev_mvps);
+        float4* eyes = const_cast<float4*>(V.eyes);
         for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < transform_count; i += gridDim.x * blockDim.x) {
             float M[16], r[16];
 #pragma unroll
@@ -380,6 +390,11 @@ __global__ void __launch_bounds__(256) k_clear(const DeviceView* __restrict__ vi
             for (int k = 0; k < 4; ++k)
                 reinterpret_cast<float4*>(out + 16 * (size_t)i)[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2],
                                                                                   r[4 * k + 3]);
+            if (eyes) {
+                float o[3] = {0.0f, 0.0f, 0.0f};
+                const bool ok = s_eye_ok && object_eye(M, s_eye, o);
+                eyes[i] = make_float4(o[0], o[1], o[2], ok ? 1.0f : 0.0f);
+            }
             if (prev) {
                 m4m(s_vp[1], M, r);
 #pragma unroll
