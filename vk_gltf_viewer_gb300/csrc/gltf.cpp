@@ -11,6 +11,7 @@
 #include "vkgv.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -282,14 +283,14 @@ std::vector<uint8_t> read_file(const std::string& path) {
 }
 
 std::vector<uint8_t> base64(const std::string& s, size_t start) {
-    static int8_t table[256];
-    static bool init = false;
-    if (!init) {
-        std::memset(table, -1, sizeof(table));
+    // built once, thread-safely (a function-local static)
+    static const std::array<int8_t, 256> table = [] {
+        std::array<int8_t, 256> t;
+        t.fill(-1);
         const char* a = "ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789+/";
-        for (int i = 0; i < 64; ++i) table[uint8_t(a[i])] = int8_t(i);
-        init = true;
-    }
+        for (int i = 0; i < 64; ++i) t[uint8_t(a[i])] = int8_t(i);
+        return t;
+    }();
     std::vector<uint8_t> out;
     uint32_t acc = 0;
     int bits = 0;

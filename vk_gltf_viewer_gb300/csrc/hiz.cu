@@ -18,6 +18,8 @@
 // than exchanged), keeping levels 1-3 in shared memory and reading the depth
 // image once.  The last CTA of a view to finish computes the remaining top
 // levels from global memory.
+#include <atomic>
+
 #include "kernels.cuh"
 
 namespace vkgv {
@@ -285,10 +287,16 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
 
 void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t* status,
                 cudaStream_t stream) {
-    static bool attr_set = false;
-    if (!attr_set) {
+    // The dynamic shared-memory limit is a per-device function attribute:
+    // set it once for each device a launch runs on (setting it twice is
+    // harmless, so concurrent first launches need no lock).
+    static std::atomic<uint64_t> attr_devices{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (!bit || !(attr_devices.load(std::memory_order_acquire) & bit)) {
         cudaFuncSetAttribute(k_hiz, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemFloats * (int)sizeof(float));
-        attr_set = true;
+        attr_devices.fetch_or(bit, std::memory_order_release);
     }
     dim3 grid(tiles_x ? tiles_x : 1, tiles_y ? tiles_y : 1, nviews);
     launch_pdl(k_hiz, grid, dim3(kThreads), kSmemFloats * sizeof(float), stream, views, status);
