@@ -644,11 +644,16 @@ def main():
         peak, peak_src = float(json.loads(peaks_path.read_text())["hbm_gbs"]), "measured"
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
     traffic = None
+    prof_instr = prof_meshlets = None
     prof = ROOT / "profiles" / "raster_meshlets_c2_1080p.md"
     if prof.exists():
         for line in prof.read_text().splitlines():
             if line.startswith("dram_bytes_per_launch:"):
                 traffic = int(line.split(":")[1].strip())
+            elif line.startswith("warp_instructions_per_launch:"):
+                prof_instr = int(line.split(":")[1].strip())
+            elif line.startswith("meshlets_per_launch:"):
+                prof_meshlets = int(line.split(":")[1].strip())
 
     # ---- batched leg: 256 uneven views in one graph launch
     batched = None
@@ -685,6 +690,19 @@ def main():
         cpu = {"value": n_cpu / tc, "unit": "views/s", "cores": threads, "kind": "port",
                "sample": f"{n_cpu} steady-state frames of the same workload (oracle/oracle.c, {threads} threads)"}
 
+    # The raster is bound by instruction issue, not HBM: its warp
+    # instructions per launch (the ncu count per meshlet, scaled to this
+    # run's survivors) against the SMs' issue rate at the sampled clock.
+    issue = None
+    if dominant == "raster1" and prof_instr and prof_meshlets and dom_ms > 0:
+        csum = clocks.summary()
+        mhz = csum.get("sm_mhz") or 2070.0
+        instr = prof_instr / prof_meshlets * surv
+        peak_issue = 152 * 4 * mhz * 1e6
+        issue = {"warp_instructions": instr, "achieved": instr / (dom_ms / 1000.0), "peak": peak_issue,
+                 "unit": "warp instructions/s", "frac": instr / (dom_ms / 1000.0) / peak_issue,
+                 "note": "152 SMs x 4 schedulers x 1 warp instruction per cycle at the sampled SM clock; "
+                         "instruction count from the ncu capture of profiles/raster_meshlets_c2_1080p.md"}
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
@@ -704,7 +722,8 @@ def main():
                          "cached": tune1["cached"], "table": tune1["table"]},
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                         "algorithmic_bytes": dom_bytes, "kernel_ms": dom_ms},
+                         "algorithmic_bytes": dom_bytes, "kernel_ms": dom_ms,
+                         "issue": issue},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "stages_ms": stages,
