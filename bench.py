@@ -644,7 +644,7 @@ def main():
         peak, peak_src = float(json.loads(peaks_path.read_text())["hbm_gbs"]), "measured"
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
     traffic = None
-    prof_instr = prof_meshlets = None
+    prof_instr = prof_meshlets = prof_atom = prof_atom_busy = prof_ncu_us = None
     prof = ROOT / "profiles" / "raster_meshlets_c2_1080p.md"
     if prof.exists():
         for line in prof.read_text().splitlines():
@@ -654,6 +654,12 @@ def main():
                 prof_instr = int(line.split(":")[1].strip())
             elif line.startswith("meshlets_per_launch:"):
                 prof_meshlets = int(line.split(":")[1].strip())
+            elif line.startswith("atomic_sectors_per_launch:"):
+                prof_atom = int(line.split(":")[1].strip())
+            elif line.startswith("l2_atomic_unit_busy_pct:"):
+                prof_atom_busy = float(line.split(":")[1].strip())
+            elif line.startswith("ncu_duration_us:"):
+                prof_ncu_us = float(line.split(":")[1].strip())
 
     # ---- batched leg: 256 uneven views in one graph launch
     batched = None
@@ -703,6 +709,16 @@ def main():
                  "unit": "warp instructions/s", "frac": instr / (dom_ms / 1000.0) / peak_issue,
                  "note": "152 SMs x 4 schedulers x 1 warp instruction per cycle at the sampled SM clock; "
                          "instruction count from the ncu capture of profiles/raster_meshlets_c2_1080p.md"}
+    # The L2 atomic bound of the same launch: its 64-bit atomicMax count and
+    # the L2 atomic units' busy fraction from the ncu capture, rescaled from
+    # the capture's duration to this run's.
+    atomic = None
+    if dominant == "raster1" and prof_atom and prof_atom_busy is not None and prof_ncu_us and dom_ms > 0:
+        atomic = {"atomics": prof_atom / (prof_meshlets or surv) * surv, "unit": "64-bit atomicMax/s",
+                  "achieved": prof_atom / (prof_meshlets or surv) * surv / (dom_ms / 1000.0),
+                  "frac": prof_atom_busy / 100.0 * prof_ncu_us / (dom_ms * 1000.0),
+                  "note": "L2 atomic-unit busy fraction (lts__d_atomic_input_cycles_active) from the ncu capture "
+                          "of profiles/raster_meshlets_c2_1080p.md, scaled by its duration over this run's"}
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
@@ -723,7 +739,7 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                          "algorithmic_bytes": dom_bytes, "kernel_ms": dom_ms,
-                         "issue": issue},
+                         "issue": issue, "atomic": atomic},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "stages_ms": stages,
