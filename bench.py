@@ -712,6 +712,14 @@ def main():
     # The L2 atomic bound of the same launch: its 64-bit atomicMax count and
     # the L2 atomic units' busy fraction from the ncu capture, rescaled from
     # the capture's duration to this run's.
+    # Whole-frame algorithmic bytes (12 B per draw, 4 B per survivor, the
+    # unique geometry and transforms once, per pixel 8 B clear + 8 B raster
+    # write-back + 8 B HiZ read + 8 B resolve read + 4 B RGBA8 write, and the
+    # pyramid) over the frame time.
+    frame_bytes = (12 * host.draw_count + 4 * surv + g_unique + 64 * host.transforms.shape[0] + 36 * px
+                   + 4 * sum(max(1, (W1080 >> 1) >> k) * max(1, (H1080 >> 1) >> k) for k in range(10)))
+    frame_roof = {"algorithmic_bytes": frame_bytes, "achieved": frame_bytes / (ms_per_step / 1000.0) / 1e9,
+                  "unit": "GB/s", "frac": frame_bytes / (ms_per_step / 1000.0) / 1e9 / peak}
     atomic = None
     if dominant == "raster1" and prof_atom and prof_atom_busy is not None and prof_ncu_us and dom_ms > 0:
         atomic = {"atomics": prof_atom / (prof_meshlets or surv) * surv, "unit": "64-bit atomicMax/s",
@@ -739,7 +747,7 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                          "algorithmic_bytes": dom_bytes, "kernel_ms": dom_ms,
-                         "issue": issue, "atomic": atomic},
+                         "issue": issue, "atomic": atomic, "frame": frame_roof},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "stages_ms": stages,
