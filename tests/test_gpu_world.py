@@ -2,8 +2,8 @@
 bit-identical to the oracle's recursive walk at many animation times, the
 MeshletDraw list bit-identical at the full torus-grid size (2,057 nodes,
 843,776 draws), hand trees with a node reached twice, meshless nodes and
-empty primitives, a frame rendered from the device-built buffers, and the
-argument checks."""
+empty primitives, a frame rendered from the device-built buffers, an animated
+scene through one captured frame graph, and the argument checks."""
 import ctypes as C
 
 import numpy as np
@@ -152,5 +152,46 @@ def test_world_argument_checks(renderer):
         rc = lib.vkgv_world_update_transforms(renderer.ctx, dw.handle, C.c_float(0.0), buf.data_ptr() + 4,
                                               torch.cuda.current_stream().cuda_stream)
         assert rc == abi.INVALID_ARG
+    finally:
+        dw.close()
+
+
+def test_animated_scene_through_a_captured_graph(renderer):
+    """Per-frame animation in batched mode: the world kernels rewrite the
+    transforms between launches of one captured two-view frame graph, and
+    each launch matches the oracle frame at that animation time."""
+    import dataclasses
+
+    from vk_gltf_viewer_gb300.renderer import DeviceScene, ViewBuffers
+
+    base = small_grid()
+    mesh = base.meshes[0]
+    world = grid_world(mesh.meshlet_count, mesh.position_scale, grid=(4, 4, 2))
+    host = dataclasses.replace(base, transforms=ob.world_transforms(world, 0.0), draws=ob.world_draws(world))
+    dev = DeviceScene(host, "cuda")
+    dw = DeviceWorld(renderer, world)
+    centre = scene.grid_centre() * 0.25
+    cams, sizes = [], [(240, 160), (160, 200)]
+    for off in ((7.0, 4.0, 6.0), (-6.0, 3.0, 7.5)):
+        eye = centre + np.array(off)
+        cams.append(scene.camera(tuple(eye), tuple(centre), scene.safe_up(eye, centre), 70.0, 1.5))
+    views = [ViewBuffers.allocate(w, h, c, host.draw_count) for c, (w, h) in zip(cams, sizes)]
+    flags = abi.CULL_FRUSTUM | abi.CULL_CONE | abi.RESOLVE_FLAT | abi.WRITE_IDS
+    try:
+        dw.build_draws(dev.draws)
+        dw.update_transforms(0.0, dev.transforms)
+        g = renderer.capture(dev, views, flags)
+        try:
+            for t in (0.3, 1.7, 2.9):
+                dw.update_transforms(t, dev.transforms)
+                g.launch()
+                torch.cuda.synchronize()
+                osc = ob.OracleScene(dataclasses.replace(host, transforms=ob.world_transforms(world, t)))
+                for v, cam in zip(views, cams):
+                    e = ob.frame(osc, cam, v.width, v.height, oracle_flags(flags))
+                    assert np.array_equal(u32(v.visbuffer), e["ids"]), t
+            assert renderer.device_status() == (0, 0)
+        finally:
+            g.close()
     finally:
         dw.close()
