@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-motion", action="store_true", help="skip the motion-vector frame")
     p.add_argument("--no-world", action="store_true", help="skip the node-tree transform and draw-list leg")
+    p.add_argument("--no-texture", action="store_true", help="skip the texture decode leg")
     p.add_argument("--world-only", action="store_true",
                    help="run only the node-tree transform and draw-list leg (for profiling); prints its own JSON line")
     p.add_argument("--adjoint-only", action="store_true",
@@ -406,6 +407,61 @@ def run_world(r, host, local, args, stream, peak):
     return out
 
 
+def run_texture(r, local, args, stream, peak):
+    """Base-colour texture decode: BC1 and BC3 blocks of an 8192^2 texture
+    into RGBA8 on the device (k_decode_bc), and a 2048^2 RGBA8 PNG on the
+    host (the C2 texture size)."""
+    import zlib
+
+    import numpy as np
+    import torch
+
+    from vk_gltf_viewer_gb300 import abi, texture
+
+    out = {}
+    rng = np.random.default_rng(3)
+    w = h = 8192
+    for name, fmt, bsize in (("bc1", abi.BC1, 8), ("bc3", abi.BC3, 16)):
+        blocks = torch.from_numpy(rng.integers(0, 256, size=(w // 4) * (h // 4) * bsize, dtype=np.uint8)).cuda(local)
+        rgba = torch.empty((h, w, 4), dtype=torch.uint8, device=f"cuda:{local}")
+        lib = abi.load()
+        for _ in range(3):
+            abi.check(lib.vkgv_decode_bc(r.ctx, fmt, blocks.data_ptr(), w, h, rgba.data_ptr(), stream.cuda_stream), r.ctx)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(10):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lib.vkgv_decode_bc(r.ctx, fmt, blocks.data_ptr(), w, h, rgba.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+            ts.append((e0, e1))
+        torch.cuda.synchronize()
+        ms = statistics.median(a.elapsed_time(b) for a, b in ts)
+        nbytes = blocks.numel() + rgba.numel()
+        gbs = nbytes / (ms / 1000.0) / 1e9
+        out[name + "_8192"] = {"ms": ms, "bytes": nbytes, "achieved_gbs": gbs, "frac": gbs / peak,
+                               "texels_per_s": w * h / (ms / 1000.0)}
+        del blocks, rgba
+    # a 2048^2 RGBA8 PNG (dynamic DEFLATE, Paeth-filtered rows) on the host
+    px = rng.integers(0, 256, size=(2048, 2048, 4), dtype=np.uint8)
+    px[:, 1::2] = px[:, ::2]  # some redundancy for the compressor
+    raw = bytearray()
+    for row in px:
+        raw += b"\x00" + row.tobytes()
+    import struct
+    def chunk(kind, data):
+        return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+    png = (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", 2048, 2048, 8, 6, 0, 0, 0))
+           + chunk(b"IDAT", zlib.compress(bytes(raw), 6)) + chunk(b"IEND", b""))
+    t0 = time.perf_counter()
+    img = texture.decode_png(png)
+    png_ms = 1000.0 * (time.perf_counter() - t0)
+    assert img.shape == (2048, 2048, 4)
+    out["png_2048_host_ms"] = png_ms
+    out["png_bytes"] = len(png)
+    return out
+
+
 def run_adjoint(r, local, args, stream):
     """Adjoint legs: the 64-view 512^2 icosphere-5 case and the batched
     512-view uneven-resolution icosphere-8 case (one graph per step)."""
@@ -672,6 +728,11 @@ def main():
     if not args.no_world:
         tree = run_world(r, host, local, args, stream, peak)
 
+    # ---- texture decode (device BC blocks, host PNG)
+    tex = None
+    if not args.no_texture:
+        tex = run_texture(r, local, args, stream, peak)
+
     # ---- adjoint legs (ms/view)
     adjoint = None
     if not args.no_adjoint:
@@ -762,6 +823,8 @@ def main():
             out["motion"] = motion
         if tree:
             out["world"] = tree
+        if tex:
+            out["texture"] = tex
         print(json.dumps(out), flush=True)
     if pg:
         pg.destroy_process_group()

@@ -515,6 +515,25 @@ typedef struct vkgv_gltf vkgv_gltf;
  * in the materials (the reference leaves albedoIndex invalid,
  * assets.cpp:510-514, and loads no images). */
 #define VKGV_GLTF_TEXTURE_REFERENCES 1u
+/* Also read every texture's encoded image (a file, a data URI or a
+ * bufferView; the MSFT_texture_dds source when present) for
+ * vkgv_gltf_get_texture_image. */
+#define VKGV_GLTF_IMAGES 2u
+
+enum vkgv_image_kind {
+    VKGV_IMAGE_UNKNOWN = 0,
+    VKGV_IMAGE_PNG = 1,
+    VKGV_IMAGE_DDS = 2,
+    VKGV_IMAGE_JPEG = 3,
+    VKGV_IMAGE_KTX2 = 4
+};
+
+typedef struct vkgv_gltf_image {
+    const uint8_t* data;   /* encoded bytes, owned by the asset (NULL: none) */
+    uint64_t size;
+    uint32_t kind;         /* vkgv_image_kind, from the magic bytes */
+    uint32_t _pad;
+} vkgv_gltf_image;
 
 typedef struct vkgv_gltf_info {
     uint32_t primitive_count;
@@ -547,7 +566,53 @@ int vkgv_gltf_get_materials(const vkgv_gltf* asset, vkgv_material* out, uint32_t
 /* The node tree, meshes and animations as a vkgv_world_desc whose arrays
  * live until vkgv_gltf_free. */
 int vkgv_gltf_get_world(const vkgv_gltf* asset, vkgv_world_desc* out);
+/* The encoded image of texture `texture` (loaded with VKGV_GLTF_IMAGES). */
+int vkgv_gltf_get_texture_image(const vkgv_gltf* asset, uint32_t texture, vkgv_gltf_image* out);
 void vkgv_gltf_free(vkgv_gltf* asset);
+
+/* -------------------------------------------------------- texture decode */
+/* Base-colour images for the textured resolve.  The reference's image
+ * loading is an empty task (src/vk_gltf_viewer/assets.cpp:467-471); these
+ * decode the published formats: PNG on the host (own DEFLATE), and the
+ * block-compressed formats of DDS files (MSFT_texture_dds) on the device. */
+typedef struct vkgv_image vkgv_image;
+
+/* PNG (all colour types and bit depths, Adam7, tRNS) -> RGBA8 on the host;
+ * 16-bit samples keep their high byte.  On failure a message goes to
+ * error (if given). */
+int vkgv_image_decode_png(const void* data, uint64_t size, vkgv_image** out_image, char* error,
+                          uint32_t error_capacity);
+/* Size and RGBA8 pixels (row-major, R in the low byte) of a decoded image. */
+int vkgv_image_get(const vkgv_image* image, uint32_t* width, uint32_t* height, const uint8_t** rgba);
+void vkgv_image_free(vkgv_image* image);
+
+enum vkgv_block_format {
+    VKGV_BC1 = 1,   /* DXT1: RGB565 pair + 2-bit indices (1-bit alpha when c0 <= c1) */
+    VKGV_BC2 = 2,   /* DXT3: explicit 4-bit alpha + BC1 colours                      */
+    VKGV_BC3 = 3,   /* DXT5: interpolated alpha + BC1 colours                        */
+    VKGV_BC4 = 4,   /* one interpolated channel (R)                                  */
+    VKGV_BC5 = 5    /* two interpolated channels (R, G)                              */
+};
+
+typedef struct vkgv_dds_info {
+    uint32_t width;
+    uint32_t height;
+    uint32_t mip_count;
+    uint32_t format;         /* vkgv_block_format */
+    uint32_t srgb;           /* DXGI *_UNORM_SRGB */
+    uint32_t _pad;
+    uint64_t data_offset;    /* byte offset of the top mip's blocks */
+    uint64_t data_size;      /* bytes of the top mip */
+} vkgv_dds_info;
+
+/* Reads a DDS header (FourCC DXT1-5 / ATI1 / ATI2 / BC4U / BC5U, or DX10
+ * with a BC1-BC5 DXGI format); VKGV_INVALID_ARG for anything else. */
+int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* out);
+/* Decodes width x height texels of BC blocks (device, row-major blocks of
+ * 8 or 16 bytes, aligned to the block size) into RGBA8 (device
+ * uint32[width * height], 4-byte aligned). */
+int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
+                   uint64_t rgba_out, void* stream);
 
 /* ---------------------------------------------- host scene producers (A15) */
 /* Replace the glTF import + meshletiser (src/vk_gltf_viewer/assets.cpp:288-430)

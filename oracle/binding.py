@@ -103,6 +103,7 @@ def load() -> C.CDLL:
         lib.orc_sin_series.argtypes = [C.c_float]
         lib.orc_asin_series.restype = C.c_float
         lib.orc_asin_series.argtypes = [C.c_float]
+        lib.orc_decode_bc.argtypes = [U32, P, U32, U32, P]
         lib.orc_half_rn.restype = C.c_uint16
         lib.orc_half_rn.argtypes = [C.c_float]
         lib.orc_from_linear.restype = C.c_float
@@ -401,3 +402,14 @@ def sin_series(x: float) -> float:
 
 def asin_series(z: float) -> float:
     return float(load().orc_asin_series(z))
+
+
+def decode_bc(fmt: int, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
+    """BC1-BC5 blocks -> uint32 RGBA8 texels (h, w)."""
+    blocks = np.ascontiguousarray(blocks, np.uint8)
+    need = ((w + 3) // 4) * ((h + 3) // 4) * (8 if fmt in (1, 4) else 16)
+    if blocks.size < need:
+        raise ValueError(f"{blocks.size} block bytes, {need} needed")
+    out = np.zeros(w * h, np.uint32)
+    load().orc_decode_bc(fmt, _addr(blocks), w, h, _addr(out))
+    return out.reshape(h, w)

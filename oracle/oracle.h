@@ -227,6 +227,11 @@ void orc_trs_matrix(const float t[3], const float q[4], const float s[3], float 
 float orc_sin_series(float x);
 float orc_asin_series(float z);
 
+/* ---------------------------------------------------------- texture.c */
+/* BC1-BC5 blocks (format 1..5, row-major blocks of 8 or 16 bytes) into
+ * RGBA8 texels (R in the low byte). */
+void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t h, uint32_t* rgba);
+
 /* Single-fragment helpers exported for the known-answer tests. */
 float orc_from_linear(float c);
 float orc_to_linear(float c);

@@ -38,10 +38,11 @@ def test_c_layout_matches_ctypes(tmp_path):
         "vkgv_config": abi.Config, "vkgv_mesh_info": abi.MeshInfo, "vkgv_meshlet_cone": abi.MeshletCone,
         "vkgv_node": abi.Node, "vkgv_anim_sampler": abi.AnimSampler, "vkgv_anim_channel": abi.AnimChannel,
         "vkgv_world_desc": abi.WorldDesc, "vkgv_gltf_info": abi.GltfInfo, "vkgv_gltf_primitive": abi.GltfPrimitive,
+        "vkgv_gltf_image": abi.GltfImage, "vkgv_dds_info": abi.DdsInfo,
     }
     lines = []
     for cname, cls in structs.items():
-        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        lines.append(f'printf("{cname} @sizeof %zu\\n", sizeof({cname}));')
         for f in cls._fields_:
             lines.append(f'printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
     src = tmp_path / "probe.c"
@@ -62,7 +63,7 @@ def test_c_layout_matches_ctypes(tmp_path):
             parts = line.split()
             got[(parts[0], parts[1])] = int(parts[2])
     for cname, cls in structs.items():
-        assert got[(cname, "size")] == C.sizeof(cls), cname
+        assert got[(cname, "@sizeof")] == C.sizeof(cls), cname
         for f in cls._fields_:
             assert got[(cname, f[0])] == getattr(cls, f[0]).offset, (cname, f[0])
 

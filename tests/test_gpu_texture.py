@@ -1,0 +1,101 @@
+"""Block-compressed textures decoded on the device (k_decode_bc) are
+bit-identical to the oracle's decoder for BC1-BC5 at block-aligned and ragged
+sizes, and a glTF asset whose base colour comes from an embedded DDS
+(MSFT_texture_dds) and PNG renders, textured, like the oracle frame of the
+same decoded images."""
+import dataclasses
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import binding as ob
+from vk_gltf_viewer_gb300 import abi, gltf, scene, texture
+from vk_gltf_viewer_gb300.gltf_export import Builder
+from vk_gltf_viewer_gb300.renderer import ViewBuffers
+from vk_gltf_viewer_gb300.world import grid_world
+
+from gpu_util import oracle_flags, rgba_close, small_grid, u32, u64
+from png_util import encode
+from test_texture_decode import _dds
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("fmt", [abi.BC1, abi.BC2, abi.BC3, abi.BC4, abi.BC5])
+@pytest.mark.parametrize("size", [(4, 4), (37, 21), (256, 128), (3, 5)])
+def test_bc_decode_matches_oracle(renderer, fmt, size):
+    w, h = size
+    rng = np.random.default_rng(fmt * 1000 + w)
+    bsize = 8 if fmt in (abi.BC1, abi.BC4) else 16
+    blocks = rng.integers(0, 256, size=((w + 3) // 4) * ((h + 3) // 4) * bsize, dtype=np.uint8)
+    if fmt in (abi.BC1, abi.BC4):  # both orders of the two end points
+        blocks[::16] = np.minimum(blocks[::16], 127)
+    got = texture.decode_bc(renderer, fmt, blocks, w, h)
+    torch.cuda.synchronize()
+    exp = ob.decode_bc(fmt, blocks, w, h)
+    assert np.array_equal(got.cpu().numpy().reshape(h, w, 4).view(np.uint32)[..., 0], exp)
+
+
+def test_gltf_with_dds_and_png_textures(renderer, tmp_path):
+    base = small_grid()
+    mesh = base.meshes[0]
+    world = grid_world(mesh.meshlet_count, mesh.position_scale, grid=(4, 4, 2), animated=False)
+    rng = np.random.default_rng(5)
+    b = Builder()
+    pos = b.accessor(mesh.positions.astype(np.float32))
+    uv = b.accessor(mesh.uvs.astype(np.float32))
+    idx = b.accessor(mesh.indices.reshape(-1).astype(np.uint32))
+    for material in (0, 1):  # mesh 0 uses the DDS texture, mesh 1 the PNG one
+        b.add("meshes", {"primitives": [{"attributes": {"POSITION": pos, "TEXCOORD_0": uv}, "indices": idx,
+                                         "material": material}]})
+    dds_blocks = rng.integers(0, 256, size=16 * 16 * 16, dtype=np.uint8)  # 64 x 64 texels of BC3
+    dds = _dds(b"DXT5", 64, 64, dds_blocks.tobytes())
+    png_pixels = rng.integers(0, 256, size=(32, 48, 4))
+    png = encode(png_pixels, 6, 8, rng)
+    img_dds = b.add("images", {"bufferView": b._view(dds), "mimeType": "image/vnd-ms.dds"})
+    img_png = b.add("images", {"bufferView": b._view(png), "mimeType": "image/png"})
+    b.add("textures", {"source": img_png, "extensions": {"MSFT_texture_dds": {"source": img_dds}}})
+    b.add("textures", {"source": img_png})
+    xf = {"KHR_texture_transform": {"scale": [4.0, 4.0]}}
+    b.add("materials", {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0, "extensions": xf}}})
+    b.add("materials", {"pbrMetallicRoughness": {"baseColorTexture": {"index": 1, "extensions": xf}}})
+    for k, n in enumerate(world.nodes):
+        node = {"translation": [float(x) for x in n["translation"]], "rotation": [float(x) for x in n["rotation"]],
+                "scale": [float(x) for x in n["scale"]]}
+        if n["mesh_index"] != abi.INVALID_HANDLE:
+            node["mesh"] = k % 2
+        f, c = int(n["first_child"]), int(n["child_count"])
+        if c:
+            node["children"] = [int(x) for x in world.children[f:f + c]]
+        b.add("nodes", node)
+    b.gltf["scenes"] = [{"nodes": [int(r) for r in world.roots]}]
+    path = b.write_glb(tmp_path / "textured.glb")
+
+    host, iworld = gltf.load(path, images=True, renderer=renderer)
+    assert len(host.textures) == 2
+    assert np.array_equal(host.textures[0].data.reshape(64, 64, 4).view(np.uint32)[..., 0],
+                          ob.decode_bc(abi.BC3, dds_blocks, 64, 64))
+    assert np.array_equal(host.textures[1].data, png_pixels.astype(np.uint8))
+    assert host.materials[1]["albedo_index"] == 0 and host.materials[2]["albedo_index"] == 1
+    dev, dw = gltf.device_scene(renderer, host, iworld)
+    try:
+        ohost = dataclasses.replace(host, transforms=ob.world_transforms(iworld, 0.0), draws=ob.world_draws(iworld))
+        osc = ob.OracleScene(ohost)
+        centre = scene.grid_centre() * 0.25
+        eye = centre + np.array([6.0, 5.0, 7.0])
+        cam = scene.camera(tuple(eye), tuple(centre), scene.safe_up(eye, centre), 70.0, 1.6)
+        flags = abi.CULL_FRUSTUM | abi.RESOLVE_TEXTURED | abi.WRITE_IDS
+        v = ViewBuffers.allocate(320, 200, cam, host.draw_count)
+        renderer.frame(dev, [v], flags)
+        torch.cuda.synchronize()
+        e = ob.frame(osc, cam, 320, 200, oracle_flags(flags))
+        assert (u64(v.depth_id) != 0).sum() > 2000
+        assert np.array_equal(u32(v.visbuffer), e["ids"])
+        ok, bad = rgba_close(u32(v.color), e["rgba"])
+        assert ok, bad
+        # both primitives (DDS and PNG materials) are on screen
+        prims = {int(host.draws[i >> 7][0]) for i in np.unique(u32(v.visbuffer)) if i != 0xFFFFFFFF}
+        assert prims == {0, 1}
+    finally:
+        dw.close()

@@ -189,14 +189,26 @@ class GltfPrimitive(C.Structure):
                 ("meshlet_count", C.c_uint32), ("_pad", C.c_uint32)]
 
 
+class GltfImage(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("size", C.c_uint64), ("kind", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class DdsInfo(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("mip_count", C.c_uint32), ("format", C.c_uint32),
+                ("srgb", C.c_uint32), ("_pad", C.c_uint32), ("data_offset", C.c_uint64), ("data_size", C.c_uint64)]
+
+
 GLTF_TEXTURE_REFERENCES = 1
+GLTF_IMAGES = 2
+IMAGE_UNKNOWN, IMAGE_PNG, IMAGE_DDS, IMAGE_JPEG, IMAGE_KTX2 = 0, 1, 2, 3, 4
+BC1, BC2, BC3, BC4, BC5 = 1, 2, 3, 4, 5
 PATH_TRANSLATION, PATH_ROTATION, PATH_SCALE, PATH_WEIGHTS = 1, 2, 3, 4
 INTERP_LINEAR, INTERP_STEP, INTERP_CUBICSPLINE = 0, 1, 2
 MAX_NODE_DEPTH = 64
 
 EXPECTED_SIZES = {"Meshlet": 36, "Vertex": 24, "MeshletDraw": 12, "Primitive": 64, "Material": 48, "Camera": 352,
                   "Node": 52, "AnimSampler": 32, "AnimChannel": 16, "WorldDesc": 96,
-                  "GltfInfo": 40, "GltfPrimitive": 24}
+                  "GltfInfo": 40, "GltfPrimitive": 24, "GltfImage": 24, "DdsInfo": 40}
 
 _P = C.c_void_p
 _U32 = C.c_uint32
@@ -247,7 +259,13 @@ _PROTOS = {
     "vkgv_gltf_get_primitive": (C.c_int, [_P, _U32, C.POINTER(GltfPrimitive)]),
     "vkgv_gltf_get_materials": (C.c_int, [_P, _P, _U32]),
     "vkgv_gltf_get_world": (C.c_int, [_P, C.POINTER(WorldDesc)]),
+    "vkgv_gltf_get_texture_image": (C.c_int, [_P, _U32, C.POINTER(GltfImage)]),
     "vkgv_gltf_free": (None, [_P]),
+    "vkgv_image_decode_png": (C.c_int, [_P, _U64, C.POINTER(_P), C.c_char_p, _U32]),
+    "vkgv_image_get": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_P)]),
+    "vkgv_image_free": (None, [_P]),
+    "vkgv_dds_parse": (C.c_int, [_P, _U64, C.POINTER(DdsInfo)]),
+    "vkgv_decode_bc": (C.c_int, [_P, _U32, _U64, _U32, _U32, _U64, _P]),
     "vkgv_set_profiling": (C.c_int, [_P, C.c_int32]),
     "vkgv_stage_times": (C.c_int, [_P, C.POINTER(C.c_float), _U32]),
 }

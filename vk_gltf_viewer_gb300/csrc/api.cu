@@ -673,6 +673,20 @@ int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, 
 }
 
 
+int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
+                   uint64_t rgba_out, void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (format < VKGV_BC1 || format > VKGV_BC5) return fail(ctx, VKGV_INVALID_ARG, "unknown block format");
+    if (width == 0 || height == 0) return VKGV_OK;
+    if (width > 16384 || height > 16384) return fail(ctx, VKGV_LIMIT_EXCEEDED, "texture edge exceeds 16384");
+    const uint64_t block_align = (format == VKGV_BC1 || format == VKGV_BC4) ? 8u : 16u;
+    if (!blocks || !rgba_out || (blocks & (block_align - 1)) || (rgba_out & 3u))
+        return fail(ctx, VKGV_INVALID_ARG, "blocks must be aligned to the block size and rgba_out to 4 bytes");
+    launch_decode_bc(reinterpret_cast<const uint8_t*>(blocks), format, width, height,
+                     reinterpret_cast<uint32_t*>(rgba_out), reinterpret_cast<cudaStream_t>(stream_));
+    return check_launch(ctx);
+}
+
 int vkgv_world_create(vkgv_ctx* ctx, const vkgv_world_desc* desc, vkgv_world** out_world) {
     if (!ctx) return VKGV_INVALID_ARG;
     if (!desc || !out_world) return fail(ctx, VKGV_INVALID_ARG, "desc and out_world must be non-NULL");

@@ -588,6 +588,7 @@ struct vkgv_gltf {
     std::vector<vkgv_anim_sampler> samplers;
     std::vector<vkgv_anim_channel> channels;
     uint32_t texture_count = 0, image_count = 0;
+    std::vector<std::vector<uint8_t>> texture_images;  // per texture (VKGV_GLTF_IMAGES), may be empty
 
     ~vkgv_gltf() {
         for (vkgv_mesh* m : meshes) vkgv_mesh_free(m);
@@ -615,7 +616,33 @@ void check_asset(const JValue& root) {
     }
 }
 
-void import_asset(vkgv_gltf& G, const JValue& root, std::vector<std::vector<uint8_t>>& buffers, uint32_t flags) {
+// The encoded bytes of a glTF image: a base64 data URI, a file next to the
+// asset, or a bufferView.
+std::vector<uint8_t> image_bytes(const JValue& img, const JValue& root, const std::vector<std::vector<uint8_t>>& buffers,
+                                 const std::string& dir) {
+    if (const JValue* uri = img.get("uri")) {
+        if (uri->kind != JValue::String) fail("image.uri must be a string");
+        if (uri->s.rfind("data:", 0) == 0) {
+            const size_t comma = uri->s.find(',');
+            if (comma == std::string::npos || uri->s.find(";base64") == std::string::npos)
+                fail("only base64 data URIs are supported");
+            return base64(uri->s, comma + 1);
+        }
+        return read_file(dir + percent_decode(uri->s));
+    }
+    const int64_t bv = index_of(img, "bufferView");
+    const JValue& views = array_of(root, "bufferViews");
+    if (bv < 0 || size_t(bv) >= views.items.size()) fail("image without uri or a valid bufferView");
+    const JValue& v = views.items[size_t(bv)];
+    const int64_t b = index_of(v, "buffer"), off = index_of(v, "byteOffset", 0), len = index_of(v, "byteLength");
+    if (b < 0 || size_t(b) >= buffers.size() || len < 0 || size_t(off + len) > buffers[size_t(b)].size())
+        fail("image bufferView out of range");
+    const uint8_t* base = buffers[size_t(b)].data() + off;
+    return std::vector<uint8_t>(base, base + len);
+}
+
+void import_asset(vkgv_gltf& G, const JValue& root, std::vector<std::vector<uint8_t>>& buffers, uint32_t flags,
+                  const std::string& dir) {
     Reader R(root, buffers);
 
     // primitives (assets.cpp:288-430): positions, indices (generated when
@@ -713,6 +740,21 @@ void import_asset(vkgv_gltf& G, const JValue& root, std::vector<std::vector<uint
     }
     G.texture_count = uint32_t(array_of(root, "textures").items.size());
     G.image_count = uint32_t(array_of(root, "images").items.size());
+    if (flags & VKGV_GLTF_IMAGES) {
+        // each texture's image; a MSFT_texture_dds source takes precedence
+        const JValue& images = array_of(root, "images");
+        const JValue& textures = array_of(root, "textures");
+        G.texture_images.assign(textures.items.size(), std::vector<uint8_t>());
+        for (size_t t = 0; t < textures.items.size(); ++t) {
+            const JValue& tx = textures.items[t];
+            int64_t src = index_of(tx, "source");
+            if (const JValue* ext = tx.get("extensions"))
+                if (const JValue* dds = ext->get("MSFT_texture_dds")) src = index_of(*dds, "source", src);
+            if (src < 0) continue;
+            if (size_t(src) >= images.items.size()) fail("texture source out of range");
+            G.texture_images[t] = image_bytes(images.items[size_t(src)], root, buffers, dir);
+        }
+    }
 
     // nodes (DecomposeNodeMatrices) and the first scene's roots
     // (world.cpp:55-76: scenes.front().nodeIndices)
@@ -881,7 +923,7 @@ extern "C" int vkgv_gltf_load(const char* path, uint32_t flags, vkgv_gltf** out,
             data.resize(length);
             buffers.push_back(std::move(data));
         }
-        import_asset(*G, root, buffers, flags);
+        import_asset(*G, root, buffers, flags, dir);
     } catch (const ImportError& e) {
         put_error(error, error_capacity, e.msg);
         delete G;
@@ -944,6 +986,23 @@ extern "C" int vkgv_gltf_get_world(const vkgv_gltf* g, vkgv_world_desc* out) {
     out->sampler_count = uint32_t(g->samplers.size());
     out->channels = g->channels.data();
     out->channel_count = uint32_t(g->channels.size());
+    return VKGV_OK;
+}
+
+extern "C" int vkgv_gltf_get_texture_image(const vkgv_gltf* g, uint32_t texture, vkgv_gltf_image* out) {
+    if (!g || !out) return VKGV_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    if (texture >= g->texture_images.size()) return VKGV_INVALID_ARG;
+    const std::vector<uint8_t>& d = g->texture_images[texture];
+    out->data = d.empty() ? nullptr : d.data();
+    out->size = d.size();
+    static const uint8_t png[8] = {137, 80, 78, 71, 13, 10, 26, 10};
+    static const uint8_t ktx2[8] = {0xAB, 0x4B, 0x54, 0x58, 0x20, 0x32, 0x30, 0xBB};
+    if (d.size() >= 8 && !std::memcmp(d.data(), png, 8)) out->kind = VKGV_IMAGE_PNG;
+    else if (d.size() >= 4 && !std::memcmp(d.data(), "DDS ", 4)) out->kind = VKGV_IMAGE_DDS;
+    else if (d.size() >= 3 && d[0] == 0xFF && d[1] == 0xD8 && d[2] == 0xFF) out->kind = VKGV_IMAGE_JPEG;
+    else if (d.size() >= 8 && !std::memcmp(d.data(), ktx2, 8)) out->kind = VKGV_IMAGE_KTX2;
+    else out->kind = VKGV_IMAGE_UNKNOWN;
     return VKGV_OK;
 }
 

@@ -180,4 +180,8 @@ void launch_world_transforms(const WorldArgs& W, float time, float* transforms, 
 // k_world_draws: the MeshletDraw list as 3 words per draw.
 void launch_world_draws(const WorldArgs& W, uint32_t* draws, uint32_t sm_count, cudaStream_t stream);
 
+// k_decode_bc: BC1-BC5 blocks -> RGBA8, one thread per texel.
+void launch_decode_bc(const uint8_t* blocks, uint32_t format, uint32_t w, uint32_t h, uint32_t* rgba,
+                      cudaStream_t stream);
+
 }  // namespace vkgv

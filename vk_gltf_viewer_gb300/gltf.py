@@ -18,12 +18,17 @@ from . import abi, scene
 from .world import NODE_DTYPE, DeviceWorld, HostWorld, Sampler
 
 
-def load(path, texture_references: bool = False) -> tuple[scene.HostScene, HostWorld]:
+def load(path, texture_references: bool = False, images: bool = False,
+         renderer=None) -> tuple[scene.HostScene, HostWorld]:
+    """With `images`, the base-colour textures are decoded too (PNG on the
+    host, DDS block formats on the renderer's device) into the scene's
+    texture table, indexed like the glTF textures, and the materials keep
+    their texture references."""
     lib = abi.load()
     h = C.c_void_p()
     err = C.create_string_buffer(512)
-    rc = lib.vkgv_gltf_load(str(Path(path)).encode(), abi.GLTF_TEXTURE_REFERENCES if texture_references else 0,
-                            C.byref(h), err, len(err))
+    flags = (abi.GLTF_TEXTURE_REFERENCES if (texture_references or images) else 0) | (abi.GLTF_IMAGES if images else 0)
+    rc = lib.vkgv_gltf_load(str(Path(path)).encode(), flags, C.byref(h), err, len(err))
     if rc != abi.OK:
         raise abi.VkgvError(rc, err.value.decode(errors="replace"))
     try:
@@ -41,13 +46,24 @@ def load(path, texture_references: bool = False) -> tuple[scene.HostScene, HostW
         d = abi.WorldDesc()
         abi.check(lib.vkgv_gltf_get_world(h, C.byref(d)))
         world = _world_from_desc(d)
+        textures = []
+        if images:
+            from . import texture
+            for t in range(info.texture_count):
+                gi = abi.GltfImage()
+                abi.check(lib.vkgv_gltf_get_texture_image(h, t, C.byref(gi)))
+                if not gi.data:
+                    rgba = np.full((1, 1, 4), 255, np.uint8)  # a texture without an image samples white
+                else:
+                    rgba = texture.load_image(C.string_at(gi.data, gi.size), gi.kind, renderer)
+                textures.append(scene.Texture(np.ascontiguousarray(rgba), abi.TEXTURE_RGBA8))
     finally:
         lib.vkgv_gltf_free(h)
     draws = world.draw_list()
     t = len(world.visits())
     transforms = np.tile(scene.to_column_major(np.eye(4)), (max(t, 0), 1)).reshape(t, 16)
     host = scene.HostScene(meshes=meshes, prim_materials=prim_materials, materials=mats, transforms=transforms,
-                           node_meshes=[], draws=draws)
+                           node_meshes=[], draws=draws, textures=textures)
     return host, world
 
 
