@@ -132,9 +132,25 @@ struct Frag {
     const vkgv_vertex* vx[3];
     const vkgv_material* mat;
     uint32_t transform_index;
+    uint32_t color[3];  // the vertices' RGBA8 (textured resolve only)
+    uint32_t uv[3];     // the vertices' two binary16 UVs, u in the low half (textured resolve only)
     float l[3];
     float pos[3];  // the interpolated clip position x, y, w (motion vectors only)
 };
+
+// A 24-byte vertex record read as three 8-byte words: (x, y), (z, colour),
+// (normal + pad, uv).  Vertex buffers are 8-byte aligned (the raster reads
+// positions as float2 too).
+__device__ __forceinline__ void load_vertex(const vkgv_vertex* v, bool full, float& x, float& y, float& z,
+                                            uint32_t& color, uint32_t& uv) {
+    const uint2* r = reinterpret_cast<const uint2*>(v);
+    const uint2 a = __ldg(r), b = __ldg(r + 1);
+    x = __uint_as_float(a.x);
+    y = __uint_as_float(a.y);
+    z = __uint_as_float(b.x);
+    color = b.y;
+    uv = full ? __ldg(r + 2).y : 0u;
+}
 
 // Loads a 4x4 node-table matrix (16-byte aligned rows of the table).
 __device__ __forceinline__ void load_m4(const float* src, float m[16]) {
@@ -179,7 +195,7 @@ __device__ __forceinline__ float interp3(const float l[3], float v0, float v1, f
     return fadd(fadd(fmul(l[0], v0), fmul(l[1], v1)), fmul(l[2], v2));
 }
 
-template <bool MOTION>
+template <bool MOTION, bool TEXTURED>
 __device__ void frag_setup(const SceneArgs& S, const DeviceView& V, uint32_t px, uint32_t py, uint32_t id, Frag& f) {
     const uint32_t d = id >> VKGV_TRIANGLE_BITS, t = id & ((1u << VKGV_TRIANGLE_BITS) - 1u);
     const vkgv_meshlet_draw dr = S.draws[d];
@@ -196,7 +212,9 @@ __device__ void frag_setup(const SceneArgs& S, const DeviceView& V, uint32_t px,
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         f.vx[k] = verts + vidx[tri[k]];
-        m4v(mvp, f.vx[k]->position[0], f.vx[k]->position[1], f.vx[k]->position[2], 1.0f, c[k]);
+        float x, y, z;
+        load_vertex(f.vx[k], TEXTURED, x, y, z, f.color[k], f.uv[k]);
+        m4v(mvp, x, y, z, 1.0f, c[k]);
     }
     // Perspective-correct barycentrics: the clip-space weights whose point
     // projects to the pixel centre are proportional to a x b.
@@ -232,12 +250,13 @@ __device__ void shade_textured(const SceneArgs& S, const Frag& f, const float* u
     float col[4], uv[2];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        col[k] = interp3(f.l, unorm[f.vx[0]->color[k]], unorm[f.vx[1]->color[k]], unorm[f.vx[2]->color[k]]);
+        col[k] = interp3(f.l, unorm[(f.color[0] >> (8 * k)) & 255u], unorm[(f.color[1] >> (8 * k)) & 255u],
+                         unorm[(f.color[2] >> (8 * k)) & 255u]);
 #pragma unroll
     for (int k = 0; k < 2; ++k)
-        uv[k] = interp3(f.l, __half2float(__ushort_as_half(f.vx[0]->uv[k])),
-                        __half2float(__ushort_as_half(f.vx[1]->uv[k])),
-                        __half2float(__ushort_as_half(f.vx[2]->uv[k])));
+        uv[k] = interp3(f.l, __half2float(__ushort_as_half((unsigned short)(f.uv[0] >> (16 * k)))),
+                        __half2float(__ushort_as_half((unsigned short)(f.uv[1] >> (16 * k)))),
+                        __half2float(__ushort_as_half((unsigned short)(f.uv[2] >> (16 * k)))));
     float sampled[4] = {1.0f, 1.0f, 1.0f, 1.0f};
     if (mat.albedo_index != VKGV_INVALID_HANDLE && mat.albedo_index < S.texture_count) {
         // transformUv (mesh_common.h.glsl:129-135): rotate, scale, offset
@@ -287,7 +306,8 @@ __device__ uint32_t motion_vector(const SceneArgs& S, const DeviceView& V, const
     float px = 0.0f, py = 0.0f, pw = 0.0f;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float x = f.vx[k]->position[0], y = f.vx[k]->position[1], z = f.vx[k]->position[2];
+        const float2 xy = __ldg(reinterpret_cast<const float2*>(f.vx[k]->position));
+        const float x = xy.x, y = xy.y, z = __ldg(&f.vx[k]->position[2]);
         // m4v's order: ((m0 x + m1 y) + m2 z) + m3
         const float cx = fadd(fadd(fadd(fmul(rx[0], x), fmul(rx[1], y)), fmul(rx[2], z)), fmul(rx[3], 1.0f));
         const float cy = fadd(fadd(fadd(fmul(ry[0], x), fmul(ry[1], y)), fmul(ry[2], z)), fmul(ry[3], 1.0f));
@@ -330,7 +350,7 @@ __global__ void __launch_bounds__(256, 6) k_resolve(SceneArgs S, const DeviceVie
             float lin[4];
             if (TEXTURED || MOTION) {
                 Frag f;
-                frag_setup<MOTION>(S, V, p % w, p / w, id, f);
+                frag_setup<MOTION, TEXTURED>(S, V, p % w, p / w, id, f);
                 if (MOTION) mv = motion_vector(S, V, f);
                 if (TEXTURED) {
                     shade_textured(S, f, s_unorm, lin);
