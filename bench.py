@@ -312,6 +312,35 @@ def run_adjoint_case(r, local, level, displace, tex_size, sizes, seed, steps, wa
     return out
 
 
+def _meshopt_throughput() -> dict:
+    """EXT_meshopt_compression ATTRIBUTES decode on the host: 1M vertex
+    records of 16 bytes (slowly varying, like quantised positions), written
+    by the package's encoder, decoded through the C ABI."""
+    import ctypes
+
+    import numpy as np
+
+    from vk_gltf_viewer_gb300 import abi
+    from vk_gltf_viewer_gb300.gltf_export import meshopt_encode_attributes
+    rng = np.random.default_rng(17)
+    count, stride = 1 << 20, 16
+    data = (np.cumsum(rng.integers(-2, 3, (count, stride), dtype=np.int16), 0, dtype=np.int16) & 0xFF).astype(np.uint8)
+    stream = meshopt_encode_attributes(data)
+    out = np.empty(count * stride, np.uint8)
+    lib = abi.load()
+    times = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        abi.check(lib.vkgv_meshopt_decode(out.ctypes.data, count, stride, ctypes.c_char_p(stream), len(stream),
+                                          abi.MESHOPT_ATTRIBUTES, abi.MESHOPT_FILTER_NONE))
+        times.append(time.perf_counter() - t0)
+    assert out.tobytes() == data.tobytes()
+    t = statistics.median(times)
+    return {"decoded_bytes": int(out.size), "stream_bytes": len(stream), "ms": 1000.0 * t,
+            "gb_per_s": out.size / t / 1e9, "threads": min(16, os.cpu_count() or 1),
+            "note": "host, blocks split over threads after a serial scan of block starts"}
+
+
 def run_world(r, host, local, args, stream, peak):
     """World::updateTransformBuffer and World::rebuildDrawBuffer of the torus
     grid as a node tree (root, 8 layers, 2,048 animated tori, 1,098 channels;
@@ -387,6 +416,16 @@ def run_world(r, host, local, args, stream, peak):
                               "draws": int(ih.draws.shape[0]), "nodes": int(iw.nodes.size),
                               "note": "host: JSON + GLB parse, accessors, meshlets of the 40k-triangle torus, "
                                       "node tree, samplers, host draw list"}
+        # the same asset with EXT_meshopt_compression vertex and index views
+        cpath = write_world(Path(tmp) / "grid_meshopt.glb", [mesh], wh, meshopt=True)
+        loads = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            ch, _ = gltf.load(cpath)
+            loads.append(1000.0 * (time.perf_counter() - t0))
+        assert np.array_equal(ch.meshes[0].positions, ih.meshes[0].positions)
+        out["gltf_import"]["meshopt"] = {"ms": statistics.median(loads), "bytes": cpath.stat().st_size}
+    out["meshopt_decode"] = _meshopt_throughput()
     if not args.no_cpu_baseline:
         from oracle import binding as ob
         n_t = n_d = 0

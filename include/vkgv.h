@@ -508,7 +508,8 @@ int vkgv_world_build_draws(vkgv_ctx* ctx, vkgv_world* world, uint64_t draw_buffe
  * material), baseColorFactor, alphaCutoff, doubleSided, node matrices
  * decomposed into TRS, the first scene's root nodes, and every animation's
  * samplers and channels.  COLOR_0 and TEXCOORD_0 are kept when present.
- * EXT_meshopt_compression is refused (VKGV_INVALID_ARG with a message). */
+ * EXT_meshopt_compression buffer views are decoded (vkgv_meshopt_decode,
+ * the views in parallel); fallback buffers are never read. */
 typedef struct vkgv_gltf vkgv_gltf;
 
 /* Also store baseColorTexture's texture index and its KHR_texture_transform
@@ -569,6 +570,33 @@ int vkgv_gltf_get_world(const vkgv_gltf* asset, vkgv_world_desc* out);
 /* The encoded image of texture `texture` (loaded with VKGV_GLTF_IMAGES). */
 int vkgv_gltf_get_texture_image(const vkgv_gltf* asset, uint32_t texture, vkgv_gltf_image* out);
 void vkgv_gltf_free(vkgv_gltf* asset);
+
+/* One EXT_meshopt_compression bufferView: `size` bytes of stream at src
+ * decoded into count x stride bytes at dst (host memory), then filtered in
+ * place.  Replaces the per-view body of MeshoptDecompressor::ExecuteRange
+ * (src/vk_gltf_viewer/assets.cpp:111-166), which calls meshoptimizer's
+ * meshopt_decodeVertexBuffer / meshopt_decodeIndexBuffer /
+ * meshopt_decodeIndexSequence and meshopt_decodeFilterOct / Quat / Exp.
+ * Strides: ATTRIBUTES a multiple of 4 up to 256 (OCTAHEDRAL 4 or 8,
+ * QUATERNION 8); TRIANGLES and INDICES 2 or 4, TRIANGLES count a multiple
+ * of 3; filters only with ATTRIBUTES.  VKGV_INVALID_ARG for anything else
+ * and for a stream that does not decode to exactly its declared size (the
+ * reference ignores that status, assets.cpp:146-147). */
+typedef enum vkgv_meshopt_mode {
+    VKGV_MESHOPT_ATTRIBUTES = 0,
+    VKGV_MESHOPT_TRIANGLES = 1,
+    VKGV_MESHOPT_INDICES = 2
+} vkgv_meshopt_mode;
+
+typedef enum vkgv_meshopt_filter {
+    VKGV_MESHOPT_FILTER_NONE = 0,
+    VKGV_MESHOPT_FILTER_OCTAHEDRAL = 1,
+    VKGV_MESHOPT_FILTER_QUATERNION = 2,
+    VKGV_MESHOPT_FILTER_EXPONENTIAL = 3
+} vkgv_meshopt_filter;
+
+int vkgv_meshopt_decode(void* dst, uint64_t count, uint64_t stride, const void* src, uint64_t size, int mode,
+                        int filter);
 
 /* -------------------------------------------------------- texture decode */
 /* Base-colour images for the textured resolve.  The reference's image

@@ -1,5 +1,5 @@
-"""Malformed inputs to the host-side readers (glTF JSON / GLB, PNG / DEFLATE,
-DDS): seeded byte mutations, truncations and insertions of valid files
+"""Malformed inputs to the host-side readers (glTF JSON / GLB with and
+without EXT_meshopt_compression, PNG / DEFLATE, DDS): seeded byte mutations, truncations and insertions of valid files
 either load or fail with a status, in a child process so that a crash or a
 hang would fail the test instead of the run."""
 import os
@@ -39,8 +39,8 @@ CHILD = textwrap.dedent("""
             at = int(rng.integers(0, len(data)))
             data[at:at + 4] = bytes([b"0123456789[]{{}}\\",:"[int(rng.integers(0, 16))]]) * 4
         try:
-            if kind == "glb" or kind == "gltf":
-                out = path.with_name("mut." + kind)
+            if kind in ("glb", "gltf", "meshopt"):
+                out = path.with_name("mut." + ("glb" if kind == "meshopt" else kind))
                 out.write_bytes(bytes(data))
                 gltf.load(out, images=False)
             elif kind == "png":
@@ -72,9 +72,12 @@ def _asset(tmp_path):
     return b
 
 
-@pytest.mark.parametrize("kind", ["glb", "gltf", "png", "dds"])
+@pytest.mark.parametrize("kind", ["glb", "gltf", "meshopt", "png", "dds"])
 def test_mutated_inputs_fail_cleanly(built, tmp_path, kind):
-    if kind == "glb":
+    if kind == "meshopt":  # EXT_meshopt_compression streams in the GLB's binary chunk
+        from test_meshopt import _scene_builder
+        path = _scene_builder(True, np.random.default_rng(2)).write_glb(tmp_path / "m.glb")
+    elif kind == "glb":
         path = _asset(tmp_path).write_glb(tmp_path / "a.glb")
     elif kind == "gltf":
         path = _asset(tmp_path).write_gltf(tmp_path / "a.gltf")

@@ -214,8 +214,8 @@ def _error(tmp_path, mutate, match):
 def test_import_errors(built, tmp_path):
     _error(tmp_path, lambda b: b.gltf["meshes"][0]["primitives"][0]["attributes"].pop("POSITION"), "POSITION")
     _error(tmp_path, lambda b: b.gltf["meshes"][1]["primitives"][0].__setitem__("mode", 0), "TRIANGLES")
-    _error(tmp_path, lambda b: b.gltf["extensionsRequired"].append("EXT_meshopt_compression"),
-           "EXT_meshopt_compression")
+    _error(tmp_path, lambda b: b.gltf["extensionsRequired"].append("KHR_draco_mesh_compression"),
+           "KHR_draco_mesh_compression")
     _error(tmp_path, lambda b: b.gltf["asset"].__setitem__("version", "1.0"), "glTF 2.0")
     _error(tmp_path, lambda b: b.gltf["nodes"][0]["children"].append(17), "child")
     _error(tmp_path, lambda b: b.gltf["accessors"][0].__setitem__("count", 10 ** 6), "exceeds")

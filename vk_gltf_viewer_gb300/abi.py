@@ -205,6 +205,8 @@ BC1, BC2, BC3, BC4, BC5 = 1, 2, 3, 4, 5
 PATH_TRANSLATION, PATH_ROTATION, PATH_SCALE, PATH_WEIGHTS = 1, 2, 3, 4
 INTERP_LINEAR, INTERP_STEP, INTERP_CUBICSPLINE = 0, 1, 2
 MAX_NODE_DEPTH = 64
+MESHOPT_ATTRIBUTES, MESHOPT_TRIANGLES, MESHOPT_INDICES = 0, 1, 2
+MESHOPT_FILTER_NONE, MESHOPT_FILTER_OCTAHEDRAL, MESHOPT_FILTER_QUATERNION, MESHOPT_FILTER_EXPONENTIAL = 0, 1, 2, 3
 
 EXPECTED_SIZES = {"Meshlet": 36, "Vertex": 24, "MeshletDraw": 12, "Primitive": 64, "Material": 48, "Camera": 352,
                   "Node": 52, "AnimSampler": 32, "AnimChannel": 16, "WorldDesc": 96,
@@ -261,6 +263,7 @@ _PROTOS = {
     "vkgv_gltf_get_world": (C.c_int, [_P, C.POINTER(WorldDesc)]),
     "vkgv_gltf_get_texture_image": (C.c_int, [_P, _U32, C.POINTER(GltfImage)]),
     "vkgv_gltf_free": (None, [_P]),
+    "vkgv_meshopt_decode": (C.c_int, [_P, _U64, _U64, _P, _U64, C.c_int, C.c_int]),
     "vkgv_image_decode_png": (C.c_int, [_P, _U64, C.POINTER(_P), C.c_char_p, _U32]),
     "vkgv_image_get": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_P)]),
     "vkgv_image_free": (None, [_P]),

@@ -47,7 +47,9 @@ def _compile(src: Path, verbose_ptxas: bool) -> Path:
         return obj
     cmd = [nvcc(), *ARCH, *COMMON, "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
-        cmd = [nvcc(), "-x", "c++", *COMMON, "-c", str(src), "-o", str(obj)]
+        # host float arithmetic (filters, scene producers) must round alike on
+        # x86-64 and aarch64: no fused multiply-adds
+        cmd = [nvcc(), "-x", "c++", *COMMON, "-Xcompiler", "-ffp-contract=off", "-c", str(src), "-o", str(obj)]
     elif verbose_ptxas:
         cmd.insert(1, "-Xptxas=-v")
     res = subprocess.run(cmd, capture_output=True, text=True)

@@ -6,18 +6,21 @@
 // which is absent from its tree; this is an own JSON and GLB reader that
 // follows the glTF 2.0 specification for what the reference asks fastgltf
 // for: GenerateMeshIndices, DecomposeNodeMatrices, KHR_mesh_quantization and
-// KHR_texture_transform.  EXT_meshopt_compression (meshoptimizer's codecs,
-// also absent) is reported as unsupported.  Host code, run once per asset.
+// KHR_texture_transform, and EXT_meshopt_compression buffer views, decoded
+// by meshopt.cpp (meshoptimizer's codecs are absent too).  Host code, run
+// once per asset.
 #include "vkgv.h"
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <new>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -395,8 +398,8 @@ uint32_t component_as_index(const uint8_t* p, uint32_t ct) {
 // ------------------------------------------------------------------ asset
 
 struct View {
-    uint32_t buffer;
-    size_t offset, length, stride;
+    const uint8_t* data;  // the view's first byte: in its buffer, or the decoded copy
+    size_t length, stride;
 };
 
 struct Accessor {
@@ -407,22 +410,125 @@ struct Accessor {
     const JValue* json = nullptr;
 };
 
+// One EXT_meshopt_compression bufferView to decode.
+struct CompressedView {
+    size_t view;
+    const uint8_t* src;
+    size_t size, count, stride;
+    int mode, filter;
+};
+
+int meshopt_enum(const JValue& o, const char* key, const char* def, const char* const* names, int n) {
+    const JValue* v = o.get(key);
+    if (!v && def) return 0;
+    if (!v || v->kind != JValue::String) fail(std::string("EXT_meshopt_compression.") + key + " missing");
+    for (int i = 0; i < n; ++i)
+        if (v->s == names[i]) return i;
+    fail(std::string("EXT_meshopt_compression.") + key + " '" + v->s + "' is not known");
+}
+
+}  // namespace
+
+namespace vkgv {
+size_t meshopt_threaded_bytes();
+int meshopt_decode(void* dst, uint64_t count, uint64_t stride, const void* src, uint64_t size, int mode, int filter,
+                   unsigned threads);
+}  // namespace vkgv
+
+namespace {
+
+// Decodes the compressed views (assets.cpp:111-166 runs them as a task set
+// over the bufferViews): small views in parallel, one thread each, then the
+// large ones one at a time with their blocks split over the threads.
+void decode_views(const std::vector<CompressedView>& jobs, std::vector<std::vector<uint8_t>>& out) {
+    out.resize(jobs.size());
+    for (size_t i = 0; i < jobs.size(); ++i) out[i].resize(jobs[i].count * jobs[i].stride);
+    const unsigned hw = std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<int> status(jobs.size(), VKGV_OK);
+    std::vector<size_t> small, large;
+    size_t small_bytes = 0;
+    for (size_t i = 0; i < jobs.size(); ++i) {
+        if (out[i].size() >= vkgv::meshopt_threaded_bytes()) {
+            large.push_back(i);
+        } else {
+            small.push_back(i);
+            small_bytes += out[i].size();
+        }
+    }
+    auto run = [&](size_t i, unsigned threads) {
+        const CompressedView& j = jobs[i];
+        status[i] = vkgv::meshopt_decode(out[i].data(), j.count, j.stride, j.src, j.size, j.mode, j.filter, threads);
+    };
+    const size_t threads = small_bytes < (size_t(1) << 20) ? 1 : std::min<size_t>(small.size(), hw);
+    if (threads <= 1) {
+        for (size_t i : small) run(i, 1);
+    } else {
+        std::atomic<size_t> next{0};
+        std::vector<std::thread> pool;
+        for (size_t t = 0; t < threads; ++t)
+            pool.emplace_back([&] {
+                for (size_t k; (k = next.fetch_add(1)) < small.size();) run(small[k], 1);
+            });
+        for (auto& th : pool) th.join();
+    }
+    for (size_t i : large) run(i, hw);
+    for (size_t i = 0; i < jobs.size(); ++i) {
+        if (status[i] == VKGV_OUT_OF_MEMORY) throw std::bad_alloc();
+        if (status[i] != VKGV_OK)
+            fail("EXT_meshopt_compression bufferView " + std::to_string(jobs[i].view) + " does not decode");
+    }
+}
+
 class Reader {
 public:
-    Reader(const JValue& root, std::vector<std::vector<uint8_t>>& buffers) : root_(root), buffers_(buffers) {
+    // placeholder[b]: buffer b is an EXT_meshopt_compression fallback without data
+    Reader(const JValue& root, const std::vector<std::vector<uint8_t>>& buffers, const std::vector<bool>& placeholder)
+        : root_(root) {
+        static const char* const kModes[] = {"ATTRIBUTES", "TRIANGLES", "INDICES"};
+        static const char* const kFilters[] = {"NONE", "OCTAHEDRAL", "QUATERNION", "EXPONENTIAL"};
+        std::vector<CompressedView> jobs;
         for (const JValue& v : array_of(root, "bufferViews").items) {
-            View bv;
-            int64_t b = index_of(v, "buffer");
-            if (b < 0 || size_t(b) >= buffers.size()) fail("bufferView.buffer out of range");
-            bv.buffer = uint32_t(b);
-            bv.offset = size_t(index_of(v, "byteOffset", 0));
+            View bv{nullptr, 0, 0};
             const int64_t len = index_of(v, "byteLength");
             if (len < 0) fail("bufferView.byteLength missing");
-            bv.length = size_t(len);
             bv.stride = size_t(index_of(v, "byteStride", 0));
-            if (bv.offset + bv.length > buffers[bv.buffer].size()) fail("bufferView exceeds its buffer");
+            const JValue* ext = v.get("extensions");
+            const JValue* mc = ext ? ext->get("EXT_meshopt_compression") : nullptr;
+            if (mc) {
+                CompressedView j;
+                j.view = views_.size();
+                const int64_t b = index_of(*mc, "buffer"), off = index_of(*mc, "byteOffset", 0);
+                const int64_t size = index_of(*mc, "byteLength"), stride = index_of(*mc, "byteStride");
+                const int64_t count = index_of(*mc, "count");
+                if (b < 0 || size_t(b) >= buffers.size()) fail("EXT_meshopt_compression.buffer out of range");
+                if (size < 0 || stride <= 0 || count < 0) fail("EXT_meshopt_compression without byteLength, byteStride or count");
+                if (placeholder[size_t(b)]) fail("EXT_meshopt_compression data in a buffer without data");
+                if (size_t(off + size) > buffers[size_t(b)].size()) fail("EXT_meshopt_compression data exceeds its buffer");
+                j.mode = meshopt_enum(*mc, "mode", nullptr, kModes, 3);
+                j.filter = meshopt_enum(*mc, "filter", "NONE", kFilters, 4);
+                // a stream holds at most 64 vertices per byte (attributes) or
+                // one index per byte (index codecs): larger counts are malformed
+                const double most = j.mode == VKGV_MESHOPT_ATTRIBUTES ? 64.0 * double(size) + 256.0 : 3.0 * double(size);
+                if (double(count) > most) fail("EXT_meshopt_compression.count exceeds what its data can hold");
+                j.src = buffers[size_t(b)].data() + off;
+                j.size = size_t(size);
+                j.count = size_t(count);
+                j.stride = size_t(stride);
+                bv.length = j.count * j.stride;
+                jobs.push_back(j);
+            } else {
+                const int64_t b = index_of(v, "buffer");
+                if (b < 0 || size_t(b) >= buffers.size()) fail("bufferView.buffer out of range");
+                if (placeholder[size_t(b)]) fail("bufferView reads a buffer without data (an EXT_meshopt_compression fallback)");
+                const size_t off = size_t(index_of(v, "byteOffset", 0));
+                bv.length = size_t(len);
+                if (off + bv.length > buffers[size_t(b)].size()) fail("bufferView exceeds its buffer");
+                bv.data = buffers[size_t(b)].data() + off;
+            }
             views_.push_back(bv);
         }
+        decode_views(jobs, decoded_);
+        for (size_t i = 0; i < jobs.size(); ++i) views_[jobs[i].view].data = decoded_[i].data();
         for (const JValue& a : array_of(root, "accessors").items) {
             Accessor ac;
             ac.view = index_of(a, "bufferView");
@@ -461,7 +567,7 @@ public:
             const View& v = views_[size_t(a.view)];
             const size_t stride = v.stride ? v.stride : elem;
             if (a.count && a.offset + (a.count - 1) * stride + elem > v.length) fail("accessor exceeds its bufferView");
-            const uint8_t* base = buffers_[v.buffer].data() + v.offset + a.offset;
+            const uint8_t* base = v.data + a.offset;
             for (size_t k = 0; k < a.count; ++k) f(k, base + k * stride, cs);
         }
     }
@@ -489,8 +595,8 @@ public:
 
 private:
     const JValue& root_;
-    std::vector<std::vector<uint8_t>>& buffers_;
     std::vector<View> views_;
+    std::vector<std::vector<uint8_t>> decoded_;  // EXT_meshopt_compression views
     std::vector<Accessor> accessors_;
 
     // accessor.sparse: values replace the listed elements.
@@ -514,8 +620,8 @@ private:
         const size_t ioff = size_t(index_of(*ij, "byteOffset", 0)), voff = size_t(index_of(*vj, "byteOffset", 0));
         const size_t elem = size_t(cs) * a.ncomp;
         if (ioff + count * ics > I.length || voff + count * elem > V.length) fail("sparse data exceeds its bufferView");
-        const uint8_t* ib = buffers_[I.buffer].data() + I.offset + ioff;
-        const uint8_t* vb = buffers_[V.buffer].data() + V.offset + voff;
+        const uint8_t* ib = I.data + ioff;
+        const uint8_t* vb = V.data + voff;
         for (size_t i = 0; i < count; ++i) {
             const uint32_t k = component_as_index(ib + i * ics, ict);
             if (k >= a.count) fail("sparse index out of range");
@@ -597,8 +703,7 @@ struct vkgv_gltf {
 
 namespace {
 
-// The asset version and the extensions it requires; compressed buffer views
-// (EXT_meshopt_compression) are refused before any buffer is read.
+// The asset version and the extensions it requires.
 void check_asset(const JValue& root) {
     const JValue* asset = root.get("asset");
     if (!asset || !asset->get("version") || asset->get("version")->kind != JValue::String ||
@@ -606,13 +711,8 @@ void check_asset(const JValue& root) {
         fail("not a glTF 2.0 asset");
     for (const JValue& e : array_of(root, "extensionsRequired").items) {
         if (e.kind != JValue::String) continue;
-        if (e.s != "KHR_mesh_quantization" && e.s != "KHR_texture_transform")
+        if (e.s != "KHR_mesh_quantization" && e.s != "KHR_texture_transform" && e.s != "EXT_meshopt_compression")
             fail("required extension " + e.s + " is not supported");
-    }
-    for (const JValue& v : array_of(root, "bufferViews").items) {
-        const JValue* ext = v.get("extensions");
-        if (ext && ext->get("EXT_meshopt_compression"))
-            fail("EXT_meshopt_compression buffer views are not supported (meshoptimizer's codecs)");
     }
 }
 
@@ -641,9 +741,9 @@ std::vector<uint8_t> image_bytes(const JValue& img, const JValue& root, const st
     return std::vector<uint8_t>(base, base + len);
 }
 
-void import_asset(vkgv_gltf& G, const JValue& root, std::vector<std::vector<uint8_t>>& buffers, uint32_t flags,
-                  const std::string& dir) {
-    Reader R(root, buffers);
+void import_asset(vkgv_gltf& G, const JValue& root, const std::vector<std::vector<uint8_t>>& buffers,
+                  const std::vector<bool>& placeholder, uint32_t flags, const std::string& dir) {
+    Reader R(root, buffers, placeholder);
 
     // primitives (assets.cpp:288-430): positions, indices (generated when
     // absent), meshlets of 64 vertices / 124 triangles; colour and UV are
@@ -901,12 +1001,23 @@ extern "C" int vkgv_gltf_load(const char* path, uint32_t flags, vkgv_gltf** out,
         check_asset(root);
         std::vector<std::vector<uint8_t>> buffers;
         const JValue& bufs = array_of(root, "buffers");
+        std::vector<bool> placeholder(bufs.items.size(), false);
         for (size_t i = 0; i < bufs.items.size(); ++i) {
             const JValue& b = bufs.items[i];
             const int64_t blen = index_of(b, "byteLength");
             if (blen < 0) fail("buffer.byteLength missing");
             const size_t length = size_t(blen);
             const JValue* uri = b.get("uri");
+            // EXT_meshopt_compression's fallback buffer holds the uncompressed
+            // data for loaders without the extension: never read
+            const JValue* bext = b.get("extensions");
+            const JValue* mc = bext ? bext->get("EXT_meshopt_compression") : nullptr;
+            const JValue* fb = mc ? mc->get("fallback") : nullptr;
+            if (fb && fb->kind == JValue::Bool && fb->b && !(i == 0 && !uri && have_bin)) {
+                placeholder[i] = true;
+                buffers.emplace_back();
+                continue;
+            }
             std::vector<uint8_t> data;
             if (!uri) {
                 if (i != 0 || !have_bin) fail("buffer without uri outside a GLB");
@@ -923,7 +1034,7 @@ extern "C" int vkgv_gltf_load(const char* path, uint32_t flags, vkgv_gltf** out,
             data.resize(length);
             buffers.push_back(std::move(data));
         }
-        import_asset(*G, root, buffers, flags, dir);
+        import_asset(*G, root, buffers, placeholder, flags, dir);
     } catch (const ImportError& e) {
         put_error(error, error_capacity, e.msg);
         delete G;

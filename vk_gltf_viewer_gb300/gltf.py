@@ -67,6 +67,19 @@ def load(path, texture_references: bool = False, images: bool = False,
     return host, world
 
 
+def meshopt_decode(data: bytes, count: int, stride: int, mode: int,
+                   filter: int = abi.MESHOPT_FILTER_NONE) -> np.ndarray:
+    """One EXT_meshopt_compression bufferView decoded (and filtered) into
+    ``count * stride`` bytes, as MeshoptDecompressor::ExecuteRange does per
+    view (src/vk_gltf_viewer/assets.cpp:111-166).  Raises ``VkgvError`` for a
+    stream that does not decode to exactly its declared size."""
+    lib = abi.load()
+    out = np.empty(count * stride, np.uint8)
+    src = bytes(data)
+    abi.check(lib.vkgv_meshopt_decode(out.ctypes.data, count, stride, src, len(src), mode, filter))
+    return out
+
+
 def _copy(ptr, n, dtype):
     dtype = np.dtype(dtype)
     if n == 0 or not ptr:
