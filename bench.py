@@ -498,6 +498,75 @@ def run_texture(r, local, args, stream, peak):
     assert img.shape == (2048, 2048, 4)
     out["png_2048_host_ms"] = png_ms
     out["png_bytes"] = len(png)
+    # a 2048^2 4:2:0 JPEG: entropy decode on the host, pixels on the device
+    jpg = _synthetic_jpeg(2048, 2048, rng)
+    t0 = time.perf_counter()
+    j = texture.Jpeg(jpg)
+    host_ms = 1000.0 * (time.perf_counter() - t0)
+    for _ in range(3):
+        j.to_rgba(r, stream)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        j.to_rgba(r, stream)
+        e1.record(stream)
+        ts.append((e0, e1))
+    torch.cuda.synchronize()
+    dev_ms = statistics.median(a.elapsed_time(b) for a, b in ts)
+    coef_bytes = sum(p.nbytes for p in j.planes)
+    out["jpeg_2048"] = {"bytes": len(jpg), "host_entropy_ms": host_ms, "device_ms": dev_ms,
+                        "coefficient_bytes": int(coef_bytes),
+                        "note": "4:2:0, blocks from 256 random coefficient sets, 8-bit AC codes; device time "
+                                "includes the pageable copy of the coefficient planes, the IDCT and the colour pass"}
+    j.close()
+    return out
+
+
+def _synthetic_jpeg(w: int, h: int, rng) -> bytes:
+    """A valid baseline 4:2:0 JPEG of w x h (multiples of 16): every block one
+    of 256 random coefficient sets (magnitudes falling with frequency, DC
+    differences 0), coded with one 1-bit DC code and 8-bit AC codes."""
+    import struct
+
+    import numpy as np
+
+    sym_index = {}
+    pool = []
+    for _ in range(256):
+        bits = [0]  # DC: size 0
+        k = 1
+        while k < 64:
+            run = int(rng.integers(0, 4))
+            if k + run >= 64 or rng.random() < 0.04 * k ** 0.5:
+                break
+            k += run
+            v = int(rng.integers(1, max(2, 200 // (k + 2)) + 1)) * (1 if rng.random() < 0.5 else -1)
+            size = abs(v).bit_length()
+            sym = (run << 4) | size
+            code = sym_index.setdefault(sym, len(sym_index))
+            bits += [(code >> i) & 1 for i in range(7, -1, -1)]
+            bits += [((v if v > 0 else v + (1 << size) - 1) >> i) & 1 for i in range(size - 1, -1, -1)]
+            k += 1
+        if k < 64:
+            code = sym_index.setdefault(0x00, len(sym_index))
+            bits += [(code >> i) & 1 for i in range(7, -1, -1)]
+        pool.append(np.array(bits, np.uint8))
+    mcus = (w // 16) * (h // 16)
+    choice = rng.integers(0, 256, mcus * 6)
+    stream = np.concatenate([pool[c] for c in choice])
+    stream = np.concatenate([stream, np.ones(-len(stream) % 8, np.uint8)])
+    data = np.packbits(stream).tobytes().replace(b"\xff", b"\xff\x00")
+    values = sorted(sym_index, key=sym_index.get)
+    seg = lambda m, body: struct.pack(">BBH", 0xFF, m, len(body) + 2) + body
+    q = bytes([4] * 64)
+    out = b"\xff\xd8" + seg(0xDB, b"\x00" + q) + seg(0xDB, b"\x01" + q)
+    out += seg(0xC0, struct.pack(">BHHB", 8, h, w, 3) + bytes([1, 0x22, 0, 2, 0x11, 1, 3, 0x11, 1]))
+    dc = bytes([0x00, 1] + [0] * 15 + [0])
+    ac = bytes([0x10] + [0] * 7 + [len(values)] + [0] * 8) + bytes(values)
+    out += seg(0xC4, dc) + seg(0xC4, ac)
+    out += seg(0xDA, bytes([3, 1, 0x00, 2, 0x00, 3, 0x00, 0, 63, 0])) + data + b"\xff\xd9"
     return out
 
 

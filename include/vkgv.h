@@ -642,6 +642,42 @@ int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* out);
 int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
                    uint64_t rgba_out, void* stream);
 
+/* JPEG (the reference links wuffs for it, wuffs_implementation.cpp:1-5):
+ * sequential DCT, Huffman, 8-bit; 1 component or 3 (YCbCr, or RGB per an
+ * Adobe transform 0 / component ids 'R','G','B'); sampling factors 1-4 with
+ * integral ratios; restart intervals; interleaved or single-component
+ * scans.  Progressive, lossless and arithmetic-coded files are refused.
+ * The entropy decode runs on the host into dequantized coefficient planes;
+ * vkgv_jpeg_to_rgba runs the IDCT, chroma upsampling (replication) and the
+ * JFIF colour conversion on the device, in pinned fixed-point arithmetic. */
+typedef struct vkgv_jpeg vkgv_jpeg;
+
+typedef struct vkgv_jpeg_info {
+    uint32_t width;
+    uint32_t height;
+    uint32_t components;     /* 1 or 3 */
+    uint32_t rgb;            /* 3 components stored as R, G, B (no YCbCr conversion) */
+    uint32_t hmax;           /* largest sampling factors */
+    uint32_t vmax;
+    uint32_t h[3];           /* sampling factors per component */
+    uint32_t v[3];
+    uint32_t blocks_w[3];    /* coefficient planes, in 8x8 blocks (MCU-padded) */
+    uint32_t blocks_h[3];
+} vkgv_jpeg_info;
+
+int vkgv_jpeg_decode_coefficients(const void* data, uint64_t size, vkgv_jpeg** out_jpeg, char* error,
+                                  uint32_t error_capacity);
+int vkgv_jpeg_get_info(const vkgv_jpeg* jpeg, vkgv_jpeg_info* out);
+/* Component c's blocks_w x blocks_h blocks in raster order, each 64 int16
+ * coefficients in natural (row-major) order, already multiplied by the
+ * quantisation step (clamped to int16). */
+int vkgv_jpeg_get_coefficients(const vkgv_jpeg* jpeg, uint32_t component, const int16_t** out);
+/* IDCT + upsampling + colour conversion into width x height RGBA8 (device
+ * uint32[], 4-byte aligned; alpha 255); the coefficients are copied in
+ * through the context's scratch, so the vkgv_jpeg may be freed on return. */
+int vkgv_jpeg_to_rgba(vkgv_ctx* ctx, const vkgv_jpeg* jpeg, uint64_t rgba_out, void* stream);
+void vkgv_jpeg_free(vkgv_jpeg* jpeg);
+
 /* ---------------------------------------------- host scene producers (A15) */
 /* Replace the glTF import + meshletiser (src/vk_gltf_viewer/assets.cpp:288-430)
  * for procedural scenes, and the camera update (src/vk_gltf_viewer/camera.cpp). */

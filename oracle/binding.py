@@ -104,6 +104,8 @@ def load() -> C.CDLL:
         lib.orc_asin_series.restype = C.c_float
         lib.orc_asin_series.argtypes = [C.c_float]
         lib.orc_decode_bc.argtypes = [U32, P, U32, U32, P]
+        lib.orc_jpeg_idct.argtypes = [P, U32, U32, P]
+        lib.orc_jpeg_color.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, P]
         lib.orc_half_rn.restype = C.c_uint16
         lib.orc_half_rn.argtypes = [C.c_float]
         lib.orc_from_linear.restype = C.c_float
@@ -413,3 +415,33 @@ def decode_bc(fmt: int, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
     out = np.zeros(w * h, np.uint32)
     load().orc_decode_bc(fmt, _addr(blocks), w, h, _addr(out))
     return out.reshape(h, w)
+
+
+def jpeg_rgba(info, planes) -> np.ndarray:
+    """JPEG pixels from its coefficient planes: `info` has width, height,
+    components, rgb, hmax, vmax, h, v, blocks_w, blocks_h (as
+    vkgv_jpeg_info); planes[c] is (blocks_h * blocks_w * 64) int16.
+    Returns (height, width) uint32 RGBA8."""
+    lib = load()
+    samples, pitch, rx, ry = [], [], [], []
+    for c in range(info.components):
+        bw, bh = int(info.blocks_w[c]), int(info.blocks_h[c])
+        coef = np.ascontiguousarray(planes[c], np.int16)
+        assert coef.size == bw * bh * 64
+        plane = np.zeros(bw * bh * 64, np.uint8)
+        lib.orc_jpeg_idct(_addr(coef), bw, bh, _addr(plane))
+        samples.append(plane)
+        pitch.append(bw * 8)
+        rx.append(int(info.hmax) // int(info.h[c]))
+        ry.append(int(info.vmax) // int(info.v[c]))
+    while len(samples) < 3:
+        samples.append(samples[0])
+        pitch.append(0)
+        rx.append(1)
+        ry.append(1)
+    arr = [np.asarray(a, np.uint32) for a in (pitch, rx, ry)]
+    out = np.zeros(int(info.width) * int(info.height), np.uint32)
+    lib.orc_jpeg_color(_addr(samples[0]), _addr(samples[1]), _addr(samples[2]), _addr(arr[0]), _addr(arr[1]),
+                       _addr(arr[2]), int(info.width), int(info.height), int(info.components), int(info.rgb),
+                       _addr(out))
+    return out.reshape(int(info.height), int(info.width))

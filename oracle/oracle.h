@@ -231,6 +231,13 @@ float orc_asin_series(float z);
 /* BC1-BC5 blocks (format 1..5, row-major blocks of 8 or 16 bytes) into
  * RGBA8 texels (R in the low byte). */
 void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t h, uint32_t* rgba);
+/* JPEG pixels from dequantized natural-order coefficient blocks: one
+ * component's IDCT into an 8-bit plane (blocks_w * 8 wide), then the
+ * upsampled colour conversion of 1 or 3 planes into RGBA8. */
+void orc_jpeg_idct(const int16_t* coef, uint32_t blocks_w, uint32_t blocks_h, uint8_t* plane);
+void orc_jpeg_color(const uint8_t* p0, const uint8_t* p1, const uint8_t* p2, const uint32_t pitch[3],
+                    const uint32_t rx[3], const uint32_t ry[3], uint32_t w, uint32_t h, uint32_t components,
+                    uint32_t rgb, uint32_t* out);
 
 /* Single-fragment helpers exported for the known-answer tests. */
 float orc_from_linear(float c);

@@ -110,3 +110,86 @@ void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t 
             }
         }
 }
+
+/*
+ * JPEG, the pixel half (the reference links wuffs for JPEG,
+ * src/vk_gltf_viewer/wuffs_implementation.cpp:1-5; it is absent, so parity
+ * with it is unpinned).  From dequantized natural-order coefficient blocks:
+ *   the 8x8 inverse DCT, f(x, y) = sum_u sum_v c(u)/2 c(v)/2 F(v, u)
+ *   cos((2x+1) u pi/16) cos((2y+1) v pi/16), c(0) = 1/sqrt(2), evaluated in
+ *   the pinned fixed point: constants K[x][u] = round(8192 c(u)/2 cos(..))
+ *   (derived here from the formula), the row pass rounded to 3 fractional
+ *   bits ((sum + 512) >> 10), the column pass (sum + 2^15) >> 16, + 128,
+ *   clamped to 0..255;
+ *   chroma upsampling by replication, and the JFIF YCbCr -> RGB conversion
+ *   with 16-bit fixed-point constants 1.402, 0.344136, 0.714136, 1.772
+ *   (91881, 22554, 46802, 116130), rounded by + 2^15 before >> 16.
+ */
+#include <math.h>
+
+static int32_t jpeg_k[8][8];
+static int jpeg_k_ready;
+
+static void jpeg_constants(void) {
+    if (jpeg_k_ready) return;
+    for (int x = 0; x < 8; ++x)
+        for (int u = 0; u < 8; ++u) {
+            const double cu = u == 0 ? 1.0 / sqrt(2.0) : 1.0;
+            jpeg_k[x][u] = (int32_t)lround(8192.0 * cu / 2.0 * cos((2 * x + 1) * u * acos(-1.0) / 16.0));
+        }
+    jpeg_k_ready = 1;
+}
+
+static int32_t asr(int64_t v, int s) { return (int32_t)(v >= 0 ? v >> s : -((-v - 1) >> s) - 1); }
+
+void orc_jpeg_idct(const int16_t* coef, uint32_t blocks_w, uint32_t blocks_h, uint8_t* plane) {
+    jpeg_constants();
+    const size_t pitch = (size_t)blocks_w * 8;
+    for (uint32_t by = 0; by < blocks_h; ++by)
+        for (uint32_t bx = 0; bx < blocks_w; ++bx) {
+            const int16_t* F = coef + ((size_t)by * blocks_w + bx) * 64;
+            int32_t t[8][8];
+            for (int v = 0; v < 8; ++v)
+                for (int x = 0; x < 8; ++x) {
+                    int64_t sum = 0;
+                    for (int u = 0; u < 8; ++u) sum += (int64_t)jpeg_k[x][u] * F[v * 8 + u];
+                    t[v][x] = asr(sum + 512, 10);
+                }
+            for (int y = 0; y < 8; ++y)
+                for (int x = 0; x < 8; ++x) {
+                    int64_t sum = 0;
+                    for (int v = 0; v < 8; ++v) sum += (int64_t)jpeg_k[y][v] * t[v][x];
+                    int32_t s = asr(sum + 32768, 16) + 128;
+                    s = s < 0 ? 0 : (s > 255 ? 255 : s);
+                    plane[((size_t)by * 8 + y) * pitch + (size_t)bx * 8 + x] = (uint8_t)s;
+                }
+        }
+}
+
+static int32_t clamp255(int32_t v) { return v < 0 ? 0 : (v > 255 ? 255 : v); }
+
+void orc_jpeg_color(const uint8_t* p0, const uint8_t* p1, const uint8_t* p2, const uint32_t pitch[3],
+                    const uint32_t rx[3], const uint32_t ry[3], uint32_t w, uint32_t h, uint32_t components,
+                    uint32_t rgb, uint32_t* out) {
+    const uint8_t* planes[3] = {p0, p1, p2};
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            int32_t c[3] = {0, 0, 0};
+            for (uint32_t k = 0; k < components; ++k)
+                c[k] = planes[k][(size_t)(y / ry[k]) * pitch[k] + x / rx[k]];
+            int32_t r, g, b;
+            if (components == 1) {
+                r = g = b = c[0];
+            } else if (rgb) {
+                r = c[0];
+                g = c[1];
+                b = c[2];
+            } else {
+                const int32_t cb = c[1] - 128, cr = c[2] - 128;
+                r = clamp255(c[0] + asr((int64_t)91881 * cr + 32768, 16));
+                g = clamp255(c[0] + asr((int64_t)-22554 * cb - (int64_t)46802 * cr + 32768, 16));
+                b = clamp255(c[0] + asr((int64_t)116130 * cb + 32768, 16));
+            }
+            out[(size_t)y * w + x] = (uint32_t)r | ((uint32_t)g << 8) | ((uint32_t)b << 16) | 0xFF000000u;
+        }
+}

@@ -38,7 +38,7 @@ def test_c_layout_matches_ctypes(tmp_path):
         "vkgv_config": abi.Config, "vkgv_mesh_info": abi.MeshInfo, "vkgv_meshlet_cone": abi.MeshletCone,
         "vkgv_node": abi.Node, "vkgv_anim_sampler": abi.AnimSampler, "vkgv_anim_channel": abi.AnimChannel,
         "vkgv_world_desc": abi.WorldDesc, "vkgv_gltf_info": abi.GltfInfo, "vkgv_gltf_primitive": abi.GltfPrimitive,
-        "vkgv_gltf_image": abi.GltfImage, "vkgv_dds_info": abi.DdsInfo,
+        "vkgv_gltf_image": abi.GltfImage, "vkgv_dds_info": abi.DdsInfo, "vkgv_jpeg_info": abi.JpegInfo,
     }
     lines = []
     for cname, cls in structs.items():

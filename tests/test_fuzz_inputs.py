@@ -1,5 +1,5 @@
 """Malformed inputs to the host-side readers (glTF JSON / GLB with and
-without EXT_meshopt_compression, PNG / DEFLATE, DDS): seeded byte mutations, truncations and insertions of valid files
+without EXT_meshopt_compression, PNG / DEFLATE, JPEG, DDS): seeded byte mutations, truncations and insertions of valid files
 either load or fail with a status, in a child process so that a crash or a
 hang would fail the test instead of the run."""
 import os
@@ -45,6 +45,8 @@ CHILD = textwrap.dedent("""
                 gltf.load(out, images=False)
             elif kind == "png":
                 texture.decode_png(bytes(data))
+            elif kind == "jpeg":
+                texture.Jpeg(bytes(data)).close()
             else:
                 texture.parse_dds(bytes(data))
             ok += 1
@@ -72,7 +74,7 @@ def _asset(tmp_path):
     return b
 
 
-@pytest.mark.parametrize("kind", ["glb", "gltf", "meshopt", "png", "dds"])
+@pytest.mark.parametrize("kind", ["glb", "gltf", "meshopt", "png", "jpeg", "dds"])
 def test_mutated_inputs_fail_cleanly(built, tmp_path, kind):
     if kind == "meshopt":  # EXT_meshopt_compression streams in the GLB's binary chunk
         from test_meshopt import _scene_builder
@@ -81,6 +83,12 @@ def test_mutated_inputs_fail_cleanly(built, tmp_path, kind):
         path = _asset(tmp_path).write_glb(tmp_path / "a.glb")
     elif kind == "gltf":
         path = _asset(tmp_path).write_gltf(tmp_path / "a.gltf")
+    elif kind == "jpeg":
+        from jpeg_util import encode as jpeg_encode
+        rng = np.random.default_rng(0)
+        path = tmp_path / "a.jpg"
+        path.write_bytes(jpeg_encode(rng.integers(0, 256, (19, 27, 3)), sampling=((2, 2), (1, 1), (1, 1)),
+                                     restart=2, rng=rng)[0])
     elif kind == "png":
         from png_util import encode
         rng = np.random.default_rng(0)

@@ -1,6 +1,7 @@
 """Block-compressed textures decoded on the device (k_decode_bc) are
 bit-identical to the oracle's decoder for BC1-BC5 at block-aligned and ragged
-sizes, and a glTF asset whose base colour comes from an embedded DDS
+sizes; JPEG pixels (k_jpeg_idct, k_jpeg_color) are bit-identical to the
+oracle's from the same coefficients; and a glTF asset whose base colour comes from an embedded DDS
 (MSFT_texture_dds) and PNG renders, textured, like the oracle frame of the
 same decoded images."""
 import dataclasses
@@ -35,6 +36,41 @@ def test_bc_decode_matches_oracle(renderer, fmt, size):
     torch.cuda.synchronize()
     exp = ob.decode_bc(fmt, blocks, w, h)
     assert np.array_equal(got.cpu().numpy().reshape(h, w, 4).view(np.uint32)[..., 0], exp)
+
+
+@pytest.mark.parametrize("case", range(13))
+@pytest.mark.parametrize("size", [(37, 45), (1, 1), (17, 64), (300, 517)])
+def test_jpeg_pixels_match_oracle(renderer, case, size):
+    """k_jpeg_idct + k_jpeg_color against the oracle, from the same
+    coefficient planes: every sampling layout, grey, RGB, ragged sizes."""
+    from jpeg_util import encode as jpeg_encode
+    from test_jpeg import CASES, _image
+
+    img = _image(*size, seed=case)
+    data, _ = jpeg_encode(img, rng=np.random.default_rng(case), **CASES[case])
+    j = texture.Jpeg(data)
+    got = j.to_rgba(renderer)
+    torch.cuda.synchronize()
+    exp = ob.jpeg_rgba(j.info, [p.reshape(-1) for p in j.planes])
+    assert np.array_equal(got.cpu().numpy().view(np.uint32)[..., 0], exp)
+
+
+def test_jpeg_through_load_image_and_freed_source(renderer):
+    """decode_jpeg frees the host coefficients before the device finishes:
+    the copy is staged, so the pixels are still the oracle's."""
+    from jpeg_util import encode as jpeg_encode
+    from test_jpeg import _image
+
+    img = _image(1024, 768, seed=3)
+    data, _ = jpeg_encode(img, rng=np.random.default_rng(1), sampling=((2, 2), (1, 1), (1, 1)), restart=7)
+    outs = [texture.decode_jpeg(data, renderer) for _ in range(3)]  # scratch reuse across calls
+    torch.cuda.synchronize()
+    j = texture.Jpeg(data)
+    exp = ob.jpeg_rgba(j.info, [p.reshape(-1) for p in j.planes])
+    for o in outs:
+        assert np.array_equal(o.cpu().numpy().view(np.uint32)[..., 0], exp)
+    via = texture.load_image(data, abi.IMAGE_JPEG, renderer)
+    assert np.array_equal(via.view(np.uint32)[..., 0], exp)
 
 
 def test_gltf_with_dds_and_png_textures(renderer, tmp_path):

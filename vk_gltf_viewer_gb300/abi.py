@@ -198,6 +198,12 @@ class DdsInfo(C.Structure):
                 ("srgb", C.c_uint32), ("_pad", C.c_uint32), ("data_offset", C.c_uint64), ("data_size", C.c_uint64)]
 
 
+class JpegInfo(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("components", C.c_uint32), ("rgb", C.c_uint32),
+                ("hmax", C.c_uint32), ("vmax", C.c_uint32), ("h", C.c_uint32 * 3), ("v", C.c_uint32 * 3),
+                ("blocks_w", C.c_uint32 * 3), ("blocks_h", C.c_uint32 * 3)]
+
+
 GLTF_TEXTURE_REFERENCES = 1
 GLTF_IMAGES = 2
 IMAGE_UNKNOWN, IMAGE_PNG, IMAGE_DDS, IMAGE_JPEG, IMAGE_KTX2 = 0, 1, 2, 3, 4
@@ -210,7 +216,7 @@ MESHOPT_FILTER_NONE, MESHOPT_FILTER_OCTAHEDRAL, MESHOPT_FILTER_QUATERNION, MESHO
 
 EXPECTED_SIZES = {"Meshlet": 36, "Vertex": 24, "MeshletDraw": 12, "Primitive": 64, "Material": 48, "Camera": 352,
                   "Node": 52, "AnimSampler": 32, "AnimChannel": 16, "WorldDesc": 96,
-                  "GltfInfo": 40, "GltfPrimitive": 24, "GltfImage": 24, "DdsInfo": 40}
+                  "GltfInfo": 40, "GltfPrimitive": 24, "GltfImage": 24, "DdsInfo": 40, "JpegInfo": 72}
 
 _P = C.c_void_p
 _U32 = C.c_uint32
@@ -269,6 +275,11 @@ _PROTOS = {
     "vkgv_image_free": (None, [_P]),
     "vkgv_dds_parse": (C.c_int, [_P, _U64, C.POINTER(DdsInfo)]),
     "vkgv_decode_bc": (C.c_int, [_P, _U32, _U64, _U32, _U32, _U64, _P]),
+    "vkgv_jpeg_decode_coefficients": (C.c_int, [_P, _U64, C.POINTER(_P), C.c_char_p, _U32]),
+    "vkgv_jpeg_get_info": (C.c_int, [_P, C.POINTER(JpegInfo)]),
+    "vkgv_jpeg_get_coefficients": (C.c_int, [_P, _U32, C.POINTER(_P)]),
+    "vkgv_jpeg_to_rgba": (C.c_int, [_P, _P, _U64, _P]),
+    "vkgv_jpeg_free": (None, [_P]),
     "vkgv_set_profiling": (C.c_int, [_P, C.c_int32]),
     "vkgv_stage_times": (C.c_int, [_P, C.POINTER(C.c_float), _U32]),
 }

@@ -51,6 +51,7 @@ struct vkgv_ctx {
     Scratch diff;       // adjoint: internal raster scene of the differentiable mesh
     Scratch diff_acc;   // adjoint: float4 gradient accumulators (positions, colours, texels)
     Scratch tdet;       // determinant(M) per node transform (vkgv_scene.transform_count)
+    Scratch jpeg;       // vkgv_jpeg_to_rgba: coefficient and sample planes
     Scratch mvp;        // view_projection * M per view and node
     BigTri* big = nullptr;
     uint32_t big_cap = 0;
@@ -475,6 +476,7 @@ int vkgv_destroy(vkgv_ctx* ctx) {
     if (ctx->diff.ptr) cudaFree(ctx->diff.ptr);
     if (ctx->diff_acc.ptr) cudaFree(ctx->diff_acc.ptr);
     if (ctx->tdet.ptr) cudaFree(ctx->tdet.ptr);
+    if (ctx->jpeg.ptr) cudaFree(ctx->jpeg.ptr);
     if (ctx->mvp.ptr) cudaFree(ctx->mvp.ptr);
     if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
     if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
@@ -684,6 +686,46 @@ int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t wid
         return fail(ctx, VKGV_INVALID_ARG, "blocks must be aligned to the block size and rgba_out to 4 bytes");
     launch_decode_bc(reinterpret_cast<const uint8_t*>(blocks), format, width, height,
                      reinterpret_cast<uint32_t*>(rgba_out), reinterpret_cast<cudaStream_t>(stream_));
+    return check_launch(ctx);
+}
+
+int vkgv_jpeg_to_rgba(vkgv_ctx* ctx, const vkgv_jpeg* jpeg, uint64_t rgba_out, void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    vkgv_jpeg_info I;
+    if (!jpeg || vkgv_jpeg_get_info(jpeg, &I) != VKGV_OK) return fail(ctx, VKGV_INVALID_ARG, "jpeg must be non-NULL");
+    if (!rgba_out || (rgba_out & 3u)) return fail(ctx, VKGV_INVALID_ARG, "rgba_out must be non-NULL and 4-byte aligned");
+    const auto stream = reinterpret_cast<cudaStream_t>(stream_);
+    // per component: its coefficient plane, then its sample plane
+    size_t coef_at[3], plane_at[3], off = 0;
+    for (uint32_t c = 0; c < I.components; ++c) {
+        const size_t blocks = size_t(I.blocks_w[c]) * I.blocks_h[c];
+        coef_at[c] = off;
+        off += (blocks * 128 + 255) & ~size_t(255);
+        plane_at[c] = off;
+        off += (blocks * 64 + 255) & ~size_t(255);
+    }
+    int rc = ensure_scratch(ctx, ctx->jpeg, off, "JPEG planes");
+    if (rc) return rc;
+    auto* base = static_cast<uint8_t*>(ctx->jpeg.ptr);
+    JpegPlanes P{};
+    for (uint32_t c = 0; c < I.components; ++c) {
+        const int16_t* host = nullptr;
+        if (vkgv_jpeg_get_coefficients(jpeg, c, &host) != VKGV_OK) return fail(ctx, VKGV_INVALID_ARG, "bad JPEG");
+        const size_t blocks = size_t(I.blocks_w[c]) * I.blocks_h[c];
+        // pageable source: returns once the data is staged, so the caller may free it
+        VKGV_CUDA(ctx, cudaMemcpyAsync(base + coef_at[c], host, blocks * 128, cudaMemcpyHostToDevice, stream));
+        launch_jpeg_idct(reinterpret_cast<const int16_t*>(base + coef_at[c]), I.blocks_w[c], I.blocks_h[c],
+                         base + plane_at[c], stream);
+        P.plane[c] = base + plane_at[c];
+        P.pitch[c] = I.blocks_w[c] * 8;
+        P.rx[c] = I.hmax / I.h[c];
+        P.ry[c] = I.vmax / I.v[c];
+    }
+    P.width = I.width;
+    P.height = I.height;
+    P.components = I.components;
+    P.rgb = I.rgb;
+    launch_jpeg_color(P, reinterpret_cast<uint32_t*>(rgba_out), stream);
     return check_launch(ctx);
 }
 

@@ -181,6 +181,16 @@ void launch_world_transforms(const WorldArgs& W, float time, float* transforms, 
 void launch_world_draws(const WorldArgs& W, uint32_t* draws, uint32_t sm_count, cudaStream_t stream);
 
 // k_decode_bc: BC1-BC5 blocks -> RGBA8, one thread per texel.
+// Sample planes of a JPEG (8-bit, pitch bytes per row) for the colour
+// conversion; rx / ry = hmax / h, vmax / v of each component.
+struct JpegPlanes {
+    const uint8_t* plane[3];
+    uint32_t pitch[3], rx[3], ry[3];
+    uint32_t width, height, components, rgb;
+};
+
+void launch_jpeg_idct(const int16_t* coef, uint32_t blocks_w, uint32_t blocks_h, uint8_t* plane, cudaStream_t stream);
+void launch_jpeg_color(const JpegPlanes& P, uint32_t* rgba, cudaStream_t stream);
 void launch_decode_bc(const uint8_t* blocks, uint32_t format, uint32_t w, uint32_t h, uint32_t* rgba,
                       cudaStream_t stream);
 

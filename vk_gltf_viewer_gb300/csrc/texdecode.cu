@@ -151,7 +151,108 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc(const uint8_t* 
     }
 }
 
+// ------------------------------------------------------------------- JPEG
+// The device half of a JPEG decode (the host half, jpeg.cpp, writes the
+// dequantized coefficient planes).  Pinned fixed-point arithmetic, shared
+// with the oracle:
+//   IDCT: K[x][u] = round(8192 * c(u) / 2 * cos((2x + 1) u pi / 16)),
+//     c(0) = 1 / sqrt(2), c(u > 0) = 1; rows t[v][x] = (sum_u K[x][u] F[v][u]
+//     + 512) >> 10 (int32, 3 fractional bits kept), then columns
+//     s[y][x] = (sum_v K[y][v] t[v][x] + 2^15) >> 16 (int64), + 128, clamped
+//     to 0..255; right shifts are arithmetic.
+//   upsampling: component c at pixel (x, y) is its sample
+//     (x / (hmax / h_c), y / (vmax / v_c)) (replication).
+//   YCbCr -> RGB (JFIF): with cb = Cb - 128, cr = Cr - 128,
+//     R = Y + ((91881 cr + 32768) >> 16),
+//     G = Y + ((-22554 cb - 46802 cr + 32768) >> 16),
+//     B = Y + ((116130 cb + 32768) >> 16), each clamped to 0..255.
+
+__constant__ int32_t c_idct[8][8] = {
+    {2896, 4017, 3784, 3406, 2896, 2276, 1567, 799},     {2896, 3406, 1567, -799, -2896, -4017, -3784, -2276},
+    {2896, 2276, -1567, -4017, -2896, 799, 3784, 3406},  {2896, 799, -3784, -2276, 2896, 3406, -1567, -4017},
+    {2896, -799, -3784, 2276, 2896, -3406, -1567, 4017}, {2896, -2276, -1567, 4017, -2896, -799, 3784, -3406},
+    {2896, -3406, 1567, 799, -2896, 4017, -3784, 2276},  {2896, -4017, 3784, -3406, 2896, -2276, 1567, -799},
+};
+
+constexpr int kIdctBlocks = 32;  // 8x8 blocks per CTA, one thread per block row
+
+// Coefficient blocks (raster order over a blocks_w-wide grid) -> 8-bit
+// samples of a (blocks_w * 8)-wide plane.
+__global__ void __launch_bounds__(kIdctBlocks * 8) k_jpeg_idct(const int16_t* __restrict__ coef, uint32_t blocks,
+                                                               uint32_t blocks_w, uint8_t* __restrict__ plane) {
+    pdl_begin();
+    __shared__ int32_t t[kIdctBlocks][8][9];
+    const uint32_t local = threadIdx.x >> 3, r = threadIdx.x & 7u;
+    const uint32_t b = blockIdx.x * kIdctBlocks + local;
+    const bool live = b < blocks;
+    if (live) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(coef + (size_t)b * 64 + r * 8));
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+        int32_t f[8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            f[2 * i] = int32_t(int16_t(w[i] & 0xFFFFu));
+            f[2 * i + 1] = int32_t(int16_t(w[i] >> 16));
+        }
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+            int32_t acc = 0;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc += c_idct[x][u] * f[u];
+            t[local][r][x] = (acc + 512) >> 10;
+        }
+    }
+    __syncthreads();
+    if (!live) return;
+    uint32_t lo = 0, hi = 0;
+#pragma unroll
+    for (int x = 0; x < 8; ++x) {
+        int64_t acc = 0;
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc += int64_t(c_idct[r][v]) * t[local][v][x];
+        const int32_t s = min(255, max(0, int32_t((acc + 32768) >> 16) + 128));
+        if (x < 4) lo |= uint32_t(s) << (8 * x);
+        else hi |= uint32_t(s) << (8 * (x - 4));
+    }
+    const uint32_t bx = b % blocks_w, by = b / blocks_w;
+    *reinterpret_cast<uint2*>(plane + ((size_t)by * 8 + r) * ((size_t)blocks_w * 8) + (size_t)bx * 8) = make_uint2(lo, hi);
+}
+
+__global__ void __launch_bounds__(256) k_jpeg_color(JpegPlanes P, uint32_t* __restrict__ rgba) {
+    pdl_begin();
+    const uint32_t x = blockIdx.x * 32 + (threadIdx.x & 31u), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= P.width || y >= P.height) return;
+    int32_t c[3] = {0, 0, 0};
+#pragma unroll
+    for (uint32_t k = 0; k < 3; ++k)  // constant indices keep the parameters out of local memory
+        if (k < P.components) c[k] = P.plane[k][(size_t)(y / P.ry[k]) * P.pitch[k] + x / P.rx[k]];
+    uint32_t r, g, b;
+    if (P.components == 1) {
+        r = g = b = uint32_t(c[0]);
+    } else if (P.rgb) {
+        r = uint32_t(c[0]);
+        g = uint32_t(c[1]);
+        b = uint32_t(c[2]);
+    } else {
+        const int32_t cb = c[1] - 128, cr = c[2] - 128;
+        r = uint32_t(min(255, max(0, c[0] + ((91881 * cr + 32768) >> 16))));
+        g = uint32_t(min(255, max(0, c[0] + ((-22554 * cb - 46802 * cr + 32768) >> 16))));
+        b = uint32_t(min(255, max(0, c[0] + ((116130 * cb + 32768) >> 16))));
+    }
+    rgba[(size_t)y * P.width + x] = r | (g << 8) | (b << 16) | 0xFF000000u;
+}
+
 }  // namespace
+
+void launch_jpeg_idct(const int16_t* coef, uint32_t blocks_w, uint32_t blocks_h, uint8_t* plane, cudaStream_t stream) {
+    const uint32_t blocks = blocks_w * blocks_h;
+    launch_pdl(k_jpeg_idct, dim3((blocks + kIdctBlocks - 1) / kIdctBlocks), dim3(kIdctBlocks * 8), 0, stream, coef,
+               blocks, blocks_w, plane);
+}
+
+void launch_jpeg_color(const JpegPlanes& P, uint32_t* rgba, cudaStream_t stream) {
+    launch_pdl(k_jpeg_color, dim3((P.width + 31) / 32, (P.height + 7) / 8), dim3(256), 0, stream, P, rgba);
+}
 
 void launch_decode_bc(const uint8_t* blocks, uint32_t format, uint32_t w, uint32_t h, uint32_t* rgba,
                       cudaStream_t stream) {

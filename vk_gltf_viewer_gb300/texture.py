@@ -2,7 +2,8 @@
 ``vkgv_dds_parse``, ``vkgv_decode_bc``).
 
 PNG decodes on the host into RGBA8; DDS files hold BC1-BC5 blocks, which the
-device decodes into RGBA8.  The reference loads no images
+device decodes into RGBA8; JPEG is entropy-decoded on the host and turned
+into pixels on the device.  The reference loads no images
 (src/vk_gltf_viewer/assets.cpp:467-471).
 """
 from __future__ import annotations
@@ -57,9 +58,65 @@ def decode_bc(renderer, fmt: int, blocks, width: int, height: int, stream=None) 
     return out
 
 
+class Jpeg:
+    """A JPEG's entropy decode (host): ``info`` (``abi.JpegInfo``) and its
+    dequantized coefficient planes, ``planes[c]`` of shape
+    (blocks_h, blocks_w, 8, 8) int16 in natural order.  ``to_rgba`` runs the
+    IDCT, upsampling and colour conversion on the device."""
+
+    def __init__(self, data: bytes):
+        self._h = None
+        lib = abi.load()
+        buf = np.frombuffer(data, np.uint8)
+        h = C.c_void_p()
+        err = C.create_string_buffer(256)
+        rc = lib.vkgv_jpeg_decode_coefficients(buf.ctypes.data, buf.size, C.byref(h), err, len(err))
+        if rc != abi.OK:
+            raise abi.VkgvError(rc, err.value.decode(errors="replace"))
+        self._h = h
+        self.info = abi.JpegInfo()
+        abi.check(lib.vkgv_jpeg_get_info(h, C.byref(self.info)))
+
+    @property
+    def planes(self) -> list[np.ndarray]:
+        lib, out = abi.load(), []
+        for c in range(self.info.components):
+            ptr = C.c_void_p()
+            abi.check(lib.vkgv_jpeg_get_coefficients(self._h, c, C.byref(ptr)))
+            bw, bh = self.info.blocks_w[c], self.info.blocks_h[c]
+            out.append(np.frombuffer(C.string_at(ptr.value, bw * bh * 128), np.int16).reshape(bh, bw, 8, 8).copy())
+        return out
+
+    def to_rgba(self, renderer, stream=None) -> torch.Tensor:
+        """Device (height, width, 4) uint8 RGBA."""
+        out = torch.empty((self.info.height, self.info.width, 4), dtype=torch.uint8,
+                          device=torch.device("cuda", renderer.device))
+        abi.check(abi.load().vkgv_jpeg_to_rgba(renderer.ctx, self._h, out.data_ptr(), _stream_handle(stream)),
+                  renderer.ctx)
+        return out
+
+    def close(self):
+        if self._h:
+            abi.load().vkgv_jpeg_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def decode_jpeg(data: bytes, renderer, stream=None) -> torch.Tensor:
+    """JPEG bytes -> device (H, W, 4) uint8 RGBA (entropy decode on the host,
+    the pixels on the device)."""
+    j = Jpeg(data)
+    try:
+        return j.to_rgba(renderer, stream)
+    finally:
+        j.close()
+
+
 def load_image(data: bytes, kind: int, renderer=None) -> np.ndarray:
-    """Encoded image -> host (H, W, 4) uint8 RGBA: PNG on the host, DDS on
-    the device (needs a renderer)."""
+    """Encoded image -> host (H, W, 4) uint8 RGBA: PNG on the host, DDS and
+    JPEG on the device (they need a renderer)."""
     if kind == abi.IMAGE_PNG:
         return decode_png(data)
     if kind == abi.IMAGE_DDS:
@@ -69,5 +126,11 @@ def load_image(data: bytes, kind: int, renderer=None) -> np.ndarray:
         img = decode_bc(renderer, info.format, blocks, info.width, info.height)
         torch.cuda.synchronize()
         return img.cpu().numpy()
-    names = {abi.IMAGE_JPEG: "JPEG", abi.IMAGE_KTX2: "KTX2"}
+    if kind == abi.IMAGE_JPEG:
+        if renderer is None:
+            raise ValueError("JPEG images decode on the device: pass a renderer")
+        img = decode_jpeg(data, renderer)
+        torch.cuda.synchronize()
+        return img.cpu().numpy()
+    names = {abi.IMAGE_KTX2: "KTX2"}
     raise abi.VkgvError(abi.INVALID_ARG, f"{names.get(kind, 'unknown')} images are not decoded")
