@@ -297,7 +297,7 @@ constexpr int32_t kSmallExtent = 1 << 14;
 enum TriKind : int { kDrop = 0, kFast = 1, kSlowClip = 2, kSlowSetup = 3 };
 
 #ifndef VKGV_RASTER_WARPS_PER_SM
-#define VKGV_RASTER_WARPS_PER_SM 32
+#define VKGV_RASTER_WARPS_PER_SM 28
 #endif
 
 // Small triangles whose clamped bbox has at most this many pixels are
