@@ -619,7 +619,11 @@ enum vkgv_block_format {
     VKGV_BC2 = 2,   /* DXT3: explicit 4-bit alpha + BC1 colours                      */
     VKGV_BC3 = 3,   /* DXT5: interpolated alpha + BC1 colours                        */
     VKGV_BC4 = 4,   /* one interpolated channel (R)                                  */
-    VKGV_BC5 = 5    /* two interpolated channels (R, G)                              */
+    VKGV_BC5 = 5,   /* two interpolated channels (R, G)                              */
+    VKGV_BC1_OPAQUE = 6, /* BC1 read as Vulkan's BC1_RGB formats: the three-colour
+                          * mode's fourth entry is opaque black                      */
+    VKGV_RGBA8 = 7  /* uncompressed RGBA8 texels (reported by vkgv_ktx2_parse only;
+                     * not a vkgv_decode_bc format)                                 */
 };
 
 typedef struct vkgv_dds_info {
@@ -627,7 +631,7 @@ typedef struct vkgv_dds_info {
     uint32_t height;
     uint32_t mip_count;
     uint32_t format;         /* vkgv_block_format */
-    uint32_t srgb;           /* DXGI *_UNORM_SRGB */
+    uint32_t srgb;           /* DXGI *_UNORM_SRGB, or a KTX2 *_SRGB vkFormat */
     uint32_t _pad;
     uint64_t data_offset;    /* byte offset of the top mip's blocks */
     uint64_t data_size;      /* bytes of the top mip */
@@ -636,6 +640,15 @@ typedef struct vkgv_dds_info {
 /* Reads a DDS header (FourCC DXT1-5 / ATI1 / ATI2 / BC4U / BC5U, or DX10
  * with a BC1-BC5 DXGI format); VKGV_INVALID_ARG for anything else. */
 int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* out);
+/* Reads a KTX 2.0 header (the container of KHR_texture_basisu, which the
+ * reference enables in fastgltf, assets.cpp:539, and links ktx_read for):
+ * a 2D texture (one layer, one face) without supercompression whose vkFormat
+ * is BC1-BC5 UNORM / SRGB (131-139, 141) or R8G8B8A8 UNORM / SRGB (37, 43),
+ * into the same fields as a DDS file (level 0; format VKGV_BC1_OPAQUE for
+ * BC1_RGB, VKGV_RGBA8 for R8G8B8A8).  BasisU (vkFormat 0) and
+ * supercompressed files, SNORM formats, cube maps, arrays and 3D textures
+ * are VKGV_INVALID_ARG. */
+int vkgv_ktx2_parse(const void* data, uint64_t size, vkgv_dds_info* out);
 /* Decodes width x height texels of BC blocks (device, row-major blocks of
  * 8 or 16 bytes, aligned to the block size) into RGBA8 (device
  * uint32[width * height], 4-byte aligned). */

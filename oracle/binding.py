@@ -409,7 +409,7 @@ def asin_series(z: float) -> float:
 def decode_bc(fmt: int, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
     """BC1-BC5 blocks -> uint32 RGBA8 texels (h, w)."""
     blocks = np.ascontiguousarray(blocks, np.uint8)
-    need = ((w + 3) // 4) * ((h + 3) // 4) * (8 if fmt in (1, 4) else 16)
+    need = ((w + 3) // 4) * ((h + 3) // 4) * (8 if fmt in (1, 4, 6) else 16)
     if blocks.size < need:
         raise ValueError(f"{blocks.size} block bytes, {need} needed")
     out = np.zeros(w * h, np.uint32)

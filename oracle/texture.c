@@ -12,7 +12,9 @@
  *   BC2 alpha: 4-bit value * 17;
  *   8-value channel blocks (a0 > a1): ((7 - j) a0 + j a1 + 3) / 7, j = 1..6;
  *   6-value channel blocks: ((5 - j) a0 + j a1 + 2) / 5, j = 1..4, then 0 and 255.
- * BC4 gives (r, 0, 0, 255), BC5 (r, g, 0, 255).
+ * BC4 gives (r, 0, 0, 255), BC5 (r, g, 0, 255).  Format 6 is BC1 read as
+ * Vulkan's BC1_RGB formats: the three-colour mode's fourth entry is opaque
+ * black.
  */
 #include "oracle.h"
 
@@ -25,7 +27,9 @@ static void expand565(unsigned c, unsigned out[3]) {
     out[2] = (b << 3) | (b >> 2);
 }
 
-/* The 16 RGBA texels of a BC1-layout colour block. */
+/* The 16 RGBA texels of a BC1-layout colour block; three_allowed = 2 is
+ * BC1 read as Vulkan's BC1_RGB formats (the fourth three-mode entry is
+ * opaque black). */
 static void colour_block(const uint8_t* p, int three_allowed, uint32_t out[16]) {
     unsigned c0 = p[0] | (p[1] << 8), c1 = p[2] | (p[3] << 8);
     unsigned pal[4][4];
@@ -45,7 +49,7 @@ static void colour_block(const uint8_t* p, int three_allowed, uint32_t out[16]) 
         }
     }
     pal[0][3] = pal[1][3] = pal[2][3] = 255;
-    pal[3][3] = four ? 255 : 0;
+    pal[3][3] = (four || three_allowed == 2) ? 255 : 0;
     uint32_t bits = (uint32_t)p[4] | ((uint32_t)p[5] << 8) | ((uint32_t)p[6] << 16) | ((uint32_t)p[7] << 24);
     for (int i = 0; i < 16; ++i) {
         unsigned c = (bits >> (2 * i)) & 3u;
@@ -72,7 +76,7 @@ static void channel_block(const uint8_t* p, unsigned out[16]) {
 
 void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t h, uint32_t* rgba) {
     uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
-    size_t bsize = (format == 1 || format == 4) ? 8 : 16;
+    size_t bsize = (format == 1 || format == 4 || format == 6) ? 8 : 16;
     for (uint32_t by = 0; by < bh; ++by)
         for (uint32_t bx = 0; bx < bw; ++bx) {
             const uint8_t* p = blocks + ((size_t)by * bw + bx) * bsize;
@@ -82,6 +86,9 @@ void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t 
             switch (format) {
                 case 1:
                     colour_block(p, 1, tex);
+                    break;
+                case 6:
+                    colour_block(p, 2, tex);
                     break;
                 case 2:
                     colour_block(p + 8, 0, col);

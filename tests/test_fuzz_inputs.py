@@ -1,5 +1,5 @@
 """Malformed inputs to the host-side readers (glTF JSON / GLB with and
-without EXT_meshopt_compression, PNG / DEFLATE, JPEG, DDS): seeded byte mutations, truncations and insertions of valid files
+without EXT_meshopt_compression, PNG / DEFLATE, JPEG, KTX2, DDS): seeded byte mutations, truncations and insertions of valid files
 either load or fail with a status, in a child process so that a crash or a
 hang would fail the test instead of the run."""
 import os
@@ -47,6 +47,8 @@ CHILD = textwrap.dedent("""
                 texture.decode_png(bytes(data))
             elif kind == "jpeg":
                 texture.Jpeg(bytes(data)).close()
+            elif kind == "ktx2":
+                texture.parse_ktx2(bytes(data))
             else:
                 texture.parse_dds(bytes(data))
             ok += 1
@@ -74,7 +76,7 @@ def _asset(tmp_path):
     return b
 
 
-@pytest.mark.parametrize("kind", ["glb", "gltf", "meshopt", "png", "jpeg", "dds"])
+@pytest.mark.parametrize("kind", ["glb", "gltf", "meshopt", "png", "jpeg", "ktx2", "dds"])
 def test_mutated_inputs_fail_cleanly(built, tmp_path, kind):
     if kind == "meshopt":  # EXT_meshopt_compression streams in the GLB's binary chunk
         from test_meshopt import _scene_builder
@@ -89,6 +91,10 @@ def test_mutated_inputs_fail_cleanly(built, tmp_path, kind):
         path = tmp_path / "a.jpg"
         path.write_bytes(jpeg_encode(rng.integers(0, 256, (19, 27, 3)), sampling=((2, 2), (1, 1), (1, 1)),
                                      restart=2, rng=rng)[0])
+    elif kind == "ktx2":
+        from test_texture_decode import _ktx2
+        path = tmp_path / "a.ktx2"
+        path.write_bytes(_ktx2(137, 12, 8, bytes(range(96))))
     elif kind == "png":
         from png_util import encode
         rng = np.random.default_rng(0)

@@ -23,14 +23,14 @@ from test_texture_decode import _dds
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("fmt", [abi.BC1, abi.BC2, abi.BC3, abi.BC4, abi.BC5])
+@pytest.mark.parametrize("fmt", [abi.BC1, abi.BC2, abi.BC3, abi.BC4, abi.BC5, abi.BC1_OPAQUE])
 @pytest.mark.parametrize("size", [(4, 4), (37, 21), (256, 128), (3, 5)])
 def test_bc_decode_matches_oracle(renderer, fmt, size):
     w, h = size
     rng = np.random.default_rng(fmt * 1000 + w)
-    bsize = 8 if fmt in (abi.BC1, abi.BC4) else 16
+    bsize = 8 if fmt in (abi.BC1, abi.BC4, abi.BC1_OPAQUE) else 16
     blocks = rng.integers(0, 256, size=((w + 3) // 4) * ((h + 3) // 4) * bsize, dtype=np.uint8)
-    if fmt in (abi.BC1, abi.BC4):  # both orders of the two end points
+    if fmt in (abi.BC1, abi.BC4, abi.BC1_OPAQUE):  # both orders of the two end points
         blocks[::16] = np.minimum(blocks[::16], 127)
     got = texture.decode_bc(renderer, fmt, blocks, w, h)
     torch.cuda.synchronize()
@@ -53,6 +53,16 @@ def test_jpeg_pixels_match_oracle(renderer, case, size):
     torch.cuda.synchronize()
     exp = ob.jpeg_rgba(j.info, [p.reshape(-1) for p in j.planes])
     assert np.array_equal(got.cpu().numpy().view(np.uint32)[..., 0], exp)
+
+
+def test_ktx2_through_load_image(renderer):
+    from test_texture_decode import _ktx2
+
+    rng = np.random.default_rng(4)
+    for vk, fmt, bsize in ((131, abi.BC1_OPAQUE, 8), (137, abi.BC3, 16), (141, abi.BC5, 16)):
+        blocks = rng.integers(0, 256, 10 * 6 * bsize, dtype=np.uint8)
+        got = texture.load_image(_ktx2(vk, 37, 22, blocks.tobytes()), abi.IMAGE_KTX2, renderer)
+        assert np.array_equal(got.view(np.uint32)[..., 0], ob.decode_bc(fmt, blocks, 37, 22))
 
 
 def test_jpeg_through_load_image_and_freed_source(renderer):

@@ -1,8 +1,10 @@
 """Texture decode on the host: the PNG decoder returns exactly the pixels a
 PNG encoder was given, for every colour type and bit depth, every filter
 type, Adam7 interlacing, tRNS, split IDAT chunks and stored / fixed /
-dynamic DEFLATE blocks; corrupt files are refused.  The DDS header reader,
-and the oracle's BC decoder on hand-derived blocks."""
+dynamic DEFLATE blocks; corrupt files are refused.  The DDS and KTX2 header
+readers, the importer's choice of texture source, and the oracle's BC
+decoder on hand-derived blocks."""
+import ctypes as C
 import struct
 import zlib
 
@@ -137,3 +139,82 @@ def test_oracle_bc_known_answers(built):
     out = ob.decode_bc(abi.BC2, np.frombuffer(blk, np.uint8), 4, 4)
     assert out[0, 0] == _rgba(85, 0, 170, 0) and out[0, 1] == _rgba(0, 0, 255, 17)
     assert out[0, 2] >> 24 == 5 * 17 and out[0, 3] >> 24 == 255
+
+
+def _ktx2(vk_format: int, w: int, h: int, payload: bytes, scheme: int = 0, faces: int = 1, layers: int = 0,
+          depth: int = 0) -> bytes:
+    """A KTX 2.0 file with one level (no DFD or key/value data)."""
+    ident = bytes([0xAB, 0x4B, 0x54, 0x58, 0x20, 0x32, 0x30, 0xBB, 0x0D, 0x0A, 0x1A, 0x0A])
+    header = struct.pack("<9I", vk_format, 1, w, h, depth, layers, faces, 1, scheme)
+    index = struct.pack("<4I2Q", 0, 0, 0, 0, 0, 0)
+    offset = 12 + len(header) + len(index) + 24
+    offset += -offset % 16
+    level = struct.pack("<3Q", offset, len(payload), len(payload))
+    head = ident + header + index + level
+    return head + bytes(offset - len(head)) + payload
+
+
+def test_ktx2_headers(built):
+    blocks = bytes(range(8)) * 6  # 3 x 2 blocks of 8 bytes
+    for vk, fmt, srgb in ((133, abi.BC1, 0), (131, abi.BC1_OPAQUE, 0), (132, abi.BC1_OPAQUE, 1), (139, abi.BC4, 0)):
+        info, got = texture.parse_ktx2(_ktx2(vk, 11, 6, blocks))
+        assert (info.width, info.height, info.format, info.srgb) == (11, 6, fmt, srgb)
+        assert got.tobytes() == blocks
+    info, _ = texture.parse_ktx2(_ktx2(138, 8, 4, bytes(32)))
+    assert (info.format, info.srgb) == (abi.BC3, 1)
+    rgba = bytes(range(256)) * 3
+    info, got = texture.parse_ktx2(_ktx2(43, 16, 12, rgba))
+    assert (info.format, info.srgb, info.data_size) == (abi.RGBA8, 1, 768)
+    assert np.array_equal(texture.load_image(_ktx2(37, 16, 12, rgba), abi.IMAGE_KTX2).reshape(-1),
+                          np.frombuffer(rgba, np.uint8))
+    bad = [_ktx2(0, 4, 4, bytes(64)),                  # BasisU (vkFormat undefined)
+           _ktx2(133, 4, 4, bytes(8), scheme=2),       # zstd supercompression
+           _ktx2(133, 4, 4, bytes(48), faces=6),       # cube map
+           _ktx2(140, 4, 4, bytes(8)),                 # BC4 SNORM
+           _ktx2(146, 4, 4, bytes(16)),                # BC7
+           _ktx2(133, 16, 16, bytes(8)),               # too little data
+           b"DDS " + bytes(200)]
+    for data in bad:
+        with pytest.raises(abi.VkgvError):
+            texture.parse_ktx2(data)
+
+
+def test_oracle_bc1_opaque_known_answer(built):
+    """Vulkan's BC1_RGB formats: the three-colour mode's fourth entry is
+    opaque black instead of transparent black."""
+    blk = struct.pack("<HHI", 0x001F, 0xF800, 0b11100100)
+    out = ob.decode_bc(abi.BC1_OPAQUE, np.frombuffer(blk, np.uint8), 4, 4)
+    assert list(out[0]) == [_rgba(0, 0, 255), _rgba(255, 0, 0), _rgba(128, 0, 128), _rgba(0, 0, 0, 255)]
+
+
+def test_gltf_texture_sources(built, tmp_path):
+    """MSFT_texture_dds takes precedence; a KHR_texture_basisu (KTX2) source
+    is used only when the texture has no base source; the extensions the
+    reference enables may be required."""
+    from test_gltf_import import make_asset
+
+    b, _ = make_asset()
+    ktx = _ktx2(133, 4, 4, bytes(8))
+    dds = _dds(b"DXT1", 4, 4, bytes(8))
+    png = encode(np.zeros((2, 2, 4), np.int64), 6, 8, np.random.default_rng(0))
+    views = [b._view(x) for x in (png, ktx, dds)]
+    b.gltf["images"] = [{"bufferView": v, "mimeType": m} for v, m in
+                        zip(views, ["image/png", "image/ktx2", "image/vnd-ms.dds"])]
+    b.gltf["textures"] = [{"source": 0, "extensions": {"KHR_texture_basisu": {"source": 1}}},
+                          {"extensions": {"KHR_texture_basisu": {"source": 1}}},
+                          {"source": 0, "extensions": {"MSFT_texture_dds": {"source": 2}}}]
+    b.gltf["extensionsRequired"] = ["KHR_texture_basisu", "MSFT_texture_dds", "KHR_lights_punctual"]
+    path = b.write_glb(tmp_path / "t.glb")
+    lib = abi.load()
+    h = C.c_void_p()
+    err = C.create_string_buffer(256)
+    assert lib.vkgv_gltf_load(str(path).encode(), abi.GLTF_IMAGES, C.byref(h), err, len(err)) == abi.OK, err.value
+    try:
+        kinds = []
+        for t in range(3):
+            gi = abi.GltfImage()
+            abi.check(lib.vkgv_gltf_get_texture_image(h, t, C.byref(gi)))
+            kinds.append(gi.kind)
+    finally:
+        lib.vkgv_gltf_free(h)
+    assert kinds == [abi.IMAGE_PNG, abi.IMAGE_KTX2, abi.IMAGE_DDS]

@@ -678,10 +678,10 @@ int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, 
 int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
                    uint64_t rgba_out, void* stream_) {
     if (!ctx) return VKGV_INVALID_ARG;
-    if (format < VKGV_BC1 || format > VKGV_BC5) return fail(ctx, VKGV_INVALID_ARG, "unknown block format");
+    if (format < VKGV_BC1 || format > VKGV_BC1_OPAQUE) return fail(ctx, VKGV_INVALID_ARG, "unknown block format");
     if (width == 0 || height == 0) return VKGV_OK;
     if (width > 16384 || height > 16384) return fail(ctx, VKGV_LIMIT_EXCEEDED, "texture edge exceeds 16384");
-    const uint64_t block_align = (format == VKGV_BC1 || format == VKGV_BC4) ? 8u : 16u;
+    const uint64_t block_align = (format == VKGV_BC1 || format == VKGV_BC4 || format == VKGV_BC1_OPAQUE) ? 8u : 16u;
     if (!blocks || !rgba_out || (blocks & (block_align - 1)) || (rgba_out & 3u))
         return fail(ctx, VKGV_INVALID_ARG, "blocks must be aligned to the block size and rgba_out to 4 bytes");
     launch_decode_bc(reinterpret_cast<const uint8_t*>(blocks), format, width, height,

@@ -711,8 +711,14 @@ void check_asset(const JValue& root) {
         fail("not a glTF 2.0 asset");
     for (const JValue& e : array_of(root, "extensionsRequired").items) {
         if (e.kind != JValue::String) continue;
-        if (e.s != "KHR_mesh_quantization" && e.s != "KHR_texture_transform" && e.s != "EXT_meshopt_compression")
-            fail("required extension " + e.s + " is not supported");
+        // the extensions the reference enables in its parser (assets.cpp:536-541);
+        // KHR_lights_punctual is read by nothing on this path
+        static const char* const kKnown[] = {"EXT_meshopt_compression", "KHR_mesh_quantization",
+                                             "KHR_texture_transform", "KHR_texture_basisu", "MSFT_texture_dds",
+                                             "KHR_lights_punctual"};
+        bool known = false;
+        for (const char* k : kKnown) known = known || e.s == k;
+        if (!known) fail("required extension " + e.s + " is not supported");
     }
 }
 
@@ -841,15 +847,20 @@ void import_asset(vkgv_gltf& G, const JValue& root, const std::vector<std::vecto
     G.texture_count = uint32_t(array_of(root, "textures").items.size());
     G.image_count = uint32_t(array_of(root, "images").items.size());
     if (flags & VKGV_GLTF_IMAGES) {
-        // each texture's image; a MSFT_texture_dds source takes precedence
+        // each texture's image: a MSFT_texture_dds source takes precedence;
+        // a KHR_texture_basisu (KTX2) source is used only without a base
+        // source, which then is the fallback for BasisU-compressed KTX2
         const JValue& images = array_of(root, "images");
         const JValue& textures = array_of(root, "textures");
         G.texture_images.assign(textures.items.size(), std::vector<uint8_t>());
         for (size_t t = 0; t < textures.items.size(); ++t) {
             const JValue& tx = textures.items[t];
             int64_t src = index_of(tx, "source");
-            if (const JValue* ext = tx.get("extensions"))
+            if (const JValue* ext = tx.get("extensions")) {
+                if (const JValue* ktx = ext->get("KHR_texture_basisu"))
+                    if (src < 0) src = index_of(*ktx, "source");
                 if (const JValue* dds = ext->get("MSFT_texture_dds")) src = index_of(*dds, "source", src);
+            }
             if (src < 0) continue;
             if (size_t(src) >= images.items.size()) fail("texture source out of range");
             G.texture_images[t] = image_bytes(images.items[size_t(src)], root, buffers, dir);

@@ -519,3 +519,56 @@ extern "C" int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* ou
     if (out->width == 0 || out->height == 0 || offset + out->data_size > size) return VKGV_INVALID_ARG;
     return VKGV_OK;
 }
+
+// KTX 2.0: the 12-byte identifier, nine uint32 header words (vkFormat,
+// typeSize, pixelWidth, pixelHeight, pixelDepth, layerCount, faceCount,
+// levelCount, supercompressionScheme), the index (DFD and KVD offsets and
+// lengths as uint32, SGD as uint64) and one {byteOffset, byteLength,
+// uncompressedByteLength} uint64 triple per level, level 0 the largest.
+extern "C" int vkgv_ktx2_parse(const void* data, uint64_t size, vkgv_dds_info* out) {
+    static const uint8_t kId[12] = {0xAB, 'K', 'T', 'X', ' ', '2', '0', 0xBB, '\r', '\n', 0x1A, '\n'};
+    if (!data || !out) return VKGV_INVALID_ARG;
+    const uint8_t* p = static_cast<const uint8_t*>(data);
+    std::memset(out, 0, sizeof(*out));
+    if (size < 80 + 24 || std::memcmp(p, kId, 12) != 0) return VKGV_INVALID_ARG;
+    const uint32_t vk_format = le32(p + 12), width = le32(p + 20), height = le32(p + 24);
+    const uint32_t depth = le32(p + 28), layers = le32(p + 32), faces = le32(p + 36);
+    const uint32_t levels = le32(p + 40), scheme = le32(p + 44);
+    if (scheme != 0 || vk_format == 0) return VKGV_INVALID_ARG;  // BasisU / supercompressed
+    if (width == 0 || height == 0 || depth > 1 || layers > 1 || faces != 1) return VKGV_INVALID_ARG;
+    uint32_t fmt = 0, srgb = 0;
+    switch (vk_format) {  // VkFormat values
+        case 131: fmt = VKGV_BC1_OPAQUE; break;           // BC1_RGB_UNORM_BLOCK
+        case 132: fmt = VKGV_BC1_OPAQUE; srgb = 1; break;  // BC1_RGB_SRGB_BLOCK
+        case 133: fmt = VKGV_BC1; break;
+        case 134: fmt = VKGV_BC1; srgb = 1; break;
+        case 135: fmt = VKGV_BC2; break;
+        case 136: fmt = VKGV_BC2; srgb = 1; break;
+        case 137: fmt = VKGV_BC3; break;
+        case 138: fmt = VKGV_BC3; srgb = 1; break;
+        case 139: fmt = VKGV_BC4; break;                   // BC4_UNORM_BLOCK
+        case 141: fmt = VKGV_BC5; break;                   // BC5_UNORM_BLOCK
+        case 37: fmt = VKGV_RGBA8; break;                  // R8G8B8A8_UNORM
+        case 43: fmt = VKGV_RGBA8; srgb = 1; break;        // R8G8B8A8_SRGB
+        default: return VKGV_INVALID_ARG;
+    }
+    uint64_t offset, length;
+    std::memcpy(&offset, p + 80, 8);
+    std::memcpy(&length, p + 88, 8);
+    uint64_t need;
+    if (fmt == VKGV_RGBA8) {
+        need = uint64_t(width) * height * 4;
+    } else {
+        const uint64_t bw = (uint64_t(width) + 3) / 4, bh = (uint64_t(height) + 3) / 4;
+        need = bw * bh * ((fmt == VKGV_BC1 || fmt == VKGV_BC4 || fmt == VKGV_BC1_OPAQUE) ? 8u : 16u);
+    }
+    if (length < need || offset > size || size - offset < need) return VKGV_INVALID_ARG;
+    out->width = width;
+    out->height = height;
+    out->mip_count = levels ? levels : 1;
+    out->format = fmt;
+    out->srgb = srgb;
+    out->data_offset = offset;
+    out->data_size = need;
+    return VKGV_OK;
+}

@@ -7,7 +7,8 @@
 //   RGB565 -> 8 bits: (r5 << 3 | r5 >> 2), (g6 << 2 | g6 >> 4)
 //   BC1 (c0 > c1) and BC2/BC3 colours: c2 = (2 c0 + c1 + 1) / 3,
 //                                      c3 = (c0 + 2 c1 + 1) / 3
-//   BC1 (c0 <= c1): c2 = (c0 + c1 + 1) / 2, c3 = transparent black
+//   BC1 (c0 <= c1): c2 = (c0 + c1 + 1) / 2, c3 = transparent black (opaque
+//     black for VKGV_BC1_OPAQUE, Vulkan's BC1_RGB formats)
 //   BC2 alpha: a4 * 17
 //   BC3 alpha / BC4 / BC5 channels (a0 > a1): a_i = ((7 - i) a0 + i a1 + 3) / 7
 //     for the interpolated codes i = 1..6 (indices 2..7);
@@ -33,7 +34,7 @@ __device__ __forceinline__ uint32_t rgb565(uint32_t c) {
 __device__ __forceinline__ uint32_t ch(uint32_t c, int k) { return (c >> (8 * k)) & 255u; }
 
 // The four RGBA entries of a BC1-layout colour block (words lo = c0 | c1 << 16).
-__device__ __forceinline__ void colour_palette(uint32_t lo, bool allow_three, uint32_t pal[4]) {
+__device__ __forceinline__ void colour_palette(uint32_t lo, bool allow_three, bool opaque, uint32_t pal[4]) {
     const uint32_t c0 = lo & 0xFFFFu, c1 = lo >> 16;
     const uint32_t a = rgb565(c0), b = rgb565(c1);
     const bool four = !allow_three || c0 > c1;
@@ -47,7 +48,7 @@ __device__ __forceinline__ void colour_palette(uint32_t lo, bool allow_three, ui
     pal[0] = a | 0xFF000000u;
     pal[1] = b | 0xFF000000u;
     pal[2] = p2 | 0xFF000000u;
-    pal[3] = four ? (p3 | 0xFF000000u) : 0u;
+    pal[3] = four ? (p3 | 0xFF000000u) : (opaque ? 0xFF000000u : 0u);
 }
 
 // The 4 values of row r of an interpolated channel block (8 bytes, as lo/hi
@@ -89,9 +90,10 @@ __device__ __forceinline__ void decode_row(const uint4& q, uint32_t format, uint
         return;
     }
     // colour block: words 0-1 (BC1) or 2-3 (BC2 / BC3, always four colours)
-    const uint32_t clo = format == VKGV_BC1 ? q.x : q.z, cidx = format == VKGV_BC1 ? q.y : q.w;
+    const bool bc1 = format == VKGV_BC1 || format == VKGV_BC1_OPAQUE;
+    const uint32_t clo = bc1 ? q.x : q.z, cidx = bc1 ? q.y : q.w;
     uint32_t pal[4];
-    colour_palette(clo, format == VKGV_BC1, pal);
+    colour_palette(clo, bc1, format == VKGV_BC1_OPAQUE, pal);
     const uint32_t row = (cidx >> (8 * r)) & 255u;
 #pragma unroll
     for (int x = 0; x < 4; ++x) texel[x] = pal[(row >> (2 * x)) & 3u];
@@ -119,7 +121,7 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc(const uint8_t* 
     const uint32_t bx = (blockIdx.x * kDecodeWarps + warp) * 8 + (lane >> 2);
     const uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
     if (bx >= bw) return;
-    const bool wide = format != VKGV_BC1 && format != VKGV_BC4;
+    const bool wide = format != VKGV_BC1 && format != VKGV_BC4 && format != VKGV_BC1_OPAQUE;
     uint4 q[kDecodeDepth];
 #pragma unroll
     for (int k = 0; k < kDecodeDepth; ++k) {

@@ -46,6 +46,18 @@ def parse_dds(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
     return info, blocks
 
 
+def parse_ktx2(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
+    """KTX2 bytes -> (header info, level 0's bytes): BC1-BC5 blocks or
+    RGBA8 texels (``info.format`` is ``abi.RGBA8`` for those)."""
+    buf = np.frombuffer(data, np.uint8)
+    info = abi.DdsInfo()
+    rc = abi.load().vkgv_ktx2_parse(buf.ctypes.data, buf.size, C.byref(info))
+    if rc != abi.OK:
+        raise abi.VkgvError(rc, "not a KTX2 file with uncompressed BC1-BC5 or RGBA8 data "
+                                "(BasisU and supercompressed files are not decoded)")
+    return info, buf[info.data_offset:info.data_offset + info.data_size].copy()
+
+
 def decode_bc(renderer, fmt: int, blocks, width: int, height: int, stream=None) -> torch.Tensor:
     """BC1-BC5 blocks -> device (height, width, 4) uint8 RGBA, decoded by
     k_decode_bc.  `blocks` is a numpy array or a device tensor of bytes."""
@@ -115,8 +127,9 @@ def decode_jpeg(data: bytes, renderer, stream=None) -> torch.Tensor:
 
 
 def load_image(data: bytes, kind: int, renderer=None) -> np.ndarray:
-    """Encoded image -> host (H, W, 4) uint8 RGBA: PNG on the host, DDS and
-    JPEG on the device (they need a renderer)."""
+    """Encoded image -> host (H, W, 4) uint8 RGBA: PNG and RGBA8 KTX2 on the
+    host; DDS, block-compressed KTX2 and JPEG on the device (they need a
+    renderer)."""
     if kind == abi.IMAGE_PNG:
         return decode_png(data)
     if kind == abi.IMAGE_DDS:
@@ -132,5 +145,13 @@ def load_image(data: bytes, kind: int, renderer=None) -> np.ndarray:
         img = decode_jpeg(data, renderer)
         torch.cuda.synchronize()
         return img.cpu().numpy()
-    names = {abi.IMAGE_KTX2: "KTX2"}
-    raise abi.VkgvError(abi.INVALID_ARG, f"{names.get(kind, 'unknown')} images are not decoded")
+    if kind == abi.IMAGE_KTX2:
+        info, payload = parse_ktx2(data)
+        if info.format == abi.RGBA8:
+            return payload.reshape(info.height, info.width, 4)
+        if renderer is None:
+            raise ValueError("KTX2 block-compressed images decode on the device: pass a renderer")
+        img = decode_bc(renderer, info.format, payload, info.width, info.height)
+        torch.cuda.synchronize()
+        return img.cpu().numpy()
+    raise abi.VkgvError(abi.INVALID_ARG, "unknown image format")
