@@ -656,10 +656,11 @@ int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t wid
                    uint64_t rgba_out, void* stream);
 
 /* JPEG (the reference links wuffs for it, wuffs_implementation.cpp:1-5):
- * sequential DCT, Huffman, 8-bit; 1 component or 3 (YCbCr, or RGB per an
- * Adobe transform 0 / component ids 'R','G','B'); sampling factors 1-4 with
- * integral ratios; restart intervals; interleaved or single-component
- * scans.  Progressive, lossless and arithmetic-coded files are refused.
+ * sequential or progressive DCT, Huffman, 8-bit; 1 component or 3 (YCbCr,
+ * or RGB per an Adobe transform 0 / component ids 'R','G','B'); sampling
+ * factors 1-4 with integral ratios; restart intervals; interleaved or
+ * single-component scans.  Lossless, hierarchical and arithmetic-coded
+ * files are refused.
  * The entropy decode runs on the host into dequantized coefficient planes;
  * vkgv_jpeg_to_rgba runs the IDCT, chroma upsampling (replication) and the
  * JFIF colour conversion on the device, in pinned fixed-point arithmetic. */

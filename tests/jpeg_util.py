@@ -1,8 +1,9 @@
-"""A baseline JPEG encoder for the decoder tests (ITU-T T.81, sequential DCT,
-Huffman): grey, YCbCr (JFIF) or RGB (Adobe transform 0, or component ids
+"""A JPEG encoder for the decoder tests (ITU-T T.81, sequential or
+progressive DCT, Huffman): grey, YCbCr (JFIF) or RGB (Adobe transform 0, or component ids
 'R', 'G', 'B'); any sampling factors with integral ratios; 8- or 16-bit
 quantisation tables; restart intervals; interleaved or one scan per
-component.  Huffman tables are built from the symbol frequencies (lengths
+component; progressive scan scripts with spectral bands, successive
+approximation and end-of-band runs.  Huffman tables are built from the symbol frequencies (lengths
 limited to 16 by the standard's adjustment, the all-ones code reserved), so
 no standard table is needed.  Returns the file and the dequantized
 natural-order coefficients the decoder must produce, per component, in the
@@ -134,8 +135,11 @@ def _blocks(plane: np.ndarray, bw: int, bh: int) -> np.ndarray:
 
 def encode(image: np.ndarray, mode: str = "ycc", sampling=((1, 1), (1, 1), (1, 1)), quality: int = 90,
            restart: int = 0, interleaved: bool = True, rgb_ids: bool = False, qt16: bool = False,
-           rng=None) -> tuple[bytes, list[np.ndarray]]:
-    """image: (H, W) grey or (H, W, 3) RGB uint8."""
+           progressive: bool = False, rng=None) -> tuple[bytes, list[np.ndarray]]:
+    """image: (H, W) grey or (H, W, 3) RGB uint8.  With `progressive`, a
+    SOF2 file whose scan script (DC first and refinement scans, interleaved
+    when `interleaved`; AC bands with successive approximation) is drawn
+    from `rng`."""
     rng = rng or np.random.default_rng(0)
     img = np.asarray(image, np.float64)
     h, w = img.shape[:2]
@@ -171,11 +175,15 @@ def encode(image: np.ndarray, mode: str = "ycc", sampling=((1, 1), (1, 1), (1, 1
         quant.append(qc)
         deq = np.clip(qc * q, -32768, 32767).astype(np.int16)
         scan_dims.append((-(-cw // 8), -(-ch // 8)))
+        sw, sh = scan_dims[-1]
+        mask = np.zeros((bh, bw), bool)
+        mask[:sh, :sw] = True
         if single:  # a one-component scan codes only the blocks the image needs
-            sw, sh = scan_dims[-1]
-            mask = np.zeros((bh, bw), bool)
-            mask[:sh, :sw] = True
             deq[~mask] = 0
+        elif progressive:  # AC scans have one component; DC scans cover the MCUs
+            ac = deq.copy()
+            ac[..., 0, 0] = 0
+            deq[~mask] -= ac[~mask]
         expected.append(deq)
 
     def block_symbols(qc, pred):
@@ -211,6 +219,10 @@ def encode(image: np.ndarray, mode: str = "ycc", sampling=((1, 1), (1, 1), (1, 1
         for c in range(len(comps)):
             sw, sh = scan_dims[c]
             scan_list.append(([c], [[(c, [(bx, by)])] for by in range(sh) for bx in range(sw)]))
+
+    if progressive:
+        return _write(_progressive_scans(quant, sampling, mcux, mcuy, scan_dims, restart, single, rng), mode, rgb_ids,
+                      tables, tq, qt16, ids_for(rgb_ids), h, w, sampling, len(comps), restart, True), expected
 
     # symbols per scan, then tables from all frequencies
     coded = []
@@ -279,3 +291,199 @@ def encode(image: np.ndarray, mode: str = "ycc", sampling=((1, 1), (1, 1), (1, 1
         out += bw_.out
     out += b"\xff\xd9"
     return bytes(out), expected
+
+
+def ids_for(rgb_ids: bool) -> list[int]:
+    return [ord("R"), ord("G"), ord("B")] if rgb_ids else [1, 2, 3]
+
+
+def _extra(v: int, size: int) -> int:
+    return v if v >= 0 else v + (1 << size) - 1
+
+
+def _progressive_scans(quant, sampling, mcux, mcuy, scan_dims, restart, single, rng):
+    """A random valid scan script and each scan's items: ("huff", class,
+    table, symbol), ("raw", value, bits) and ("rst",)."""
+    nc = len(quant)
+    t_of = lambda c: 0 if c == 0 else 1
+    scans = []
+    al0 = int(rng.integers(0, 3))  # DC point transform, refined down to 0
+    dc_groups = [list(range(nc))] if (not single and nc > 1) else [[c] for c in range(nc)]
+    script = [("dc", g, 0, 0, 0, al0) for g in dc_groups]
+    for c in range(nc):
+        a0 = int(rng.integers(0, 3))
+        split = int(rng.integers(1, 63))
+        script += [("ac", [c], 1, split, 0, a0), ("ac", [c], split + 1, 63, 0, a0)]
+        for al in range(a0 - 1, -1, -1):
+            if rng.random() < 0.5:
+                script.append(("ac", [c], 1, 63, al + 1, al))
+            else:
+                script += [("ac", [c], 1, split, al + 1, al), ("ac", [c], split + 1, 63, al + 1, al)]
+    for al in range(al0 - 1, -1, -1):
+        script += [("dc", g, 0, 0, al + 1, al) for g in dc_groups]
+    # each coefficient's bits in order: the DC first scans, the AC scans from
+    # the highest Al down (first scans before their refinements), then the
+    # DC refinements (a stable sort keeps the bands' order)
+    script.sort(key=lambda x: (0 if x[0] == "dc" and x[4] == 0 else 2 if x[0] == "dc" else 1, -x[5]))
+    zz = ZZ
+    for kind, comps_in, ss, se, ah, al in script:
+        items = []
+        if kind == "dc" and len(comps_in) > 1:
+            units = [[(c, [(ux * sampling[c][0] + x, uy * sampling[c][1] + y)
+                           for y in range(sampling[c][1]) for x in range(sampling[c][0])]) for c in comps_in]
+                     for uy in range(mcuy) for ux in range(mcux)]
+        else:
+            c = comps_in[0]
+            sw, shh = scan_dims[c]
+            units = [[(c, [(bx, by)])] for by in range(shh) for bx in range(sw)]
+        pred = {c: 0 for c in comps_in}
+        eob = {"run": 0, "bits": []}
+        cap = int(rng.choice([1, 3, 40, 32767]))
+
+        def flush_eob():
+            if eob["run"]:
+                r = eob["run"].bit_length() - 1
+                items.append(("huff", "ac", t_of(comps_in[0]), r << 4))
+                if r:
+                    items.append(("raw", eob["run"] - (1 << r), r))
+                items.extend(("raw", b, 1) for b in eob["bits"])
+                eob["run"], eob["bits"] = 0, []
+
+        for i, unit in enumerate(units):
+            if restart and i and i % restart == 0:
+                flush_eob()
+                items.append(("rst",))
+                pred = {c: 0 for c in comps_in}
+            for c, coords in unit:
+                for (bx, by) in coords:
+                    q = [int(v) for v in quant[c][by, bx].reshape(64)]
+                    zq = [q[zz[k]] for k in range(64)]
+                    if kind == "dc" and ah == 0:
+                        v = zq[0] >> al
+                        diff = v - pred[c]
+                        pred[c] = v
+                        sz = _sizes(diff)
+                        items.append(("huff", "dc", t_of(c), sz))
+                        if sz:
+                            items.append(("raw", _extra(diff, sz), sz))
+                    elif kind == "dc":
+                        items.append(("raw", (zq[0] >> al) & 1, 1))
+                    elif ah == 0:
+                        vals = [(1 if zq[k] > 0 else -1) * (abs(zq[k]) >> al) for k in range(ss, se + 1)]
+                        nz = [j for j, v in enumerate(vals) if v]
+                        if not nz:
+                            eob["run"] += 1
+                            if eob["run"] == cap:
+                                flush_eob()
+                            continue
+                        flush_eob()
+                        run = 0
+                        for j, v in enumerate(vals[:nz[-1] + 1]):
+                            if v == 0:
+                                run += 1
+                                continue
+                            while run > 15:
+                                items.append(("huff", "ac", t_of(c), 0xF0))
+                                run -= 16
+                            sz = _sizes(v)
+                            items.append(("huff", "ac", t_of(c), (run << 4) | sz))
+                            items.append(("raw", _extra(v, sz), sz))
+                            run = 0
+                        if nz[-1] < se - ss:
+                            eob["run"] = 1
+                            if cap == 1:
+                                flush_eob()
+                    else:
+                        # refinement: history = bits above al; corrections for
+                        # coefficients already nonzero, new ones as run/size 1
+                        events = []  # ("corr", bit) / ("zero",) since the last symbol
+                        last_new = -1
+                        band = list(range(ss, se + 1))
+                        new_pos = [k for k in band if (abs(zq[k]) >> (al + 1)) == 0 and (abs(zq[k]) >> al) == 1]
+                        if new_pos:
+                            flush_eob()
+                        for k in band:
+                            a = abs(zq[k]) >> al
+                            if (abs(zq[k]) >> (al + 1)) != 0:
+                                events.append(("corr", a & 1))
+                            elif a == 0:
+                                events.append(("zero",))
+                            else:
+                                while sum(1 for e in events if e[0] == "zero") >= 16:
+                                    items.append(("huff", "ac", t_of(c), 0xF0))
+                                    zeros = 0
+                                    while zeros < 16:
+                                        e = events.pop(0)
+                                        if e[0] == "zero":
+                                            zeros += 1
+                                        else:
+                                            items.append(("raw", e[1], 1))
+                                r = sum(1 for e in events if e[0] == "zero")
+                                items.append(("huff", "ac", t_of(c), (r << 4) | 1))
+                                items.append(("raw", 1 if zq[k] > 0 else 0, 1))
+                                items.extend(("raw", e[1], 1) for e in events if e[0] == "corr")
+                                events = []
+                                last_new = k
+                        if last_new != se:
+                            # the rest of the band (its correction bits) joins an end-of-band run
+                            eob["run"] += 1
+                            eob["bits"].extend(e[1] for e in events if e[0] == "corr")
+                            if eob["run"] == cap:
+                                flush_eob()
+        flush_eob()
+        scans.append((comps_in, ss, se, ah, al, items))
+    return scans
+
+
+def _write(scans, mode, rgb_ids, tables, tq, qt16, ids, h, w, sampling, ncomp, restart, progressive) -> bytes:
+    out = bytearray(b"\xff\xd8")
+
+    def seg(marker: int, body: bytes):
+        out.extend(struct.pack(">BBH", 0xFF, marker, len(body) + 2) + body)
+
+    if mode == "rgb" and not rgb_ids:
+        seg(0xEE, b"Adobe" + struct.pack(">HHHB", 100, 0, 0, 0))
+    elif mode != "rgb":
+        seg(0xE0, b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00")
+    for t in sorted(set(tq)):
+        vals = [int(tables[t][ZZ[k]]) for k in range(64)]
+        if qt16:
+            seg(0xDB, bytes([0x10 | t]) + struct.pack(">64H", *vals))
+        else:
+            seg(0xDB, bytes([t] + vals))
+    sof = struct.pack(">BHHB", 8, h, w, ncomp)
+    for c in range(ncomp):
+        sof += bytes([ids[c], (sampling[c][0] << 4) | sampling[c][1], tq[c]])
+    seg(0xC2 if progressive else 0xC0, sof)
+    if restart:
+        seg(0xDD, struct.pack(">H", restart))
+    for comps_in, ss, se, ah, al, items in scans:
+        freq = {}
+        for it in items:
+            if it[0] == "huff":
+                d = freq.setdefault((it[1], it[2]), {})
+                d[it[3]] = d.get(it[3], 0) + 1
+        huff = {k: Table(v) for k, v in freq.items()}
+        for (kind, t), table in sorted(huff.items()):
+            seg(0xC4, table.segment(0 if kind == "dc" else 1, t))
+        sos = bytes([len(comps_in)])
+        for c in comps_in:
+            t = 0 if c == 0 else 1
+            sos += bytes([ids[c], (t << 4) | t])
+        seg(0xDA, sos + bytes([ss, se, (ah << 4) | al]))
+        bw = BitWriter()
+        rst = 0
+        for it in items:
+            if it[0] == "rst":
+                bw.pad()
+                bw.out += bytes([0xFF, 0xD0 + rst])
+                rst = (rst + 1) & 7
+            elif it[0] == "huff":
+                code, n = huff[(it[1], it[2])].code[it[3]]
+                bw.put(code, n)
+            else:
+                bw.put(it[1], it[2])
+        bw.pad()
+        out += bw.out
+    out += b"\xff\xd9"
+    return bytes(out)

@@ -45,7 +45,7 @@ CHILD = textwrap.dedent("""
                 gltf.load(out, images=False)
             elif kind == "png":
                 texture.decode_png(bytes(data))
-            elif kind == "jpeg":
+            elif kind in ("jpeg", "jpeg_progressive"):
                 texture.Jpeg(bytes(data)).close()
             elif kind == "ktx2":
                 texture.parse_ktx2(bytes(data))
@@ -76,7 +76,7 @@ def _asset(tmp_path):
     return b
 
 
-@pytest.mark.parametrize("kind", ["glb", "gltf", "meshopt", "png", "jpeg", "ktx2", "dds"])
+@pytest.mark.parametrize("kind", ["glb", "gltf", "meshopt", "png", "jpeg", "jpeg_progressive", "ktx2", "dds"])
 def test_mutated_inputs_fail_cleanly(built, tmp_path, kind):
     if kind == "meshopt":  # EXT_meshopt_compression streams in the GLB's binary chunk
         from test_meshopt import _scene_builder
@@ -85,12 +85,12 @@ def test_mutated_inputs_fail_cleanly(built, tmp_path, kind):
         path = _asset(tmp_path).write_glb(tmp_path / "a.glb")
     elif kind == "gltf":
         path = _asset(tmp_path).write_gltf(tmp_path / "a.gltf")
-    elif kind == "jpeg":
+    elif kind in ("jpeg", "jpeg_progressive"):
         from jpeg_util import encode as jpeg_encode
         rng = np.random.default_rng(0)
         path = tmp_path / "a.jpg"
         path.write_bytes(jpeg_encode(rng.integers(0, 256, (19, 27, 3)), sampling=((2, 2), (1, 1), (1, 1)),
-                                     restart=2, rng=rng)[0])
+                                     restart=2, progressive=kind == "jpeg_progressive", rng=rng)[0])
     elif kind == "ktx2":
         from test_texture_decode import _ktx2
         path = tmp_path / "a.ktx2"

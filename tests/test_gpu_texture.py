@@ -81,6 +81,12 @@ def test_jpeg_through_load_image_and_freed_source(renderer):
         assert np.array_equal(o.cpu().numpy().view(np.uint32)[..., 0], exp)
     via = texture.load_image(data, abi.IMAGE_JPEG, renderer)
     assert np.array_equal(via.view(np.uint32)[..., 0], exp)
+    # the same image as a progressive file: the same coefficients, so the same pixels
+    prog, _ = jpeg_encode(img, rng=np.random.default_rng(1), sampling=((2, 2), (1, 1), (1, 1)), restart=7,
+                          progressive=True)
+    got = texture.decode_jpeg(prog, renderer)
+    torch.cuda.synchronize()
+    assert np.array_equal(got.cpu().numpy().view(np.uint32)[..., 0], exp)
 
 
 def test_gltf_with_dds_and_png_textures(renderer, tmp_path):

@@ -2,9 +2,9 @@
 empty: src/vk_gltf_viewer/assets.cpp:467-471).  The host entropy decoder
 returns exactly the dequantized coefficients a T.81 encoder wrote, for grey,
 YCbCr and RGB files, every sampling layout, 8- and 16-bit tables, restart
-intervals and single-component scans; the oracle's fixed-point IDCT is
-pinned against the float64 inverse DCT; malformed files fail with a
-message."""
+intervals and single-component scans, sequential or progressive; the
+oracle's fixed-point IDCT is pinned against the float64 inverse DCT;
+malformed files fail with a message."""
 import math
 
 import numpy as np
@@ -56,6 +56,22 @@ def test_coefficients_round_trip(built, case, size):
         assert np.array_equal(g, e)
 
 
+@pytest.mark.parametrize("case", range(len(CASES)))
+@pytest.mark.parametrize("size", [(37, 45), (1, 1), (70, 90)])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_progressive_coefficients_round_trip(built, case, size, seed):
+    """SOF2 files: DC first / refinement scans (interleaved or not), AC bands
+    with successive approximation, end-of-band runs of random lengths and
+    restart intervals decode to exactly the coefficients encoded."""
+    kw = CASES[case]
+    img = _image(*size, seed=case)
+    data, expected = encode(img, rng=np.random.default_rng(seed * 100 + case), progressive=True, **kw)
+    assert data[data.index(b"\xff\xc2"):][:2] == b"\xff\xc2"
+    got = texture.Jpeg(data).planes
+    for g, e in zip(got, expected):
+        assert np.array_equal(g, e)
+
+
 def test_oracle_idct_is_the_inverse_dct(built):
     """The pinned fixed-point IDCT is within 1 of the float64 inverse DCT
     rounded, on random and extreme blocks (constants derived in the oracle)."""
@@ -101,7 +117,8 @@ def test_errors(built):
     sos = _first(data, 0xDA)
     cases = {
         "not a JPEG": b"\x89PNG" + data[4:],
-        "progressive": data.replace(b"\xff\xc0", b"\xff\xc2", 1),
+        "DC coefficient only": data.replace(b"\xff\xc0", b"\xff\xc2", 1),  # a sequential scan in SOF2
+        "differential": data.replace(b"\xff\xc0", b"\xff\xc6", 1),
         "arithmetic": data.replace(b"\xff\xc0", b"\xff\xc9", 1),
         "ends early": data[:sos + 40],
         "restart marker": data.replace(b"\xff\xd1", b"\xff\xd3", 1),

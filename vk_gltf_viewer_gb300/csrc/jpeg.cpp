@@ -9,8 +9,11 @@
 //     largest, at most 10 blocks per MCU;
 //   - DQT (8- and 16-bit tables), DHT (canonical codes, lengths 1-16), DRI
 //     with RST0-7 markers, interleaved scans and single-component scans;
-//   - progressive, lossless, hierarchical and arithmetic-coded images are
-//     refused.
+//   - SOF2 progressive images: DC first / refinement scans (interleaved or
+//     not) and AC first / refinement scans of spectral bands with
+//     end-of-band runs (T.81 G.1.2), coefficients accumulated quantized and
+//     multiplied by the table in use at each component's first scan;
+//   - lossless, hierarchical and arithmetic-coded images are refused.
 // Each block's Huffman-coded DC difference and AC run/size pairs are decoded
 // into its natural-order coefficients times the quantisation step, clamped
 // to int16; blocks lie in the component's MCU-padded block grid, in raster
@@ -186,7 +189,12 @@ struct Decoder {
     Component comp[3];
     uint32_t ncomp = 0, width = 0, height = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0;
     uint32_t restart = 0;
-    bool have_frame = false, adobe = false;
+    bool have_frame = false, adobe = false, progressive = false;
+    // progressive: coefficients accumulate quantized over the scans and are
+    // multiplied by the table each component's first scan used
+    uint16_t latched[3][64];
+    bool latched_set[3] = {false, false, false};
+    uint32_t eobrun = 0;  // blocks left in the current end-of-band run
     uint8_t adobe_transform = 1;
 
     Decoder(const uint8_t* d, size_t s, vkgv_jpeg& o) : data(d), size(s), out(o) {}
@@ -284,6 +292,90 @@ struct Decoder {
         }
     }
 
+    // Progressive scans (T.81 G.1.2), on quantized coefficients: a DC scan
+    // codes the difference of the point-transformed DC (pred << al) or, when
+    // refining, one bit of it; an AC scan codes a spectral band [ss, se] of
+    // one component, with end-of-band runs over blocks.
+    void dc_first(BitReader& br, const Huffman& hd, int32_t& pred, int al, int16_t* dst) {
+        const int t = br.symbol(hd);
+        if (t > 15) bad("DC difference above 15 bits");
+        pred = int32_t(uint32_t(pred) + uint32_t(extend(br.bits(t), t)));
+        dst[0] = clamp16(int64_t(pred) * (int64_t(1) << al));
+    }
+    static void dc_refine(BitReader& br, int al, int16_t* dst) {
+        if (br.bits(1)) dst[0] = int16_t(dst[0] | (1 << al));
+    }
+    void ac_first(BitReader& br, const Huffman& ha, int ss, int se, int al, int16_t* dst) {
+        if (eobrun > 0) {
+            --eobrun;
+            return;
+        }
+        const uint8_t* nat = zigzag().natural;
+        for (int k = ss; k <= se;) {
+            const int rs = br.symbol(ha);
+            const int r = rs >> 4, sz = rs & 15;
+            if (sz == 0) {
+                if (r < 15) {  // this block and (2^r - 1 + r extra bits) more end here
+                    eobrun = (1u << r) - 1u + br.bits(r);
+                    break;
+                }
+                k += 16;
+                continue;
+            }
+            k += r;
+            if (k > se) bad("AC coefficients past the end of the band");
+            dst[nat[k]] = clamp16(int64_t(extend(br.bits(sz), sz)) * (int64_t(1) << al));
+            ++k;
+        }
+    }
+    void ac_refine(BitReader& br, const Huffman& ha, int ss, int se, int al, int16_t* dst) {
+        const uint8_t* nat = zigzag().natural;
+        const int p1 = 1 << al, m1 = -(1 << al);
+        // a coefficient already nonzero takes one correction bit
+        auto correct = [&](int16_t& c) {
+            if (br.bits(1) && (c & p1) == 0) c = clamp16(int32_t(c) + (c >= 0 ? p1 : m1));
+        };
+        int k = ss;
+        if (eobrun == 0) {
+            while (k <= se) {
+                const int rs = br.symbol(ha);
+                int r = rs >> 4;
+                const int sz = rs & 15;
+                int value = 0;
+                if (sz == 0) {
+                    if (r < 15) {  // end of band: the rest of this block is refined below
+                        eobrun = (1u << r) + br.bits(r);
+                        break;
+                    }
+                    // r = 15: sixteen coefficients still zero are passed
+                } else {
+                    if (sz != 1) bad("refinement coefficient of more than one bit");
+                    value = br.bits(1) ? p1 : m1;
+                }
+                // pass r coefficients still zero (correcting the nonzero ones
+                // on the way), then give the next zero one `value`
+                while (k <= se) {
+                    int16_t& c = dst[nat[k++]];
+                    if (c != 0) {
+                        correct(c);
+                    } else if (r == 0) {
+                        if (value) c = int16_t(value);
+                        break;
+                    } else {
+                        --r;
+                    }
+                }
+            }
+        }
+        if (eobrun > 0) {
+            for (; k <= se; ++k) {
+                int16_t& c = dst[nat[k]];
+                if (c != 0) correct(c);
+            }
+            --eobrun;
+        }
+    }
+
     // Returns the position after the scan's entropy-coded data.
     const uint8_t* scan(const uint8_t* seg, uint32_t len, const uint8_t* data_begin, const uint8_t* data_end) {
         if (!have_frame) bad("scan before the frame header");
@@ -304,7 +396,7 @@ struct Decoder {
                 if (idx[j] == c) bad("component twice in a scan");
             idx[i] = c;
             const uint32_t td = seg[2 + 2 * i] >> 4, ta = seg[2 + 2 * i] & 15;
-            if (td > 3 || ta > 3 || !dc[td].defined || !ac[ta].defined) bad("scan uses an undefined Huffman table");
+            if (td > 3 || ta > 3) bad("bad Huffman table id");
             hd[i] = &dc[td];
             ha[i] = &ac[ta];
             if (!qt_defined[comp[c].tq]) bad("component uses an undefined quantisation table");
@@ -313,7 +405,25 @@ struct Decoder {
         }
         if (ns > 1 && per_mcu > 10) bad("more than 10 blocks per MCU");
         const uint8_t* tail = seg + 1 + 2 * ns;
-        if (tail[0] != 0 || tail[1] != 63 || tail[2] != 0) bad("progressive scan parameters in a sequential JPEG");
+        const int ss = tail[0], se = tail[1], ah = tail[2] >> 4, al = tail[2] & 15;
+        if (!progressive) {
+            if (ss != 0 || se != 63 || ah != 0 || al != 0) bad("progressive scan parameters in a sequential JPEG");
+        } else {
+            if (ss > se || se > 63 || ah > 13 || al > 13) bad("bad progressive scan parameters");
+            if (ss == 0 && se != 0) bad("a progressive DC scan must code the DC coefficient only");
+            if (ss > 0 && ns != 1) bad("a progressive AC scan must have one component");
+            if (ah != 0 && ah != al + 1) bad("a refinement scan must add one bit");
+        }
+        const bool dc_scan = ss == 0, refine = ah != 0;
+        for (uint32_t i = 0; i < ns; ++i) {
+            if ((!progressive || (dc_scan && !refine)) && !hd[i]->defined) bad("scan uses an undefined Huffman table");
+            if ((!progressive || !dc_scan) && !ha[i]->defined) bad("scan uses an undefined Huffman table");
+            if (progressive && !latched_set[idx[i]]) {
+                std::memcpy(latched[idx[i]], q[i], sizeof(q[i]));
+                latched_set[idx[i]] = true;
+            }
+        }
+        eobrun = 0;
         BitReader br(data_begin, data_end);
         int32_t pred[3] = {0, 0, 0};
         const uint32_t units_w = ns == 1 ? comp[idx[0]].scan_w : mcux;
@@ -329,6 +439,7 @@ struct Decoder {
                 br.p += 2;
                 br.at_marker = false;
                 pred[0] = pred[1] = pred[2] = 0;
+                eobrun = 0;
             }
             const uint32_t ux = uint32_t(u % units_w), uy = uint32_t(u / units_w);
             for (uint32_t i = 0; i < ns; ++i) {
@@ -338,7 +449,11 @@ struct Decoder {
                     for (uint32_t x = 0; x < bw; ++x) {
                         const uint32_t gx = ux * bw + x, gy = uy * bh + y;
                         int16_t* dst = out.coef[idx[i]].data() + (size_t(gy) * k.blocks_w + gx) * 64;
-                        block(br, *hd[i], *ha[i], q[i], pred[i], dst);
+                        if (!progressive) block(br, *hd[i], *ha[i], q[i], pred[i], dst);
+                        else if (dc_scan && !refine) dc_first(br, *hd[i], pred[i], al, dst);
+                        else if (dc_scan) dc_refine(br, al, dst);
+                        else if (!refine) ac_first(br, *ha[i], ss, se, al, dst);
+                        else ac_refine(br, *ha[i], ss, se, al, dst);
                     }
             }
         }
@@ -371,7 +486,11 @@ struct Decoder {
             p += len;
             switch (m) {
             case 0xC0: case 0xC1: frame(seg, body); break;
-            case 0xC2: case 0xC6: case 0xCA: case 0xCE: bad("progressive JPEG is not supported");
+            case 0xC2:
+                progressive = true;
+                frame(seg, body);
+                break;
+            case 0xC6: case 0xCA: case 0xCE: bad("differential or arithmetic progressive JPEG is not supported");
             case 0xC3: case 0xC5: case 0xC7: case 0xCB: case 0xCF: bad("lossless or hierarchical JPEG is not supported");
             case 0xC9: case 0xCD: case 0xCC: bad("arithmetic-coded JPEG is not supported");
             case 0xC4: tables_h(seg, body); break;
@@ -393,6 +512,14 @@ struct Decoder {
         if (!have_frame) bad("no frame header");
         for (uint32_t c = 0; c < ncomp; ++c)
             if (!comp[c].decoded) bad("a component has no scan");
+        if (progressive) {
+            const uint8_t* nat = zigzag().natural;
+            for (uint32_t c = 0; c < ncomp; ++c) {
+                int16_t* f = out.coef[c].data();
+                for (size_t b = 0; b < out.coef[c].size() / 64; ++b, f += 64)
+                    for (int k = 0; k < 64; ++k) f[nat[k]] = clamp16(int64_t(f[nat[k]]) * latched[c][k]);
+            }
+        }
         vkgv_jpeg_info& I = out.info;
         I.width = width;
         I.height = height;
