@@ -128,6 +128,9 @@ def test_errors(built):
     twelve = bytearray(data)
     twelve[sof + 4] = 12
     cases["8-bit"] = bytes(twelve)
+    huge = bytearray(data)  # a 16000 x 16000 frame over a few hundred bytes of data
+    huge[sof + 5:sof + 9] = bytes([0x3E, 0x80, 0x3E, 0x80])
+    cases["too short"] = bytes(huge)
     for match, bad in cases.items():
         with pytest.raises(abi.VkgvError, match=match):
             texture.Jpeg(bad)

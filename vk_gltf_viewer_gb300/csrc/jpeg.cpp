@@ -231,6 +231,12 @@ struct Decoder {
         if (ncomp > 1 && per_mcu > 10) bad("more than 10 blocks per MCU");
         mcux = (width + 8 * hmax - 1) / (8 * hmax);
         mcuy = (height + 8 * vmax - 1) / (8 * vmax);
+        // every block of the first component takes at least one bit of some
+        // scan: a file too small for its frame is refused before the
+        // coefficient planes are allocated
+        const uint64_t first_blocks = uint64_t((width * comp[0].h + hmax - 1) / hmax + 7) / 8 *
+                                      (uint64_t((height * comp[0].v + vmax - 1) / vmax + 7) / 8);
+        if (uint64_t(size) * 8 < first_blocks) bad("JPEG data too short for its frame size");
         for (uint32_t c = 0; c < ncomp; ++c) {
             Component& k = comp[c];
             k.blocks_w = mcux * k.h;
