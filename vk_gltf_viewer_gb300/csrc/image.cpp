@@ -145,7 +145,9 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t size, size_t limit
     if (flg & 0x20) fail("zlib preset dictionaries are not supported");
     BitReader br(data + 2, size - 2);
     std::vector<uint8_t> out;
-    out.reserve(limit);
+    // DEFLATE expands at most about 1032:1 (258-byte matches coded in 2 bits),
+    // so a small stream cannot claim a huge buffer up front
+    out.reserve(std::min(limit, size * 1032 + 1024));
     int last = 0;
     while (!last) {
         last = int(br.bits(1));
