@@ -19,7 +19,8 @@ namespace {
 
 constexpr uint32_t kRing = 4;                 // in-flight frames sharing staging slots
 constexpr uint32_t kCountersPerView = 8;      // see DeviceView::counters
-constexpr uint32_t kGlobalCounters = 8;       // [0] pass-1 big queue, [1] pass-2 big queue, [6..7] raster work
+constexpr uint32_t kGlobalCounters = 8;       // [0] pass-1 big queue, [1] pass-2 big queue, [2..3] adjoint
+                                              // shade work, [6..7] raster work
 constexpr uint32_t kDefaultBigCapacity = 1u << 21;
 
 struct Scratch {
@@ -988,7 +989,7 @@ void diff_record(vkgv_ctx* ctx, const DiffPlan& D, const DeviceView* dv, uint32_
     launch_raster(D.P.S, dv, n, l1, ctx->raster, ctx->big, ctx->counters + 0, ctx->big_cap, ctx->counters + 6, ctx->status,
                   ctx->sm_count, stream);
     if (backward && D.acc_bytes) cudaMemsetAsync(ctx->diff_acc.ptr, 0, D.acc_bytes, stream);
-    launch_diff_shade(D.A, dv, n, D.P.max_px, backward, stream);
+    launch_diff_shade(D.A, dv, n, D.P.max_px, backward, ctx->counters + 2, ctx->sm_count, stream);
     if (backward) launch_diff_scatter(D.A, stream);
 }
 

@@ -235,168 +235,261 @@ __device__ __forceinline__ void clip_ab(const float* VP, const float* q, float n
     b = __fadd_rn(__fmaf_rn(-ny, wh, yh), __fmaf_rn(-ny, wl, yl));
 }
 
+// One pixel of the forward image (BACKWARD = false) or of the gradient pass.
+template <bool BACKWARD>
+__device__ __forceinline__ void shade_pixel(const DiffArgs& A, const DeviceView& V, const float* VP, float sn, float cs,
+                                            uint32_t p, float& loss_acc) {
+    const uint32_t w = V.w;
+    const uint32_t lo = (uint32_t)V.depth_id[p];
+    float tgt[3] = {0.0f, 0.0f, 0.0f};
+    const bool mse = V.diff_target != nullptr;
+    if (BACKWARD && mse) {
+        tgt[0] = V.diff_target[3 * p];
+        tgt[1] = V.diff_target[3 * p + 1];
+        tgt[2] = V.diff_target[3 * p + 2];
+    }
+    if (lo == 0) {
+        if (BACKWARD) loss_acc += A.scale * (tgt[0] * tgt[0] + tgt[1] * tgt[1] + tgt[2] * tgt[2]);
+        else if (V.diff_rgb) V.diff_rgb[3 * p] = V.diff_rgb[3 * p + 1] = V.diff_rgb[3 * p + 2] = 0.0f;
+        return;
+    }
+    const uint4 tvi = A.tri_verts[lo - 1u];
+    // The sample point is the fp32 NDC of the pixel centre.
+    const float nx = fsub(fmul(fdiv(fadd((float)(p % w), 0.5f), (float)V.w), 2.0f), 1.0f);
+    const float ny = fsub(fmul(fdiv(fadd((float)(p / w), 0.5f), (float)V.h), 2.0f), 1.0f);
+    const uint32_t vi[3] = {tvi.x, tvi.y, tvi.z};
+    float4 P0[3], P1[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        P0[k] = A.vpack[2 * (size_t)vi[k]];
+        P1[k] = A.vpack[2 * (size_t)vi[k] + 1];
+    }
+    float a[3], b[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float q[3] = {P0[k].x, P0[k].y, P0[k].z};
+        if (BACKWARD) {
+            clip_ab(VP, q, nx, ny, a[k], b[k]);
+        } else {
+            // the forward image needs fp32 accuracy only (no cancellation
+            // reaches a gradient)
+            float c[4];
+            m4v(VP, q[0], q[1], q[2], 1.0f, c);
+            a[k] = fsub(c[0], fmul(nx, c[3]));
+            b[k] = fsub(c[1], fmul(ny, c[3]));
+        }
+    }
+    float l[3] = {fsub(fmul(a[1], b[2]), fmul(a[2], b[1])), fsub(fmul(a[2], b[0]), fmul(a[0], b[2])),
+                  fsub(fmul(a[0], b[1]), fmul(a[1], b[0]))};
+    const float sum = fadd(fadd(l[0], l[1]), l[2]);
+    if (!(sum != 0.0f)) {  // degenerate: shaded as empty, no gradient
+        if (BACKWARD) loss_acc += A.scale * (tgt[0] * tgt[0] + tgt[1] * tgt[1] + tgt[2] * tgt[2]);
+        else if (V.diff_rgb) V.diff_rgb[3 * p] = V.diff_rgb[3 * p + 1] = V.diff_rgb[3 * p + 2] = 0.0f;
+        return;
+    }
+    float lam[3] = {fdiv(l[0], sum), fdiv(l[1], sum), fdiv(l[2], sum)};
+    float C[3][3], UV[3][2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        C[k][0] = P0[k].w, C[k][1] = P1[k].x, C[k][2] = P1[k].y;
+        UV[k][0] = P1[k].z, UV[k][1] = P1[k].w;
+    }
+    float col[3], uv[2];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+        col[j] = fadd(fadd(fmul(lam[0], C[0][j]), fmul(lam[1], C[1][j])), fmul(lam[2], C[2][j]));
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+        uv[j] = fadd(fadd(fmul(lam[0], UV[0][j]), fmul(lam[1], UV[1][j])), fmul(lam[2], UV[2][j]));
+    const float ru = fadd(fmul(cs, uv[0]), fmul(sn, uv[1]));
+    const float rv = fadd(fmul(-sn, uv[0]), fmul(cs, uv[1]));
+    const float tu = fadd(fmul(ru, A.uv_scale[0]), A.uv_offset[0]);
+    const float tv = fadd(fmul(rv, A.uv_scale[1]), A.uv_offset[1]);
+    const float tx = fsub(fmul(tu, (float)A.tex_w), 0.5f), ty = fsub(fmul(tv, (float)A.tex_h), 0.5f);
+    const float fx = floorf(tx), fy = floorf(ty);
+    const float ax = fsub(tx, fx), ay = fsub(ty, fy);
+    const int x0 = wrap((int)fx, (int)A.tex_w), x1 = wrap((int)fx + 1, (int)A.tex_w);
+    const int y0 = wrap((int)fy, (int)A.tex_h), y1 = wrap((int)fy + 1, (int)A.tex_h);
+    const size_t i00 = 3 * ((size_t)y0 * A.tex_w + x0), i01 = 3 * ((size_t)y0 * A.tex_w + x1);
+    const size_t i10 = 3 * ((size_t)y1 * A.tex_w + x0), i11 = 3 * ((size_t)y1 * A.tex_w + x1);
+    float T00[3], T01[3], T10[3], T11[3], tex[3], rgb[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        T00[j] = A.texture[i00 + j];
+        T01[j] = A.texture[i01 + j];
+        T10[j] = A.texture[i10 + j];
+        T11[j] = A.texture[i11 + j];
+        const float top = fadd(T00[j], fmul(ax, fsub(T01[j], T00[j])));
+        const float bot = fadd(T10[j], fmul(ax, fsub(T11[j], T10[j])));
+        tex[j] = fadd(top, fmul(ay, fsub(bot, top)));
+        rgb[j] = fmul(fmul(col[j], A.albedo[j]), tex[j]);
+    }
+    if (!BACKWARD) {
+        if (V.diff_rgb) {
+            V.diff_rgb[3 * p] = rgb[0];
+            V.diff_rgb[3 * p + 1] = rgb[1];
+            V.diff_rgb[3 * p + 2] = rgb[2];
+        }
+        return;
+    }
+    // ---- backward
+    float g[3], dcol[3], dtex[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (mse) {
+            const float r = rgb[j] - tgt[j];
+            loss_acc += A.scale * r * r;
+            g[j] = 2.0f * A.scale * r;
+        } else {
+            g[j] = V.diff_grad[3 * p + j];
+        }
+        dcol[j] = g[j] * A.albedo[j] * tex[j];
+        dtex[j] = g[j] * col[j] * A.albedo[j];
+    }
+    if (A.acc_tex) {
+        const float w00 = (1.0f - ax) * (1.0f - ay), w01 = ax * (1.0f - ay);
+        const float w10 = (1.0f - ax) * ay, w11 = ax * ay;
+        atomicAdd(A.acc_tex + i00 / 3, make_float4(dtex[0] * w00, dtex[1] * w00, dtex[2] * w00, 0.0f));
+        atomicAdd(A.acc_tex + i01 / 3, make_float4(dtex[0] * w01, dtex[1] * w01, dtex[2] * w01, 0.0f));
+        atomicAdd(A.acc_tex + i10 / 3, make_float4(dtex[0] * w10, dtex[1] * w10, dtex[2] * w10, 0.0f));
+        atomicAdd(A.acc_tex + i11 / 3, make_float4(dtex[0] * w11, dtex[1] * w11, dtex[2] * w11, 0.0f));
+    }
+    // d tex / d uv' through the bilinear weights
+    float dtu = 0.0f, dtv = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        dtu += dtex[j] * ((1.0f - ay) * (T01[j] - T00[j]) + ay * (T11[j] - T10[j]));
+        dtv += dtex[j] * ((1.0f - ax) * (T10[j] - T00[j]) + ax * (T11[j] - T01[j]));
+    }
+    dtu *= (float)A.tex_w;
+    dtv *= (float)A.tex_h;
+    const float dru = dtu * A.uv_scale[0], drv = dtv * A.uv_scale[1];
+    const float du = cs * dru - sn * drv, dv = sn * dru + cs * drv;
+    float dlam[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        dlam[k] = dcol[0] * C[k][0] + dcol[1] * C[k][1] + dcol[2] * C[k][2] + du * UV[k][0] + dv * UV[k][1];
+        if (A.acc_col)
+            atomicAdd(A.acc_col + vi[k], make_float4(dcol[0] * lam[k], dcol[1] * lam[k], dcol[2] * lam[k], 0.0f));
+    }
+    if (!A.acc_pos) return;
+    const float dot = lam[0] * dlam[0] + lam[1] * dlam[1] + lam[2] * dlam[2];
+    const float dl[3] = {(dlam[0] - dot) / sum, (dlam[1] - dot) / sum, (dlam[2] - dot) / sum};
+    // l = a x b: dL/da = b x dl, dL/db = dl x a
+    const float da[3] = {b[1] * dl[2] - b[2] * dl[1], b[2] * dl[0] - b[0] * dl[2], b[0] * dl[1] - b[1] * dl[0]};
+    const float db[3] = {dl[1] * a[2] - dl[2] * a[1], dl[2] * a[0] - dl[0] * a[2], dl[0] * a[1] - dl[1] * a[0]};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float dx = da[k], dy = db[k], dw = -nx * da[k] - ny * db[k];
+        atomicAdd(A.acc_pos + vi[k], make_float4(VP[0] * dx + VP[1] * dy + VP[3] * dw,
+                                                 VP[4] * dx + VP[5] * dy + VP[7] * dw,
+                                                 VP[8] * dx + VP[9] * dy + VP[11] * dw, 0.0f));
+    }
+}
+
+// One thread per pixel over a (max pixels / 256, views) grid: for views past
+// kShadeMaxViews.
 template <bool BACKWARD>
 __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView* __restrict__ views) {
     const DeviceView& V = views[blockIdx.y];
-    const uint32_t w = V.w, n = V.w * V.h;
+    const uint32_t n = V.w * V.h;
     float VP[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) VP[k] = V.cam->view_projection[k];
     float sn, cs;
     sincosf(A.uv_rotation, &sn, &cs);
     float loss_acc = 0.0f;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const uint32_t lo = (uint32_t)V.depth_id[p];
-        float tgt[3] = {0.0f, 0.0f, 0.0f};
-        const bool mse = V.diff_target != nullptr;
-        if (BACKWARD && mse) {
-            tgt[0] = V.diff_target[3 * p];
-            tgt[1] = V.diff_target[3 * p + 1];
-            tgt[2] = V.diff_target[3 * p + 2];
-        }
-        if (lo == 0) {
-            if (BACKWARD) loss_acc += A.scale * (tgt[0] * tgt[0] + tgt[1] * tgt[1] + tgt[2] * tgt[2]);
-            else if (V.diff_rgb) V.diff_rgb[3 * p] = V.diff_rgb[3 * p + 1] = V.diff_rgb[3 * p + 2] = 0.0f;
-            continue;
-        }
-        const uint4 tvi = A.tri_verts[lo - 1u];
-        // The sample point is the fp32 NDC of the pixel centre.
-        const float nx = fsub(fmul(fdiv(fadd((float)(p % w), 0.5f), (float)V.w), 2.0f), 1.0f);
-        const float ny = fsub(fmul(fdiv(fadd((float)(p / w), 0.5f), (float)V.h), 2.0f), 1.0f);
-        const uint32_t vi[3] = {tvi.x, tvi.y, tvi.z};
-        float4 P0[3], P1[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            P0[k] = A.vpack[2 * (size_t)vi[k]];
-            P1[k] = A.vpack[2 * (size_t)vi[k] + 1];
-        }
-        float a[3], b[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float q[3] = {P0[k].x, P0[k].y, P0[k].z};
-            if (BACKWARD) {
-                clip_ab(VP, q, nx, ny, a[k], b[k]);
-            } else {
-                // the forward image needs fp32 accuracy only (no cancellation
-                // reaches a gradient)
-                float c[4];
-                m4v(VP, q[0], q[1], q[2], 1.0f, c);
-                a[k] = fsub(c[0], fmul(nx, c[3]));
-                b[k] = fsub(c[1], fmul(ny, c[3]));
-            }
-        }
-        float l[3] = {fsub(fmul(a[1], b[2]), fmul(a[2], b[1])), fsub(fmul(a[2], b[0]), fmul(a[0], b[2])),
-                      fsub(fmul(a[0], b[1]), fmul(a[1], b[0]))};
-        const float sum = fadd(fadd(l[0], l[1]), l[2]);
-        if (!(sum != 0.0f)) {  // degenerate: shaded as empty, no gradient
-            if (BACKWARD) loss_acc += A.scale * (tgt[0] * tgt[0] + tgt[1] * tgt[1] + tgt[2] * tgt[2]);
-            else if (V.diff_rgb) V.diff_rgb[3 * p] = V.diff_rgb[3 * p + 1] = V.diff_rgb[3 * p + 2] = 0.0f;
-            continue;
-        }
-        float lam[3] = {fdiv(l[0], sum), fdiv(l[1], sum), fdiv(l[2], sum)};
-        float C[3][3], UV[3][2];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            C[k][0] = P0[k].w, C[k][1] = P1[k].x, C[k][2] = P1[k].y;
-            UV[k][0] = P1[k].z, UV[k][1] = P1[k].w;
-        }
-        float col[3], uv[2];
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-            col[j] = fadd(fadd(fmul(lam[0], C[0][j]), fmul(lam[1], C[1][j])), fmul(lam[2], C[2][j]));
-#pragma unroll
-        for (int j = 0; j < 2; ++j)
-            uv[j] = fadd(fadd(fmul(lam[0], UV[0][j]), fmul(lam[1], UV[1][j])), fmul(lam[2], UV[2][j]));
-        const float ru = fadd(fmul(cs, uv[0]), fmul(sn, uv[1]));
-        const float rv = fadd(fmul(-sn, uv[0]), fmul(cs, uv[1]));
-        const float tu = fadd(fmul(ru, A.uv_scale[0]), A.uv_offset[0]);
-        const float tv = fadd(fmul(rv, A.uv_scale[1]), A.uv_offset[1]);
-        const float tx = fsub(fmul(tu, (float)A.tex_w), 0.5f), ty = fsub(fmul(tv, (float)A.tex_h), 0.5f);
-        const float fx = floorf(tx), fy = floorf(ty);
-        const float ax = fsub(tx, fx), ay = fsub(ty, fy);
-        const int x0 = wrap((int)fx, (int)A.tex_w), x1 = wrap((int)fx + 1, (int)A.tex_w);
-        const int y0 = wrap((int)fy, (int)A.tex_h), y1 = wrap((int)fy + 1, (int)A.tex_h);
-        const size_t i00 = 3 * ((size_t)y0 * A.tex_w + x0), i01 = 3 * ((size_t)y0 * A.tex_w + x1);
-        const size_t i10 = 3 * ((size_t)y1 * A.tex_w + x0), i11 = 3 * ((size_t)y1 * A.tex_w + x1);
-        float T00[3], T01[3], T10[3], T11[3], tex[3], rgb[3];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            T00[j] = A.texture[i00 + j];
-            T01[j] = A.texture[i01 + j];
-            T10[j] = A.texture[i10 + j];
-            T11[j] = A.texture[i11 + j];
-            const float top = fadd(T00[j], fmul(ax, fsub(T01[j], T00[j])));
-            const float bot = fadd(T10[j], fmul(ax, fsub(T11[j], T10[j])));
-            tex[j] = fadd(top, fmul(ay, fsub(bot, top)));
-            rgb[j] = fmul(fmul(col[j], A.albedo[j]), tex[j]);
-        }
-        if (!BACKWARD) {
-            if (V.diff_rgb) {
-                V.diff_rgb[3 * p] = rgb[0];
-                V.diff_rgb[3 * p + 1] = rgb[1];
-                V.diff_rgb[3 * p + 2] = rgb[2];
-            }
-            continue;
-        }
-        // ---- backward
-        float g[3], dcol[3], dtex[3];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            if (mse) {
-                const float r = rgb[j] - tgt[j];
-                loss_acc += A.scale * r * r;
-                g[j] = 2.0f * A.scale * r;
-            } else {
-                g[j] = V.diff_grad[3 * p + j];
-            }
-            dcol[j] = g[j] * A.albedo[j] * tex[j];
-            dtex[j] = g[j] * col[j] * A.albedo[j];
-        }
-        if (A.acc_tex) {
-            const float w00 = (1.0f - ax) * (1.0f - ay), w01 = ax * (1.0f - ay);
-            const float w10 = (1.0f - ax) * ay, w11 = ax * ay;
-            atomicAdd(A.acc_tex + i00 / 3, make_float4(dtex[0] * w00, dtex[1] * w00, dtex[2] * w00, 0.0f));
-            atomicAdd(A.acc_tex + i01 / 3, make_float4(dtex[0] * w01, dtex[1] * w01, dtex[2] * w01, 0.0f));
-            atomicAdd(A.acc_tex + i10 / 3, make_float4(dtex[0] * w10, dtex[1] * w10, dtex[2] * w10, 0.0f));
-            atomicAdd(A.acc_tex + i11 / 3, make_float4(dtex[0] * w11, dtex[1] * w11, dtex[2] * w11, 0.0f));
-        }
-        // d tex / d uv' through the bilinear weights
-        float dtu = 0.0f, dtv = 0.0f;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            dtu += dtex[j] * ((1.0f - ay) * (T01[j] - T00[j]) + ay * (T11[j] - T10[j]));
-            dtv += dtex[j] * ((1.0f - ax) * (T10[j] - T00[j]) + ax * (T11[j] - T01[j]));
-        }
-        dtu *= (float)A.tex_w;
-        dtv *= (float)A.tex_h;
-        const float dru = dtu * A.uv_scale[0], drv = dtv * A.uv_scale[1];
-        const float du = cs * dru - sn * drv, dv = sn * dru + cs * drv;
-        float dlam[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            dlam[k] = dcol[0] * C[k][0] + dcol[1] * C[k][1] + dcol[2] * C[k][2] + du * UV[k][0] + dv * UV[k][1];
-            if (A.acc_col)
-                atomicAdd(A.acc_col + vi[k], make_float4(dcol[0] * lam[k], dcol[1] * lam[k], dcol[2] * lam[k], 0.0f));
-        }
-        if (!A.acc_pos) continue;
-        const float dot = lam[0] * dlam[0] + lam[1] * dlam[1] + lam[2] * dlam[2];
-        const float dl[3] = {(dlam[0] - dot) / sum, (dlam[1] - dot) / sum, (dlam[2] - dot) / sum};
-        // l = a x b: dL/da = b x dl, dL/db = dl x a
-        const float da[3] = {b[1] * dl[2] - b[2] * dl[1], b[2] * dl[0] - b[0] * dl[2], b[0] * dl[1] - b[1] * dl[0]};
-        const float db[3] = {dl[1] * a[2] - dl[2] * a[1], dl[2] * a[0] - dl[0] * a[2], dl[0] * a[1] - dl[1] * a[0]};
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float dx = da[k], dy = db[k], dw = -nx * da[k] - ny * db[k];
-            atomicAdd(A.acc_pos + vi[k], make_float4(VP[0] * dx + VP[1] * dy + VP[3] * dw,
-                                                     VP[4] * dx + VP[5] * dy + VP[7] * dw,
-                                                     VP[8] * dx + VP[9] * dy + VP[11] * dw, 0.0f));
-        }
-    }
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        shade_pixel<BACKWARD>(A, V, VP, sn, cs, p, loss_acc);
     if (BACKWARD && A.loss) {
         // warp-reduce the loss, one atomic per warp
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
         if ((threadIdx.x & 31) == 0) atomicAdd(A.loss, loss_acc);
+    }
+}
+
+// Persistent form: one wave of resident CTAs takes chunks of kShadeChunk
+// pixels (all views' chunks numbered in view order) from a global counter,
+// so CTAs of background pixels do not retire early and leave the SMs below
+// their register-limited residency, and views smaller than the largest
+// cost no empty CTAs.  The last CTA to finish returns the counters to zero.
+constexpr uint32_t kShadeChunk = 1024;
+constexpr uint32_t kShadeMaxViews = 4096;
+
+template <bool BACKWARD>
+__global__ void __launch_bounds__(256) k_diff_shade_chunks(DiffArgs A, const DeviceView* __restrict__ views,
+                                                           uint32_t nviews, uint32_t* work) {
+    __shared__ uint32_t s_pre[kShadeMaxViews + 1];
+    __shared__ uint32_t s_item;
+    for (uint32_t v = threadIdx.x; v < nviews; v += blockDim.x)
+        s_pre[v + 1] = (views[v].w * views[v].h + kShadeChunk - 1) / kShadeChunk;
+    if (threadIdx.x == 0) s_pre[0] = 0;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // inclusive scan of s_pre[1..nviews]: lane-contiguous segments, then
+        // a warp scan of the segment sums
+        const uint32_t lane = threadIdx.x, seg = (nviews + 31) / 32;
+        const uint32_t b = 1 + lane * seg, e = min(b + seg, nviews + 1);
+        uint32_t sum = 0;
+        for (uint32_t i = b; i < e; ++i) sum += s_pre[i];
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += t;
+        }
+        uint32_t run = incl - sum;
+        for (uint32_t i = b; i < e; ++i) {
+            run += s_pre[i];
+            s_pre[i] = run;
+        }
+    }
+    __syncthreads();
+    const uint32_t total = s_pre[nviews];
+    float sn, cs;
+    sincosf(A.uv_rotation, &sn, &cs);
+    float VP[16];
+    uint32_t cur = 0xffffffffu;
+    float loss_acc = 0.0f;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(work, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        __syncthreads();
+        if (item >= total) break;
+        // the view holding the chunk: the last v with s_pre[v] <= item
+        uint32_t v = 0, hi = nviews;
+        while (v + 1 < hi) {
+            const uint32_t mid = (v + hi) >> 1;
+            if (s_pre[mid] <= item) v = mid;
+            else hi = mid;
+        }
+        const DeviceView& V = views[v];
+        if (v != cur) {
+            cur = v;
+#pragma unroll
+            for (int k = 0; k < 16; ++k) VP[k] = V.cam->view_projection[k];
+        }
+        const uint32_t n = V.w * V.h, base = (item - s_pre[v]) * kShadeChunk;
+#pragma unroll 1
+        for (uint32_t j = threadIdx.x; j < kShadeChunk; j += 256) {
+            const uint32_t p = base + j;
+            if (p < n) shade_pixel<BACKWARD>(A, V, VP, sn, cs, p, loss_acc);
+        }
+    }
+    if (BACKWARD && A.loss) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) loss_acc += __shfl_xor_sync(0xffffffffu, loss_acc, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(A.loss, loss_acc);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(work + 1, 1u) == gridDim.x - 1) {
+            work[0] = 0;
+            work[1] = 0;
+        }
     }
 }
 
@@ -439,7 +532,22 @@ void launch_diff_scatter(const DiffArgs& A, cudaStream_t stream) {
 }
 
 void launch_diff_shade(const DiffArgs& A, const DeviceView* views, uint32_t nviews, uint64_t max_px, bool backward,
-                       cudaStream_t stream) {
+                       uint32_t* work, uint32_t sm_count, cudaStream_t stream) {
+    if (nviews <= kShadeMaxViews && work) {
+        int per_sm = 0;
+        const cudaError_t e = backward
+            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_diff_shade_chunks<true>, 256, 0)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_diff_shade_chunks<false>, 256, 0);
+        if (e == cudaSuccess && per_sm > 0) {
+            const uint32_t blocks = sm_count * (uint32_t)per_sm;
+            if (backward)
+                k_diff_shade_chunks<true><<<blocks, 256, 0, stream>>>(A, views, nviews, work);
+            else
+                k_diff_shade_chunks<false><<<blocks, 256, 0, stream>>>(A, views, nviews, work);
+            return;
+        }
+        cudaGetLastError();
+    }
     uint32_t bx = (uint32_t)((max_px + 255) / 256);
     if (bx > 65535u) bx = 65535u;
     if (bx == 0) bx = 1;

@@ -122,7 +122,7 @@ void launch_diff_setup(const DiffSetup& S, cudaStream_t stream);
 // Conservative normal cones of every meshlet from the current positions.
 void launch_diff_cones(const DiffSetup& S, cudaStream_t stream);
 void launch_diff_shade(const DiffArgs& A, const DeviceView* views, uint32_t nviews, uint64_t max_px, bool backward,
-                       cudaStream_t stream);
+                       uint32_t* work, uint32_t sm_count, cudaStream_t stream);
 // Adds the float4 accumulators of A into the caller's gradient arrays.
 void launch_diff_scatter(const DiffArgs& A, cudaStream_t stream);
 
