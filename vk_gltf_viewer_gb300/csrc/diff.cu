@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
 // so CTAs of background pixels do not retire early and leave the SMs below
 // their register-limited residency, and views smaller than the largest
 // cost no empty CTAs.  The last CTA to finish returns the counters to zero.
-constexpr uint32_t kShadeChunk = 1024;
+constexpr uint32_t kShadeChunk = 4096;
 constexpr uint32_t kShadeMaxViews = 4096;
 
 template <bool BACKWARD>
