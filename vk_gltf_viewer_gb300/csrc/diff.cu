@@ -409,19 +409,19 @@ __global__ void __launch_bounds__(256) k_diff_shade(DiffArgs A, const DeviceView
     }
 }
 
-// Persistent form: one wave of resident CTAs takes chunks of kShadeChunk
-// pixels (all views' chunks numbered in view order) from a global counter,
-// so CTAs of background pixels do not retire early and leave the SMs below
-// their register-limited residency, and views smaller than the largest
+// Persistent form: one wave of resident CTAs whose warps take chunks of
+// kShadeChunk pixels (all views' chunks numbered in view order) from a
+// global counter, so warps of background pixels neither retire early (which
+// left the SMs below their register-limited residency) nor wait at a CTA
+// barrier for warps of covered pixels, and views smaller than the largest
 // cost no empty CTAs.  The last CTA to finish returns the counters to zero.
-constexpr uint32_t kShadeChunk = 4096;
+constexpr uint32_t kShadeChunk = 512;
 constexpr uint32_t kShadeMaxViews = 4096;
 
 template <bool BACKWARD>
 __global__ void __launch_bounds__(256) k_diff_shade_chunks(DiffArgs A, const DeviceView* __restrict__ views,
                                                            uint32_t nviews, uint32_t* work) {
     __shared__ uint32_t s_pre[kShadeMaxViews + 1];
-    __shared__ uint32_t s_item;
     for (uint32_t v = threadIdx.x; v < nviews; v += blockDim.x)
         s_pre[v + 1] = (views[v].w * views[v].h + kShadeChunk - 1) / kShadeChunk;
     if (threadIdx.x == 0) s_pre[0] = 0;
@@ -453,10 +453,11 @@ __global__ void __launch_bounds__(256) k_diff_shade_chunks(DiffArgs A, const Dev
     uint32_t cur = 0xffffffffu;
     float loss_acc = 0.0f;
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(work, 1u);
-        __syncthreads();
-        const uint32_t item = s_item;
-        __syncthreads();
+        // each warp takes its own chunks: no CTA barrier holds a warp of
+        // background pixels behind one of covered pixels
+        uint32_t item = 0;
+        if ((threadIdx.x & 31u) == 0) item = atomicAdd(work, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= total) break;
         // the view holding the chunk: the last v with s_pre[v] <= item
         uint32_t v = 0, hi = nviews;
@@ -473,7 +474,7 @@ __global__ void __launch_bounds__(256) k_diff_shade_chunks(DiffArgs A, const Dev
         }
         const uint32_t n = V.w * V.h, base = (item - s_pre[v]) * kShadeChunk;
 #pragma unroll 1
-        for (uint32_t j = threadIdx.x; j < kShadeChunk; j += 256) {
+        for (uint32_t j = threadIdx.x & 31u; j < kShadeChunk; j += 32) {
             const uint32_t p = base + j;
             if (p < n) shade_pixel<BACKWARD>(A, V, VP, sn, cs, p, loss_acc);
         }
