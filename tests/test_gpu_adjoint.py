@@ -309,3 +309,48 @@ def test_adjoint_graph_rejects_bad_passes(renderer, su):
     with pytest.raises(abi.VkgvError):
         # backward without a target or an upstream gradient
         diff.capture_step(renderer, su.scene, su.views, passes=abi.DIFF_BACKWARD)
+
+
+def test_uneven_views_forward_and_gradients(renderer):
+    """Views of different sizes (partial 512-pixel chunks, a 33 x 17 and a
+    512 x 40 view) in one call: the persistent shade maps every chunk to its
+    view and pixels, for the forward image and the gradients."""
+    sizes = [(96, 64), (200, 150), (33, 17), (512, 40)]
+    rng = np.random.default_rng(9)
+    mesh = scene.icosphere(3)
+    nv = mesh.positions.shape[0]
+    colors = rng.uniform(0, 1, size=(nv, 3)).astype(np.float32)
+    texture = rng.uniform(0, 1, size=(64, 64, 3)).astype(np.float32)
+    sc = diff.DiffScene.create(mesh, colors, texture)
+    cams, views = [], []
+    for w, h in sizes:
+        v = rng.normal(size=3)
+        eye = 3.0 * v / np.linalg.norm(v)
+        cam = scene.camera(tuple(eye), (0, 0, 0), scene.safe_up(eye, (0, 0, 0)), 60.0, w / h)
+        cams.append(cam)
+        views.append(diff.DiffViewBuffers.allocate(w, h, cam))
+    out = [torch.zeros(w * h * 3, device="cuda") for w, h in sizes]
+    diff.forward(renderer, sc, views, out)
+    torch.cuda.synchronize()
+    ids = [v.ids() for v in views]
+    assert all((i != abi.VISBUFFER_CLEAR).any() for i in ids)
+    for (w, h), cam, o, idv in zip(sizes, cams, out, ids):
+        _, ref, _ = ob.diff_f64(mesh, mesh.positions, colors, mesh.uvs, texture, vp_of(cam), w, h, idv, want_rgb=True)
+        assert np.abs(o.cpu().numpy() - ref).max() < 5e-4
+    targets = [rng.uniform(0, 1, size=w * h * 3).astype(np.float32) for w, h in sizes]
+    scale = 1.0 / (3 * sum(w * h for w, h in sizes))
+    gp, gc, gt = torch.zeros_like(sc.positions), torch.zeros_like(sc.colors), torch.zeros_like(sc.texture)
+    loss = torch.zeros(1, device="cuda")
+    diff.backward(renderer, sc, views, gp, gc, gt, targets=[torch.from_numpy(t).cuda() for t in targets],
+                  scale=scale, loss=loss)
+    torch.cuda.synchronize()
+    ref_loss, ref = 0.0, None
+    for (w, h), cam, t, idv in zip(sizes, cams, targets, ids):
+        lv, _, g = ob.diff_f64(mesh, mesh.positions, colors, mesh.uvs, texture, vp_of(cam), w, h, idv, target=t,
+                               scale=scale, want_grads=True)
+        ref_loss += lv
+        ref = g if ref is None else tuple(a + b for a, b in zip(ref, g))
+    assert abs(float(loss.item()) - ref_loss) <= 1e-4 * abs(ref_loss)
+    for name, g, r in (("positions", gp, ref[0]), ("colors", gc, ref[1]), ("texels", gt, ref[2])):
+        g = g.cpu().numpy().reshape(-1)
+        assert np.linalg.norm(g - r) / np.linalg.norm(r) < 1e-3, name
