@@ -20,7 +20,7 @@ namespace {
 constexpr uint32_t kRing = 4;                 // in-flight frames sharing staging slots
 constexpr uint32_t kCountersPerView = 8;      // see DeviceView::counters
 constexpr uint32_t kGlobalCounters = 8;       // [0] pass-1 big queue, [1] pass-2 big queue, [2..3] adjoint
-                                              // shade work, [6..7] raster work
+                                              // shade work, [4..5] resolve work, [6..7] raster work
 constexpr uint32_t kDefaultBigCapacity = 1u << 21;
 
 struct Scratch {
@@ -342,12 +342,12 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
         cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0);
         launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, ctx->status, ctx->side_stream);
         cudaEventRecord(ctx->join_ev, ctx->side_stream);
-        launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
+        launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, ctx->counters + 4, ctx->sm_count, stream);
         cudaStreamWaitEvent(stream, ctx->join_ev, 0);
     } else {
         if (pyramid) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, ctx->status, stream);
         zone(9);
-        if (resolve) launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, stream);
+        if (resolve) launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, ctx->counters + 4, ctx->sm_count, stream);
     }
     zone(10);
     if (!resolve) launch_finalize(dv, n, stream);
@@ -669,7 +669,7 @@ int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, 
     if (rc) return rc;
     rc = commit_views(ctx, slot, 1, stream);
     if (rc) return rc;
-    launch_resolve(P.S, dv, 1, P.max_w, P.max_h, flags, stream);
+    launch_resolve(P.S, dv, 1, P.max_w, P.max_h, flags, ctx->counters + 4, ctx->sm_count, stream);
     rc = check_launch(ctx);
     if (rc) return rc;
     return close_slot(ctx, slot, stream);

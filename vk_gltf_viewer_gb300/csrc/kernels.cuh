@@ -62,7 +62,7 @@ void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews,
 void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t* status,
                 cudaStream_t stream);
 void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h,
-                    uint32_t flags, cudaStream_t stream);
+                    uint32_t flags, uint32_t* work, uint32_t sm_count, cudaStream_t stream);
 void launch_finalize(const DeviceView* views, uint32_t nviews, cudaStream_t stream);
 
 // ---- adjoint of the resolve

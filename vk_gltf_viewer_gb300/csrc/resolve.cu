@@ -326,6 +326,55 @@ __device__ uint32_t motion_vector(const SceneArgs& S, const DeviceView& V, const
            ((uint32_t)__half_as_ushort(__float2half_rn(fsub(prev_y, cur_y))) << 16);
 }
 
+// One pixel of the resolve: its id, and its colour and motion vector.
+// The outputs a resolve writes for one view (null where the flags skip them).
+struct ResolveOut {
+    uint32_t* ids;
+    uint32_t* rgba;
+    uint32_t* motion;
+};
+
+template <bool MOTION>
+__device__ __forceinline__ ResolveOut resolve_outputs(const DeviceView& V, uint32_t flags) {
+    return {(flags & VKGV_WRITE_IDS) ? V.ids : nullptr,
+            (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED)) ? V.rgba : nullptr, MOTION ? V.motion : nullptr};
+}
+
+template <bool TEXTURED, bool MOTION>
+__device__ __forceinline__ void resolve_pixel(const SceneArgs& S, const DeviceView& V, const float* s_unorm,
+                                              const ResolveOut& o, uint32_t w, uint32_t p) {
+    uint32_t* ids = o.ids;
+    uint32_t* rgba = o.rgba;
+    uint32_t* motion = o.motion;
+    const uint32_t lo = (uint32_t)__ldcs(V.depth_id + p);
+    const uint32_t id = lo ? lo - 1u : VKGV_VISBUFFER_CLEAR;
+    if (ids) __stcs(ids + p, id);
+    if (!rgba && !MOTION) return;
+    uint32_t out = 0, mv = 0;
+    if (id != VKGV_VISBUFFER_CLEAR) {
+        float lin[4];
+        if (TEXTURED || MOTION) {
+            Frag f;
+            frag_setup<MOTION, TEXTURED>(S, V, p % w, p / w, id, f);
+            if (MOTION) mv = motion_vector(S, V, f);
+            if (TEXTURED) {
+                shade_textured(S, f, s_unorm, lin);
+            } else {
+                const float4 a = *reinterpret_cast<const float4*>(f.mat->albedo_factor);
+                lin[0] = a.x, lin[1] = a.y, lin[2] = a.z, lin[3] = a.w;
+            }
+        } else {
+            const vkgv_meshlet_draw dr = S.draws[id >> VKGV_TRIANGLE_BITS];
+            const vkgv_material& mat = S.mats[S.prims[dr.primitive_index].material_index];
+            const float4 a = *reinterpret_cast<const float4*>(mat.albedo_factor);
+            lin[0] = a.x, lin[1] = a.y, lin[2] = a.z, lin[3] = a.w;
+        }
+        if (rgba) out = TEXTURED ? pack_rgba_fast(lin) : pack_rgba(lin);
+    }
+    if (rgba) __stcs(rgba + p, out);
+    if (MOTION) __stcs(motion + p, mv);
+}
+
 template <bool TEXTURED, bool MOTION>
 __global__ void __launch_bounds__(256, 6) k_resolve(SceneArgs S, const DeviceView* __restrict__ views, uint32_t flags) {
     pdl_begin();
@@ -336,38 +385,81 @@ __global__ void __launch_bounds__(256, 6) k_resolve(SceneArgs S, const DeviceVie
         __syncthreads();
     }
     const uint32_t w = V.w, n = V.w * V.h;
-    uint32_t* ids = (flags & VKGV_WRITE_IDS) ? V.ids : nullptr;
-    uint32_t* rgba = (flags & (VKGV_RESOLVE_FLAT | VKGV_RESOLVE_TEXTURED)) ? V.rgba : nullptr;
-    uint32_t* motion = MOTION ? V.motion : nullptr;
+    const ResolveOut o = resolve_outputs<MOTION>(V, flags);
     if (blockIdx.x == 0 && threadIdx.x == 0) finalize_view(V);
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const uint32_t lo = (uint32_t)__ldcs(V.depth_id + p);
-        const uint32_t id = lo ? lo - 1u : VKGV_VISBUFFER_CLEAR;
-        if (ids) __stcs(ids + p, id);
-        if (!rgba && !MOTION) continue;
-        uint32_t out = 0, mv = 0;
-        if (id != VKGV_VISBUFFER_CLEAR) {
-            float lin[4];
-            if (TEXTURED || MOTION) {
-                Frag f;
-                frag_setup<MOTION, TEXTURED>(S, V, p % w, p / w, id, f);
-                if (MOTION) mv = motion_vector(S, V, f);
-                if (TEXTURED) {
-                    shade_textured(S, f, s_unorm, lin);
-                } else {
-                    const float4 a = *reinterpret_cast<const float4*>(f.mat->albedo_factor);
-                    lin[0] = a.x, lin[1] = a.y, lin[2] = a.z, lin[3] = a.w;
-                }
-            } else {
-                const vkgv_meshlet_draw dr = S.draws[id >> VKGV_TRIANGLE_BITS];
-                const vkgv_material& mat = S.mats[S.prims[dr.primitive_index].material_index];
-                const float4 a = *reinterpret_cast<const float4*>(mat.albedo_factor);
-                lin[0] = a.x, lin[1] = a.y, lin[2] = a.z, lin[3] = a.w;
-            }
-            if (rgba) out = TEXTURED ? pack_rgba_fast(lin) : pack_rgba(lin);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        resolve_pixel<TEXTURED, MOTION>(S, V, s_unorm, o, w, p);
+}
+
+// Several views: one wave of resident CTAs whose warps take chunks of
+// kResolveChunk pixels (all views' chunks numbered in view order) from a
+// global counter, so views smaller than the largest cost no empty CTAs.
+// The warp that takes a view's first chunk finalizes the view; the last CTA
+// to finish returns the counters to zero.
+constexpr uint32_t kResolveChunk = 2048;
+constexpr uint32_t kResolveMaxViews = 4096;
+
+template <bool TEXTURED, bool MOTION>
+__global__ void __launch_bounds__(256, 6) k_resolve_chunks(SceneArgs S, const DeviceView* __restrict__ views,
+                                                           uint32_t nviews, uint32_t flags, uint32_t* work) {
+    pdl_begin();
+    __shared__ float s_unorm[256];
+    __shared__ uint32_t s_pre[kResolveMaxViews + 1];
+    if (TEXTURED) s_unorm[threadIdx.x] = fdiv((float)threadIdx.x, 255.0f);  // blockDim.x == 256
+    for (uint32_t v = threadIdx.x; v < nviews; v += blockDim.x)
+        s_pre[v + 1] = (views[v].w * views[v].h + kResolveChunk - 1) / kResolveChunk;
+    if (threadIdx.x == 0) s_pre[0] = 0;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // inclusive scan of s_pre[1..nviews]: lane-contiguous segments, then
+        // a warp scan of the segment sums
+        const uint32_t lane = threadIdx.x, seg = (nviews + 31) / 32;
+        const uint32_t b = 1 + lane * seg, e = min(b + seg, nviews + 1);
+        uint32_t sum = 0;
+        for (uint32_t i = b; i < e; ++i) sum += s_pre[i];
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += t;
         }
-        if (rgba) __stcs(rgba + p, out);
-        if (MOTION) __stcs(motion + p, mv);
+        uint32_t run = incl - sum;
+        for (uint32_t i = b; i < e; ++i) {
+            run += s_pre[i];
+            s_pre[i] = run;
+        }
+    }
+    __syncthreads();
+    const uint32_t total = s_pre[nviews];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t item = 0;
+        if (lane == 0) item = atomicAdd(work, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        uint32_t v = 0, hi = nviews;
+        while (v + 1 < hi) {
+            const uint32_t mid = (v + hi) >> 1;
+            if (s_pre[mid] <= item) v = mid;
+            else hi = mid;
+        }
+        const DeviceView& V = views[v];
+        if (item == s_pre[v] && lane == 0) finalize_view(V);
+        const uint32_t w = V.w, n = V.w * V.h, base = (item - s_pre[v]) * kResolveChunk;
+        const ResolveOut o = resolve_outputs<MOTION>(V, flags);
+#pragma unroll 1
+        for (uint32_t j = lane; j < kResolveChunk; j += 32) {
+            const uint32_t p = base + j;
+            if (p < n) resolve_pixel<TEXTURED, MOTION>(S, V, s_unorm, o, w, p);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(work + 1, 1u) == gridDim.x - 1) {
+            work[0] = 0;
+            work[1] = 0;
+        }
     }
 }
 
@@ -449,13 +541,34 @@ __global__ void k_finalize(const DeviceView* __restrict__ views, uint32_t nviews
 
 }  // namespace
 
+template <bool T, bool M>
+bool launch_resolve_chunks(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t flags,
+                           uint32_t* work, uint32_t sm_count, cudaStream_t stream) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resolve_chunks<T, M>, 256, 0) != cudaSuccess ||
+        per_sm <= 0) {
+        cudaGetLastError();
+        return false;
+    }
+    launch_pdl(k_resolve_chunks<T, M>, dim3(sm_count * (uint32_t)per_sm), dim3(256), 0, stream, S, views, nviews,
+               flags, work);
+    return true;
+}
+
 void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h,
-                    uint32_t flags, cudaStream_t stream) {
+                    uint32_t flags, uint32_t* work, uint32_t sm_count, cudaStream_t stream) {
+    const bool tex = (flags & VKGV_RESOLVE_TEXTURED) != 0, mv = (flags & VKGV_WRITE_MOTION) != 0;
+    if (nviews > 1 && nviews <= kResolveMaxViews && work && sm_count) {
+        const bool done = tex && mv ? launch_resolve_chunks<true, true>(S, views, nviews, flags, work, sm_count, stream)
+                          : tex     ? launch_resolve_chunks<true, false>(S, views, nviews, flags, work, sm_count, stream)
+                          : mv      ? launch_resolve_chunks<false, true>(S, views, nviews, flags, work, sm_count, stream)
+                                    : launch_resolve_chunks<false, false>(S, views, nviews, flags, work, sm_count, stream);
+        if (done) return;
+    }
     const uint64_t px = (uint64_t)max_w * max_h;
     uint32_t bx = (uint32_t)((px + 255) / 256);
     if (bx > 65535u) bx = 65535u;
     dim3 grid(bx, nviews);
-    const bool tex = (flags & VKGV_RESOLVE_TEXTURED) != 0, mv = (flags & VKGV_WRITE_MOTION) != 0;
     if (tex && mv)
         launch_pdl(k_resolve<true, true>, grid, dim3(256), 0, stream, S, views, flags);
     else if (tex)
