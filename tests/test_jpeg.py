@@ -140,3 +140,35 @@ def test_errors(built):
         texture.Jpeg(wide)
     # a missing EOI is accepted: the scans are complete
     assert texture.Jpeg(data[:-2]).info.width == 24
+
+
+@pytest.mark.parametrize("progressive", [False, True])
+def test_restart_intervals_decoded_on_threads(built, progressive):
+    """Enough restart intervals for the threaded entropy decode (runs of
+    intervals on several threads): the same coefficients, and a restart
+    marker out of order or a damaged interval still fails."""
+    img = _image(512, 384, seed=3)
+    data, expected = encode(img, rng=np.random.default_rng(5), sampling=((2, 2), (1, 1), (1, 1)), restart=3,
+                            progressive=progressive)
+    for g, e in zip(texture.Jpeg(data).planes, expected):
+        assert np.array_equal(g, e)
+    # the 40th restart marker of the first scan renumbered
+    sos = data.index(b"\xff\xda")
+    at, k = sos, 0
+    while k < 40:
+        at = data.index(b"\xff", at + 1)
+        if 0xD0 <= data[at + 1] <= 0xD7:
+            k += 1
+    bad = bytearray(data)
+    bad[at + 1] = 0xD0 + ((bad[at + 1] - 0xD0 + 3) & 7)
+    with pytest.raises(abi.VkgvError, match="restart marker"):
+        texture.Jpeg(bytes(bad))
+    # entropy bytes of a middle interval damaged: an error, never a crash
+    bad = bytearray(data)
+    for j in range(at - 12, at - 2):
+        if bad[j] not in (0xFF, 0x00):
+            bad[j] ^= 0x5A
+    try:
+        texture.Jpeg(bytes(bad)).close()
+    except abi.VkgvError:
+        pass

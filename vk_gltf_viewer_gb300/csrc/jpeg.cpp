@@ -29,6 +29,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 struct vkgv_jpeg {
@@ -194,7 +195,6 @@ struct Decoder {
     // multiplied by the table each component's first scan used
     uint16_t latched[3][64];
     bool latched_set[3] = {false, false, false};
-    uint32_t eobrun = 0;  // blocks left in the current end-of-band run
     uint8_t adobe_transform = 1;
 
     Decoder(const uint8_t* d, size_t s, vkgv_jpeg& o) : data(d), size(s), out(o) {}
@@ -311,7 +311,7 @@ struct Decoder {
     static void dc_refine(BitReader& br, int al, int16_t* dst) {
         if (br.bits(1)) dst[0] = int16_t(dst[0] | (1 << al));
     }
-    void ac_first(BitReader& br, const Huffman& ha, int ss, int se, int al, int16_t* dst) {
+    static void ac_first(BitReader& br, const Huffman& ha, int ss, int se, int al, int16_t* dst, uint32_t& eobrun) {
         if (eobrun > 0) {
             --eobrun;
             return;
@@ -334,7 +334,7 @@ struct Decoder {
             ++k;
         }
     }
-    void ac_refine(BitReader& br, const Huffman& ha, int ss, int se, int al, int16_t* dst) {
+    static void ac_refine(BitReader& br, const Huffman& ha, int ss, int se, int al, int16_t* dst, uint32_t& eobrun) {
         const uint8_t* nat = zigzag().natural;
         const int p1 = 1 << al, m1 = -(1 << al);
         // a coefficient already nonzero takes one correction bit
@@ -388,9 +388,9 @@ struct Decoder {
         if (len < 1) bad("short scan header");
         const uint32_t ns = seg[0];
         if (ns < 1 || ns > ncomp || len < 4 + 2 * ns) bad("bad scan header");
-        uint32_t idx[3];
-        const Huffman* hd[3];
-        const Huffman* ha[3];
+        uint32_t idx[3] = {0, 0, 0};
+        const Huffman* hd[3] = {nullptr, nullptr, nullptr};
+        const Huffman* ha[3] = {nullptr, nullptr, nullptr};
         uint16_t q[3][64];
         uint32_t per_mcu = 0;
         for (uint32_t i = 0; i < ns; ++i) {
@@ -429,43 +429,133 @@ struct Decoder {
                 latched_set[idx[i]] = true;
             }
         }
-        eobrun = 0;
-        BitReader br(data_begin, data_end);
-        int32_t pred[3] = {0, 0, 0};
         const uint32_t units_w = ns == 1 ? comp[idx[0]].scan_w : mcux;
         const uint32_t units_h = ns == 1 ? comp[idx[0]].scan_h : mcuy;
         const uint64_t units = uint64_t(units_w) * units_h;
-        uint32_t next_rst = 0;
-        for (uint64_t u = 0; u < units; ++u) {
-            if (restart && u && u % restart == 0) {
-                br.finish_interval(true);
-                if (br.p + 1 >= data_end || br.p[0] != 0xFF || br.p[1] != 0xD0 + next_rst)
-                    bad("missing or out-of-order restart marker");
-                next_rst = (next_rst + 1) & 7;
-                br.p += 2;
-                br.at_marker = false;
-                pred[0] = pred[1] = pred[2] = 0;
-                eobrun = 0;
-            }
-            const uint32_t ux = uint32_t(u % units_w), uy = uint32_t(u / units_w);
-            for (uint32_t i = 0; i < ns; ++i) {
-                Component& k = comp[idx[i]];
-                const uint32_t bh = ns == 1 ? 1 : k.v, bw = ns == 1 ? 1 : k.h;
-                for (uint32_t y = 0; y < bh; ++y)
-                    for (uint32_t x = 0; x < bw; ++x) {
-                        const uint32_t gx = ux * bw + x, gy = uy * bh + y;
-                        int16_t* dst = out.coef[idx[i]].data() + (size_t(gy) * k.blocks_w + gx) * 64;
-                        if (!progressive) block(br, *hd[i], *ha[i], q[i], pred[i], dst);
-                        else if (dc_scan && !refine) dc_first(br, *hd[i], pred[i], al, dst);
-                        else if (dc_scan) dc_refine(br, al, dst);
-                        else if (!refine) ac_first(br, *ha[i], ss, se, al, dst);
-                        else ac_refine(br, *ha[i], ss, se, al, dst);
-                    }
-            }
+        ScanPlan S{ns, {idx[0], idx[1], idx[2]}, {hd[0], hd[1], hd[2]}, {ha[0], ha[1], ha[2]}, {}, units_w,
+                   ss, se, al, dc_scan, refine, data_end};
+        std::memcpy(S.q, q, sizeof(q));
+        // restart intervals are independent (predictors and end-of-band runs
+        // restart): with many of them, threads decode runs of intervals
+        const uint64_t intervals = restart ? (units + restart - 1) / restart : 1;
+        const unsigned hw = std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+        if (intervals >= 8 && hw > 1 && units * per_mcu >= 4096) {
+            std::vector<const uint8_t*> starts;
+            if (find_intervals(data_begin, data_end, intervals, starts))
+                return decode_parallel(S, units, intervals, starts, std::min<uint64_t>(hw, intervals / 2));
         }
+        BitReader br(data_begin, data_end);
+        decode_units(br, S, 0, units, 0);
         br.finish_interval(false);
         for (uint32_t i = 0; i < ns; ++i) comp[idx[i]].decoded = true;
         return br.p;
+    }
+
+    // What decoding a scan needs besides the bits.
+    struct ScanPlan {
+        uint32_t ns, idx[3];
+        const Huffman* hd[3];
+        const Huffman* ha[3];
+        uint16_t q[3][64];
+        uint32_t units_w;
+        int ss, se, al;
+        bool dc_scan, refine;
+        const uint8_t* data_end;
+    };
+
+    // Units [u0, u1) (whole restart intervals), the first one at an interval
+    // start; `rst` is the number of the first restart marker expected.
+    void decode_units(BitReader& br, const ScanPlan& S, uint64_t u0, uint64_t u1, uint32_t rst) {
+        int32_t pred[3] = {0, 0, 0};
+        uint32_t eobrun = 0;
+        for (uint64_t u = u0; u < u1; ++u) {
+            if (restart && u != u0 && u % restart == 0) {
+                expect_restart(br, S.data_end, rst);
+                rst = (rst + 1) & 7;
+                pred[0] = pred[1] = pred[2] = 0;
+                eobrun = 0;
+            }
+            const uint32_t ux = uint32_t(u % S.units_w), uy = uint32_t(u / S.units_w);
+            for (uint32_t i = 0; i < S.ns; ++i) {
+                Component& k = comp[S.idx[i]];
+                const uint32_t bh = S.ns == 1 ? 1 : k.v, bw = S.ns == 1 ? 1 : k.h;
+                for (uint32_t y = 0; y < bh; ++y)
+                    for (uint32_t x = 0; x < bw; ++x) {
+                        const uint32_t gx = ux * bw + x, gy = uy * bh + y;
+                        int16_t* dst = out.coef[S.idx[i]].data() + (size_t(gy) * k.blocks_w + gx) * 64;
+                        if (!progressive) block(br, *S.hd[i], *S.ha[i], S.q[i], pred[i], dst);
+                        else if (S.dc_scan && !S.refine) dc_first(br, *S.hd[i], pred[i], S.al, dst);
+                        else if (S.dc_scan) dc_refine(br, S.al, dst);
+                        else if (!S.refine) ac_first(br, *S.ha[i], S.ss, S.se, S.al, dst, eobrun);
+                        else ac_refine(br, *S.ha[i], S.ss, S.se, S.al, dst, eobrun);
+                    }
+            }
+        }
+    }
+
+    // At the end of a restart interval: only padding left, then RST<rst>.
+    static void expect_restart(BitReader& br, const uint8_t* data_end, uint32_t rst) {
+        br.finish_interval(true);
+        if (br.p + 1 >= data_end || br.p[0] != 0xFF || br.p[1] != 0xD0 + rst)
+            bad("missing or out-of-order restart marker");
+        br.p += 2;
+        br.at_marker = false;
+    }
+
+    // The start of each restart interval, where the serial reader would find
+    // it: after the first 0xFF not followed by 0x00, which must be the next
+    // RST marker.  False (the serial decoder then reports the fault) when
+    // the markers are missing, out of order or too few.
+    static bool find_intervals(const uint8_t* p, const uint8_t* end, uint64_t intervals,
+                               std::vector<const uint8_t*>& starts) {
+        starts.push_back(p);
+        for (uint64_t k = 0; k + 1 < intervals; ++k) {
+            for (;;) {
+                if (end - p < 2) return false;
+                if (p[0] == 0xFF && p[1] != 0x00) break;
+                p += p[0] == 0xFF ? 2 : 1;
+            }
+            if (p[1] != 0xD0 + (k & 7)) return false;
+            p += 2;
+            starts.push_back(p);
+        }
+        return true;
+    }
+
+    // Runs of whole intervals on `threads` threads; the fault of the first
+    // failing run is reported, as the serial decoder would report it.
+    const uint8_t* decode_parallel(const ScanPlan& S, uint64_t units, uint64_t intervals,
+                                   const std::vector<const uint8_t*>& starts, uint64_t threads) {
+        std::vector<std::string> errors(threads);
+        std::vector<char> failed(threads, 0);
+        const uint8_t* tail = nullptr;
+        auto run = [&](uint64_t t) {
+            const uint64_t i0 = intervals * t / threads, i1 = intervals * (t + 1) / threads;
+            try {
+                BitReader br(starts[i0], S.data_end);
+                decode_units(br, S, i0 * restart, std::min(units, i1 * restart), uint32_t(i0 & 7));
+                if (i1 < intervals) {
+                    expect_restart(br, S.data_end, uint32_t((i1 - 1) & 7));
+                } else {
+                    br.finish_interval(false);
+                    tail = br.p;
+                }
+            } catch (const JpegError& e) {
+                errors[t] = e.msg;
+                failed[t] = 1;
+            } catch (...) {
+                errors[t] = "JPEG decode failed";
+                failed[t] = 1;
+            }
+        };
+        std::vector<std::thread> pool;
+        for (uint64_t t = 1; t < threads; ++t) pool.emplace_back(run, t);
+        run(0);
+        for (auto& th : pool) th.join();
+        for (uint64_t t = 0; t < threads; ++t)
+            if (failed[t]) bad(errors[t]);
+        for (uint32_t i = 0; i < S.ns; ++i) comp[S.idx[i]].decoded = true;
+        return tail;
     }
 
     void run() {
