@@ -516,7 +516,13 @@ def run_texture(r, local, args, stream, peak):
     torch.cuda.synchronize()
     dev_ms = statistics.median(a.elapsed_time(b) for a, b in ts)
     coef_bytes = sum(p.nbytes for p in j.planes)
+    # the same image with a restart marker every 16 MCUs: intervals on host threads
+    jr = _synthetic_jpeg(2048, 2048, np.random.default_rng(3), restart=16)
+    t0 = time.perf_counter()
+    texture.Jpeg(jr).close()
+    restart_ms = 1000.0 * (time.perf_counter() - t0)
     out["jpeg_2048"] = {"bytes": len(jpg), "host_entropy_ms": host_ms, "device_ms": dev_ms,
+                        "host_entropy_ms_restart_16": restart_ms,
                         "coefficient_bytes": int(coef_bytes),
                         "note": "4:2:0, blocks from 256 random coefficient sets, 8-bit AC codes; device time "
                                 "includes the pageable copy of the coefficient planes, the IDCT and the colour pass"}
@@ -524,10 +530,11 @@ def run_texture(r, local, args, stream, peak):
     return out
 
 
-def _synthetic_jpeg(w: int, h: int, rng) -> bytes:
+def _synthetic_jpeg(w: int, h: int, rng, restart: int = 0) -> bytes:
     """A valid baseline 4:2:0 JPEG of w x h (multiples of 16): every block one
     of 256 random coefficient sets (magnitudes falling with frequency, DC
-    differences 0), coded with one 1-bit DC code and 8-bit AC codes."""
+    differences 0), coded with one 1-bit DC code and 8-bit AC codes; with
+    `restart`, a restart marker every `restart` MCUs."""
     import struct
 
     import numpy as np
@@ -555,9 +562,14 @@ def _synthetic_jpeg(w: int, h: int, rng) -> bytes:
         pool.append(np.array(bits, np.uint8))
     mcus = (w // 16) * (h // 16)
     choice = rng.integers(0, 256, mcus * 6)
-    stream = np.concatenate([pool[c] for c in choice])
-    stream = np.concatenate([stream, np.ones(-len(stream) % 8, np.uint8)])
-    data = np.packbits(stream).tobytes().replace(b"\xff", b"\xff\x00")
+    step = restart or mcus
+    data = b""
+    for k, first in enumerate(range(0, mcus, step)):
+        bits = np.concatenate([pool[c] for c in choice[6 * first:6 * min(first + step, mcus)]])
+        bits = np.concatenate([bits, np.ones(-len(bits) % 8, np.uint8)])  # pad with 1-bits
+        data += np.packbits(bits).tobytes().replace(b"\xff", b"\xff\x00")
+        if first + step < mcus:
+            data += bytes([0xFF, 0xD0 + (k & 7)])
     values = sorted(sym_index, key=sym_index.get)
     seg = lambda m, body: struct.pack(">BBH", 0xFF, m, len(body) + 2) + body
     q = bytes([4] * 64)
@@ -566,6 +578,8 @@ def _synthetic_jpeg(w: int, h: int, rng) -> bytes:
     dc = bytes([0x00, 1] + [0] * 15 + [0])
     ac = bytes([0x10] + [0] * 7 + [len(values)] + [0] * 8) + bytes(values)
     out += seg(0xC4, dc) + seg(0xC4, ac)
+    if restart:
+        out += seg(0xDD, struct.pack(">H", restart))
     out += seg(0xDA, bytes([3, 1, 0x00, 2, 0x00, 3, 0x00, 0, 63, 0])) + data + b"\xff\xd9"
     return out
 
