@@ -122,21 +122,29 @@ class ClockSampler:
 
 # --------------------------------------------------------------- reference
 
+def bench_config(draws: int, triangles: int, world: int) -> dict:
+    """The workload description both arms print."""
+    return {"workload": WORKLOAD, "flags": FLAGS_NAMES, "width": W1080, "height": H1080,
+            "draws": draws, "triangles": triangles,
+            "l2": "256 MiB buffer written between timed steps (outside the events)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+
 def run_reference(args, rank, world):
     """The reference's path on the host cores: the CPU restatement of the
     shader math (the Vulkan renderer itself cannot run here), same workload,
-    all host threads, steady state."""
+    all host threads, steady state.  Its scene and camera come from the
+    oracle's own producers (byte-identical to the product's, checked by
+    tests/test_oracle_scene.py), so this arm never loads the product library."""
     if rank != 0:
         return
-    import numpy as np
-
     from oracle import binding as ob
-    from vk_gltf_viewer_gb300 import scene
+    from oracle import scene as oscene
 
     threads = os.cpu_count() or 1
     ob.set_threads(threads)
-    host = scene.scene_torus_grid()
-    cam = scene.grid_camera(W1080, H1080)
+    host = oscene.scene_torus_grid()
+    cam = oscene.grid_camera(W1080, H1080)
     osc = ob.OracleScene(host)
     flags = (ob.CULL_FRUSTUM | ob.CULL_CONE | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID
              | ob.RESOLVE_TEXTURED)
@@ -148,13 +156,12 @@ def run_reference(args, rank, world):
         prev = ob.frame(osc, cam, W1080, H1080, flags, prev_pyramid=prev)["pyramid"]
     dt = time.perf_counter() - t0
     v = args.steps / dt
-    del np
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "views/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "flags": FLAGS_NAMES},
+        "config": bench_config(host.draw_count, host.triangle_count, world),
         "cpu_baseline": {"value": v, "unit": "views/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} steady-state frames of the workload on {threads} host threads"},
         "e2e": {"value": v, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -915,10 +922,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "views/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "flags": FLAGS_NAMES, "width": W1080, "height": H1080,
-                       "draws": host.draw_count, "triangles": host.triangle_count,
-                       "l2": "256 MiB buffer written between timed steps (outside the events)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "config": bench_config(host.draw_count, host.triangle_count, world),
             "e2e": {"value": e2e_value, "unit": "views/s", "h2d_bytes_per_step": 352,
                     "d2h_bytes_per_step": W1080 * H1080 * 4,
                     "note": "camera H2D + frame + RGBA8 D2H per step; the D2H of step i overlaps step i+1 "
