@@ -9,6 +9,7 @@ Vulkan mesh-shader device, which does not exist here).
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -62,6 +63,58 @@ class OrcAnimSampler(C.Structure):
 
 
 _lib = None
+_ref = None
+REF_LIB = HERE / "_ref" / "libvkgv_ref.so"
+
+
+def reference_sources() -> Path | None:
+    """The reference's source tree when it is present on this machine (the
+    reference build of _ref/ needs its shaders/ directory); None elsewhere."""
+    root = Path(os.environ.get("VKGV_REFERENCE", "/root/reference"))
+    return root if (root / "shaders" / "common.h.glsl").exists() else None
+
+
+def build_ref() -> Path | None:
+    """Compiles the reference's shared GLSL headers in their C++ mode into
+    _ref/libvkgv_ref.so (oracle/Makefile `ref`).  Returns None when the
+    reference sources are absent, or the library already built earlier."""
+    src = reference_sources()
+    if src is None:
+        return REF_LIB if REF_LIB.exists() else None
+    res = subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={src}"], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"reference header build failed:\n{res.stdout}\n{res.stderr}")
+    return REF_LIB
+
+
+def load_ref() -> C.CDLL | None:
+    """The reference-header library (see build_ref), or None if unbuilt."""
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists() and build_ref() is None:
+            return None
+        lib = C.CDLL(str(REF_LIB))
+        U32 = C.c_uint32
+        lib.ref_layout_count.restype = U32
+        lib.ref_layout_name.restype = C.c_char_p
+        lib.ref_layout_name.argtypes = [U32]
+        lib.ref_layout_value.restype = U32
+        lib.ref_layout_value.argtypes = [U32]
+        lib.ref_pack_visbuffer.restype = U32
+        lib.ref_pack_visbuffer.argtypes = [U32, U32]
+        lib.ref_unpack_visbuffer.argtypes = [U32, C.POINTER(U32), C.POINTER(U32)]
+        lib.ref_from_linear.restype = C.c_float
+        lib.ref_from_linear.argtypes = [C.c_float]
+        lib.ref_to_linear.restype = C.c_float
+        lib.ref_to_linear.argtypes = [C.c_float]
+        lib.ref_from_linear4.argtypes = [C.c_void_p, C.c_void_p]
+        lib.ref_to_linear4.argtypes = [C.c_void_p, C.c_void_p]
+        _ref = lib
+    return _ref
+
+
+def ref_layout(lib) -> dict[str, int]:
+    return {lib.ref_layout_name(i).decode(): int(lib.ref_layout_value(i)) for i in range(lib.ref_layout_count())}
 
 
 def build() -> Path:

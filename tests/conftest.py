@@ -21,6 +21,7 @@ def built():
 
     vbuild.build()
     binding.build()
+    binding.build_ref()
     binding.set_threads(min(8, os.cpu_count() or 1))
     return True
 
