@@ -270,9 +270,19 @@ int vkgv_cull(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view,
  * required.  All calls share the array and leave its contents behind (pass 2
  * re-tests the rejects of the preceding pass-1 call); calls that overlap on
  * the GPU race.  The first call on a device looks up the array's device
- * address, so make it before any stream capture. */
+ * address, so make it before any stream capture; the address is kept for the
+ * lifetime of the device's primary context (not valid across a
+ * cudaDeviceReset).  Device-side faults (an out-of-range meshlet index, a
+ * full survivor list) are recorded in the array's status words, cleared by
+ * each pass-1 call: read them with vkgv_cull_static_status. */
 int vkgv_cull_static(const vkgv_scene* scene, const vkgv_view* view, uint32_t flags,
                      uint32_t pass, void* stream);
+/* No counterpart in the reference.  Reads the status words that
+ * vkgv_cull_static calls on the current device left since the last pass-1
+ * call (code 0 = none; otherwise the first recorded fault, as
+ * vkgv_device_status reports it) and clears them.  Ordered after the work on
+ * `stream`, which it synchronises; allocates nothing. */
+int vkgv_cull_static_status(void* stream, uint32_t* out_code, uint32_t* out_detail);
 /* Mesh shader + raster + fragment shader
  * (shaders/visbuffer/visbuffer.mesh.glsl:30-104, visbuffer.frag.glsl:28-39):
  * rasterises draw_list[first .. *draw_count) into view->depth_id with a

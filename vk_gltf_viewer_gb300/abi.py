@@ -230,6 +230,7 @@ _PROTOS = {
     "vkgv_clear": (C.c_int, [_P, C.POINTER(View), _P]),
     "vkgv_cull": (C.c_int, [_P, C.POINTER(Scene), C.POINTER(View), _U32, _U32, _P]),
     "vkgv_cull_static": (C.c_int, [C.POINTER(Scene), C.POINTER(View), _U32, _U32, _P]),
+    "vkgv_cull_static_status": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32)]),
     "vkgv_raster": (C.c_int, [_P, C.POINTER(Scene), C.POINTER(View), _U64, _U64, _U32, _P]),
     "vkgv_hiz_reduce": (C.c_int, [_P, C.POINTER(View), _P]),
     "vkgv_resolve": (C.c_int, [_P, C.POINTER(Scene), C.POINTER(View), _U32, _P]),

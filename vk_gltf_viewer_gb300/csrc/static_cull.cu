@@ -20,7 +20,12 @@
 //     overlap on the GPU race with each other;
 //   - the first call on a device resolves the array's device address with
 //     cudaGetSymbolAddress on that device, so make that first call before
-//     any stream capture begins.
+//     any stream capture begins; the address is kept for the lifetime of the
+//     device's primary context (a cudaDeviceReset ends it, so do not call
+//     these entry points after one);
+//   - device-side faults (a draw whose meshlet index is out of range, a
+//     survivor list too short) go to the array's status words, which a pass-1
+//     call clears; vkgv_cull_static_status reads and clears them.
 #include <mutex>
 
 #include "kernels.cuh"
@@ -147,5 +152,26 @@ extern "C" int vkgv_cull_static(const vkgv_scene* scene, const vkgv_view* view, 
     launch_cull(S, &s->view, 1, flags, pass, s->status, sm_count, stream);
     launch_finalize(&s->view, 1, stream);
     if (cudaGetLastError() != cudaSuccess) return VKGV_CUDA_ERROR;
+    return VKGV_OK;
+}
+
+extern "C" int vkgv_cull_static_status(void* stream_, uint32_t* out_code, uint32_t* out_detail) {
+    if (!out_code || !out_detail) return VKGV_INVALID_ARG;
+    StaticScratch* s = nullptr;
+    uint32_t sm_count = 1;
+    int rc = scratch_for_current_device(&s, &sm_count);
+    if (rc != VKGV_OK) return rc;
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    uint32_t words[2] = {0u, 0u};
+    // stream-ordered after the culls on `stream`; the words then start again
+    // from zero for the calls that follow
+    if (cudaMemcpyAsync(words, s->status, sizeof(words), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess ||
+        cudaMemsetAsync(s->status, 0, sizeof(words), stream) != cudaSuccess) {
+        cudaGetLastError();
+        return VKGV_CUDA_ERROR;
+    }
+    *out_code = words[0];
+    *out_detail = words[1];
     return VKGV_OK;
 }
