@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--batched-only", action="store_true",
                    help="run only the batched leg (for profiling); prints its own JSON line")
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-c1", action="store_true", help="skip the icosphere (C1) single-view leg")
     p.add_argument("--no-motion", action="store_true", help="skip the motion-vector frame")
     p.add_argument("--no-world", action="store_true", help="skip the node-tree transform and draw-list leg")
     p.add_argument("--no-texture", action="store_true", help="skip the texture decode leg")
@@ -172,15 +173,22 @@ def run_reference(args, rank, world):
 
 def run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier):
     """Batched leg: the uneven views rendered in one captured graph launch,
-    steady state (each view reads its own previous pyramid)."""
+    steady state (each view reads its own previous pyramid).  Under N ranks
+    the views are sharded by pixel count (sharding.shard_views), so every
+    view is rendered once across the ranks; the value is all views over the
+    slowest rank's time."""
     import numpy as np
     import torch
 
-    from vk_gltf_viewer_gb300 import scene
+    from vk_gltf_viewer_gb300 import scene, sharding
     from vk_gltf_viewer_gb300.renderer import ViewBuffers
 
+    rank = int(os.environ.get("RANK", "0"))
+    poses = scene.batch_views(args.batch_views)
+    mine = sharding.shard_views([w * h for _, w, h in poses], world, rank)
     bv = []
-    for bcam, w, h in scene.batch_views(args.batch_views):
+    for i in mine:
+        bcam, w, h = poses[i]
         vb = ViewBuffers.allocate(w, h, bcam, host.draw_count, device=f"cuda:{local}", prev_pyramid="alias",
                                   survivors=False)
         bv.append(vb)
@@ -214,7 +222,7 @@ def run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier):
     tb = torch.tensor([b0.elapsed_time(b1) / 1000.0], device=f"cuda:{local}")
     if pg:
         pg.all_reduce(tb, op=pg.ReduceOp.MAX)
-    bval = world * bsteps * len(bv) / float(tb.item())
+    bval = bsteps * len(poses) / float(tb.item())
     kernels_per_launch = bgraph.kernel_count()
     bgraph.close()
 
@@ -235,21 +243,75 @@ def run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier):
     ts = torch.tensor([s0.elapsed_time(s1) / 1000.0], device=f"cuda:{local}")
     if pg:
         pg.all_reduce(ts, op=pg.ReduceOp.MAX)
-    sval = world * bsteps * len(bv) / float(ts.item())
+    sval = bsteps * len(poses) / float(ts.item())
     for g in singles:
         g.close()
     r.close()
-    out = {"value": bval, "unit": "views/s", "views_per_launch": len(bv), "steps": bsteps,
+    out = {"value": bval, "unit": "views/s", "views_per_launch": len(poses), "views_this_rank": len(bv),
+           "steps": bsteps,
            "single_view_same_poses": {"value": sval, "unit": "views/s",
                                       "ms_per_pass": 1000.0 * float(ts.item()) / bsteps},
            "speedup_vs_single_view_same_poses": bval / sval,
            "autotune": {"bin_size": tune["bin_size"], "meshlets_per_cta": tune["meshlets_per_cta"],
                         "cached": tune["cached"], "table": tune["table"]},
            "ms_per_launch": 1000.0 * float(tb.item()) / bsteps, "kernels_per_launch": kernels_per_launch,
-           "mean_pixels_per_view": float(np.mean([vb.width * vb.height for vb in bv])),
+           "mean_pixels_per_view": float(np.mean([w * h for _, w, h in poses])),
            "stages_ms": stages,
-           "config": f"{len(bv)} poses on a radius-30 sphere around the grid centre, sizes uniform over "
+           "sharding": f"{len(bv)} of {len(poses)} views on rank {rank} of {world} (pixel-balanced)",
+           "config": f"{len(poses)} poses on a radius-30 sphere around the grid centre, sizes uniform over "
                      "256^2, 512x384, 1024x576, 1280x720, 1920x1080"}
+    return out
+
+
+def run_c1(local, args, stream, flush, cpu: bool):
+    """C1: the level-6 icosphere (81,920 triangles) at 1280x720, camera at
+    (0, 0, 3) with a 60 degree field of view, frustum + cone culling, no HiZ,
+    flat resolve; one captured single-view frame per step, L2 flushed between
+    steps; beside it the oracle on all host threads."""
+    import torch
+
+    from vk_gltf_viewer_gb300 import abi, scene
+    from vk_gltf_viewer_gb300.renderer import DeviceScene, Renderer, ViewBuffers
+
+    w, h = 1280, 720
+    host = scene.scene_icosphere(6)
+    cam = scene.camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, w / h)
+    flags = abi.CULL_FRUSTUM | abi.CULL_CONE | abi.RESOLVE_FLAT | abi.WRITE_IDS
+    r = Renderer(local)
+    dev = DeviceScene(host, f"cuda:{local}")
+    v = ViewBuffers.allocate(w, h, cam, host.draw_count, device=f"cuda:{local}", pyramid=False)
+    r.frame(dev, [v], flags)
+    g = r.capture(dev, [v], flags)
+    for _ in range(max(3, args.warmup)):
+        g.launch()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        starts[i].record(stream)
+        g.launch()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps
+    out = {"value": 1000.0 / ms, "unit": "views/s", "ms_per_view": ms, "triangles": host.triangle_count,
+           "draws": host.draw_count, "survivors": int(v.survivor_count.item()), "kernels_per_frame": g.kernel_count(),
+           "config": "icosphere level 6 (81,920 tris), 1280x720, eye (0,0,3), 60 deg, frustum + cone, no HiZ, "
+                     "flat resolve, L2 flushed between steps"}
+    g.close()
+    r.close()
+    if cpu:
+        from oracle import binding as ob
+        threads = os.cpu_count() or 1
+        ob.set_threads(threads)
+        osc = ob.OracleScene(host)
+        n, t0 = 0, time.perf_counter()
+        while n < 5 or (time.perf_counter() - t0 < 3.0 and n < 200):
+            ob.frame(osc, cam, w, h, ob.CULL_FRUSTUM | ob.CULL_CONE | ob.RESOLVE_FLAT)
+            n += 1
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / tc, "unit": "views/s", "cores": threads, "kind": "port",
+                               "sample": f"{n} frames of the same view (oracle/oracle.c, {threads} threads)"}
     return out
 
 
@@ -260,10 +322,13 @@ def sphere_poses(rng, n, radius=3.0):
     return radius * v / np.linalg.norm(v, axis=1, keepdims=True)
 
 
-def run_adjoint_case(r, local, level, displace, tex_size, sizes, seed, steps, warmup, stream):
+def run_adjoint_case(r, local, level, displace, tex_size, sizes, seed, steps, warmup, stream, pg=None):
     """One adjoint workload: zero + forward + backward (MSE against target
     renders) over all views in one captured graph; returns ms/view and the
-    device memory the workload holds."""
+    device memory the workload holds.  Under N ranks each rank steps the
+    views of its pixel-balanced shard and the position, colour and texel
+    gradients are summed with one all-reduce per step (inside the timed
+    region); ms/view is over all views."""
     import numpy as np
     import torch
 
@@ -285,8 +350,16 @@ def run_adjoint_case(r, local, level, displace, tex_size, sizes, seed, steps, wa
     pos_t = mesh.positions + trng.normal(0, 0.01, size=mesh.positions.shape).astype(np.float32)
     tex_t = trng.uniform(0, 1, size=texture.shape).astype(np.float32)
     dt = diff.DiffScene.create(mesh, colors, tex_t, device=dev, positions=pos_t)
+    from vk_gltf_viewer_gb300 import sharding
+
+    world = pg.get_world_size() if pg else 1
+    rank = pg.get_rank() if pg else 0
+    eyes = sphere_poses(rng, len(sizes))
+    mine = sharding.shard_views([w * h for w, h in sizes], world, rank)
     views, targets, rgb = [], [], []
-    for eye, (w, h) in zip(sphere_poses(rng, len(sizes)), sizes):
+    for i in mine:
+        w, h = sizes[i]
+        eye = eyes[i]
         cam = scene.camera(tuple(eye), (0, 0, 0), scene.safe_up(eye, (0, 0, 0)), 60.0, w / h)
         views.append(diff.DiffViewBuffers.allocate(w, h, cam, device=dev))
         targets.append(torch.empty(w * h * 3, device=dev))
@@ -297,18 +370,30 @@ def run_adjoint_case(r, local, level, displace, tex_size, sizes, seed, steps, wa
     px = sum(w * h for w, h in sizes)
     g = diff.capture_step(r, ds, views, rgb_out=rgb, targets=targets, grad_positions=gp, grad_colors=gc,
                           grad_texture=gt, scale=1.0 / (3 * px), loss=loss)
-    for _ in range(max(3, warmup)):
+
+    def step():
         g.launch()
+        if world > 1:
+            sharding.allreduce_gradients([gp, gc, gt, loss])
+
+    for _ in range(max(3, warmup)):
+        step()
     torch.cuda.synchronize()
     free1, _ = torch.cuda.mem_get_info(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if pg:
+        pg.barrier()
     e0.record(stream)
     for _ in range(steps):
-        g.launch()
+        step()
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    out = {"ms_per_view": ms / len(sizes), "ms_per_step": ms, "views": len(sizes), "pixels_per_step": px,
+    tm = torch.tensor([e0.elapsed_time(e1) / steps], device=dev)
+    if pg:
+        pg.all_reduce(tm, op=pg.ReduceOp.MAX)
+    ms = float(tm.item())
+    out = {"ms_per_view": ms / len(sizes), "ms_per_step": ms, "views": len(sizes), "views_this_rank": len(views),
+           "pixels_per_step": px,
            "triangles": mesh.triangle_count, "vertices": nv, "texture": f"{tex_size}x{tex_size} fp32 RGB",
            "kernels_per_step": g.kernel_count(), "loss": float(loss.item()),
            "device_bytes_held": int(free0 - free1),
@@ -591,20 +676,20 @@ def _synthetic_jpeg(w: int, h: int, rng, restart: int = 0) -> bytes:
     return out
 
 
-def run_adjoint(r, local, args, stream):
+def run_adjoint(r, local, args, stream, pg=None):
     """Adjoint legs: the 64-view 512^2 icosphere-5 case and the batched
     512-view uneven-resolution icosphere-8 case (one graph per step)."""
     import numpy as np
 
     steps = max(3, min(args.steps, 10))
-    c4 = run_adjoint_case(r, local, 5, 0.0, 1024, [(512, 512)] * 64, 41, steps, args.warmup, stream)
+    c4 = run_adjoint_case(r, local, 5, 0.0, 1024, [(512, 512)] * 64, 41, steps, args.warmup, stream, pg)
     c4["config"] = ("icosphere level 5 (20,480 tris), per-vertex colours U(0,1), 1024^2 fp32 texture, 64 views "
                     "512^2 on a radius-3 sphere, MSE vs renders of N(0,0.01^2)-perturbed positions and a "
                     "separately seeded texture; step = zero + forward + backward in one graph")
     rng = np.random.default_rng(77)
     sides = rng.integers(256, 1025, size=512)
     c5 = run_adjoint_case(r, local, 8, 0.02, 2048, [(int(s), int(s)) for s in sides], 43, max(2, steps // 3),
-                          args.warmup, stream)
+                          args.warmup, stream, pg)
     c5["config"] = ("icosphere level 8 (1,310,720 tris) with seeded normal displacement 0.02, 2048^2 fp32 "
                     "texture, 512 square views with sides uniform in [256, 1024] on a radius-3 sphere; "
                     "zero + forward + backward (visibility recomputed) in one graph")
@@ -661,7 +746,7 @@ def main():
         r.close()
         return
     if args.adjoint_only:
-        out = run_adjoint(r, local, args, stream)
+        out = run_adjoint(r, local, args, stream, pg)
         if rank == 0:
             print(json.dumps({"metric": METRIC, "adjoint": out}), flush=True)
         r.close()
@@ -852,6 +937,11 @@ def main():
         batched = run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier)
         batched["speedup_vs_single_view"] = batched["value"] / value
 
+    # ---- C1: the icosphere single view
+    c1 = None
+    if not args.no_c1:
+        c1 = run_c1(local, args, stream, flush, cpu=rank == 0 and not args.no_cpu_baseline)
+
     # ---- node tree: animated transforms and the draw list on the device
     tree = None
     if not args.no_world:
@@ -865,7 +955,7 @@ def main():
     # ---- adjoint legs (ms/view)
     adjoint = None
     if not args.no_adjoint:
-        adjoint = run_adjoint(r, local, args, stream)
+        adjoint = run_adjoint(r, local, args, stream, pg)
 
     # ---- CPU baseline: the oracle on the host cores, bounded sample
     cpu = None
@@ -942,7 +1032,16 @@ def main():
             "device_status": list(status),
         }
         if batched:
+            # the metric's own comparison at the top level: batched views/s
+            # and its ratio to the same poses through the single-view path
+            out["batched_value"] = batched["value"]
+            out["batched_speedup_same_poses"] = batched["speedup_vs_single_view_same_poses"]
+            out["batched_speedup_vs_c2_single_view"] = batched["speedup_vs_single_view"]
             out["batched"] = batched
+        if c1:
+            out["c1_value"] = c1["value"]
+            out["c1_cpu_value"] = (c1.get("cpu_baseline") or {}).get("value")
+            out["c1"] = c1
         if adjoint:
             out["adjoint"] = adjoint
         if motion:

@@ -339,17 +339,23 @@ class OrcDiffScene(C.Structure):
 def diff_f64(mesh, positions, colors, uvs, texture, vp16, w: int, h: int, ids: np.ndarray,
              target: np.ndarray | None = None, scale: float = 1.0, albedo=(1.0, 1.0, 1.0), uv_offset=(0.0, 0.0),
              uv_scale=(1.0, 1.0), uv_rotation: float = 0.0, want_rgb=False, want_grads=False,
-             cells: np.ndarray | None = None):
+             cells: np.ndarray | None = None, freeze: np.ndarray | None = None,
+             margin: np.ndarray | None = None):
     """float64 shading/loss/gradients at fixed visibility `ids` (uint32 per
     pixel).  Parameters are converted to float64.  Returns (loss, rgb or None,
     (gpos, gcol, gtex) or None).  `cells`, an int32 array of 2*w*h, receives
-    each pixel's unwrapped bilinear cell (INT32_MIN for empty pixels)."""
+    each pixel's unwrapped bilinear cell (INT32_MIN for empty pixels).
+    `freeze` (int32, 2*w*h, as `cells` reports them) holds each pixel's
+    bilinear cell fixed (orc_diff_f64_frozen).  `margin` (float64, w*h)
+    receives each pixel's distance in texels to the nearest texel-centre
+    line (-1 for empty pixels)."""
     lib = load()
-    if not hasattr(lib.orc_diff_f64, "_typed"):
-        lib.orc_diff_f64.restype = C.c_double
-        lib.orc_diff_f64.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
-                                     C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
-        lib.orc_diff_f64._typed = True
+    if not hasattr(lib.orc_diff_f64_frozen, "_typed"):
+        lib.orc_diff_f64_frozen.restype = C.c_double
+        lib.orc_diff_f64_frozen.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                            C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.orc_diff_f64_frozen._typed = True
     keep = [np.ascontiguousarray(mesh.meshlets), np.ascontiguousarray(mesh.vertex_indices),
             np.ascontiguousarray(mesh.primitive_indices), np.ascontiguousarray(positions, np.float64),
             np.ascontiguousarray(colors, np.float64), np.ascontiguousarray(uvs, np.float64),
@@ -368,11 +374,26 @@ def diff_f64(mesh, positions, colors, uvs, texture, vp16, w: int, h: int, ids: n
     grads = None
     if want_grads:
         grads = (np.zeros(keep[3].size), np.zeros(keep[4].size), np.zeros(keep[6].size))
-    loss = lib.orc_diff_f64(C.addressof(s), _addr(vp), w, h, _addr(ids), _addr(tgt) if tgt is not None else None,
-                            float(scale), _addr(rgb) if rgb is not None else None,
-                            *(tuple(_addr(g) for g in grads) if grads else (None, None, None)),
-                            _cells_addr(cells, w, h))
+    frz = None
+    if freeze is not None:
+        frz = np.ascontiguousarray(freeze, np.int32)
+        if frz.size != 2 * w * h:
+            raise ValueError("freeze needs 2 int32 per pixel")
+    loss = lib.orc_diff_f64_frozen(C.addressof(s), _addr(vp), w, h, _addr(ids),
+                                   _addr(tgt) if tgt is not None else None, float(scale),
+                                   _addr(rgb) if rgb is not None else None,
+                                   *(tuple(_addr(g) for g in grads) if grads else (None, None, None)),
+                                   _cells_addr(cells, w, h), _addr(frz) if frz is not None else None,
+                                   _margin_addr(margin, w, h))
     return float(loss), rgb, grads
+
+
+def _margin_addr(margin, w, h):
+    if margin is None:
+        return None
+    if margin.dtype != np.float64 or margin.size != w * h or not margin.flags.c_contiguous:
+        raise ValueError("margin must be a contiguous float64 array of w*h")
+    return _addr(margin)
 
 
 def _cells_addr(cells, w, h):

@@ -978,6 +978,18 @@ static int wrapi(int64_t i, int64_t n) {
 double orc_diff_f64(const orc_diff_scene* s, const float vpf[16], uint32_t w, uint32_t h, const uint32_t* ids,
                     const float* target, double scale, double* rgb_out, double* gpos, double* gcol, double* gtex,
                     int32_t* cells) {
+    return orc_diff_f64_frozen(s, vpf, w, h, ids, target, scale, rgb_out, gpos, gcol, gtex, cells, NULL, NULL);
+}
+
+/* As orc_diff_f64; with `freeze` (2 per pixel, as `cells` reports them) each
+ * covered pixel samples the bilinear patch of its frozen cell, extended
+ * linearly past the cell's texel centres: the smooth piece of the filtered
+ * texture that holds the pixel's sample at the frozen parameters, whose
+ * derivative is the gradient there.  A finite difference of this loss is
+ * free of the derivative jumps at texel centres. */
+double orc_diff_f64_frozen(const orc_diff_scene* s, const float vpf[16], uint32_t w, uint32_t h, const uint32_t* ids,
+                           const float* target, double scale, double* rgb_out, double* gpos, double* gcol,
+                           double* gtex, int32_t* cells, const int32_t* freeze, double* margin) {
     double vp[16];
     for (int k = 0; k < 16; ++k) vp[k] = vpf[k];
     const double cs = cos(s->uv_rotation), sn = sin(s->uv_rotation);
@@ -991,6 +1003,7 @@ double orc_diff_f64(const orc_diff_scene* s, const float vpf[16], uint32_t w, ui
             const uint32_t id = ids[p];
             double shade[3] = {0, 0, 0};
             if (cells) cells[2 * p] = cells[2 * p + 1] = INT32_MIN;
+            if (margin) margin[p] = -1.0;
             if (id == 0xFFFFFFFFu) {
                 if (rgb_out)
                     for (int j = 0; j < 3; ++j) rgb_out[3 * p + j] = 0.0;
@@ -1034,7 +1047,17 @@ double orc_diff_f64(const orc_diff_scene* s, const float vpf[16], uint32_t w, ui
             const double ru = cs * uv[0] + sn * uv[1], rv = -sn * uv[0] + cs * uv[1];
             const double tu = ru * s->uv_scale[0] + s->uv_offset[0], tv = rv * s->uv_scale[1] + s->uv_offset[1];
             const double tx = tu * s->tex_w - 0.5, ty = tv * s->tex_h - 0.5;
-            const double fx = floor(tx), fy = floor(ty);
+            double fx = floor(tx), fy = floor(ty);
+            if (margin) {
+                /* texels from the sample to the nearest texel-centre line,
+                 * where the bilinear derivative jumps */
+                const double mx = fmin(tx - fx, fx + 1.0 - tx), my = fmin(ty - fy, fy + 1.0 - ty);
+                margin[p] = fmin(mx, my);
+            }
+            if (freeze && freeze[2 * p] != INT32_MIN) {
+                fx = (double)freeze[2 * p];
+                fy = (double)freeze[2 * p + 1];
+            }
             const double ax = tx - fx, ay = ty - fy;
             if (cells) {
                 cells[2 * p] = (int32_t)fx;

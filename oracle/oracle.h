@@ -169,6 +169,13 @@ typedef struct orc_diff_scene {
 double orc_diff_f64(const orc_diff_scene* s, const float vp[16], uint32_t w, uint32_t h, const uint32_t* ids,
                     const float* target, double scale, double* rgb, double* gpos, double* gcol, double* gtex,
                     int32_t* cells);
+/* orc_diff_f64 with each covered pixel's bilinear cell held at freeze[2p],
+ * freeze[2p+1] (NULL: none held); see oracle.c.  margin (if non-NULL)
+ * receives, per pixel, the distance in texels from the sample to the nearest
+ * texel-centre line (-1 for an empty pixel). */
+double orc_diff_f64_frozen(const orc_diff_scene* s, const float vp[16], uint32_t w, uint32_t h, const uint32_t* ids,
+                           const float* target, double scale, double* rgb, double* gpos, double* gcol, double* gtex,
+                           int32_t* cells, const int32_t* freeze, double* margin);
 /* cells (if non-NULL) receives, per pixel, the unwrapped bilinear cell
  * (floor(u*W - 0.5), floor(v*H - 0.5)), or INT32_MIN twice for an empty
  * pixel.  Bilinear filtering is only piecewise smooth: its derivative jumps

@@ -42,15 +42,26 @@ def test_full_size_frame_bit_exact(renderer, full):
 
 
 def test_full_size_batched_views_bit_exact(renderer, full):
-    """Eight of the 256 batched poses (uneven sizes) in one launch."""
+    """Twenty of the 256 batched poses in one launch: the first four poses of
+    each of the five resolutions (256^2, 512x384, 1024x576, 1280x720,
+    1920x1080), steady state, against the oracle."""
+    picked, per = [], {}
+    for cam, w, h in scene.batch_views(256, seed=3):
+        if per.get((w, h), 0) < 4:
+            per[(w, h)] = per.get((w, h), 0) + 1
+            picked.append((cam, w, h))
+    assert sorted(per.values()) == [4] * 5
     views, exps = [], []
-    for cam, w, h in scene.batch_views(8, seed=3):
+    for cam, w, h in picked:
         first = ob.frame(full.orc, cam, w, h, oracle_flags(FLAGS))
         exps.append(ob.frame(full.orc, cam, w, h, oracle_flags(FLAGS), prev_pyramid=first["pyramid"]))
         views.append(view(full, cam, w, h, prev=first["pyramid"]))
     renderer.frame(full.dev, views, FLAGS)
     torch.cuda.synchronize()
     for v, e in zip(views, exps):
-        assert np.array_equal(u32(v.visbuffer), e["ids"])
-        assert np.array_equal(np.sort(v.survivor_list()), np.sort(e["survivors"]))
+        assert np.array_equal(u32(v.visbuffer), e["ids"]), (v.width, v.height)
+        assert np.array_equal(np.sort(v.survivor_list()), np.sort(e["survivors"])), (v.width, v.height)
         assert np.array_equal(v.pyramid.cpu().numpy()[: e["pyramid"].size], e["pyramid"])
+        ok, bad = rgba_close(u32(v.color), e["rgba"])
+        assert ok, f"{bad} pixels off by more than 1/255"
+    assert renderer.device_status() == (0, 0)
