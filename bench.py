@@ -29,10 +29,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "views/s at 1080p, 82M-tri scene: batched vs single-view CUDA; adjoint ms/view"
 WORKLOAD = ("torus grid: 2048 instances x 40,000 tris = 81.92M tris, 843,776 meshlet draws (<=64 verts/"
-            "<=124 tris), 1920x1080, two-pass frustum+cone+HiZ culling, HiZ pyramid, textured resolve, "
-            "steady state (previous frame's pyramid)")
+            "<=124 tris), 1920x1080, two-pass frustum+cone+HiZ culling (with the fine footprint test), HiZ "
+            "pyramid, textured resolve, steady state (previous frame's pyramid)")
 W1080, H1080 = 1920, 1080
-FLAGS_NAMES = "CULL_FRUSTUM|CULL_CONE|CULL_OCCLUSION|CULL_TWO_PASS|BUILD_PYRAMID|RESOLVE_TEXTURED|WRITE_IDS"
+FLAGS_NAMES = ("CULL_FRUSTUM|CULL_CONE|CULL_OCCLUSION|CULL_OCCLUSION_FINE|CULL_TWO_PASS|BUILD_PYRAMID|"
+               "RESOLVE_TEXTURED|WRITE_IDS")
 
 
 def parse():
@@ -48,6 +49,8 @@ def parse():
                    help="run only the batched leg (for profiling); prints its own JSON line")
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-c1", action="store_true", help="skip the icosphere (C1) single-view leg")
+    p.add_argument("--no-fine", action="store_true",
+                   help="leave out the fine occlusion test (CULL_OCCLUSION_FINE) of the C2 and batched frames")
     p.add_argument("--no-motion", action="store_true", help="skip the motion-vector frame")
     p.add_argument("--no-world", action="store_true", help="skip the node-tree transform and draw-list leg")
     p.add_argument("--no-texture", action="store_true", help="skip the texture decode leg")
@@ -147,8 +150,10 @@ def run_reference(args, rank, world):
     host = oscene.scene_torus_grid()
     cam = oscene.grid_camera(W1080, H1080)
     osc = ob.OracleScene(host)
-    flags = (ob.CULL_FRUSTUM | ob.CULL_CONE | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID
-             | ob.RESOLVE_TEXTURED)
+    # the same frame flags as the CUDA arm (its cone and fine occlusion
+    # tests are restated in the oracle; the ids are the same either way)
+    flags = (ob.CULL_FRUSTUM | ob.CULL_CONE | ob.CULL_OCCLUSION | ob.CULL_OCCLUSION_FINE | ob.CULL_TWO_PASS
+             | ob.BUILD_PYRAMID | ob.RESOLVE_TEXTURED)
     prev = ob.frame(osc, cam, W1080, H1080, flags)["pyramid"]
     for _ in range(max(0, args.warmup)):
         prev = ob.frame(osc, cam, W1080, H1080, flags, prev_pyramid=prev)["pyramid"]
@@ -730,6 +735,8 @@ def main():
     dev = DeviceScene(host, f"cuda:{local}")
     flags = (abi.CULL_FRUSTUM | abi.CULL_CONE | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID
              | abi.RESOLVE_TEXTURED | abi.WRITE_IDS)
+    if not args.no_fine:
+        flags |= abi.CULL_OCCLUSION_FINE
     stream = torch.cuda.current_stream()
     if args.batched_only:
         out = run_batched(r, dev, host, flags, args, local, world, pg, stream, barrier)
@@ -964,8 +971,8 @@ def main():
         threads = os.cpu_count() or 1
         ob.set_threads(threads)
         osc = ob.OracleScene(host)
-        of = (ob.CULL_FRUSTUM | ob.CULL_CONE | ob.CULL_OCCLUSION | ob.CULL_TWO_PASS | ob.BUILD_PYRAMID
-              | ob.RESOLVE_TEXTURED)
+        of = (ob.CULL_FRUSTUM | ob.CULL_CONE | ob.CULL_OCCLUSION | ob.CULL_OCCLUSION_FINE | ob.CULL_TWO_PASS
+              | ob.BUILD_PYRAMID | ob.RESOLVE_TEXTURED)
         prev = ob.frame(osc, cam, W1080, H1080, of)["pyramid"]
         n_cpu = 0
         tc0 = time.perf_counter()

@@ -214,6 +214,13 @@ enum vkgv_frame_flags {
     VKGV_WRITE_IDS = 1u << 7,           /* write the uint32 visbuffer image          */
     VKGV_SKIP_CLEAR = 1u << 8,          /* depth_id already cleared by the caller    */
     VKGV_WRITE_MOTION = 1u << 9,        /* motion vectors of the visible fragments (visbuffer.frag.glsl:38) */
+    /* An addition to VKGV_CULL_OCCLUSION (no counterpart in the reference):
+     * a draw that passes the HiZ test of visbuffer.task.glsl:54-65 is tested
+     * again against every pyramid texel under its projected box, at the
+     * finest exactly-halved level where that is at most 4 x 4 texels, and is
+     * rejected when all of them hold a depth >= the box's nearest depth (the
+     * reference's own comparison, on a finer footprint). */
+    VKGV_CULL_OCCLUSION_FINE = 1u << 10,
     /* The reference frame: application.cpp:764-1003. */
     VKGV_FRAME_REFERENCE = (1u << 0) | (1u << 1) | (1u << 4) | (1u << 6) | (1u << 7)
 };

@@ -25,6 +25,7 @@ CULL_CONE = 1 << 3
 RESOLVE_FLAT = 1 << 4
 RESOLVE_TEXTURED = 1 << 5
 BUILD_PYRAMID = 1 << 6
+CULL_OCCLUSION_FINE = 1 << 7
 
 
 class OrcPrimitive(C.Structure):
@@ -45,7 +46,8 @@ class OrcScene(C.Structure):
 
 
 class OrcPyramid(C.Structure):
-    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("levels", C.c_uint32)]
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("levels", C.c_uint32),
+                ("view_width", C.c_uint32), ("view_height", C.c_uint32)]
 
 
 class OrcWorld(C.Structure):
@@ -243,7 +245,7 @@ def cull(os_: OracleScene, cam, w: int, h: int, flags: int, pass_: int = 1, pyra
     pyr = None
     if pyramid is not None:
         pyramid = np.ascontiguousarray(pyramid, np.float32)
-        pyr = OrcPyramid(_addr(pyramid), w >> 1, h >> 1, pyramid_levels(w, h))
+        pyr = OrcPyramid(_addr(pyramid), w >> 1, h >> 1, pyramid_levels(w, h), w, h)
     cand = None if candidates is None else np.ascontiguousarray(candidates, np.uint32)
     lib.orc_cull(os_.ptr, C.addressof(cam), C.addressof(pyr) if pyr is not None else None, flags, pass_,
                  _addr(cand) if cand is not None else None, n, _addr(surv), C.addressof(ns), _addr(rej),
@@ -303,7 +305,7 @@ def frame(os_: OracleScene, cam, w: int, h: int, flags: int, prev_pyramid: np.nd
     prev = None
     if prev_pyramid is not None:
         prev_pyramid = np.ascontiguousarray(prev_pyramid, np.float32)
-        prev = OrcPyramid(_addr(prev_pyramid), w >> 1, h >> 1, pyramid_levels(w, h))
+        prev = OrcPyramid(_addr(prev_pyramid), w >> 1, h >> 1, pyramid_levels(w, h), w, h)
     lib.orc_frame(os_.ptr, C.addressof(cam), w, h, C.addressof(prev) if prev is not None else None, flags,
                   _addr(depth), _addr(ids), _addr(rgba), _addr(pyr), _addr(surv), C.addressof(ns))
     return {"depth_id": depth, "ids": ids, "rgba": rgba, "pyramid": pyr, "survivors": surv[: ns.value].copy()}

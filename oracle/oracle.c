@@ -263,6 +263,49 @@ static int hiz_level(float m, uint32_t levels) {
 /* One draw of the task shader (visbuffer.task.glsl:44-65).  Returns 1 if
  * visible; *occluded is set when the frustum test passed and the occlusion
  * test failed. */
+static int ctz32(uint32_t v) {
+    int n = 0;
+    while (!(v & 1u)) {
+        v >>= 1;
+        ++n;
+    }
+    return n;
+}
+
+/* The fine occlusion addition (ORC_CULL_OCCLUSION_FINE; no counterpart in
+ * the reference).  For a draw the HiZ test kept, the pyramid texels under
+ * its projected box [mn0, mx0] x [mn1, mx1] (level-0 texel units, widened by
+ * 1/64 texel) are read at the finest level, among those reached from the
+ * depth buffer by exact halvings (view width and height divisible by
+ * 2^(level+1)), where they are at most 4 x 4; the draw is occluded when
+ * every one of them is >= mx2, the box's nearest depth (the comparison of
+ * visbuffer.task.glsl:64).  Only with all eight corners in front of the
+ * camera (w > 0); otherwise, or with no such level, the HiZ verdict stands. */
+static int fine_occluded(const orc_pyramid* pyr, uint32_t vw, uint32_t vh, float mn0, float mx0, float mn1,
+                         float mx1, float mx2) {
+    if ((vw & 1u) || (vh & 1u) || vw == 0 || vh == 0) return 0;
+    int top = ctz32(vw) < ctz32(vh) ? ctz32(vw) - 1 : ctz32(vh) - 1;
+    if (top > (int)pyr->levels - 1) top = (int)pyr->levels - 1;
+    const int pw = (int)pyr->width, ph = (int)pyr->height;
+    int i0 = (int)floorf(mn0 * (float)pw - 0.015625f), i1 = (int)floorf(mx0 * (float)pw + 0.015625f);
+    int j0 = (int)floorf(mn1 * (float)ph - 0.015625f), j1 = (int)floorf(mx1 * (float)ph + 0.015625f);
+    i0 = i0 < 0 ? 0 : (i0 > pw - 1 ? pw - 1 : i0);
+    i1 = i1 < 0 ? 0 : (i1 > pw - 1 ? pw - 1 : i1);
+    j0 = j0 < 0 ? 0 : (j0 > ph - 1 ? ph - 1 : j0);
+    j1 = j1 < 0 ? 0 : (j1 > ph - 1 ? ph - 1 : j1);
+    for (int l = 0; l <= top; ++l) {
+        const int a0 = i0 >> l, a1 = i1 >> l, b0 = j0 >> l, b1 = j1 >> l;
+        if (a1 - a0 > 3 || b1 - b0 > 3) continue;
+        const uint32_t mw = mip_dim((uint32_t)pw, (uint32_t)l);
+        const float* img = pyr->data + mip_offset((uint32_t)pw, (uint32_t)ph, (uint32_t)l);
+        for (int y = b0; y <= b1; ++y)
+            for (int x = a0; x <= a1; ++x)
+                if (img[(size_t)y * mw + x] < mx2) return 0;
+        return 1;
+    }
+    return 0;
+}
+
 static int cull_draw(const orc_scene* s, const orc_camera* cam, const orc_pyramid* pyr,
                      uint32_t flags, uint32_t pass, uint32_t d, const float* eye, int* occluded) {
     *occluded = 0;
@@ -291,11 +334,13 @@ static int cull_draw(const orc_scene* s, const orc_camera* cam, const orc_pyrami
                                         {1, -1, 1},  {1, 1, 1},  {-1, -1, 1}, {-1, 1, 1}};
     const float* vp = pass == 1 ? cam->prev_occlusion_vp : cam->occlusion_vp;
     float mn[3] = {1.0f, 1.0f, 1.0f}, mx[3] = {-1.0f, -1.0f, -1.0f};
+    int all_front = 1;
     for (int i = 0; i < 8; ++i) {
         float p[4] = {corners[i][0] * we[0] + wc[0], corners[i][1] * we[1] + wc[1],
                       corners[i][2] * we[2] + wc[2], 1.0f};
         float clip[4];
         m4v(vp, p, clip);
+        all_front &= clip[3] > 0.0f;
         float ndx = gclamp(clip[0] / clip[3], -1.0f, 1.0f);
         float ndy = gclamp(clip[1] / clip[3], -1.0f, 1.0f);
         float q[3] = {ndx * 0.5f + 0.5f, ndy * 0.5f + 0.5f, clip[2] / clip[3]};
@@ -312,7 +357,10 @@ static int cull_draw(const orc_scene* s, const orc_camera* cam, const orc_pyrami
     uint32_t mw = mip_dim(pyr->width, (uint32_t)lvl), mh = mip_dim(pyr->height, (uint32_t)lvl);
     const float* img = pyr->data + mip_offset(pyr->width, pyr->height, (uint32_t)lvl);
     float depth = orc_min_sample(img, mw, mh, cx, cy);
-    if (depth < mx[2]) return 1;
+    if (depth < mx[2] &&
+        !((flags & ORC_CULL_OCCLUSION_FINE) && all_front &&
+          fine_occluded(pyr, pyr->view_width, pyr->view_height, mn[0], mx[0], mn[1], mx[1], mx[2])))
+        return 1;
     *occluded = 1;
     return 0;
 }
@@ -458,8 +506,9 @@ static void raster_snapped(int32_t X[3], int32_t Y[3], float Z[3], uint32_t id, 
     float dx2 = (float)(X[2] - X[0]), dy2 = (float)(Y[2] - Y[0]);
     float af = (float)A;
     float dz1 = Z[1] - Z[0], dz2 = Z[2] - Z[0];
-    float pa = (dz1 * dy2 - dz2 * dy1) / af;
-    float pb = (dz2 * dx1 - dz1 * dx2) / af;
+    float ra = 1.0f / af; /* one reciprocal of the area for both slopes */
+    float pa = (dz1 * dy2 - dz2 * dy1) * ra;
+    float pb = (dz2 * dx1 - dz1 * dx2) * ra;
     uint64_t lo = (uint64_t)id + 1u;
     for (int64_t py = py0; py <= py1; ++py) {
         int32_t sy = (int32_t)py * 256 + 128;
@@ -516,7 +565,11 @@ void orc_raster_triangle(const float v0[4], const float v1[4], const float v2[4]
     for (int k = 0; k < n; ++k) {
         float cw = cur[k][3];
         if (!(cw > 0.0f)) return;
-        float xd = cur[k][0] / cw, yd = cur[k][1] / cw, zd = cur[k][2] / cw;
+        /* perspective divide as one correctly rounded reciprocal of w and
+         * three products (the division's precision is the implementation's
+         * to choose, application.cpp:326-340) */
+        float rw = 1.0f / cw;
+        float xd = cur[k][0] * rw, yd = cur[k][1] * rw, zd = cur[k][2] * rw;
         float xf = xd * hw + hw, yf = yd * hh + hh;
         float sx = xf * 256.0f, sy = yf * 256.0f;
         if (!(fabsf(sx) < 1073741824.0f) || !(fabsf(sy) < 1073741824.0f)) return;
@@ -953,7 +1006,7 @@ void orc_frame(const orc_scene* s, const orc_camera* cam, uint32_t w, uint32_t h
               pyramid_out;
     if (two) {
         orc_hiz(depth_id, w, h, pyramid_out);
-        orc_pyramid cur = {pyramid_out, w >> 1, h >> 1, orc_pyramid_levels(w, h)};
+        orc_pyramid cur = {pyramid_out, w >> 1, h >> 1, orc_pyramid_levels(w, h), w, h};
         uint32_t ns2 = 0;
         orc_cull(s, cam, &cur, flags, 2, rej, nr, survivors + ns1, &ns2, NULL, NULL);
         orc_raster(s, cam, w, h, survivors + ns1, ns2, depth_id);

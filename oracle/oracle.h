@@ -92,6 +92,9 @@ typedef struct orc_scene {
 typedef struct orc_pyramid {
     float* data;
     uint32_t width, height, levels;
+    /* the depth buffer it reduces (0: unknown; the fine occlusion test then
+     * stays off) */
+    uint32_t view_width, view_height;
 } orc_pyramid;
 
 enum {
@@ -101,7 +104,8 @@ enum {
     ORC_CULL_CONE = 1u << 3,
     ORC_RESOLVE_FLAT = 1u << 4,
     ORC_RESOLVE_TEXTURED = 1u << 5,
-    ORC_BUILD_PYRAMID = 1u << 6
+    ORC_BUILD_PYRAMID = 1u << 6,
+    ORC_CULL_OCCLUSION_FINE = 1u << 7
 };
 
 void orc_set_threads(int n);

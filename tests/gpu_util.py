@@ -11,7 +11,7 @@ from vk_gltf_viewer_gb300.renderer import DeviceScene, ViewBuffers
 
 ORACLE_FLAGS = {
     abi.CULL_FRUSTUM: ob.CULL_FRUSTUM, abi.CULL_OCCLUSION: ob.CULL_OCCLUSION, abi.CULL_TWO_PASS: ob.CULL_TWO_PASS,
-    abi.CULL_CONE: ob.CULL_CONE,
+    abi.CULL_CONE: ob.CULL_CONE, abi.CULL_OCCLUSION_FINE: ob.CULL_OCCLUSION_FINE,
     abi.RESOLVE_FLAT: ob.RESOLVE_FLAT, abi.RESOLVE_TEXTURED: ob.RESOLVE_TEXTURED,
     abi.BUILD_PYRAMID: ob.BUILD_PYRAMID,
 }

@@ -65,3 +65,24 @@ def test_full_size_batched_views_bit_exact(renderer, full):
         ok, bad = rgba_close(u32(v.color), e["rgba"])
         assert ok, f"{bad} pixels off by more than 1/255"
     assert renderer.device_status() == (0, 0)
+
+
+def test_full_size_fine_occlusion_bit_exact(renderer, full):
+    """The C2 frame and four batched poses with the fine occlusion test: the
+    oracle's survivors, and the same ids as without it."""
+    flags = FLAGS | abi.CULL_OCCLUSION_FINE
+    poses = [(scene.grid_camera(1920, 1080), 1920, 1080)] + scene.batch_views(4, seed=3)
+    views, base_views, exps = [], [], []
+    for cam, w, h in poses:
+        first = ob.frame(full.orc, cam, w, h, oracle_flags(FLAGS))
+        exps.append(ob.frame(full.orc, cam, w, h, oracle_flags(flags), prev_pyramid=first["pyramid"]))
+        views.append(view(full, cam, w, h, prev=first["pyramid"]))
+        base_views.append(view(full, cam, w, h, prev=first["pyramid"]))
+    renderer.frame(full.dev, views, flags)
+    renderer.frame(full.dev, base_views, FLAGS)
+    torch.cuda.synchronize()
+    for v, b, e in zip(views, base_views, exps):
+        assert np.array_equal(np.sort(v.survivor_list()), np.sort(e["survivors"])), (v.width, v.height)
+        assert np.array_equal(u32(v.visbuffer), e["ids"])
+        assert np.array_equal(u32(v.visbuffer), u32(b.visbuffer))
+        assert v.survivor_list().size < b.survivor_list().size

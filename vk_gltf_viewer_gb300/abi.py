@@ -41,6 +41,7 @@ BUILD_PYRAMID = 1 << 6
 WRITE_IDS = 1 << 7
 SKIP_CLEAR = 1 << 8
 WRITE_MOTION = 1 << 9
+CULL_OCCLUSION_FINE = 1 << 10
 
 # passes of vkgv_diff_graph_capture
 DIFF_ZERO_GRADS = 1

@@ -49,6 +49,7 @@ struct vkgv_ctx {
     Scratch survivors;  // per view: capacity draw_count
     Scratch rejected;   // per view: capacity draw_count
     Scratch deferred;   // per view: capacity draw_count
+    Scratch reject_samples;  // per view: capacity draw_count (8 B each)
     Scratch diff;       // adjoint: internal raster scene of the differentiable mesh
     Scratch diff_acc;   // adjoint: float4 gradient accumulators (positions, colours, texels)
     Scratch tdet;       // determinant(M) per node transform (vkgv_scene.transform_count)
@@ -211,6 +212,11 @@ int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, 
     if (rc) return rc;
     rc = ensure_scratch(ctx, ctx->deferred, per_view * n, "deferred meshlet lists");
     if (rc) return rc;
+    const bool two_pass = (flags & VKGV_CULL_TWO_PASS) && (flags & VKGV_CULL_OCCLUSION);
+    if (two_pass) {
+        rc = ensure_scratch(ctx, ctx->reject_samples, 2 * per_view * n, "pass-1 reject samples");
+        if (rc) return rc;
+    }
     bool need_surv = false;
     for (uint32_t i = 0; i < n; ++i) need_surv |= views[i].survivors == 0;
     if (need_surv) {
@@ -261,6 +267,9 @@ int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, 
         }
         d.rejected = reinterpret_cast<uint32_t*>(ctx->rejected.ptr) + (size_t)i * std::max<uint32_t>(D, 1);
         d.deferred = reinterpret_cast<uint32_t*>(ctx->deferred.ptr) + (size_t)i * std::max<uint32_t>(D, 1);
+        d.reject_samples = two_pass ? reinterpret_cast<unsigned long long*>(ctx->reject_samples.ptr) +
+                                          (size_t)i * std::max<uint32_t>(D, 1)
+                                    : nullptr;
         d.counters = ctx->counters + kGlobalCounters + kCountersPerView * i;
         P.max_w = std::max(P.max_w, v.width);
         P.max_h = std::max(P.max_h, v.height);
@@ -474,6 +483,7 @@ int vkgv_destroy(vkgv_ctx* ctx) {
     if (ctx->survivors.ptr) cudaFree(ctx->survivors.ptr);
     if (ctx->rejected.ptr) cudaFree(ctx->rejected.ptr);
     if (ctx->deferred.ptr) cudaFree(ctx->deferred.ptr);
+    if (ctx->reject_samples.ptr) cudaFree(ctx->reject_samples.ptr);
     if (ctx->diff.ptr) cudaFree(ctx->diff.ptr);
     if (ctx->diff_acc.ptr) cudaFree(ctx->diff_acc.ptr);
     if (ctx->tdet.ptr) cudaFree(ctx->tdet.ptr);

@@ -61,6 +61,12 @@ struct DeviceView {
     // per node: the raster eye in the node's object space and 1 (0 for a
     // singular transform or no eye), for the cone test; filled by the clear
     const float4* eyes;
+    // per pass-1 occlusion reject (same slot as `rejected`): the HiZ sample
+    // that rejected it (nearest AABB depth, level, texel footprint), so that
+    // pass 2 can repeat the lookup on the new pyramid without projecting the
+    // box again when the occlusion camera and pyramid shape are unchanged;
+    // null: pass 2 recomputes
+    unsigned long long* reject_samples;
 };
 
 struct SceneArgs {

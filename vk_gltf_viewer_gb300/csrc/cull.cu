@@ -29,16 +29,81 @@ __device__ __forceinline__ int hiz_level(float m, uint32_t levels) {
     return e < 0 ? 0 : (e > top ? top : e);
 }
 
+// The fine occlusion addition (VKGV_CULL_OCCLUSION_FINE): every pyramid
+// texel under the projected box [mn0, mx0] x [mn1, mx1] (level-0 texel
+// units, widened by 1/64 texel) at the finest level that is reached from the
+// view's depth buffer by exact halvings and holds the box in at most 4 x 4
+// texels; occluded when all of them are >= mx2.  No such level (an odd view
+// side, or a box too large) leaves the HiZ verdict.  The oracle restates the
+// same integer footprint and fp32 products.
+__device__ __forceinline__ bool fine_occluded(const float* pyr, uint32_t pw0, uint32_t ph0, uint32_t plevels,
+                                              uint32_t vw, uint32_t vh, float mn0, float mx0, float mn1, float mx1,
+                                              float mx2) {
+    if ((vw & 1u) || (vh & 1u) || vw == 0 || vh == 0) return false;
+    int top = min(__ffs((int)vw), __ffs((int)vh)) - 2;  // min(ctz) - 1
+    top = min(top, (int)plevels - 1);
+    const int pw = (int)pw0, ph = (int)ph0;
+    int i0 = (int)floorf(fsub(fmul(mn0, (float)pw), 0.015625f)), i1 = (int)floorf(fadd(fmul(mx0, (float)pw), 0.015625f));
+    int j0 = (int)floorf(fsub(fmul(mn1, (float)ph), 0.015625f)), j1 = (int)floorf(fadd(fmul(mx1, (float)ph), 0.015625f));
+    i0 = min(max(i0, 0), pw - 1);
+    i1 = min(max(i1, 0), pw - 1);
+    j0 = min(max(j0, 0), ph - 1);
+    j1 = min(max(j1, 0), ph - 1);
+    for (int l = 0; l <= top; ++l) {
+        const int a0 = i0 >> l, a1 = i1 >> l, b0 = j0 >> l, b1 = j1 >> l;
+        if (a1 - a0 > 3 || b1 - b0 > 3) continue;
+        const uint32_t mw = mip_dim(pw0, (uint32_t)l);
+        const float* img = pyr + mip_offset(pw0, ph0, (uint32_t)l);
+        for (int y = b0; y <= b1; ++y)
+            for (int x = a0; x <= a1; ++x)
+                if (__ldg(img + (size_t)y * mw + x) < mx2) return false;
+        return true;
+    }
+    return false;
+}
+
 struct CullResult {
     bool visible;
     bool occluded;
+    unsigned long long sample;  // the HiZ sample of an occlusion test (see pack_sample)
 };
+
+// One HiZ lookup as 64 bits: the nearest AABB depth's bits (high word), the
+// mip level (4 bits), the first footprint texel (12 + 12 bits: mips are at
+// most 4096 wide) and whether the footprint also takes the next texel on
+// each axis.  A footprint's second texel, when footprint_axis reports one,
+// is the next texel or the same one (clamped at the edge), and the MIN of a
+// texel with itself is that texel, so the flags record only a distinct next
+// texel.
+__device__ __forceinline__ unsigned long long pack_sample(float maxz, int lvl, int x0, int x1, int nx, int y0, int y1,
+                                                          int ny) {
+    const uint32_t lo = ((uint32_t)lvl << 28) | ((uint32_t)x0 << 16) | ((uint32_t)y0 << 4) |
+                        ((nx == 2 && x1 != x0) ? 2u : 0u) | ((ny == 2 && y1 != y0) ? 1u : 0u);
+    return ((unsigned long long)__float_as_uint(maxz) << 32) | lo;
+}
+
+// Repeats a packed lookup on a pyramid of the same shape: visible iff the
+// footprint's MIN depth is below the nearest AABB depth.
+__device__ __forceinline__ bool sample_visible(unsigned long long key, const float* pyr, uint32_t pw0, uint32_t ph0) {
+    const uint32_t lo = (uint32_t)key;
+    const float maxz = __uint_as_float((uint32_t)(key >> 32));
+    const uint32_t lvl = lo >> 28, x0 = (lo >> 16) & 0xfffu, y0 = (lo >> 4) & 0xfffu;
+    const uint32_t mw = mip_dim(pw0, lvl);
+    const float* img = pyr + mip_offset(pw0, ph0, lvl);
+    float depth = __ldg(img + (size_t)y0 * mw + x0);
+    if (lo & 2u) depth = gmin(depth, __ldg(img + (size_t)y0 * mw + x0 + 1));
+    if (lo & 1u) {
+        depth = gmin(depth, __ldg(img + (size_t)(y0 + 1) * mw + x0));
+        if (lo & 2u) depth = gmin(depth, __ldg(img + (size_t)(y0 + 1) * mw + x0 + 1));
+    }
+    return depth < maxz;
+}
 
 __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceView& V, const float* frustum, const float* eye,
                                                const float* occl_vp, const float* pyr, uint32_t pw0,
                                                uint32_t ph0, uint32_t plevels, uint32_t flags, uint32_t d,
                                                bool retest, uint32_t* status) {
-    CullResult res{false, false};
+    CullResult res{false, false, 0ull};
     const vkgv_meshlet_draw dr = S.draws[d];
     const vkgv_primitive* prim = &S.prims[dr.primitive_index];
     if (dr.meshlet_index >= prim->meshlet_count) {
@@ -124,11 +189,13 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
             }
     }
     float mn0 = 1.0f, mn1 = 1.0f, mn2 = 1.0f, mx0 = -1.0f, mx1 = -1.0f, mx2 = -1.0f;
+    bool all_front = true;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const uint32_t sg = (kCornerSigns >> (3 * i)) & 7u;
         const int a = (int)(sg & 1u), b = (int)((sg >> 1) & 1u), c = (int)(sg >> 2);
         const float clip[4] = {rows[0][a][b][c], rows[1][a][b][c], rows[2][a][b][c], rows[3][a][b][c]};
+        all_front &= clip[3] > 0.0f;
         float ndx = gclamp(fdiv(clip[0], clip[3]), -1.0f, 1.0f);
         float ndy = gclamp(fdiv(clip[1], clip[3]), -1.0f, 1.0f);
         float qx = fadd(fmul(ndx, 0.5f), 0.5f), qy = fadd(fmul(ndy, 0.5f), 0.5f);
@@ -157,10 +224,12 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
         depth = gmin(depth, __ldg(img + (size_t)y1 * mw + x0));
         if (nx == 2) depth = gmin(depth, __ldg(img + (size_t)y1 * mw + x1));
     }
-    if (depth < mx2) {
+    if (depth < mx2 && !((flags & VKGV_CULL_OCCLUSION_FINE) && all_front &&
+                          fine_occluded(pyr, pw0, ph0, plevels, V.w, V.h, mn0, mx0, mn1, mx1, mx2))) {
         res.visible = true;
     } else {
         res.occluded = true;
+        res.sample = pack_sample(mx2, lvl, x0, x1, nx, y0, y1, ny);
     }
     return res;
 }
@@ -184,6 +253,29 @@ __device__ __forceinline__ void warp_append(bool flag, uint32_t value, uint32_t*
     }
 }
 
+// warp_append of a value and its packed HiZ sample into parallel arrays
+// (the sample array may be null).
+__device__ __forceinline__ void warp_append2(bool flag, uint32_t value, unsigned long long sample, uint32_t* list,
+                                             unsigned long long* samples, uint32_t* counter, uint32_t capacity,
+                                             uint32_t* status) {
+    const unsigned mask = __ballot_sync(0xffffffffu, flag);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (flag) {
+        uint32_t slot = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+        if (slot < capacity) {
+            list[slot] = value;
+            if (samples) samples[slot] = sample;
+        } else {
+            report(status, kStatusListOverflow, slot);
+        }
+    }
+}
+
 // pass 1: candidates are all draws [0, D); survivors -> survivors[0..),
 //         occlusion rejects -> rejected.
 // pass 2: candidates are rejected[0, counters[1]); survivors are appended at
@@ -197,6 +289,7 @@ __global__ void __launch_bounds__(256, 5) k_cull(SceneArgs S, const DeviceView* 
     __shared__ float s_vp[16];
     __shared__ float s_eye[3];
     __shared__ int s_eye_ok;
+    __shared__ int s_same;
     if (threadIdx.x < 24) s_frustum[threadIdx.x] = (&cam->frustum[0][0])[threadIdx.x];
     if (threadIdx.x < 16)
         s_vp[threadIdx.x] = pass == 1 ? cam->prev_occlusion_view_projection[threadIdx.x]
@@ -207,6 +300,17 @@ __global__ void __launch_bounds__(256, 5) k_cull(SceneArgs S, const DeviceView* 
 #pragma unroll
         for (int k = 0; k < 16; ++k) vp[k] = cam->view_projection[k];
         s_eye_ok = (flags & VKGV_CULL_CONE) && S.cone_table && eye_from_vp(vp, s_eye);
+    }
+    if (threadIdx.x == 64) {
+        // Pass 2 can repeat the pass-1 lookups when the occlusion camera and
+        // the pyramid's shape are unchanged (a static camera): the same box
+        // projects to the same footprint.
+        int same = pass == 2 && V.reject_samples != nullptr && V.prev_pyr != nullptr && V.prev_levels != 0 &&
+                   V.prev_w0 == (V.w >> 1) && V.prev_h0 == (V.h >> 1) && V.prev_levels == V.pyr_levels;
+        for (int k = 0; same && k < 16; ++k)
+            same = __float_as_uint(cam->prev_occlusion_view_projection[k]) ==
+                   __float_as_uint(cam->occlusion_view_projection[k]);
+        s_same = same;
     }
     __syncthreads();
     const float* eye = s_eye_ok ? s_eye : nullptr;
@@ -234,22 +338,34 @@ __global__ void __launch_bounds__(256, 5) k_cull(SceneArgs S, const DeviceView* 
     // Grid-stride with a warp-uniform trip count so the ballots stay converged.
     const uint32_t start = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t warp_start = start & ~31u;
+    const bool repeat = s_same != 0 && pyr != nullptr;
     for (uint32_t base = warp_start; base < n; base += stride) {
         const uint32_t i = base + (threadIdx.x & 31);
         bool vis = false, occ = false;
+        unsigned long long sample = 0ull;
         uint32_t d = 0;
         if (i < n) {
             d = pass == 1 ? i : V.rejected[i];
-            if (d < S.draw_count) {
-                CullResult r = cull_one(S, V, s_frustum, eye, s_vp, pyr, pw0, ph0, pl, flags, d, pass == 2, status);
-                vis = r.visible;
-                occ = r.occluded;
-            } else {
+            if (d >= S.draw_count) {
                 report(status, kStatusBadIndex, d);
+            } else {
+                // the repeated HiZ lookup when it applies; a draw it keeps
+                // under the fine test takes the full test (which needs the box)
+                const int coarse = repeat ? (int)sample_visible(V.reject_samples[i], pyr, pw0, ph0) : -1;
+                if (coarse == 0 || (coarse == 1 && !(flags & VKGV_CULL_OCCLUSION_FINE))) {
+                    vis = coarse == 1;
+                } else {
+                    CullResult r = cull_one(S, V, s_frustum, eye, s_vp, pyr, pw0, ph0, pl, flags, d, pass == 2,
+                                            status);
+                    vis = r.visible;
+                    occ = r.occluded;
+                    sample = r.sample;
+                }
             }
         }
         warp_append(vis, d, out_list, out_counter, cap, status);
-        if (collect_rejects) warp_append(occ, d, V.rejected, &V.counters[1], S.draw_count, status);
+        if (collect_rejects)
+            warp_append2(occ, d, sample, V.rejected, V.reject_samples, &V.counters[1], S.draw_count, status);
     }
 }
 

@@ -264,20 +264,16 @@ __device__ __forceinline__ void shade_pixel(const DiffArgs& A, const DeviceView&
         P0[k] = A.vpack[2 * (size_t)vi[k]];
         P1[k] = A.vpack[2 * (size_t)vi[k] + 1];
     }
+    // a and b from the compensated clip transform in both passes: on a
+    // sub-pixel triangle whose UVs span a large part of the texture (around
+    // the poles and the u seam of an equirectangular map) the plain fp32
+    // form's barycentric error becomes a texel-sized UV error in the
+    // forward image too.
     float a[3], b[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float q[3] = {P0[k].x, P0[k].y, P0[k].z};
-        if (BACKWARD) {
-            clip_ab(VP, q, nx, ny, a[k], b[k]);
-        } else {
-            // the forward image needs fp32 accuracy only (no cancellation
-            // reaches a gradient)
-            float c[4];
-            m4v(VP, q[0], q[1], q[2], 1.0f, c);
-            a[k] = fsub(c[0], fmul(nx, c[3]));
-            b[k] = fsub(c[1], fmul(ny, c[3]));
-        }
+        clip_ab(VP, q, nx, ny, a[k], b[k]);
     }
     float l[3] = {fsub(fmul(a[1], b[2]), fmul(a[2], b[1])), fsub(fmul(a[2], b[0]), fmul(a[0], b[2])),
                   fsub(fmul(a[0], b[1]), fmul(a[1], b[0]))};

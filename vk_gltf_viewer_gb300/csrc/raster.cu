@@ -125,8 +125,9 @@ __device__ __noinline__ void setup_and_raster(int32_t X0, int32_t Y0, float Z0, 
     const float dx2 = __int2float_rn(X2 - X0), dy2 = __int2float_rn(Y2 - Y0);
     const float af = __ll2float_rn(A);
     const float dz1 = fsub(Z1, Z0), dz2 = fsub(Z2, Z0);
-    const float pa = fdiv(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), af);
-    const float pb = fdiv(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), af);
+    const float ra = __frcp_rn(af);
+    const float pa = fmul(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), ra);
+    const float pb = fmul(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), ra);
     const int64_t bw = px1 - px0 + 1, bh = py1 - py0 + 1;
     if (bw * bh <= (int64_t)c.small_area) {
         raster_rect(X, Y, bias, Z0, pa, pb, id, (int)px0, (int)py0, (int)px1, (int)py1, c.depth, c.w);
@@ -159,7 +160,9 @@ __device__ __noinline__ void setup_and_raster(int32_t X0, int32_t Y0, float Z0, 
 
 __device__ __forceinline__ bool snap(const float4& v, const RasterCtx& c, int32_t& X, int32_t& Y, float& Z) {
     if (!(v.w > 0.0f)) return false;
-    const float xd = fdiv(v.x, v.w), yd = fdiv(v.y, v.w), zd = fdiv(v.z, v.w);
+    // one correctly rounded reciprocal of w and three products
+    const float rw = __frcp_rn(v.w);
+    const float xd = fmul(v.x, rw), yd = fmul(v.y, rw), zd = fmul(v.z, rw);
     const float xf = fadd(fmul(xd, c.hw), c.hw), yf = fadd(fmul(yd, c.hh), c.hh);
     const float sx = fmul(xf, 256.0f), sy = fmul(yf, 256.0f);
     if (!(fabsf(sx) < 1073741824.0f) || !(fabsf(sy) < 1073741824.0f)) return false;
@@ -234,6 +237,19 @@ __device__ __noinline__ void raster_clipped(float4 v0, float4 v1, float4 v2, boo
 
 // Views per raster launch (the launcher splits larger batches).
 constexpr uint32_t kRasterMaxViews = 1024;
+
+// What the per-meshlet header chain resolves for one work item.
+struct ItemHeader {
+    const uint32_t* vidx;       // the meshlet's vertex indices
+    const uint8_t* tri;         // its triangle-index bytes
+    const vkgv_vertex* verts;   // the primitive's vertex stream
+    uint32_t d;                 // meshlet draw index
+    uint32_t v;                 // view (in this launch)
+    uint32_t transform;         // node transform index
+    uint8_t vc, tc;             // vertex and triangle counts
+    uint8_t double_sided;       // material flag
+    uint8_t bad;                // an index out of range: reported, skipped
+};
 
 struct RasterParams {
     SceneArgs S;
@@ -403,8 +419,9 @@ __device__ __forceinline__ void raster_small(uint32_t ct, const uint8_t* sidx8, 
         const float dx2 = __int2float_rn(x[2] - x[0]), dy2 = __int2float_rn(y[2] - y[0]);
         const float af = __ll2float_rn(Ap);
         const float dz1 = fsub(z1, z0), dz2 = fsub(z2, z0);
-        const float pa = fdiv(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), af);
-        const float pb = fdiv(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), af);
+        const float ra = __frcp_rn(af);
+        const float pa = fmul(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), ra);
+        const float pb = fmul(fsub(fmul(dz2, dx1), fmul(dz1, dx2)), ra);
         const uint32_t id = (d << 7) | ct;
         if (bw * bh <= kLaneArea) {
             const unsigned long long lo = (unsigned long long)id + 1ull;
@@ -553,11 +570,9 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
     // views are drawn roughly in order (their depth buffers stay in L2) and
     // no warp idles while work is left.
     const uint32_t warps_total = gridDim.x * WARPS;
-    const uint32_t grab = max(1u, min(16u, total / (warps_total * 8u)));
+    const uint32_t grab = max(1u, min(32u, total / (warps_total * 8u)));
     uint32_t cur_v = 0xffffffffu;
     const DeviceView* Vp = P.views;
-    const uint32_t* list = nullptr;
-    uint32_t first = 0;
     // the warp's raster context lives in shared memory (fewer live registers)
     __shared__ RasterCtx s_ctx[WARPS];
     RasterCtx& c = s_ctx[warp];
@@ -569,6 +584,12 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
         c.chunk = P.chunk;
         c.status = P.status;
     }
+    // Per-meshlet headers of the current run, resolved one item per lane so
+    // that the dependent loads (list entry -> draw -> primitive -> meshlet
+    // record, material) of up to 32 meshlets are in flight together instead
+    // of one meshlet after another.
+    __shared__ ItemHeader s_hdr[WARPS][32];
+    ItemHeader* hdr = s_hdr[warp];
     // the next run is requested while the current one is drawn, so the
     // atomic's round trip is off the critical path
     // Warps beyond the first `total` have nothing to take (each of the
@@ -580,20 +601,60 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
         if (base >= total) break;
         if (lane == 0) next = atomicAdd(P.work, grab);
         const uint32_t stop = min(base + grab, total);
-        // the view holding `base`: the last v with s_pre[v] <= base
-        uint32_t v = 0, hi = nv;
-        while (v + 1 < hi) {
-            const uint32_t mid = (v + hi) >> 1;
-            if (s_pre[mid] <= base) v = mid;
-            else hi = mid;
+        {
+            const uint32_t g = base + (uint32_t)lane;
+            ItemHeader h;
+            h.d = 0xffffffffu;
+            h.v = 0;
+            h.bad = 1;
+            if (g < stop) {
+                // the view holding g: the last v with s_pre[v] <= g
+                uint32_t v = 0, hi = nv;
+                while (v + 1 < hi) {
+                    const uint32_t mid = (v + hi) >> 1;
+                    if (s_pre[mid] <= g) v = mid;
+                    else hi = mid;
+                }
+                const uint32_t* list;
+                uint32_t n, first;
+                view_work<SLOW>(P, P.views[v], list, n, first);
+                const uint32_t d = list[first + (g - s_pre[v])];
+                h.v = v;
+                h.d = d;
+                if (d < P.S.draw_count) {
+                    const vkgv_meshlet_draw dr = P.S.draws[d];
+                    const vkgv_primitive* prim = &P.S.prims[dr.primitive_index];
+                    if (dr.meshlet_index < prim->meshlet_count) {
+                        const vkgv_meshlet* ml =
+                            reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
+                        const uint32_t vc = ml->vertex_count, tc = ml->triangle_count;
+                        if (vc <= VKGV_MAX_VERTICES && tc <= VKGV_MAX_PRIMITIVES) {
+                            h.vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
+                            h.tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset;
+                            h.verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
+                            h.transform = dr.transform_index;
+                            h.vc = (uint8_t)vc;
+                            h.tc = (uint8_t)tc;
+                            h.double_sided = P.S.mats[prim->material_index].double_sided != 0 ? 1 : 0;
+                            h.bad = 0;
+                        }
+                    }
+                }
+            }
+            __syncwarp();  // every lane is done with the previous run's headers
+            hdr[lane] = h;
         }
-        for (uint32_t g = base; g < stop; ++g) {
-            while (g >= s_pre[v + 1]) ++v;
+        __syncwarp();
+        for (uint32_t k = 0; k < stop - base; ++k) {
+            const ItemHeader& H = hdr[k];
+            const uint32_t v = H.v, d = H.d;
+            if (H.bad) {
+                if (lane == 0) report(P.status, kStatusBadIndex, d);
+                continue;
+            }
             if (v != cur_v) {
                 cur_v = v;
                 Vp = P.views + v;
-                uint32_t n;
-                view_work<SLOW>(P, *Vp, list, n, first);
                 __syncwarp();
                 if (lane == 0) {
                     c.depth = Vp->depth_id;
@@ -607,33 +668,18 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
                 __syncwarp();
             }
             const DeviceView& V = *Vp;
-            const uint32_t d = list[first + (g - s_pre[v])];
-            if (d >= P.S.draw_count) {
-                if (lane == 0) report(P.status, kStatusBadIndex, d);
-                continue;
-            }
-            const vkgv_meshlet_draw dr = P.S.draws[d];
-            const vkgv_primitive* prim = &P.S.prims[dr.primitive_index];
-            if (dr.meshlet_index >= prim->meshlet_count) {
-                if (lane == 0) report(P.status, kStatusBadIndex, d);
-                continue;
-            }
-            const vkgv_meshlet* ml = reinterpret_cast<const vkgv_meshlet*>(prim->meshlet_buffer) + dr.meshlet_index;
-            const uint32_t vc = ml->vertex_count, tc = ml->triangle_count;
-            if (vc > VKGV_MAX_VERTICES || tc > VKGV_MAX_PRIMITIVES) {
-                if (lane == 0) report(P.status, kStatusBadIndex, d);
-                continue;
-            }
-            const uint32_t* vidx = reinterpret_cast<const uint32_t*>(prim->vertex_index_buffer) + ml->vertex_offset;
-            const uint8_t* tri = reinterpret_cast<const uint8_t*>(prim->primitive_index_buffer) + ml->triangle_offset;
-            const vkgv_vertex* verts = reinterpret_cast<const vkgv_vertex*>(prim->vertex_buffer);
-            const bool double_sided = P.S.mats[prim->material_index].double_sided != 0;
+            const uint32_t vc = H.vc, tc = H.tc;
+            const uint32_t* vidx = H.vidx;
+            const uint8_t* tri = H.tri;
+            const vkgv_vertex* verts = H.verts;
+            const bool double_sided = H.double_sided != 0;
+            const uint32_t transform_index = H.transform;
             // mvp = VP * M, one element per lane (lanes 0-15); lane 16 takes the
             // sign source determinant(M) of visbuffer.mesh.glsl:71.
-            const float* Mg = P.S.transforms + 16 * (size_t)dr.transform_index;
-            const bool have_tdet = P.S.tdets != nullptr && dr.transform_index < P.S.transform_count;
-            if (lane < 16 && V.mvps && dr.transform_index < P.S.transform_count) {
-                s_mvp[warp][lane] = __ldg(V.mvps + 16 * (size_t)dr.transform_index + lane);
+            const float* Mg = P.S.transforms + 16 * (size_t)transform_index;
+            const bool have_tdet = P.S.tdets != nullptr && transform_index < P.S.transform_count;
+            if (lane < 16 && V.mvps && transform_index < P.S.transform_count) {
+                s_mvp[warp][lane] = __ldg(V.mvps + 16 * (size_t)transform_index + lane);
             } else if (lane < 16) {
                 const int cc = lane >> 2, j = lane & 3;
                 const float4 mc = __ldg(reinterpret_cast<const float4*>(Mg) + cc);
@@ -641,7 +687,7 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
                                               fmul(s_vp[warp][2 * 4 + j], mc.z)),
                                          fmul(s_vp[warp][3 * 4 + j], mc.w));
             } else if (lane == 16 && have_tdet) {
-                s_tdet[warp] = P.S.tdets[dr.transform_index];
+                s_tdet[warp] = P.S.tdets[transform_index];
             } else if (lane == 16) {
                 float M[16];
     #pragma unroll
