@@ -369,6 +369,32 @@ __device__ __forceinline__ int classify(uint32_t i0, uint32_t i1, uint32_t i2, u
     return small ? kFast : kSlowSetup;
 }
 
+// First stage of the fast instance, on every triangle: 0 = dropped (an
+// index out of range, outcode reject, unsnapped vertex, or no pixel centre
+// in its clamped bounding box), 2 = needs the slow instance (a vertex
+// outside the near/far planes or the guard band), 1 = a candidate for the
+// compacted second stage (raster_small), which applies the backface test
+// (visbuffer.mesh.glsl:86-101), the zero-area test and the size limits.
+// The tests only filter, so their order does not change what is drawn; the
+// cheap ones run here on every triangle, the others only on the candidates.
+__device__ __forceinline__ int prefilter(uint32_t i0, uint32_t i1, uint32_t i2, uint32_t vc, const int4* svtx,
+                                         const RasterCtx& c, uint32_t d) {
+    if (i0 >= vc || i1 >= vc || i2 >= vc) {
+        report(c.status, kStatusBadIndex, d);
+        return 0;
+    }
+    const int4 q0 = svtx[i0], q1 = svtx[i1], q2 = svtx[i2];
+    const uint32_t f0 = (uint32_t)q0.w, f1 = (uint32_t)q1.w, f2 = (uint32_t)q2.w;
+    if (f0 & f1 & f2 & 63) return 0;  // outcode reject
+    if ((f0 | f1 | f2) & (OC_ZLO | OC_ZHI | kFlagGuard)) return 2;
+    if (!(f0 & f1 & f2 & kFlagSnapped)) return 0;
+    const int32_t minx = min(q0.x, min(q1.x, q2.x)), maxx = max(q0.x, max(q1.x, q2.x));
+    const int32_t miny = min(q0.y, min(q1.y, q2.y)), maxy = max(q0.y, max(q1.y, q2.y));
+    const int32_t qx0 = max((minx - 128 + 255) >> 8, 0), qx1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
+    const int32_t qy0 = max((miny - 128 + 255) >> 8, 0), qy1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
+    return (qx0 > qx1 || qy0 > qy1) ? 0 : 1;
+}
+
 // One sample of a small triangle: int32 edge functions (the extent bound of
 // kFast keeps them exact), top-left bias, plane depth clamped to [0, 1].
 __device__ __forceinline__ void small_sample(const int32_t* x, const int32_t* y, uint32_t bias, float z0, float pa,
@@ -386,28 +412,59 @@ __device__ __forceinline__ void small_sample(const int32_t* x, const int32_t* y,
     }
 }
 
-// Setup and raster of up to 32 compacted kFast triangles, one per lane (ct =
-// meshlet-local triangle index, 0xffffffff = none).  A triangle whose
+// Second stage of the fast instance: up to 32 compacted candidates, one
+// per lane (ct = meshlet-local triangle index, 0xffffffff = none).  A
+// candidate that is back-facing or of zero area is dropped; one whose bbox
+// exceeds small_area pixels or whose extent leaves int32 edge values needs
+// the slow instance (the return value); the rest are set up and
+// rasterised.  A triangle whose
 // clamped bbox has at most kLaneArea pixels is rasterised by its own lane;
 // the larger ones are spread over the warp by an inclusive scan of their
 // bbox areas.
-__device__ __forceinline__ void raster_small(uint32_t ct, const uint8_t* sidx8, const int4* svtx, uint32_t d,
-                                             const RasterCtx& c, TriRec* recs, uint32_t* ends, int lane) {
+__device__ __forceinline__ bool raster_small(uint32_t ct, const uint8_t* sidx8, const int4* svtx, const float4* clip,
+                                             bool double_sided, float tdet, uint32_t d, const RasterCtx& c,
+                                             TriRec* recs, uint32_t* ends, int lane) {
     uint32_t coop_area = 0;
+    bool slow = false;
+    int4 q0, q1, q2;
+    int32_t A = 0;  // the area of a live (small) triangle fits int32
+    int32_t px0 = 0, px1 = 0, py0 = 0, py1 = 0;
+    bool live = false;
     if (ct != 0xffffffffu) {
-        const int4 q0 = svtx[sidx8[3 * ct]], q1 = svtx[sidx8[3 * ct + 1]], q2 = svtx[sidx8[3 * ct + 2]];
-        const int64_t A = (int64_t)(q1.x - q0.x) * (q2.y - q0.y) - (int64_t)(q1.y - q0.y) * (q2.x - q0.x);
+        const uint32_t i0 = sidx8[3 * ct], i1 = sidx8[3 * ct + 1], i2 = sidx8[3 * ct + 2];
+        q0 = svtx[i0], q1 = svtx[i1], q2 = svtx[i2];
+        bool back = false;
+        if (!double_sided) {
+            const float4 a = clip[i0], b = clip[i1], cc = clip[i2];
+            const float det = det3(a.x, a.y, a.w, b.x, b.y, b.w, cc.x, cc.y, cc.w);
+            back = tdet < 0.0f ? det < 0.0f : det > 0.0f;
+        }
+        if (!back) {
+            const int32_t minx = min(q0.x, min(q1.x, q2.x)), maxx = max(q0.x, max(q1.x, q2.x));
+            const int32_t miny = min(q0.y, min(q1.y, q2.y)), maxy = max(q0.y, max(q1.y, q2.y));
+            if (maxx - minx < kSmallExtent && maxy - miny < kSmallExtent) {
+                // edge values of such a triangle stay inside int32
+                A = (q1.x - q0.x) * (q2.y - q0.y) - (q1.y - q0.y) * (q2.x - q0.x);
+                px0 = max((minx - 128 + 255) >> 8, 0), px1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
+                py0 = max((miny - 128 + 255) >> 8, 0), py1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
+                if (A != 0) {
+                    live = (uint32_t)((px1 - px0 + 1) * (py1 - py0 + 1)) <= c.small_area;
+                    slow = !live;
+                }
+            } else {
+                const int64_t A64 = (int64_t)(q1.x - q0.x) * (q2.y - q0.y) - (int64_t)(q1.y - q0.y) * (q2.x - q0.x);
+                slow = A64 != 0;
+            }
+        }
+    }
+    if (live) {
         int32_t x[3] = {q0.x, q1.x, q2.x}, y[3] = {q0.y, q1.y, q2.y};
         float z0 = __int_as_float(q0.z), z1 = __int_as_float(q1.z), z2 = __int_as_float(q2.z);
         if (A < 0) {  // orient to positive area
             x[1] = q2.x, y[1] = q2.y, x[2] = q1.x, y[2] = q1.y;
             z1 = __int_as_float(q2.z), z2 = __int_as_float(q1.z);
         }
-        const int64_t Ap = A < 0 ? -A : A;
-        const int32_t minx = min(x[0], min(x[1], x[2])), maxx = max(x[0], max(x[1], x[2]));
-        const int32_t miny = min(y[0], min(y[1], y[2])), maxy = max(y[0], max(y[1], y[2]));
-        const int32_t px0 = max((minx - 128 + 255) >> 8, 0), px1 = min((maxx - 128) >> 8, (int32_t)c.w - 1);
-        const int32_t py0 = max((miny - 128 + 255) >> 8, 0), py1 = min((maxy - 128) >> 8, (int32_t)c.h - 1);
+        const int32_t Ap = A < 0 ? -A : A;
         const uint32_t bw = (uint32_t)(px1 - px0 + 1), bh = (uint32_t)(py1 - py0 + 1);
         uint32_t bias = 0;
 #pragma unroll
@@ -417,7 +474,7 @@ __device__ __forceinline__ void raster_small(uint32_t ct, const uint8_t* sidx8, 
         }
         const float dx1 = __int2float_rn(x[1] - x[0]), dy1 = __int2float_rn(y[1] - y[0]);
         const float dx2 = __int2float_rn(x[2] - x[0]), dy2 = __int2float_rn(y[2] - y[0]);
-        const float af = __ll2float_rn(Ap);
+        const float af = __int2float_rn(Ap);
         const float dz1 = fsub(z1, z0), dz2 = fsub(z2, z0);
         const float ra = __frcp_rn(af);
         const float pa = fmul(fsub(fmul(dz1, dy2), fmul(dz2, dy1)), ra);
@@ -476,7 +533,7 @@ __device__ __forceinline__ void raster_small(uint32_t ct, const uint8_t* sidx8, 
             }
         }
     }
-    if (__ballot_sync(0xffffffffu, coop_area != 0) == 0) return;
+    if (__ballot_sync(0xffffffffu, coop_area != 0) == 0) return slow;
     // Warp-cooperative raster: an inclusive scan of the bbox areas spreads
     // the pixels of the larger small triangles evenly over the lanes.
     uint32_t incl = coop_area;
@@ -502,6 +559,7 @@ __device__ __forceinline__ void raster_small(uint32_t ct, const uint8_t* sidx8, 
                      (unsigned long long)r.id + 1ull, c);
     }
     __syncwarp();
+    return slow;
 }
 
 // Warp-per-meshlet raster.  The fast instance (SLOW = false) handles every
@@ -519,7 +577,7 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
     // the meshlet's triangle-index bytes (<= 126 triangles)
     __shared__ uint32_t s_idx[WARPS][96];
     __shared__ TriRec s_tri[WARPS][32];
-    // ring of compacted kFast triangle indices (fast instance)
+    // ring of compacted candidate triangle indices (fast instance)
     __shared__ uint8_t s_ring[WARPS][64];
     __shared__ uint32_t s_end[WARPS][32];
     __shared__ float s_mvp[WARPS][16];
@@ -763,23 +821,20 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
                     }
                 }
             } else {
-                // Classify 32 triangles per round; the ones that reach the small
-                // raster are compacted into a ring so that setup and raster run
-                // on full warps (about a quarter of the triangles of a dense
-                // meshlet have a sample in their bounding box).
+                // Pre-filter 32 triangles per round (outcodes, snap, a pixel
+                // centre in the bbox); the candidates are compacted into a
+                // ring so that the backface, area and size tests, the setup and
+                // the raster run on full warps (at most about a quarter of the
+                // triangles of a dense meshlet have a sample in their bbox).
                 uint8_t* ring = s_ring[warp];
                 uint32_t head = 0, pending = 0;
                 for (uint32_t tbase = 0; tbase < tc; tbase += 32) {
                     const uint32_t t = tbase + lane;
-                    int kind = kDrop;
-                    if (t < tc) {
-                        TriClass k;
-                        kind = classify<false>(sidx8[3 * t], sidx8[3 * t + 1], sidx8[3 * t + 2], vc, svtx, clip,
-                                               double_sided, tdet, c, d, k);
-                    }
-                    any_slow |= kind == kSlowClip || kind == kSlowSetup;
-                    const uint32_t fm = __ballot_sync(0xffffffffu, kind == kFast);
-                    if (kind == kFast) ring[(head + pending + __popc(fm & ((1u << lane) - 1u))) & 63u] = (uint8_t)t;
+                    int kind = 0;
+                    if (t < tc) kind = prefilter(sidx8[3 * t], sidx8[3 * t + 1], sidx8[3 * t + 2], vc, svtx, c, d);
+                    any_slow |= kind == 2;
+                    const uint32_t fm = __ballot_sync(0xffffffffu, kind == 1);
+                    if (kind == 1) ring[(head + pending + __popc(fm & ((1u << lane) - 1u))) & 63u] = (uint8_t)t;
                     pending += __popc(fm);
                     const bool last = tbase + 32 >= tc;
                     while (pending >= 32 || (last && pending > 0)) {
@@ -787,7 +842,7 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
                         const uint32_t n = min(pending, 32u);
                         const uint32_t ct = lane < n ? ring[(head + lane) & 63u] : 0xffffffffu;
                         __syncwarp();
-                        raster_small(ct, sidx8, svtx, d, c, recs, ends, lane);
+                        any_slow |= raster_small(ct, sidx8, svtx, clip, double_sided, tdet, d, c, recs, ends, lane);
                         head = (head + n) & 63u;
                         pending -= n;
                     }
