@@ -36,9 +36,11 @@ __device__ __forceinline__ int hiz_level(float m, uint32_t levels) {
 // texels; occluded when all of them are >= mx2.  No such level (an odd view
 // side, or a box too large) leaves the HiZ verdict.  The oracle restates the
 // same integer footprint and fp32 products.
+// An occluding footprint is reported in *foot: level << 28 | a0 << 16 |
+// b0 << 4 | (a1 - a0) << 2 | (b1 - b0).
 __device__ __forceinline__ bool fine_occluded(const float* pyr, uint32_t pw0, uint32_t ph0, uint32_t plevels,
                                               uint32_t vw, uint32_t vh, float mn0, float mx0, float mn1, float mx1,
-                                              float mx2) {
+                                              float mx2, uint32_t* foot) {
     if ((vw & 1u) || (vh & 1u) || vw == 0 || vh == 0) return false;
     int top = min(__ffs((int)vw), __ffs((int)vh)) - 2;  // min(ctz) - 1
     top = min(top, (int)plevels - 1);
@@ -57,9 +59,25 @@ __device__ __forceinline__ bool fine_occluded(const float* pyr, uint32_t pw0, ui
         for (int y = b0; y <= b1; ++y)
             for (int x = a0; x <= a1; ++x)
                 if (__ldg(img + (size_t)y * mw + x) < mx2) return false;
+        *foot = ((uint32_t)l << 28) | ((uint32_t)a0 << 16) | ((uint32_t)b0 << 4) | ((uint32_t)(a1 - a0) << 2) |
+                (uint32_t)(b1 - b0);
         return true;
     }
     return false;
+}
+
+// Repeats a fine footprint (the low word of a fine key) on a pyramid of the
+// same shape: occluded iff every texel is >= mx2.
+__device__ __forceinline__ bool footprint_occluded(uint32_t foot, float mx2, const float* pyr, uint32_t pw0,
+                                                   uint32_t ph0) {
+    const uint32_t l = foot >> 28, a0 = (foot >> 16) & 0xfffu, b0 = (foot >> 4) & 0xfffu;
+    const uint32_t a1 = a0 + ((foot >> 2) & 3u), b1 = b0 + (foot & 3u);
+    const uint32_t mw = mip_dim(pw0, l);
+    const float* img = pyr + mip_offset(pw0, ph0, l);
+    for (uint32_t y = b0; y <= b1; ++y)
+        for (uint32_t x = a0; x <= a1; ++x)
+            if (__ldg(img + (size_t)y * mw + x) < mx2) return false;
+    return true;
 }
 
 struct CullResult {
@@ -68,18 +86,29 @@ struct CullResult {
     unsigned long long sample;  // the HiZ sample of an occlusion test (see pack_sample)
 };
 
-// One HiZ lookup as 64 bits: the nearest AABB depth's bits (high word), the
+// One occlusion verdict as 64 bits, for pass 2 to repeat.
+// HiZ key: the nearest AABB depth's bits (high word, sign bit clear), the
 // mip level (4 bits), the first footprint texel (12 + 12 bits: mips are at
 // most 4096 wide) and whether the footprint also takes the next texel on
 // each axis.  A footprint's second texel, when footprint_axis reports one,
 // is the next texel or the same one (clamped at the edge), and the MIN of a
 // texel with itself is that texel, so the flags record only a distinct next
-// texel.
+// texel.  A depth with the sign bit set (negative, -0 or a negative NaN)
+// loses to every pyramid depth (all >= +0), as +0 does: it is stored as +0.
+// Fine key (a draw the HiZ test kept and the fine test rejected; its depth
+// is then > 0): the depth's bits with the sign bit set, and the fine
+// footprint of fine_occluded.
 __device__ __forceinline__ unsigned long long pack_sample(float maxz, int lvl, int x0, int x1, int nx, int y0, int y1,
                                                           int ny) {
     const uint32_t lo = ((uint32_t)lvl << 28) | ((uint32_t)x0 << 16) | ((uint32_t)y0 << 4) |
                         ((nx == 2 && x1 != x0) ? 2u : 0u) | ((ny == 2 && y1 != y0) ? 1u : 0u);
-    return ((unsigned long long)__float_as_uint(maxz) << 32) | lo;
+    uint32_t hi = __float_as_uint(maxz);
+    if (hi & 0x80000000u) hi = 0u;
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+__device__ __forceinline__ unsigned long long pack_fine(float maxz, uint32_t foot) {
+    return ((unsigned long long)(__float_as_uint(maxz) | 0x80000000u) << 32) | foot;
 }
 
 // Repeats a packed lookup on a pyramid of the same shape: visible iff the
@@ -224,12 +253,16 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
         depth = gmin(depth, __ldg(img + (size_t)y1 * mw + x0));
         if (nx == 2) depth = gmin(depth, __ldg(img + (size_t)y1 * mw + x1));
     }
-    if (depth < mx2 && !((flags & VKGV_CULL_OCCLUSION_FINE) && all_front &&
-                          fine_occluded(pyr, pw0, ph0, plevels, V.w, V.h, mn0, mx0, mn1, mx1, mx2))) {
-        res.visible = true;
-    } else {
+    uint32_t foot = 0;
+    if (!(depth < mx2)) {
         res.occluded = true;
         res.sample = pack_sample(mx2, lvl, x0, x1, nx, y0, y1, ny);
+    } else if ((flags & VKGV_CULL_OCCLUSION_FINE) && all_front &&
+               fine_occluded(pyr, pw0, ph0, plevels, V.w, V.h, mn0, mx0, mn1, mx1, mx2, &foot)) {
+        res.occluded = true;
+        res.sample = pack_fine(mx2, foot);
+    } else {
+        res.visible = true;
     }
     return res;
 }
@@ -349,11 +382,24 @@ __global__ void __launch_bounds__(256, 5) k_cull(SceneArgs S, const DeviceView* 
             if (d >= S.draw_count) {
                 report(status, kStatusBadIndex, d);
             } else {
-                // the repeated HiZ lookup when it applies; a draw it keeps
-                // under the fine test takes the full test (which needs the box)
-                const int coarse = repeat ? (int)sample_visible(V.reject_samples[i], pyr, pw0, ph0) : -1;
-                if (coarse == 0 || (coarse == 1 && !(flags & VKGV_CULL_OCCLUSION_FINE))) {
-                    vis = coarse == 1;
+                // The repeated lookup when it applies: a fine key that still
+                // occludes, or a HiZ key that still occludes (or, without
+                // the fine test, still keeps), decides; otherwise the full
+                // test (which needs the box) runs.
+                int verdict = -1;
+                if (repeat) {
+                    const unsigned long long key = V.reject_samples[i];
+                    if (key >> 63) {
+                        const float mz = __uint_as_float((uint32_t)(key >> 32) & 0x7fffffffu);
+                        if (footprint_occluded((uint32_t)key, mz, pyr, pw0, ph0)) verdict = 0;
+                    } else {
+                        const bool coarse = sample_visible(key, pyr, pw0, ph0);
+                        if (!coarse) verdict = 0;
+                        else if (!(flags & VKGV_CULL_OCCLUSION_FINE)) verdict = 1;
+                    }
+                }
+                if (verdict >= 0) {
+                    vis = verdict == 1;
                 } else {
                     CullResult r = cull_one(S, V, s_frustum, eye, s_vp, pyr, pw0, ph0, pl, flags, d, pass == 2,
                                             status);
