@@ -221,7 +221,7 @@ __host__ __device__ __forceinline__ uint64_t mip_offset(uint32_t w0, uint32_t h0
 // tiled level (at most level 4) and the matching 2^k-times larger tiles of
 // the levels below it.  Levels with a zero dimension are never tiled.
 constexpr int kHizTileLevels = 4;
-constexpr int kHizTopTile = 8;
+constexpr int kHizTopTile = 4;
 
 __host__ __device__ __forceinline__ int hiz_tile_levels(uint32_t w, uint32_t h, uint32_t levels) {
     int k = (int)(levels < (uint32_t)kHizTileLevels ? levels : (uint32_t)kHizTileLevels);

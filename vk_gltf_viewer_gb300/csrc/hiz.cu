@@ -11,8 +11,9 @@
 // pos == size through, whose image store is out of bounds; only pos < size is
 // written here.
 //
-// Single pass: each CTA owns an 8x8 tile of level 4 and the 16x16, 32x32 and
-// 64x64 tiles of levels 3, 2, 1 above it.  For odd sizes the footprints do
+// Single pass: each CTA owns a 4x4 tile of level 4 and the 8x8, 16x16 and
+// 32x32 tiles of levels 3, 2, 1 above it (510 CTAs of 256 threads at
+// 1920x1080, several resident per SM).  For odd sizes the footprints do
 // not nest, so each CTA computes the hull of its owned tile and the
 // footprint of the level above it (a halo of a few texels, recomputed rather
 // than exchanged), keeping levels 1-3 in shared memory and reading the depth
@@ -26,15 +27,18 @@ namespace vkgv {
 
 namespace {
 
-constexpr int kCap1 = 80, kCap2 = 40, kCap3 = 20, kCap4 = 12;  // per-axis smem capacity per level
-constexpr int kThreads = 1024;
+// Per-axis shared-memory capacity per tile level: the owned tile (32, 16,
+// 8, 4 texels) plus the footprint of the level above it, which for odd
+// sizes reaches one texel further per level.
+constexpr int kCap1 = 48, kCap2 = 26, kCap3 = 14, kCap4 = 8;
+constexpr int kThreads = 256;
 // Dynamic shared memory: the tile levels, later reused by the tail as two
-// ping-pong buffers (A, B) when the top tiled mip fits.
+// ping-pong buffers (A: the top tiled mip, B: the level above it) when they
+// fit kTailMax floats; the launch sizes it to the larger of the two uses.
 constexpr int kOff2 = kCap1 * kCap1, kOff3 = kOff2 + kCap2 * kCap2, kOff4 = kOff3 + kCap3 * kCap3;
-constexpr int kTailA = 16384, kTailB = 8192;
-constexpr int kSmemFloats = kTailA + kTailB;
+constexpr int kTileFloats = kOff4 + kCap4 * kCap4;
+constexpr int kTailMax = 40960;
 constexpr int kTailAxis = 1024;  // largest tail level edge with per-axis footprint tables
-static_assert(kOff4 + kCap4 * kCap4 <= kSmemFloats, "tile levels fit the shared buffer");
 
 struct Range {
     int lo, hi;  // inclusive; empty when lo > hi
@@ -96,7 +100,8 @@ __device__ __forceinline__ float reduce_texel(int x, int y, uint32_t dw, uint32_
     return r;
 }
 
-__global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__ views, uint32_t* status) {
+__global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__ views, uint32_t* status,
+                                                  uint32_t tail_a, uint32_t tail_b) {
     pdl_begin();
     const DeviceView& V = views[blockIdx.z];
     if (!V.pyr || V.pyr_levels == 0) return;
@@ -210,12 +215,27 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
     if (!s_last) return;
     __threadfence();
     const uint32_t top_w = Kp > 0 ? (w >> Kp) : 0, top_h = Kp > 0 ? (h >> Kp) : 0;
-    const bool in_smem = Kp > 0 && top_w * top_h <= (uint32_t)kTailA;
+    const uint32_t next_px = Kp > 0 ? (w >> (Kp + 1)) * (h >> (Kp + 1)) : 0;
+    const bool in_smem = Kp > 0 && top_w * top_h <= tail_a && next_px <= tail_b;
     float* cur = smem;
-    float* nxt = smem + kTailA;
+    float* nxt = smem + tail_a;
     if (in_smem) {
+        // eight loads in flight per thread before the first store
         const float* src = V.pyr + mip_offset(w0, h0, (uint32_t)(Kp - 1));
-        for (uint32_t i = threadIdx.x; i < top_w * top_h; i += blockDim.x) cur[i] = __ldcg(src + i);
+        const uint32_t n = top_w * top_h;
+        for (uint32_t i0 = threadIdx.x; i0 < n; i0 += 8 * kThreads) {
+            float t[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t i = i0 + (uint32_t)k * kThreads;
+                t[k] = i < n ? __ldcg(src + i) : 0.0f;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t i = i0 + (uint32_t)k * kThreads;
+                if (i < n) cur[i] = t[k];
+            }
+        }
         __syncthreads();
     }
     // per-axis footprints of the current tail level: x0 | x1 << 14 | n << 28
@@ -285,8 +305,14 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
 
 }  // namespace
 
-void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t* status,
-                cudaStream_t stream) {
+void hiz_tail_floats(uint32_t w, uint32_t h, uint32_t levels, uint32_t* a, uint32_t* b) {
+    const int top = hiz_tile_levels(w, h, levels);
+    *a = top > 0 ? (w >> top) * (h >> top) : 0u;
+    *b = top > 0 ? (w >> (top + 1)) * (h >> (top + 1)) : 0u;
+}
+
+void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t tail_a,
+                uint32_t tail_b, uint32_t* status, cudaStream_t stream) {
     // The dynamic shared-memory limit is a per-device function attribute:
     // set it once for each device a launch runs on (setting it twice is
     // harmless, so concurrent first launches need no lock).
@@ -295,11 +321,14 @@ void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint
     cudaGetDevice(&dev);
     const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
     if (!bit || !(attr_devices.load(std::memory_order_acquire) & bit)) {
-        cudaFuncSetAttribute(k_hiz, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemFloats * (int)sizeof(float));
+        cudaFuncSetAttribute(k_hiz, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailMax * (int)sizeof(float));
         attr_devices.fetch_or(bit, std::memory_order_release);
     }
+    // the tail works in shared memory when its two largest levels fit
+    if ((uint64_t)tail_a + tail_b > (uint64_t)kTailMax) tail_a = tail_b = 0;
+    const uint32_t floats = tail_a + tail_b > (uint32_t)kTileFloats ? tail_a + tail_b : (uint32_t)kTileFloats;
     dim3 grid(tiles_x ? tiles_x : 1, tiles_y ? tiles_y : 1, nviews);
-    launch_pdl(k_hiz, grid, dim3(kThreads), kSmemFloats * sizeof(float), stream, views, status);
+    launch_pdl(k_hiz, grid, dim3(kThreads), floats * sizeof(float), stream, views, status, tail_a, tail_b);
 }
 
 }  // namespace vkgv
