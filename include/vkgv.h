@@ -649,7 +649,9 @@ typedef struct vkgv_dds_info {
     uint32_t mip_count;
     uint32_t format;         /* vkgv_block_format */
     uint32_t srgb;           /* DXGI *_UNORM_SRGB, or a KTX2 *_SRGB vkFormat */
-    uint32_t _pad;
+    uint32_t supercompression; /* KTX2: 0 none, 2 Zstandard (data_offset / data_size
+                                * then hold the compressed level; it decodes with
+                                * vkgv_zstd_decompress to the format's texel size) */
     uint64_t data_offset;    /* byte offset of the top mip's blocks */
     uint64_t data_size;      /* bytes of the top mip */
 } vkgv_dds_info;
@@ -659,13 +661,25 @@ typedef struct vkgv_dds_info {
 int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* out);
 /* Reads a KTX 2.0 header (the container of KHR_texture_basisu, which the
  * reference enables in fastgltf, assets.cpp:539, and links ktx_read for):
- * a 2D texture (one layer, one face) without supercompression whose vkFormat
- * is BC1-BC5 UNORM / SRGB (131-139, 141) or R8G8B8A8 UNORM / SRGB (37, 43),
- * into the same fields as a DDS file (level 0; format VKGV_BC1_OPAQUE for
- * BC1_RGB, VKGV_RGBA8 for R8G8B8A8).  BasisU (vkFormat 0) and
- * supercompressed files, SNORM formats, cube maps, arrays and 3D textures
- * are VKGV_INVALID_ARG. */
+ * a 2D texture (one layer, one face), without supercompression or with
+ * Zstandard supercompression (scheme 2), whose vkFormat is BC1-BC5 UNORM /
+ * SRGB (131-139, 141) or R8G8B8A8 UNORM / SRGB (37, 43), into the same
+ * fields as a DDS file (level 0; format VKGV_BC1_OPAQUE for BC1_RGB,
+ * VKGV_RGBA8 for R8G8B8A8; `supercompression` set to 2 for a zstd level,
+ * whose uncompressed length must be the format's texel size).  BasisU
+ * (vkFormat 0, BasisLZ scheme 1), SNORM formats, cube maps, arrays and 3D
+ * textures are VKGV_INVALID_ARG. */
 int vkgv_ktx2_parse(const void* data, uint64_t size, vkgv_dds_info* out);
+/* Zstandard (RFC 8878) decoder for KTX2 supercompression scheme 2 (libktx,
+ * which the reference links as ktx_read, CMakeLists.txt:13, inflates these
+ * with libzstd): decodes every frame of src (skippable frames skipped, no
+ * dictionaries, content checksums verified) into dst.  *out_size receives
+ * the decoded length.  VKGV_LIMIT_EXCEEDED when dst_capacity is too small,
+ * VKGV_INVALID_ARG for a corrupt or truncated stream.  Host only. */
+int vkgv_zstd_decompress(const void* src, uint64_t src_size, void* dst, uint64_t dst_capacity,
+                         uint64_t* out_size);
+/* XXH64 (seed 0) of data, the hash of the zstd content checksum. */
+uint64_t vkgv_xxh64(const void* data, uint64_t size);
 /* Decodes width x height texels of BC blocks (device, row-major blocks of
  * 8 or 16 bytes, aligned to the block size) into RGBA8 (device
  * uint32[width * height], 4-byte aligned). */

@@ -65,6 +65,34 @@ def test_ktx2_through_load_image(renderer):
         assert np.array_equal(got.view(np.uint32)[..., 0], ob.decode_bc(fmt, blocks, 37, 22))
 
 
+def test_zstd_ktx2_through_load_image(renderer):
+    """Zstandard-supercompressed KTX2 levels (committed libzstd frames of
+    block data) inflate on the host and decode on the device to the oracle's
+    texels of the same blocks."""
+    import base64
+    import json
+    import struct
+    from pathlib import Path
+
+    from test_texture_decode import _ktx2
+
+    cases = json.loads((Path(__file__).resolve().parent / "golden" / "zstd_frames.json").read_text())["cases"]
+    used = 0
+    for c in cases:
+        if c["name"] != "bc1_blocks":
+            continue
+        frame = base64.b64decode(c["frame"])
+        blocks = np.frombuffer(texture.zstd_decompress(frame, c["size"]).tobytes(), np.uint8)
+        bw = 32
+        bh = c["size"] // (8 * bw)
+        data = bytearray(_ktx2(133, 4 * bw, 4 * bh, frame, scheme=2))
+        struct.pack_into("<Q", data, 96, bw * bh * 8)  # uncompressedByteLength
+        got = texture.load_image(bytes(data), abi.IMAGE_KTX2, renderer)
+        assert np.array_equal(got.view(np.uint32)[..., 0], ob.decode_bc(abi.BC1, blocks[: bw * bh * 8], 4 * bw, 4 * bh))
+        used += 1
+    assert used == 3
+
+
 def test_jpeg_through_load_image_and_freed_source(renderer):
     """decode_jpeg frees the host coefficients before the device finishes:
     the copy is staged, so the pixels are still the oracle's."""

@@ -168,7 +168,7 @@ def test_ktx2_headers(built):
     assert np.array_equal(texture.load_image(_ktx2(37, 16, 12, rgba), abi.IMAGE_KTX2).reshape(-1),
                           np.frombuffer(rgba, np.uint8))
     bad = [_ktx2(0, 4, 4, bytes(64)),                  # BasisU (vkFormat undefined)
-           _ktx2(133, 4, 4, bytes(8), scheme=2),       # zstd supercompression
+           _ktx2(133, 4, 4, bytes(8), scheme=1),       # BasisLZ supercompression
            _ktx2(133, 4, 4, bytes(48), faces=6),       # cube map
            _ktx2(140, 4, 4, bytes(8)),                 # BC4 SNORM
            _ktx2(146, 4, 4, bytes(16)),                # BC7

@@ -196,7 +196,8 @@ class GltfImage(C.Structure):
 
 class DdsInfo(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("mip_count", C.c_uint32), ("format", C.c_uint32),
-                ("srgb", C.c_uint32), ("_pad", C.c_uint32), ("data_offset", C.c_uint64), ("data_size", C.c_uint64)]
+                ("srgb", C.c_uint32), ("supercompression", C.c_uint32), ("data_offset", C.c_uint64),
+                ("data_size", C.c_uint64)]
 
 
 class JpegInfo(C.Structure):
@@ -232,6 +233,8 @@ _PROTOS = {
     "vkgv_cull": (C.c_int, [_P, C.POINTER(Scene), C.POINTER(View), _U32, _U32, _P]),
     "vkgv_cull_static": (C.c_int, [C.POINTER(Scene), C.POINTER(View), _U32, _U32, _P]),
     "vkgv_cull_static_status": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32)]),
+    "vkgv_zstd_decompress": (C.c_int, [_P, _U64, _P, _U64, C.POINTER(_U64)]),
+    "vkgv_xxh64": (_U64, [_P, _U64]),
     "vkgv_raster": (C.c_int, [_P, C.POINTER(Scene), C.POINTER(View), _U64, _U64, _U32, _P]),
     "vkgv_hiz_reduce": (C.c_int, [_P, C.POINTER(View), _P]),
     "vkgv_resolve": (C.c_int, [_P, C.POINTER(Scene), C.POINTER(View), _U32, _P]),

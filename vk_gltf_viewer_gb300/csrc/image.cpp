@@ -536,7 +536,7 @@ extern "C" int vkgv_ktx2_parse(const void* data, uint64_t size, vkgv_dds_info* o
     const uint32_t vk_format = le32(p + 12), width = le32(p + 20), height = le32(p + 24);
     const uint32_t depth = le32(p + 28), layers = le32(p + 32), faces = le32(p + 36);
     const uint32_t levels = le32(p + 40), scheme = le32(p + 44);
-    if (scheme != 0 || vk_format == 0) return VKGV_INVALID_ARG;  // BasisU / supercompressed
+    if ((scheme != 0 && scheme != 2) || vk_format == 0) return VKGV_INVALID_ARG;  // BasisU / BasisLZ
     if (width == 0 || height == 0 || depth > 1 || layers > 1 || faces != 1) return VKGV_INVALID_ARG;
     uint32_t fmt = 0, srgb = 0;
     switch (vk_format) {  // VkFormat values
@@ -554,9 +554,10 @@ extern "C" int vkgv_ktx2_parse(const void* data, uint64_t size, vkgv_dds_info* o
         case 43: fmt = VKGV_RGBA8; srgb = 1; break;        // R8G8B8A8_SRGB
         default: return VKGV_INVALID_ARG;
     }
-    uint64_t offset, length;
+    uint64_t offset, length, raw_length;
     std::memcpy(&offset, p + 80, 8);
     std::memcpy(&length, p + 88, 8);
+    std::memcpy(&raw_length, p + 96, 8);
     uint64_t need;
     if (fmt == VKGV_RGBA8) {
         need = uint64_t(width) * height * 4;
@@ -564,13 +565,20 @@ extern "C" int vkgv_ktx2_parse(const void* data, uint64_t size, vkgv_dds_info* o
         const uint64_t bw = (uint64_t(width) + 3) / 4, bh = (uint64_t(height) + 3) / 4;
         need = bw * bh * ((fmt == VKGV_BC1 || fmt == VKGV_BC4 || fmt == VKGV_BC1_OPAQUE) ? 8u : 16u);
     }
-    if (length < need || offset > size || size - offset < need) return VKGV_INVALID_ARG;
+    if (scheme == 2) {
+        // a zstd level: its compressed bytes in the file, the texels after
+        // inflating
+        if (raw_length != need || length == 0 || offset > size || size - offset < length) return VKGV_INVALID_ARG;
+    } else if (length < need || offset > size || size - offset < need) {
+        return VKGV_INVALID_ARG;
+    }
     out->width = width;
     out->height = height;
     out->mip_count = levels ? levels : 1;
     out->format = fmt;
     out->srgb = srgb;
+    out->supercompression = scheme;
     out->data_offset = offset;
-    out->data_size = need;
+    out->data_size = scheme == 2 ? length : need;
     return VKGV_OK;
 }

@@ -46,16 +46,38 @@ def parse_dds(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
     return info, blocks
 
 
+def zstd_decompress(data, size: int) -> np.ndarray:
+    """Zstandard frames -> exactly `size` decoded bytes (vkgv_zstd_decompress)."""
+    src = np.frombuffer(data, np.uint8) if not isinstance(data, np.ndarray) else np.ascontiguousarray(data, np.uint8)
+    out = np.empty(max(1, size), np.uint8)
+    n = C.c_uint64()
+    rc = abi.load().vkgv_zstd_decompress(src.ctypes.data, src.size, out.ctypes.data, size, C.byref(n))
+    if rc != abi.OK:
+        raise abi.VkgvError(rc, "corrupt Zstandard data, or more than the expected size")
+    if n.value != size:
+        raise abi.VkgvError(abi.INVALID_ARG, f"Zstandard data decoded to {n.value} bytes, expected {size}")
+    return out[:size]
+
+
 def parse_ktx2(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
     """KTX2 bytes -> (header info, level 0's bytes): BC1-BC5 blocks or
-    RGBA8 texels (``info.format`` is ``abi.RGBA8`` for those)."""
+    RGBA8 texels (``info.format`` is ``abi.RGBA8`` for those), inflated
+    first when the level is Zstandard-supercompressed."""
     buf = np.frombuffer(data, np.uint8)
     info = abi.DdsInfo()
     rc = abi.load().vkgv_ktx2_parse(buf.ctypes.data, buf.size, C.byref(info))
     if rc != abi.OK:
-        raise abi.VkgvError(rc, "not a KTX2 file with uncompressed BC1-BC5 or RGBA8 data "
-                                "(BasisU and supercompressed files are not decoded)")
-    return info, buf[info.data_offset:info.data_offset + info.data_size].copy()
+        raise abi.VkgvError(rc, "not a KTX2 file with BC1-BC5 or RGBA8 data, uncompressed or Zstandard-"
+                                "supercompressed (BasisU files are not decoded)")
+    level = buf[info.data_offset:info.data_offset + info.data_size]
+    if info.supercompression == 2:
+        if info.format == abi.RGBA8:
+            size = info.width * info.height * 4
+        else:
+            block = 8 if info.format in (abi.BC1, abi.BC4, abi.BC1_OPAQUE) else 16
+            size = ((info.width + 3) // 4) * ((info.height + 3) // 4) * block
+        return info, zstd_decompress(level, size)
+    return info, level.copy()
 
 
 def decode_bc(renderer, fmt: int, blocks, width: int, height: int, stream=None) -> torch.Tensor:
