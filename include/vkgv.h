@@ -639,8 +639,9 @@ enum vkgv_block_format {
     VKGV_BC5 = 5,   /* two interpolated channels (R, G)                              */
     VKGV_BC1_OPAQUE = 6, /* BC1 read as Vulkan's BC1_RGB formats: the three-colour
                           * mode's fourth entry is opaque black                      */
-    VKGV_RGBA8 = 7  /* uncompressed RGBA8 texels (reported by vkgv_ktx2_parse only;
+    VKGV_RGBA8 = 7, /* uncompressed RGBA8 texels (reported by vkgv_ktx2_parse only;
                      * not a vkgv_decode_bc format)                                 */
+    VKGV_BC7 = 8    /* BPTC UNORM: eight modes of 1-3 subsets, 16-byte blocks       */
 };
 
 typedef struct vkgv_dds_info {
@@ -657,13 +658,15 @@ typedef struct vkgv_dds_info {
 } vkgv_dds_info;
 
 /* Reads a DDS header (FourCC DXT1-5 / ATI1 / ATI2 / BC4U / BC5U, or DX10
- * with a BC1-BC5 DXGI format); VKGV_INVALID_ARG for anything else. */
+ * with a BC1-BC5 or BC7 DXGI format); VKGV_INVALID_ARG for anything else
+ * (BC6H, uncompressed pixel formats). */
 int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* out);
 /* Reads a KTX 2.0 header (the container of KHR_texture_basisu, which the
  * reference enables in fastgltf, assets.cpp:539, and links ktx_read for):
  * a 2D texture (one layer, one face), without supercompression or with
  * Zstandard supercompression (scheme 2), whose vkFormat is BC1-BC5 UNORM /
- * SRGB (131-139, 141) or R8G8B8A8 UNORM / SRGB (37, 43), into the same
+ * SRGB (131-139, 141), BC7 UNORM / SRGB (145, 146) or R8G8B8A8 UNORM / SRGB
+ * (37, 43), into the same
  * fields as a DDS file (level 0; format VKGV_BC1_OPAQUE for BC1_RGB,
  * VKGV_RGBA8 for R8G8B8A8; `supercompression` set to 2 for a zstd level,
  * whose uncompressed length must be the format's texel size).  BasisU
@@ -680,9 +683,9 @@ int vkgv_zstd_decompress(const void* src, uint64_t src_size, void* dst, uint64_t
                          uint64_t* out_size);
 /* XXH64 (seed 0) of data, the hash of the zstd content checksum. */
 uint64_t vkgv_xxh64(const void* data, uint64_t size);
-/* Decodes width x height texels of BC blocks (device, row-major blocks of
- * 8 or 16 bytes, aligned to the block size) into RGBA8 (device
- * uint32[width * height], 4-byte aligned). */
+/* Decodes width x height texels of BC1-BC5 or BC7 blocks (device,
+ * row-major blocks of 8 or 16 bytes, aligned to the block size) into RGBA8
+ * (device uint32[width * height], 4-byte aligned). */
 int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
                    uint64_t rgba_out, void* stream);
 

@@ -74,9 +74,155 @@ static void channel_block(const uint8_t* p, unsigned out[16]) {
     for (int i = 0; i < 16; ++i) out[i] = pal[(bits >> (3 * i)) & 7u];
 }
 
+/* ------------------------------------------------------------------ BC7
+ * BC7 (BPTC UNORM), restated from the published format: the mode from the
+ * lowest set bit of the first byte; per mode the subset count, partition
+ * bits, rotation and index-selection bits, colour / alpha endpoint bits,
+ * p-bits (per endpoint or shared per subset) and one or two index sets;
+ * endpoints expanded to 8 bits by replicating their top bits; texels
+ * interpolated as ((64 - w) e0 + w e1 + 32) >> 6 with the 2-, 3- and 4-bit
+ * weight tables; the anchor texel of each subset stores one index bit less.
+ * A reserved mode (first byte 0) decodes to transparent black.  The
+ * partition and anchor tables below are the format's own. */
+static const uint16_t kBc7P2[64] = {
+    0xCCCC, 0x8888, 0xEEEE, 0xECC8, 0xC880, 0xFEEC, 0xFEC8, 0xEC80, 0xC800, 0xFFEC, 0xFE80, 0xE800,
+    0xFFE8, 0xFF00, 0xFFF0, 0xF000, 0xF710, 0x008E, 0x7100, 0x08CE, 0x008C, 0x7310, 0x3100, 0x8CCE,
+    0x088C, 0x3110, 0x6666, 0x366C, 0x17E8, 0x0FF0, 0x718E, 0x399C, 0xAAAA, 0xF0F0, 0x5A5A, 0x33CC,
+    0x3C3C, 0x55AA, 0x9696, 0xA55A, 0x73CE, 0x13C8, 0x324C, 0x3BDC, 0x6996, 0xC33C, 0x9966, 0x0660,
+    0x0272, 0x04E4, 0x4E40, 0x2720, 0xC936, 0x936C, 0x39C6, 0x639C, 0x9336, 0x9CC6, 0x817E, 0xE718,
+    0xCCF0, 0x0FCC, 0x7744, 0xEE22};
+/* 3-subset partitions: two bits per texel, texel 0 in the lowest bits */
+static const uint32_t kBc7P3[64] = {
+    0xAA685050, 0x6A5A5040, 0x5A5A4200, 0x5450A0A8, 0xA5A50000, 0xA0A05050, 0x5555A0A0, 0x5A5A5050,
+    0xAA550000, 0xAA555500, 0xAAAA5500, 0x90909090, 0x94949494, 0xA4A4A4A4, 0xA9A59450, 0x2A0A4250,
+    0xA5945040, 0x0A425054, 0xA5A5A500, 0x55A0A0A0, 0xA8A85454, 0x6A6A4040, 0xA4A45000, 0x1A1A0500,
+    0x0050A4A4, 0xAAA59090, 0x14696914, 0x69691400, 0xA08585A0, 0xAA821414, 0x50A4A450, 0x6A5A0200,
+    0xA9A58000, 0x5090A0A8, 0xA8A09050, 0x24242424, 0x00AA5500, 0x24924924, 0x24499224, 0x50A50A50,
+    0x500AA550, 0xAAAA4444, 0x66660000, 0xA5A0A5A0, 0x50A050A0, 0x69286928, 0x44AAAA44, 0x66666600,
+    0xAA444444, 0x54A854A8, 0x95809580, 0x96969600, 0xA85454A8, 0x80959580, 0xAA141414, 0x96960000,
+    0xAAAA1414, 0xA05050A0, 0xA0A5A5A0, 0x96000000, 0x40804080, 0xA9A8A9A8, 0xAAAAAA44, 0x2A4A5254};
+static const uint8_t kBc7A2[64] = {
+    15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 2, 8, 2, 2, 8, 8, 15, 2, 8,
+    2, 2, 8, 8, 2, 2, 15, 15, 6, 8, 2, 8, 15, 15, 2, 8, 2, 2, 2, 15, 15, 6, 6, 2, 6, 8, 15, 15, 2,
+    2, 15, 15, 15, 15, 15, 2, 2, 15};
+static const uint8_t kBc7A3a[64] = {
+    3, 3, 15, 15, 8, 3, 15, 15, 8, 8, 6, 6, 6, 5, 3, 3, 3, 3, 8, 15, 3, 3, 6, 10, 5, 8, 8, 6, 8, 5,
+    15, 15, 8, 15, 3, 5, 6, 10, 8, 15, 15, 3, 15, 5, 15, 15, 15, 15, 3, 15, 5, 5, 5, 8, 5, 10, 5,
+    10, 8, 13, 15, 12, 3, 3};
+static const uint8_t kBc7A3b[64] = {
+    15, 8, 8, 3, 15, 15, 3, 8, 15, 15, 15, 15, 15, 15, 15, 8, 15, 8, 15, 3, 15, 8, 15, 8, 3, 15, 6,
+    10, 15, 15, 10, 8, 15, 3, 15, 10, 10, 8, 9, 10, 6, 15, 8, 15, 3, 6, 6, 8, 15, 3, 15, 15, 15, 15,
+    15, 15, 15, 15, 15, 15, 3, 15, 15, 8};
+
+static const uint8_t kBc7W2[4] = {0, 21, 43, 64};
+static const uint8_t kBc7W3[8] = {0, 9, 18, 27, 37, 46, 55, 64};
+static const uint8_t kBc7W4[16] = {0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64};
+
+/* mode parameters: subsets, partition bits, rotation bits, index-selection
+ * bit, colour bits, alpha bits, p-bits per endpoint, shared p-bits, index
+ * bits, second index bits */
+static const uint8_t kBc7Mode[8][10] = {
+    {3, 4, 0, 0, 4, 0, 1, 0, 3, 0}, {2, 6, 0, 0, 6, 0, 0, 1, 3, 0}, {3, 6, 0, 0, 5, 0, 0, 0, 2, 0},
+    {2, 6, 0, 0, 7, 0, 1, 0, 2, 0}, {1, 0, 2, 1, 5, 6, 0, 0, 2, 3}, {1, 0, 2, 0, 7, 8, 0, 0, 2, 2},
+    {1, 0, 0, 0, 7, 7, 1, 0, 4, 0}, {2, 6, 0, 0, 5, 5, 1, 0, 2, 0}};
+
+static uint32_t bc7_bits(const uint8_t* b, unsigned* pos, unsigned n) {
+    uint32_t v = 0;
+    for (unsigned i = 0; i < n; ++i, ++*pos) v |= (uint32_t)((b[*pos >> 3] >> (*pos & 7)) & 1u) << i;
+    return v;
+}
+
+static unsigned bc7_expand(unsigned v, unsigned bits) {
+    v <<= 8 - bits;
+    return v | (v >> bits);
+}
+
+static unsigned bc7_interp(unsigned e0, unsigned e1, unsigned w) { return ((64 - w) * e0 + w * e1 + 32) >> 6; }
+
+static void bc7_block(const uint8_t* b, uint32_t out[16]) {
+    unsigned mode = 0;
+    while (mode < 8 && !((b[0] >> mode) & 1u)) ++mode;
+    if (mode == 8) {
+        for (int i = 0; i < 16; ++i) out[i] = 0;
+        return;
+    }
+    const uint8_t* m = kBc7Mode[mode];
+    const unsigned ns = m[0], cb = m[4], ab = m[5], ib = m[8], ib2 = m[9];
+    unsigned pos = mode + 1;
+    const unsigned part = bc7_bits(b, &pos, m[1]);
+    const unsigned rot = bc7_bits(b, &pos, m[2]);
+    const unsigned isel = bc7_bits(b, &pos, m[3]);
+    unsigned ep[3][2][4]; /* subset, endpoint, channel */
+    for (unsigned c = 0; c < 3; ++c)
+        for (unsigned s = 0; s < ns; ++s)
+            for (unsigned e = 0; e < 2; ++e) ep[s][e][c] = bc7_bits(b, &pos, cb);
+    for (unsigned s = 0; s < ns; ++s)
+        for (unsigned e = 0; e < 2; ++e) ep[s][e][3] = ab ? bc7_bits(b, &pos, ab) : 255u;
+    unsigned cbits = cb, abits = ab;
+    if (m[6]) { /* a p-bit per endpoint */
+        for (unsigned s = 0; s < ns; ++s)
+            for (unsigned e = 0; e < 2; ++e) {
+                const unsigned p = bc7_bits(b, &pos, 1);
+                for (unsigned c = 0; c < 4; ++c)
+                    if (c < 3 || ab) ep[s][e][c] = (ep[s][e][c] << 1) | p;
+            }
+        cbits = cb + 1;
+        abits = ab ? ab + 1 : 0;
+    } else if (m[7]) { /* a p-bit per subset */
+        for (unsigned s = 0; s < ns; ++s) {
+            const unsigned p = bc7_bits(b, &pos, 1);
+            for (unsigned e = 0; e < 2; ++e)
+                for (unsigned c = 0; c < 3; ++c) ep[s][e][c] = (ep[s][e][c] << 1) | p;
+        }
+        cbits = cb + 1;
+    }
+    for (unsigned s = 0; s < ns; ++s)
+        for (unsigned e = 0; e < 2; ++e) {
+            for (unsigned c = 0; c < 3; ++c) ep[s][e][c] = bc7_expand(ep[s][e][c], cbits);
+            if (ab) ep[s][e][3] = bc7_expand(ep[s][e][3], abits);
+        }
+    /* subset of each texel and the anchors (texel 0 for subset 0) */
+    unsigned sub[16], anchor[3] = {0, 16, 16};
+    for (unsigned i = 0; i < 16; ++i)
+        sub[i] = ns == 1 ? 0u : (ns == 2 ? ((kBc7P2[part] >> i) & 1u) : ((kBc7P3[part] >> (2 * i)) & 3u));
+    if (ns == 2) anchor[1] = kBc7A2[part];
+    if (ns == 3) {
+        anchor[1] = kBc7A3a[part];
+        anchor[2] = kBc7A3b[part];
+    }
+    unsigned idx[16], idx2[16];
+    for (unsigned i = 0; i < 16; ++i) {
+        const int is_anchor = i == anchor[0] || i == anchor[1] || i == anchor[2];
+        idx[i] = bc7_bits(b, &pos, ib - (is_anchor ? 1u : 0u));
+    }
+    for (unsigned i = 0; ib2 && i < 16; ++i) idx2[i] = bc7_bits(b, &pos, ib2 - (i == 0 ? 1u : 0u));
+    for (unsigned i = 0; i < 16; ++i) {
+        const unsigned s = sub[i];
+        unsigned ci = idx[i], ai = idx[i], cw_bits = ib, aw_bits = ib;
+        if (ib2) {
+            if (isel) {
+                ci = idx2[i], cw_bits = ib2;
+            } else {
+                ai = idx2[i], aw_bits = ib2;
+            }
+        }
+        const uint8_t* cw = cw_bits == 2 ? kBc7W2 : (cw_bits == 3 ? kBc7W3 : kBc7W4);
+        const uint8_t* aw = aw_bits == 2 ? kBc7W2 : (aw_bits == 3 ? kBc7W3 : kBc7W4);
+        unsigned px[4];
+        for (unsigned c = 0; c < 3; ++c) px[c] = bc7_interp(ep[s][0][c], ep[s][1][c], cw[ci]);
+        px[3] = ab ? bc7_interp(ep[s][0][3], ep[s][1][3], aw[ai]) : 255u;
+        if (rot) { /* swap alpha with R (1), G (2) or B (3) */
+            const unsigned t = px[3];
+            px[3] = px[rot - 1];
+            px[rot - 1] = t;
+        }
+        out[i] = px[0] | (px[1] << 8) | (px[2] << 16) | (px[3] << 24);
+    }
+}
+
 void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t h, uint32_t* rgba) {
     uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
-    size_t bsize = (format == 1 || format == 4 || format == 6) ? 8 : 16;
+    size_t bsize = (format == 1 || format == 4 || format == 6) ? 8 : 16; /* 8: BC7 */
     for (uint32_t by = 0; by < bh; ++by)
         for (uint32_t bx = 0; bx < bw; ++bx) {
             const uint8_t* p = blocks + ((size_t)by * bw + bx) * bsize;
@@ -101,6 +247,9 @@ void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t 
                     colour_block(p + 8, 0, col);
                     channel_block(p, ch0);
                     for (int i = 0; i < 16; ++i) tex[i] = (col[i] & 0x00FFFFFFu) | ((uint32_t)ch0[i] << 24);
+                    break;
+                case 8:
+                    bc7_block(p, tex);
                     break;
                 case 4:
                     channel_block(p, ch0);

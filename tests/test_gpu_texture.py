@@ -38,6 +38,61 @@ def test_bc_decode_matches_oracle(renderer, fmt, size):
     assert np.array_equal(got.cpu().numpy().reshape(h, w, 4).view(np.uint32)[..., 0], exp)
 
 
+def _bc7_blocks(rng, n: int, reserved: bool = True) -> np.ndarray:
+    """n random BC7 blocks, every mode equally often (and, with `reserved`,
+    blocks whose first byte is 0): any 128 bits after the mode bits are a
+    valid block."""
+    blocks = rng.integers(0, 256, size=(n, 16), dtype=np.uint8)
+    modes = np.arange(n) % (9 if reserved else 8)
+    rng.shuffle(modes)
+    for mode in range(8):
+        rows = modes == mode
+        low = (1 << (mode + 1)) - 1
+        blocks[rows, 0] = (blocks[rows, 0] & ~np.uint8(low)) | np.uint8(1 << mode)
+    blocks[modes == 8, 0] = 0
+    return blocks.reshape(-1)
+
+
+@pytest.mark.parametrize("size", [(4, 4), (37, 21), (256, 128), (3, 5), (1024, 1000)])
+def test_bc7_decode_matches_oracle(renderer, size):
+    w, h = size
+    rng = np.random.default_rng(w * 7 + h)
+    blocks = _bc7_blocks(rng, ((w + 3) // 4) * ((h + 3) // 4))
+    got = texture.decode_bc(renderer, abi.BC7, blocks, w, h)
+    torch.cuda.synchronize()
+    exp = ob.decode_bc(abi.BC7, blocks, w, h)
+    assert np.array_equal(got.cpu().numpy().reshape(h, w, 4).view(np.uint32)[..., 0], exp)
+
+
+def test_bc7_oracle_matches_texture_unit(tmp_path):
+    """Pins the BC7 oracle (and its partition, anchor and weight tables) to
+    the GPU's texture unit: a BC7 CUDA array read through a point-sampled
+    texture object decodes the same random blocks of every mode."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = tmp_path / "bc7_hw"
+    src = Path(__file__).with_name("bc7_hw.cu")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-o", str(exe), str(src)],
+                   check=True, capture_output=True, timeout=300)
+    w, h = 256, 128  # 2,048 blocks, 256 per mode
+    blocks = _bc7_blocks(np.random.default_rng(2024), (w // 4) * (h // 4), reserved=False)
+    (tmp_path / "blocks.bin").write_bytes(blocks.tobytes())
+    run = subprocess.run([str(exe), str(tmp_path / "blocks.bin"), str(tmp_path / "rgba.bin"), str(w), str(h)],
+                         capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stderr
+    hw = np.fromfile(tmp_path / "rgba.bin", np.uint32).reshape(h, w)
+    exp = ob.decode_bc(abi.BC7, blocks, w, h)
+    bad = np.argwhere(hw != exp)
+    if len(bad):
+        by, bx = bad[0] // 4
+        blk = blocks.reshape(h // 4, w // 4, 16)[by, bx]
+        raise AssertionError(f"{len(bad)} texels differ; first at {tuple(bad[0])}: texture unit "
+                             f"{hw[tuple(bad[0])]:08x}, oracle {exp[tuple(bad[0])]:08x}, block {blk.tobytes().hex()}")
+
+
 @pytest.mark.parametrize("case", range(13))
 @pytest.mark.parametrize("size", [(37, 45), (1, 1), (17, 64), (300, 517)])
 def test_jpeg_pixels_match_oracle(renderer, case, size):

@@ -104,8 +104,12 @@ def test_dds_headers(built):
     assert (info.format, info.srgb, info.data_offset) == (abi.BC1, 1, 148)
     with pytest.raises(abi.VkgvError):
         texture.parse_dds(_dds(b"DXT1", 16, 16, bytes(8)))  # too little data
+    info, _ = texture.parse_dds(_dds(b"DX10", 8, 4, bytes(32), dxgi=98))  # BC7_UNORM
+    assert (info.format, info.srgb, info.data_size) == (abi.BC7, 0, 32)
+    info, _ = texture.parse_dds(_dds(b"DX10", 8, 4, bytes(32), dxgi=99))  # BC7_UNORM_SRGB
+    assert (info.format, info.srgb) == (abi.BC7, 1)
     with pytest.raises(abi.VkgvError):
-        texture.parse_dds(_dds(b"DX10", 4, 4, bytes(16), dxgi=98))  # BC7 is not decoded
+        texture.parse_dds(_dds(b"DX10", 4, 4, bytes(16), dxgi=95))  # BC6H is not decoded
 
 
 def _rgba(r, g, b, a=255):
@@ -162,6 +166,9 @@ def test_ktx2_headers(built):
         assert got.tobytes() == blocks
     info, _ = texture.parse_ktx2(_ktx2(138, 8, 4, bytes(32)))
     assert (info.format, info.srgb) == (abi.BC3, 1)
+    for vk, srgb in ((145, 0), (146, 1)):
+        info, got = texture.parse_ktx2(_ktx2(vk, 5, 4, bytes(range(32))))
+        assert (info.format, info.srgb, got.tobytes()) == (abi.BC7, srgb, bytes(range(32)))
     rgba = bytes(range(256)) * 3
     info, got = texture.parse_ktx2(_ktx2(43, 16, 12, rgba))
     assert (info.format, info.srgb, info.data_size) == (abi.RGBA8, 1, 768)
@@ -171,7 +178,7 @@ def test_ktx2_headers(built):
            _ktx2(133, 4, 4, bytes(8), scheme=1),       # BasisLZ supercompression
            _ktx2(133, 4, 4, bytes(48), faces=6),       # cube map
            _ktx2(140, 4, 4, bytes(8)),                 # BC4 SNORM
-           _ktx2(146, 4, 4, bytes(16)),                # BC7
+           _ktx2(143, 4, 4, bytes(16)),                # BC6H
            _ktx2(133, 16, 16, bytes(8)),               # too little data
            b"DDS " + bytes(200)]
     for data in bad:
@@ -185,6 +192,118 @@ def test_oracle_bc1_opaque_known_answer(built):
     blk = struct.pack("<HHI", 0x001F, 0xF800, 0b11100100)
     out = ob.decode_bc(abi.BC1_OPAQUE, np.frombuffer(blk, np.uint8), 4, 4)
     assert list(out[0]) == [_rgba(0, 0, 255), _rgba(255, 0, 0), _rgba(128, 0, 128), _rgba(0, 0, 0, 255)]
+
+
+# BC7 mode fields: subsets, partition bits, rotation bits, index-selection
+# bits, colour bits, alpha bits, p-bit per endpoint, p-bit per subset, index
+# bits, second index bits (the format's mode table)
+BC7_MODES = {0: (3, 4, 0, 0, 4, 0, 1, 0, 3, 0), 1: (2, 6, 0, 0, 6, 0, 0, 1, 3, 0), 2: (3, 6, 0, 0, 5, 0, 0, 0, 2, 0),
+             3: (2, 6, 0, 0, 7, 0, 1, 0, 2, 0), 4: (1, 0, 2, 1, 5, 6, 0, 0, 2, 3), 5: (1, 0, 2, 0, 7, 8, 0, 0, 2, 2),
+             6: (1, 0, 0, 0, 7, 7, 1, 0, 4, 0), 7: (2, 6, 0, 0, 5, 5, 1, 0, 2, 0)}
+BC7_WEIGHTS = {2: [0, 21, 43, 64], 3: [0, 9, 18, 27, 37, 46, 55, 64],
+               4: [0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64]}
+
+
+def bc7_block(mode, ep, pbits=(), idx=(), idx2=(), part=0, rot=0, isel=0, anchors=(0,)):
+    """Packs one BC7 block from its fields, least significant bit first:
+    ep[subset][endpoint] = (r, g, b, a) at the mode's stored precision;
+    `anchors` are the texels whose first index is one bit shorter."""
+    ns, pb, rb, sb, cb, ab, epb, spb, ib, ib2 = BC7_MODES[mode]
+    fields = [(1 << mode, mode + 1), (part, pb), (rot, rb), (isel, sb)]
+    fields += [(ep[s][e][c], cb) for c in range(3) for s in range(ns) for e in range(2)]
+    fields += [(ep[s][e][3], ab) for s in range(ns) for e in range(2)] if ab else []
+    assert len(pbits) == (2 * ns if epb else ns if spb else 0)
+    fields += [(p, 1) for p in pbits]
+    fields += [(v, ib - (i in anchors)) for i, v in enumerate(idx)]
+    fields += [(v, ib2 - (i == 0)) for i, v in enumerate(idx2)]
+    word, at = 0, 0
+    for v, n in fields:
+        assert 0 <= v < (1 << n) or n == 0 and v == 0
+        word |= v << at
+        at += n
+    assert at == 128
+    return word.to_bytes(16, "little")
+
+
+def _bc7_texel(e0, e1, bits, w):
+    """One channel: endpoints of `bits` bits (p-bit included) expanded to 8 by
+    replicating their top bits, then interpolated with weight w of 64."""
+    x0, x1 = e0 << (8 - bits), e1 << (8 - bits)
+    x0, x1 = x0 | (x0 >> bits), x1 | (x1 >> bits)
+    return ((64 - w) * x0 + w * x1 + 32) >> 6
+
+
+def test_oracle_bc7_known_answers(built):
+    rng = np.random.default_rng(7)
+
+    def decode(blk):
+        return ob.decode_bc(abi.BC7, np.frombuffer(blk, np.uint8), 4, 4).reshape(-1)
+
+    def texels(out):
+        return [[(int(t) >> (8 * c)) & 255 for c in range(4)] for t in out]
+
+    # mode 6: one subset, RGBA 7 bits + a p-bit per end point, 4-bit indices
+    ep = [[(10, 20, 30, 127), (100, 50, 0, 0)]]
+    idx = [int(v) for v in rng.integers(0, 16, 16)]
+    idx[0] &= 7
+    got = texels(decode(bc7_block(6, ep, pbits=(1, 0), idx=idx)))
+    for i in range(16):
+        want = [_bc7_texel((ep[0][0][c] << 1) | 1, ep[0][1][c] << 1, 8, BC7_WEIGHTS[4][idx[i]]) for c in range(4)]
+        assert got[i] == want, i
+    # mode 5 with rotation 1: alpha swaps with red after interpolation
+    ep = [[(127, 3, 64, 200), (0, 120, 64, 17)]]
+    idx, idx2 = [int(v) for v in rng.integers(0, 4, 16)], [int(v) for v in rng.integers(0, 4, 16)]
+    idx[0] &= 1
+    idx2[0] &= 1
+    got = texels(decode(bc7_block(5, ep, idx=idx, idx2=idx2, rot=1)))
+    for i in range(16):
+        rgb = [_bc7_texel(ep[0][0][c], ep[0][1][c], 7, BC7_WEIGHTS[2][idx[i]]) for c in range(3)]
+        a = _bc7_texel(ep[0][0][3], ep[0][1][3], 8, BC7_WEIGHTS[2][idx2[i]])
+        assert got[i] == [a, rgb[1], rgb[2], rgb[0]], i
+    # mode 4: the index-selection bit gives colour the 3-bit indices; rotation 3 swaps blue
+    ep = [[(31, 0, 9, 63), (2, 17, 30, 5)]]
+    idx, idx2 = [int(v) for v in rng.integers(0, 4, 16)], [int(v) for v in rng.integers(0, 8, 16)]
+    idx[0] &= 1
+    idx2[0] &= 3
+    for isel in (0, 1):
+        got = texels(decode(bc7_block(4, ep, idx=idx, idx2=idx2, isel=isel, rot=3)))
+        for i in range(16):
+            cw = BC7_WEIGHTS[3][idx2[i]] if isel else BC7_WEIGHTS[2][idx[i]]
+            aw = BC7_WEIGHTS[2][idx[i]] if isel else BC7_WEIGHTS[3][idx2[i]]
+            rgb = [_bc7_texel(ep[0][0][c], ep[0][1][c], 5, cw) for c in range(3)]
+            a = _bc7_texel(ep[0][0][3], ep[0][1][3], 6, aw)
+            assert got[i] == [rgb[0], rgb[1], a, rgb[2]], (isel, i)
+    # mode 1, two-subset partition 13: rows 0-1 subset 0, rows 2-3 subset 1
+    # (anchor texel 15); one p-bit per subset, RGB only
+    ep = [[(63, 0, 10, 0), (0, 63, 20, 0)], [(5, 6, 7, 0), (40, 41, 42, 0)]]
+    idx = [int(v) for v in rng.integers(0, 8, 16)]
+    idx[0] &= 3
+    idx[15] &= 3
+    got = texels(decode(bc7_block(1, ep, pbits=(1, 0), idx=idx, part=13, anchors=(0, 15))))
+    for i in range(16):
+        s, p = (0, 1) if i < 8 else (1, 0)
+        want = [_bc7_texel((ep[s][0][c] << 1) | p, (ep[s][1][c] << 1) | p, 7, BC7_WEIGHTS[3][idx[i]])
+                for c in range(3)]
+        assert got[i] == want + [255], i
+    # mode 0, three-subset partition 0: columns 0-1 of rows 0-1 and column 0
+    # of row 2 subset 0, columns 2-3 of rows 0-2 subset 1, the rest subset 2;
+    # anchors at texels 0, 3 and 15
+    subset = [0, 0, 1, 1, 0, 0, 1, 1, 0, 2, 2, 1, 2, 2, 2, 2]
+    ep = [[(1, 2, 3, 0), (15, 14, 13, 0)], [(4, 4, 4, 0), (9, 0, 15, 0)], [(0, 0, 0, 0), (15, 15, 15, 0)]]
+    pbits = (1, 0, 0, 1, 1, 1)
+    idx = [int(v) for v in rng.integers(0, 8, 16)]
+    for a in (0, 3, 15):
+        idx[a] &= 3
+    got = texels(decode(bc7_block(0, ep, pbits=pbits, idx=idx, part=0, anchors=(0, 3, 15))))
+    for i in range(16):
+        s = subset[i]
+        p0, p1 = pbits[2 * s], pbits[2 * s + 1]
+        want = [_bc7_texel((ep[s][0][c] << 1) | p0, (ep[s][1][c] << 1) | p1, 5, BC7_WEIGHTS[3][idx[i]])
+                for c in range(3)]
+        assert got[i] == want + [255], i
+    # a reserved mode (first byte 0) decodes to transparent black
+    assert not decode(bytes(16)).any()
+    assert not decode(bytes([0]) + bytes(range(1, 16))).any()
 
 
 def test_gltf_texture_sources(built, tmp_path):

@@ -694,7 +694,8 @@ int vkgv_resolve(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* view, 
 int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
                    uint64_t rgba_out, void* stream_) {
     if (!ctx) return VKGV_INVALID_ARG;
-    if (format < VKGV_BC1 || format > VKGV_BC1_OPAQUE) return fail(ctx, VKGV_INVALID_ARG, "unknown block format");
+    if (format < VKGV_BC1 || (format > VKGV_BC1_OPAQUE && format != VKGV_BC7))
+        return fail(ctx, VKGV_INVALID_ARG, "unknown block format");
     if (width == 0 || height == 0) return VKGV_OK;
     if (width > 16384 || height > 16384) return fail(ctx, VKGV_LIMIT_EXCEEDED, "texture edge exceeds 16384");
     const uint64_t block_align = (format == VKGV_BC1 || format == VKGV_BC4 || format == VKGV_BC1_OPAQUE) ? 8u : 16u;

@@ -1,5 +1,5 @@
 // Block-compressed texture decode on the device: BC1-BC5 (the DXT1-5 /
-// RGTC formats a DDS base-colour texture holds, MSFT_texture_dds) into RGBA8
+// RGTC formats a DDS base-colour texture holds, MSFT_texture_dds) and BC7 into RGBA8
 // for the textured resolve.  The reference loads no images
 // (src/vk_gltf_viewer/assets.cpp:467-471); the formats are the published
 // ones, with the interpolation rounding, which they leave to the
@@ -79,8 +79,178 @@ __device__ __forceinline__ void channel_row(uint32_t lo, uint32_t hi, uint32_t r
     }
 }
 
+// BC7 (BPTC UNORM), decoded as the published format defines it: the mode from the
+// lowest set bit of the first byte; per mode the subset count, partition
+// bits, rotation and index-selection bits, colour / alpha endpoint bits,
+// p-bits (per endpoint or shared per subset) and one or two index sets;
+// endpoints expanded to 8 bits by replicating their top bits; texels
+// interpolated as ((64 - w) e0 + w e1 + 32) >> 6 with the 2-, 3- and 4-bit
+// weight tables; the anchor texel of each subset stores one index bit less.
+// A reserved mode (first byte 0) decodes to transparent black.  The
+// partition and anchor tables below are the format's own.
+__constant__ uint16_t c_bc7_p2[64] = {
+    0xCCCC, 0x8888, 0xEEEE, 0xECC8, 0xC880, 0xFEEC, 0xFEC8, 0xEC80, 0xC800, 0xFFEC, 0xFE80, 0xE800,
+    0xFFE8, 0xFF00, 0xFFF0, 0xF000, 0xF710, 0x008E, 0x7100, 0x08CE, 0x008C, 0x7310, 0x3100, 0x8CCE,
+    0x088C, 0x3110, 0x6666, 0x366C, 0x17E8, 0x0FF0, 0x718E, 0x399C, 0xAAAA, 0xF0F0, 0x5A5A, 0x33CC,
+    0x3C3C, 0x55AA, 0x9696, 0xA55A, 0x73CE, 0x13C8, 0x324C, 0x3BDC, 0x6996, 0xC33C, 0x9966, 0x0660,
+    0x0272, 0x04E4, 0x4E40, 0x2720, 0xC936, 0x936C, 0x39C6, 0x639C, 0x9336, 0x9CC6, 0x817E, 0xE718,
+    0xCCF0, 0x0FCC, 0x7744, 0xEE22};
+// 3-subset partitions: two bits per texel, texel 0 in the lowest bits
+__constant__ uint32_t c_bc7_p3[64] = {
+    0xAA685050, 0x6A5A5040, 0x5A5A4200, 0x5450A0A8, 0xA5A50000, 0xA0A05050, 0x5555A0A0, 0x5A5A5050,
+    0xAA550000, 0xAA555500, 0xAAAA5500, 0x90909090, 0x94949494, 0xA4A4A4A4, 0xA9A59450, 0x2A0A4250,
+    0xA5945040, 0x0A425054, 0xA5A5A500, 0x55A0A0A0, 0xA8A85454, 0x6A6A4040, 0xA4A45000, 0x1A1A0500,
+    0x0050A4A4, 0xAAA59090, 0x14696914, 0x69691400, 0xA08585A0, 0xAA821414, 0x50A4A450, 0x6A5A0200,
+    0xA9A58000, 0x5090A0A8, 0xA8A09050, 0x24242424, 0x00AA5500, 0x24924924, 0x24499224, 0x50A50A50,
+    0x500AA550, 0xAAAA4444, 0x66660000, 0xA5A0A5A0, 0x50A050A0, 0x69286928, 0x44AAAA44, 0x66666600,
+    0xAA444444, 0x54A854A8, 0x95809580, 0x96969600, 0xA85454A8, 0x80959580, 0xAA141414, 0x96960000,
+    0xAAAA1414, 0xA05050A0, 0xA0A5A5A0, 0x96000000, 0x40804080, 0xA9A8A9A8, 0xAAAAAA44, 0x2A4A5254};
+__constant__ uint8_t c_bc7_a2[64] = {
+    15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 2, 8, 2, 2, 8, 8, 15, 2, 8,
+    2, 2, 8, 8, 2, 2, 15, 15, 6, 8, 2, 8, 15, 15, 2, 8, 2, 2, 2, 15, 15, 6, 6, 2, 6, 8, 15, 15, 2,
+    2, 15, 15, 15, 15, 15, 2, 2, 15};
+__constant__ uint8_t c_bc7_a3a[64] = {
+    3, 3, 15, 15, 8, 3, 15, 15, 8, 8, 6, 6, 6, 5, 3, 3, 3, 3, 8, 15, 3, 3, 6, 10, 5, 8, 8, 6, 8, 5,
+    15, 15, 8, 15, 3, 5, 6, 10, 8, 15, 15, 3, 15, 5, 15, 15, 15, 15, 3, 15, 5, 5, 5, 8, 5, 10, 5,
+    10, 8, 13, 15, 12, 3, 3};
+__constant__ uint8_t c_bc7_a3b[64] = {
+    15, 8, 8, 3, 15, 15, 3, 8, 15, 15, 15, 15, 15, 15, 15, 8, 15, 8, 15, 3, 15, 8, 15, 8, 3, 15, 6,
+    10, 15, 15, 10, 8, 15, 3, 15, 10, 10, 8, 9, 10, 6, 15, 8, 15, 3, 6, 6, 8, 15, 3, 15, 15, 15, 15,
+    15, 15, 15, 15, 15, 15, 3, 15, 15, 8};
+
+__constant__ uint8_t c_bc7_w[3][16] = {{0, 21, 43, 64}, {0, 9, 18, 27, 37, 46, 55, 64},
+                                       {0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64}};
+// subsets, partition bits, rotation bits, index-selection bit, colour bits,
+// alpha bits, p-bit per endpoint, p-bit per subset, index bits, second index bits
+__constant__ uint8_t c_bc7_mode[8][10] = {
+    {3, 4, 0, 0, 4, 0, 1, 0, 3, 0}, {2, 6, 0, 0, 6, 0, 0, 1, 3, 0}, {3, 6, 0, 0, 5, 0, 0, 0, 2, 0},
+    {2, 6, 0, 0, 7, 0, 1, 0, 2, 0}, {1, 0, 2, 1, 5, 6, 0, 0, 2, 3}, {1, 0, 2, 0, 7, 8, 0, 0, 2, 2},
+    {1, 0, 0, 0, 7, 7, 1, 0, 4, 0}, {2, 6, 0, 0, 5, 5, 1, 0, 2, 0}};
+
+// n (<= 32) bits of the 128-bit block at bit `pos`, least significant first.
+__device__ __forceinline__ uint32_t bc7_bits(uint64_t lo, uint64_t hi, uint32_t pos, uint32_t n) {
+    if (n == 0) return 0u;
+    uint64_t v;
+    if (pos >= 64) v = hi >> (pos - 64);
+    else if (pos == 0) v = lo;
+    else v = (lo >> pos) | (hi << (64 - pos));
+    return (uint32_t)(v & ((1ull << n) - 1ull));
+}
+
+__device__ __forceinline__ uint32_t bc7_expand(uint32_t v, uint32_t bits) {
+    v <<= 8 - bits;
+    return v | (v >> bits);
+}
+
+// Row r (4 texels) of one BC7 block.
+__device__ void bc7_row(const uint4& q, uint32_t r, uint32_t texel[4]) {
+    const uint64_t lo = (uint64_t)q.x | ((uint64_t)q.y << 32), hi = (uint64_t)q.z | ((uint64_t)q.w << 32);
+    const uint32_t first = q.x & 0xFFu;
+    if (first == 0) {  // reserved mode
+        texel[0] = texel[1] = texel[2] = texel[3] = 0u;
+        return;
+    }
+    const uint32_t mode = (uint32_t)(__ffs((int)first) - 1);
+    const uint8_t* m = c_bc7_mode[mode];
+    const uint32_t ns = m[0], cb = m[4], ab = m[5], ib = m[8], ib2 = m[9];
+    uint32_t pos = mode + 1;
+    const uint32_t part = bc7_bits(lo, hi, pos, m[1]);
+    pos += m[1];
+    const uint32_t rot = bc7_bits(lo, hi, pos, m[2]);
+    pos += m[2];
+    const uint32_t isel = bc7_bits(lo, hi, pos, m[3]);
+    pos += m[3];
+    // endpoints: R of every endpoint, then G, then B, then alpha
+    uint32_t ep[3][2][4];
+#pragma unroll
+    for (uint32_t c = 0; c < 3; ++c)
+#pragma unroll
+        for (uint32_t s = 0; s < 3; ++s)
+#pragma unroll
+            for (uint32_t e = 0; e < 2; ++e)
+                if (s < ns) {
+                    ep[s][e][c] = bc7_bits(lo, hi, pos, cb);
+                    pos += cb;
+                }
+#pragma unroll
+    for (uint32_t s = 0; s < 3; ++s)
+#pragma unroll
+        for (uint32_t e = 0; e < 2; ++e)
+            if (s < ns) {
+                ep[s][e][3] = ab ? bc7_bits(lo, hi, pos, ab) : 255u;
+                pos += ab;
+            }
+    uint32_t cbits = cb, abits = ab;
+    if (m[6]) {
+#pragma unroll
+        for (uint32_t s = 0; s < 3; ++s)
+#pragma unroll
+            for (uint32_t e = 0; e < 2; ++e)
+                if (s < ns) {
+                    const uint32_t p = bc7_bits(lo, hi, pos++, 1);
+#pragma unroll
+                    for (uint32_t c = 0; c < 4; ++c)
+                        if (c < 3 || ab) ep[s][e][c] = (ep[s][e][c] << 1) | p;
+                }
+        cbits = cb + 1;
+        abits = ab ? ab + 1 : 0;
+    } else if (m[7]) {
+#pragma unroll
+        for (uint32_t s = 0; s < 3; ++s)
+            if (s < ns) {
+                const uint32_t p = bc7_bits(lo, hi, pos++, 1);
+#pragma unroll
+                for (uint32_t e = 0; e < 2; ++e)
+#pragma unroll
+                    for (uint32_t c = 0; c < 3; ++c) ep[s][e][c] = (ep[s][e][c] << 1) | p;
+            }
+        cbits = cb + 1;
+    }
+    const uint32_t a1 = ns == 2 ? c_bc7_a2[part] : (ns == 3 ? c_bc7_a3a[part] : 16u);
+    const uint32_t a2 = ns == 3 ? c_bc7_a3b[part] : 16u;
+    const uint32_t idx_start = pos, idx2_start = pos + 16 * ib - ns;
+#pragma unroll
+    for (uint32_t x = 0; x < 4; ++x) {
+        const uint32_t i = 4 * r + x;
+        const uint32_t s = ns == 1 ? 0u : (ns == 2 ? ((c_bc7_p2[part] >> i) & 1u) : ((c_bc7_p3[part] >> (2 * i)) & 3u));
+        // anchors before texel i each store one bit less; an anchor itself too
+        const uint32_t before = (i > 0 ? 1u : 0u) + (a1 < i ? 1u : 0u) + (a2 < i ? 1u : 0u);
+        const bool anchor = i == 0 || i == a1 || i == a2;
+        const uint32_t ix = bc7_bits(lo, hi, idx_start + i * ib - before, ib - (anchor ? 1u : 0u));
+        uint32_t ci = ix, ai = ix, cw = ib, aw = ib;
+        if (ib2) {
+            const uint32_t ix2 = bc7_bits(lo, hi, idx2_start + i * ib2 - (i > 0 ? 1u : 0u), ib2 - (i == 0 ? 1u : 0u));
+            if (isel) ci = ix2, cw = ib2;
+            else ai = ix2, aw = ib2;
+        }
+        const uint32_t wc = c_bc7_w[cw - 2][ci], wa = c_bc7_w[aw - 2][ai];
+        uint32_t px[4];
+#pragma unroll
+        for (uint32_t c = 0; c < 3; ++c) {
+            const uint32_t e0 = bc7_expand(ep[s][0][c], cbits), e1 = bc7_expand(ep[s][1][c], cbits);
+            px[c] = ((64 - wc) * e0 + wc * e1 + 32) >> 6;
+        }
+        if (ab) {
+            const uint32_t e0 = bc7_expand(ep[s][0][3], abits), e1 = bc7_expand(ep[s][1][3], abits);
+            px[3] = ((64 - wa) * e0 + wa * e1 + 32) >> 6;
+        } else {
+            px[3] = 255u;
+        }
+        if (rot) {  // swap alpha with R (1), G (2) or B (3)
+            const uint32_t t = px[3];
+            px[3] = px[rot - 1];
+            px[rot - 1] = t;
+        }
+        texel[x] = px[0] | (px[1] << 8) | (px[2] << 16) | (px[3] << 24);
+    }
+}
+
 // One block row of 4 texels from its block words.
 __device__ __forceinline__ void decode_row(const uint4& q, uint32_t format, uint32_t r, uint32_t texel[4]) {
+    if (format == VKGV_BC7) {
+        bc7_row(q, r, texel);
+        return;
+    }
     if (format == VKGV_BC4 || format == VKGV_BC5) {
         uint32_t rr[4], gg[4] = {0, 0, 0, 0};
         channel_row(q.x, q.y, r, rr);

@@ -41,7 +41,7 @@ def parse_dds(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
     info = abi.DdsInfo()
     rc = abi.load().vkgv_dds_parse(buf.ctypes.data, buf.size, C.byref(info))
     if rc != abi.OK:
-        raise abi.VkgvError(rc, "not a DDS file with BC1-BC5 data")
+        raise abi.VkgvError(rc, "not a DDS file with BC1-BC5 or BC7 data")
     blocks = buf[info.data_offset:info.data_offset + info.data_size].copy()
     return info, blocks
 
@@ -67,7 +67,7 @@ def parse_ktx2(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
     info = abi.DdsInfo()
     rc = abi.load().vkgv_ktx2_parse(buf.ctypes.data, buf.size, C.byref(info))
     if rc != abi.OK:
-        raise abi.VkgvError(rc, "not a KTX2 file with BC1-BC5 or RGBA8 data, uncompressed or Zstandard-"
+        raise abi.VkgvError(rc, "not a KTX2 file with BC1-BC5, BC7 or RGBA8 data, uncompressed or Zstandard-"
                                 "supercompressed (BasisU files are not decoded)")
     level = buf[info.data_offset:info.data_offset + info.data_size]
     if info.supercompression == 2:
