@@ -341,9 +341,13 @@ static int cull_draw(const orc_scene* s, const orc_camera* cam, const orc_pyrami
         float clip[4];
         m4v(vp, p, clip);
         all_front &= clip[3] > 0.0f;
-        float ndx = gclamp(clip[0] / clip[3], -1.0f, 1.0f);
-        float ndy = gclamp(clip[1] / clip[3], -1.0f, 1.0f);
-        float q[3] = {ndx * 0.5f + 0.5f, ndy * 0.5f + 0.5f, clip[2] / clip[3]};
+        /* clip.xy / clip.w and clip.z / clip.w (culling.h.glsl:49-52) as one correctly rounded
+         * reciprocal of w and three products: GLSL leaves a division 2.5 ulp
+         * (the perspective divide of the raster is pinned the same way) */
+        float rw = 1.0f / clip[3];
+        float ndx = gclamp(clip[0] * rw, -1.0f, 1.0f);
+        float ndy = gclamp(clip[1] * rw, -1.0f, 1.0f);
+        float q[3] = {ndx * 0.5f + 0.5f, ndy * 0.5f + 0.5f, clip[2] * rw};
         for (int k = 0; k < 3; ++k) {
             mn[k] = gmin(mn[k], q[k]);
             mx[k] = gmax(mx[k], q[k]);

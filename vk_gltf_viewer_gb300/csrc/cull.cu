@@ -225,10 +225,13 @@ __device__ __forceinline__ CullResult cull_one(const SceneArgs& S, const DeviceV
         const int a = (int)(sg & 1u), b = (int)((sg >> 1) & 1u), c = (int)(sg >> 2);
         const float clip[4] = {rows[0][a][b][c], rows[1][a][b][c], rows[2][a][b][c], rows[3][a][b][c]};
         all_front &= clip[3] > 0.0f;
-        float ndx = gclamp(fdiv(clip[0], clip[3]), -1.0f, 1.0f);
-        float ndy = gclamp(fdiv(clip[1], clip[3]), -1.0f, 1.0f);
+        // clip.xyz / clip.w as one correctly rounded reciprocal of w and three
+        // products (within GLSL's 2.5 ulp for a division)
+        const float rw = __frcp_rn(clip[3]);
+        float ndx = gclamp(fmul(clip[0], rw), -1.0f, 1.0f);
+        float ndy = gclamp(fmul(clip[1], rw), -1.0f, 1.0f);
         float qx = fadd(fmul(ndx, 0.5f), 0.5f), qy = fadd(fmul(ndy, 0.5f), 0.5f);
-        float qz = fdiv(clip[2], clip[3]);
+        float qz = fmul(clip[2], rw);
         mn0 = gmin(mn0, qx);
         mn1 = gmin(mn1, qy);
         mn2 = gmin(mn2, qz);
