@@ -1,8 +1,11 @@
-// A second, independent BC7 decoder for the BC7 parity test: the GPU's own
-// texture unit.  The blocks go into a BC7 CUDA array, one thread per texel
-// reads it through a point-sampled texture object, and the normalised texels
-// come back as RGBA8.
-//   bc7_hw <blocks.bin> <rgba.bin> <width> <height>   (width, height: multiples of 4)
+// A second, independent BC decoder for the block-compression parity tests:
+// the GPU's own texture unit.  The blocks go into a block-compressed CUDA
+// array, one thread per texel reads it through a point-sampled texture
+// object, and the normalised texels come back as RGBA8 (channels a format
+// lacks read as the texture unit returns them).
+//   bc_hw <format> <blocks.bin> <rgba.bin> <width> <height>
+// format: the library's numbering (VKGV_BC1-VKGV_BC5 = 1-5, VKGV_BC7 = 8); width,
+// height: multiples of 4.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -29,25 +32,42 @@ __global__ void k_fetch(cudaTextureObject_t tex, unsigned w, unsigned h, unsigne
     } while (0)
 
 int main(int argc, char** argv) {
-    if (argc != 5) {
-        std::fprintf(stderr, "usage: bc7_hw blocks.bin rgba.bin width height\n");
+    if (argc != 6) {
+        std::fprintf(stderr, "usage: bc_hw format blocks.bin rgba.bin width height\n");
         return 2;
     }
-    const unsigned w = (unsigned)std::atoi(argv[3]), h = (unsigned)std::atoi(argv[4]);
+    const int format = std::atoi(argv[1]);
+    const unsigned w = (unsigned)std::atoi(argv[4]), h = (unsigned)std::atoi(argv[5]);
+    cudaChannelFormatDesc desc;
+    size_t block_bytes = 16;
+    switch (format) {
+        case 1:
+            desc = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsignedBlockCompressed1);
+            block_bytes = 8;
+            break;
+        case 2: desc = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsignedBlockCompressed2); break;
+        case 3: desc = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsignedBlockCompressed3); break;
+        case 4:
+            desc = cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsignedBlockCompressed4);
+            block_bytes = 8;
+            break;
+        case 5: desc = cudaCreateChannelDesc(8, 8, 0, 0, cudaChannelFormatKindUnsignedBlockCompressed5); break;
+        case 8: desc = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsignedBlockCompressed7); break;
+        default: std::fprintf(stderr, "unknown format %d\n", format); return 2;
+    }
     if (w == 0 || h == 0 || w % 4 || h % 4 || w > 4096 || h > 4096) {
         std::fprintf(stderr, "width and height must be multiples of 4 in [4, 4096]\n");
         return 2;
     }
-    const size_t row_bytes = (size_t)(w / 4) * 16, rows = h / 4;
+    const size_t row_bytes = (size_t)(w / 4) * block_bytes, rows = h / 4;
     std::vector<unsigned char> blocks(row_bytes * rows);
-    FILE* f = std::fopen(argv[1], "rb");
+    FILE* f = std::fopen(argv[2], "rb");
     if (!f || std::fread(blocks.data(), 1, blocks.size(), f) != blocks.size()) {
-        std::fprintf(stderr, "cannot read %zu block bytes from %s\n", blocks.size(), argv[1]);
+        std::fprintf(stderr, "cannot read %zu block bytes from %s\n", blocks.size(), argv[2]);
         return 2;
     }
     std::fclose(f);
 
-    const cudaChannelFormatDesc desc = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsignedBlockCompressed7);
     cudaArray_t array = nullptr;
     CHECK(cudaMallocArray(&array, &desc, w, h));
     // a block-compressed array is copied as rows of blocks
@@ -72,9 +92,9 @@ int main(int argc, char** argv) {
     CHECK(cudaDestroyTextureObject(tex));
     CHECK(cudaFreeArray(array));
     CHECK(cudaFree(out));
-    f = std::fopen(argv[2], "wb");
+    f = std::fopen(argv[3], "wb");
     if (!f || std::fwrite(host.data(), 4, host.size(), f) != host.size()) {
-        std::fprintf(stderr, "cannot write %s\n", argv[2]);
+        std::fprintf(stderr, "cannot write %s\n", argv[3]);
         return 2;
     }
     std::fclose(f);

@@ -64,26 +64,38 @@ def test_bc7_decode_matches_oracle(renderer, size):
     assert np.array_equal(got.cpu().numpy().reshape(h, w, 4).view(np.uint32)[..., 0], exp)
 
 
-def test_bc7_oracle_matches_texture_unit(tmp_path):
-    """Pins the BC7 oracle (and its partition, anchor and weight tables) to
-    the GPU's texture unit: a BC7 CUDA array read through a point-sampled
-    texture object decodes the same random blocks of every mode."""
+@pytest.fixture(scope="module")
+def texture_unit(tmp_path_factory):
+    """Runs tests/bc_hw.cu (built here with nvcc): blocks -> RGBA8 texels
+    decoded by the GPU's texture unit from a block-compressed CUDA array."""
     import shutil
     import subprocess
     from pathlib import Path
 
+    tmp = tmp_path_factory.mktemp("bc_hw")
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    exe = tmp_path / "bc7_hw"
-    src = Path(__file__).with_name("bc7_hw.cu")
+    exe = tmp / "bc_hw"
+    src = Path(__file__).with_name("bc_hw.cu")
     subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-o", str(exe), str(src)],
                    check=True, capture_output=True, timeout=300)
+
+    def decode(fmt: int, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
+        (tmp / "blocks.bin").write_bytes(blocks.tobytes())
+        run = subprocess.run([str(exe), str(fmt), str(tmp / "blocks.bin"), str(tmp / "rgba.bin"), str(w), str(h)],
+                             capture_output=True, text=True, timeout=120)
+        assert run.returncode == 0, run.stderr
+        return np.fromfile(tmp / "rgba.bin", np.uint32).reshape(h, w)
+
+    return decode
+
+
+def test_bc7_oracle_matches_texture_unit(texture_unit):
+    """Pins the BC7 oracle (and its partition, anchor and weight tables) to
+    the GPU's texture unit: a BC7 CUDA array read through a point-sampled
+    texture object decodes the same random blocks of every mode."""
     w, h = 256, 128  # 2,048 blocks, 256 per mode
     blocks = _bc7_blocks(np.random.default_rng(2024), (w // 4) * (h // 4), reserved=False)
-    (tmp_path / "blocks.bin").write_bytes(blocks.tobytes())
-    run = subprocess.run([str(exe), str(tmp_path / "blocks.bin"), str(tmp_path / "rgba.bin"), str(w), str(h)],
-                         capture_output=True, text=True, timeout=120)
-    assert run.returncode == 0, run.stderr
-    hw = np.fromfile(tmp_path / "rgba.bin", np.uint32).reshape(h, w)
+    hw = texture_unit(abi.BC7, blocks, w, h)
     exp = ob.decode_bc(abi.BC7, blocks, w, h)
     bad = np.argwhere(hw != exp)
     if len(bad):
@@ -91,6 +103,38 @@ def test_bc7_oracle_matches_texture_unit(tmp_path):
         blk = blocks.reshape(h // 4, w // 4, 16)[by, bx]
         raise AssertionError(f"{len(bad)} texels differ; first at {tuple(bad[0])}: texture unit "
                              f"{hw[tuple(bad[0])]:08x}, oracle {exp[tuple(bad[0])]:08x}, block {blk.tobytes().hex()}")
+
+
+# Largest per-channel difference between the texture unit and the pinned
+# BC1-BC5 rounding, measured on GB300 (R, G, B, A): the formats leave the
+# interpolation's precision to the implementation and the texture unit's is
+# lower, while a layout error
+# (index or endpoint order, mode switch, alpha source) moves channels by far
+# more.
+_BC_HW_BOUND = {abi.BC1: (1, 5, 1, 0), abi.BC2: (1, 5, 1, 0), abi.BC3: (1, 5, 1, 6), abi.BC4: (7, 0, 0, 0),
+                abi.BC5: (7, 7, 0, 0)}
+
+
+@pytest.mark.parametrize("fmt", sorted(_BC_HW_BOUND))
+def test_bc1_to_bc5_layout_matches_texture_unit(texture_unit, fmt):
+    """BC1-BC5 against the texture unit's own decode of the same random
+    blocks (both endpoint orders): every channel within the measured
+    rounding bound, the channels a format lacks exactly as the oracle
+    writes them, and BC1's transparent texels (three-colour mode, code 3)
+    identical."""
+    w, h = 256, 128
+    rng = np.random.default_rng(fmt)  # the sample the bounds were measured on
+    bsize = 8 if fmt in (abi.BC1, abi.BC4) else 16
+    blocks = rng.integers(0, 256, size=(w // 4) * (h // 4) * bsize, dtype=np.uint8)
+    if fmt in (abi.BC1, abi.BC4):
+        blocks[::16] = np.minimum(blocks[::16], 127)
+    hw = texture_unit(fmt, blocks, w, h).view(np.uint8).reshape(h, w, 4).astype(np.int32)
+    exp = ob.decode_bc(fmt, blocks, w, h).view(np.uint8).reshape(h, w, 4).astype(np.int32)
+    worst = np.abs(hw - exp).reshape(-1, 4).max(axis=0)
+    assert all(int(worst[c]) <= _BC_HW_BOUND[fmt][c] for c in range(4)), (worst, _BC_HW_BOUND[fmt])
+    if fmt == abi.BC1:
+        transparent = exp[..., 3] == 0
+        assert transparent.any() and (hw[transparent] == 0).all()
 
 
 @pytest.mark.parametrize("case", range(13))
