@@ -318,7 +318,10 @@ enum TriKind : int { kDrop = 0, kFast = 1, kSlowClip = 2, kSlowSetup = 3 };
 
 // Small triangles whose clamped bbox has at most this many pixels are
 // rasterised by their own lane; larger small ones by the whole warp.
-constexpr uint32_t kLaneArea = 4;
+#ifndef VKGV_RASTER_LANE_AREA
+#define VKGV_RASTER_LANE_AREA 4
+#endif
+constexpr uint32_t kLaneArea = VKGV_RASTER_LANE_AREA;
 // Small triangles above this bbox area are queued for k_raster_big.
 #ifndef VKGV_RASTER_QUEUE_AREA
 #define VKGV_RASTER_QUEUE_AREA 16

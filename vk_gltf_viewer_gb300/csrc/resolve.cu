@@ -394,10 +394,19 @@ __global__ void __launch_bounds__(256, 6) k_resolve(SceneArgs S, const DeviceVie
 // Several views: one wave of resident CTAs whose warps take chunks of
 // kResolveChunk pixels (all views' chunks numbered in view order) from a
 // global counter, so views smaller than the largest cost no empty CTAs.
-// The warp that takes a view's first chunk finalizes the view; the last CTA
-// to finish returns the counters to zero.
+// A chunk is 64 tiles of 8 x 4 pixels (row-major over the view, one tile per
+// warp step): the pixels of a warp share more triangles and texels than a
+// 32-pixel row (256-view batch: 4.13 -> 3.89 ms).  The warp that takes a
+// view's first chunk finalizes the view; the last CTA to finish returns the
+// counters to zero.
 constexpr uint32_t kResolveChunk = 2048;
 constexpr uint32_t kResolveMaxViews = 4096;
+constexpr uint32_t kTileW = 8, kTileH = 4;  // kTileW * kTileH == 32
+
+// Tiled pixel slots of a view: whole 8 x 4 tiles, padded past its edges.
+__device__ __forceinline__ uint32_t tile_slots(uint32_t w, uint32_t h) {
+    return ((w + kTileW - 1) / kTileW) * ((h + kTileH - 1) / kTileH) * 32u;
+}
 
 template <bool TEXTURED, bool MOTION>
 __global__ void __launch_bounds__(256, 6) k_resolve_chunks(SceneArgs S, const DeviceView* __restrict__ views,
@@ -407,7 +416,7 @@ __global__ void __launch_bounds__(256, 6) k_resolve_chunks(SceneArgs S, const De
     __shared__ uint32_t s_pre[kResolveMaxViews + 1];
     if (TEXTURED) s_unorm[threadIdx.x] = fdiv((float)threadIdx.x, 255.0f);  // blockDim.x == 256
     for (uint32_t v = threadIdx.x; v < nviews; v += blockDim.x)
-        s_pre[v + 1] = (views[v].w * views[v].h + kResolveChunk - 1) / kResolveChunk;
+        s_pre[v + 1] = (tile_slots(views[v].w, views[v].h) + kResolveChunk - 1) / kResolveChunk;
     if (threadIdx.x == 0) s_pre[0] = 0;
     __syncthreads();
     if (threadIdx.x < 32) {
@@ -445,12 +454,15 @@ __global__ void __launch_bounds__(256, 6) k_resolve_chunks(SceneArgs S, const De
         }
         const DeviceView& V = views[v];
         if (item == s_pre[v] && lane == 0) finalize_view(V);
-        const uint32_t w = V.w, n = V.w * V.h, base = (item - s_pre[v]) * kResolveChunk;
+        const uint32_t w = V.w, h = V.h, base = (item - s_pre[v]) * kResolveChunk;
+        const uint32_t tiles_per_row = (w + kTileW - 1) / kTileW;
         const ResolveOut o = resolve_outputs<MOTION>(V, flags);
 #pragma unroll 1
         for (uint32_t j = lane; j < kResolveChunk; j += 32) {
-            const uint32_t p = base + j;
-            if (p < n) resolve_pixel<TEXTURED, MOTION>(S, V, s_unorm, o, w, p);
+            const uint32_t t = (base + j) >> 5;
+            const uint32_t x = (t % tiles_per_row) * kTileW + lane % kTileW;
+            const uint32_t y = (t / tiles_per_row) * kTileH + lane / kTileW;
+            if (x < w && y < h) resolve_pixel<TEXTURED, MOTION>(S, V, s_unorm, o, w, y * w + x);
         }
     }
     __syncthreads();
