@@ -544,9 +544,10 @@ def run_world(r, host, local, args, stream, peak):
 
 
 def run_texture(r, local, args, stream, peak):
-    """Base-colour texture decode: BC1 and BC3 blocks of an 8192^2 texture
-    into RGBA8 on the device (k_decode_bc), and a 2048^2 RGBA8 PNG on the
-    host (the C2 texture size)."""
+    """Base-colour texture decode: BC1, BC3 and BC7 blocks of an 8192^2
+    texture into RGBA8 on the device (k_decode_bc; the BC7 blocks take the
+    eight modes equally often), and a 2048^2 RGBA8 PNG on the host (the C2
+    texture size)."""
     import zlib
 
     import numpy as np
@@ -557,8 +558,13 @@ def run_texture(r, local, args, stream, peak):
     out = {}
     rng = np.random.default_rng(3)
     w = h = 8192
-    for name, fmt, bsize in (("bc1", abi.BC1, 8), ("bc3", abi.BC3, 16)):
-        blocks = torch.from_numpy(rng.integers(0, 256, size=(w // 4) * (h // 4) * bsize, dtype=np.uint8)).cuda(local)
+    for name, fmt, bsize in (("bc1", abi.BC1, 8), ("bc3", abi.BC3, 16), ("bc7", abi.BC7, 16)):
+        host_blocks = rng.integers(0, 256, size=((w // 4) * (h // 4), bsize), dtype=np.uint8)
+        if fmt == abi.BC7:  # mode m: the lowest set bit of the first byte is bit m
+            modes = np.arange(host_blocks.shape[0]) % 8
+            first = host_blocks[:, 0].astype(np.uint32)
+            host_blocks[:, 0] = (((first >> (modes + 1)) << (modes + 1)) | (1 << modes)).astype(np.uint8)
+        blocks = torch.from_numpy(host_blocks.reshape(-1)).cuda(local)
         rgba = torch.empty((h, w, 4), dtype=torch.uint8, device=f"cuda:{local}")
         lib = abi.load()
         for _ in range(3):

@@ -142,8 +142,33 @@ __device__ __forceinline__ uint32_t bc7_expand(uint32_t v, uint32_t bits) {
     return v | (v >> bits);
 }
 
-// Row r (4 texels) of one BC7 block.
-__device__ void bc7_row(const uint4& q, uint32_t r, uint32_t texel[4]) {
+// The BC7 tables, copied into shared memory by each CTA: lanes of a warp
+// decode blocks of different modes and partitions, and shared memory serves
+// such scattered reads in one pass where the constant cache serialises them.
+struct Bc7Tables {
+    uint32_t p3[64];
+    uint16_t p2[64];
+    uint8_t a2[64], a3a[64], a3b[64];
+    uint8_t w[3][16];
+    uint8_t mode[8][10];
+};
+
+__device__ void bc7_load_tables(Bc7Tables& t) {
+    for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) {
+        t.p3[i] = c_bc7_p3[i];
+        t.p2[i] = c_bc7_p2[i];
+        t.a2[i] = c_bc7_a2[i];
+        t.a3a[i] = c_bc7_a3a[i];
+        t.a3b[i] = c_bc7_a3b[i];
+    }
+    for (uint32_t i = threadIdx.x; i < 48; i += blockDim.x) t.w[i / 16][i % 16] = c_bc7_w[i / 16][i % 16];
+    for (uint32_t i = threadIdx.x; i < 80; i += blockDim.x) t.mode[i / 10][i % 10] = c_bc7_mode[i / 10][i % 10];
+}
+
+// Row r (4 texels) of one BC7 block.  The end points of each subset are
+// unpacked once into registers (RGBA8 after the p-bits and the bit
+// replication), then every texel selects its subset's pair.
+__device__ void bc7_row(const Bc7Tables& T, const uint4& q, uint32_t r, uint32_t texel[4]) {
     const uint64_t lo = (uint64_t)q.x | ((uint64_t)q.y << 32), hi = (uint64_t)q.z | ((uint64_t)q.w << 32);
     const uint32_t first = q.x & 0xFFu;
     if (first == 0) {  // reserved mode
@@ -151,7 +176,7 @@ __device__ void bc7_row(const uint4& q, uint32_t r, uint32_t texel[4]) {
         return;
     }
     const uint32_t mode = (uint32_t)(__ffs((int)first) - 1);
-    const uint8_t* m = c_bc7_mode[mode];
+    const uint8_t* m = T.mode[mode];
     const uint32_t ns = m[0], cb = m[4], ab = m[5], ib = m[8], ib2 = m[9];
     uint32_t pos = mode + 1;
     const uint32_t part = bc7_bits(lo, hi, pos, m[1]);
@@ -160,59 +185,45 @@ __device__ void bc7_row(const uint4& q, uint32_t r, uint32_t texel[4]) {
     pos += m[2];
     const uint32_t isel = bc7_bits(lo, hi, pos, m[3]);
     pos += m[3];
-    // endpoints: R of every endpoint, then G, then B, then alpha
-    uint32_t ep[3][2][4];
+    // Stored fields in order: R of every end point (subset-major), then G,
+    // B, then alpha, then the p-bits.  End point k = 2 s + e of channel c
+    // starts at c_base[c] + k * bits.
+    const uint32_t nep = 2 * ns;
+    const uint32_t alpha_base = pos + 3 * nep * cb, pbit_base = alpha_base + nep * ab;
+    const uint32_t cbits = cb + ((m[6] | m[7]) ? 1u : 0u);
+    const uint32_t abits = ab ? ab + m[6] : 0u;
+    uint32_t epk[6];  // packed RGBA8 of end point k
 #pragma unroll
-    for (uint32_t c = 0; c < 3; ++c)
+    for (uint32_t k = 0; k < 6; ++k) {
+        epk[k] = 0u;
+        if (k < nep) {
+            // a p-bit per end point (modes 0, 3, 6, 7) or per subset (mode 1)
+            const uint32_t pb = m[6] ? bc7_bits(lo, hi, pbit_base + k, 1) : (m[7] ? bc7_bits(lo, hi, pbit_base + k / 2, 1) : 0u);
+            uint32_t v = 0u;
 #pragma unroll
-        for (uint32_t s = 0; s < 3; ++s)
-#pragma unroll
-            for (uint32_t e = 0; e < 2; ++e)
-                if (s < ns) {
-                    ep[s][e][c] = bc7_bits(lo, hi, pos, cb);
-                    pos += cb;
-                }
-#pragma unroll
-    for (uint32_t s = 0; s < 3; ++s)
-#pragma unroll
-        for (uint32_t e = 0; e < 2; ++e)
-            if (s < ns) {
-                ep[s][e][3] = ab ? bc7_bits(lo, hi, pos, ab) : 255u;
-                pos += ab;
+            for (uint32_t c = 0; c < 3; ++c) {
+                uint32_t x = bc7_bits(lo, hi, pos + (c * nep + k) * cb, cb);
+                if (m[6] | m[7]) x = (x << 1) | pb;
+                v |= bc7_expand(x, cbits) << (8 * c);
             }
-    uint32_t cbits = cb, abits = ab;
-    if (m[6]) {
-#pragma unroll
-        for (uint32_t s = 0; s < 3; ++s)
-#pragma unroll
-            for (uint32_t e = 0; e < 2; ++e)
-                if (s < ns) {
-                    const uint32_t p = bc7_bits(lo, hi, pos++, 1);
-#pragma unroll
-                    for (uint32_t c = 0; c < 4; ++c)
-                        if (c < 3 || ab) ep[s][e][c] = (ep[s][e][c] << 1) | p;
-                }
-        cbits = cb + 1;
-        abits = ab ? ab + 1 : 0;
-    } else if (m[7]) {
-#pragma unroll
-        for (uint32_t s = 0; s < 3; ++s)
-            if (s < ns) {
-                const uint32_t p = bc7_bits(lo, hi, pos++, 1);
-#pragma unroll
-                for (uint32_t e = 0; e < 2; ++e)
-#pragma unroll
-                    for (uint32_t c = 0; c < 3; ++c) ep[s][e][c] = (ep[s][e][c] << 1) | p;
+            uint32_t a = 255u;
+            if (ab) {
+                a = bc7_bits(lo, hi, alpha_base + k * ab, ab);
+                if (m[6]) a = (a << 1) | pb;
+                a = bc7_expand(a, abits);
             }
-        cbits = cb + 1;
+            epk[k] = v | (a << 24);
+        }
     }
-    const uint32_t a1 = ns == 2 ? c_bc7_a2[part] : (ns == 3 ? c_bc7_a3a[part] : 16u);
-    const uint32_t a2 = ns == 3 ? c_bc7_a3b[part] : 16u;
-    const uint32_t idx_start = pos, idx2_start = pos + 16 * ib - ns;
+    const uint32_t a1 = ns == 2 ? T.a2[part] : (ns == 3 ? T.a3a[part] : 16u);
+    const uint32_t a2 = ns == 3 ? T.a3b[part] : 16u;
+    const uint32_t idx_start = pbit_base + (m[6] ? nep : (m[7] ? ns : 0u));
+    const uint32_t idx2_start = idx_start + 16 * ib - ns;
+    const uint32_t pmask = ns == 2 ? T.p2[part] : (ns == 3 ? T.p3[part] : 0u);
 #pragma unroll
     for (uint32_t x = 0; x < 4; ++x) {
         const uint32_t i = 4 * r + x;
-        const uint32_t s = ns == 1 ? 0u : (ns == 2 ? ((c_bc7_p2[part] >> i) & 1u) : ((c_bc7_p3[part] >> (2 * i)) & 3u));
+        const uint32_t s = ns == 1 ? 0u : (ns == 2 ? ((pmask >> i) & 1u) : ((pmask >> (2 * i)) & 3u));
         // anchors before texel i each store one bit less; an anchor itself too
         const uint32_t before = (i > 0 ? 1u : 0u) + (a1 < i ? 1u : 0u) + (a2 < i ? 1u : 0u);
         const bool anchor = i == 0 || i == a1 || i == a2;
@@ -223,18 +234,14 @@ __device__ void bc7_row(const uint4& q, uint32_t r, uint32_t texel[4]) {
             if (isel) ci = ix2, cw = ib2;
             else ai = ix2, aw = ib2;
         }
-        const uint32_t wc = c_bc7_w[cw - 2][ci], wa = c_bc7_w[aw - 2][ai];
+        const uint32_t wc = T.w[cw - 2][ci], wa = T.w[aw - 2][ai];
+        const uint32_t e0 = s == 0 ? epk[0] : (s == 1 ? epk[2] : epk[4]);
+        const uint32_t e1 = s == 0 ? epk[1] : (s == 1 ? epk[3] : epk[5]);
         uint32_t px[4];
 #pragma unroll
-        for (uint32_t c = 0; c < 3; ++c) {
-            const uint32_t e0 = bc7_expand(ep[s][0][c], cbits), e1 = bc7_expand(ep[s][1][c], cbits);
-            px[c] = ((64 - wc) * e0 + wc * e1 + 32) >> 6;
-        }
-        if (ab) {
-            const uint32_t e0 = bc7_expand(ep[s][0][3], abits), e1 = bc7_expand(ep[s][1][3], abits);
-            px[3] = ((64 - wa) * e0 + wa * e1 + 32) >> 6;
-        } else {
-            px[3] = 255u;
+        for (uint32_t c = 0; c < 4; ++c) {
+            const uint32_t w8 = c < 3 ? wc : wa;
+            px[c] = ((64 - w8) * ((e0 >> (8 * c)) & 255u) + w8 * ((e1 >> (8 * c)) & 255u) + 32) >> 6;
         }
         if (rot) {  // swap alpha with R (1), G (2) or B (3)
             const uint32_t t = px[3];
@@ -247,10 +254,6 @@ __device__ void bc7_row(const uint4& q, uint32_t r, uint32_t texel[4]) {
 
 // One block row of 4 texels from its block words.
 __device__ __forceinline__ void decode_row(const uint4& q, uint32_t format, uint32_t r, uint32_t texel[4]) {
-    if (format == VKGV_BC7) {
-        bc7_row(q, r, texel);
-        return;
-    }
     if (format == VKGV_BC4 || format == VKGV_BC5) {
         uint32_t rr[4], gg[4] = {0, 0, 0, 0};
         channel_row(q.x, q.y, r, rr);
@@ -312,6 +315,42 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc(const uint8_t* 
         if (y >= h) break;
         uint32_t texel[4];
         decode_row(q[k], format, r, texel);
+        uint32_t* dst = rgba + (size_t)y * w + (size_t)bx * 4;
+        if (bx * 4 + 4 <= w && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+            __stcs(reinterpret_cast<uint4*>(dst), make_uint4(texel[0], texel[1], texel[2], texel[3]));
+        } else {
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+                if (bx * 4 + x < w) __stcs(dst + x, texel[x]);
+        }
+    }
+}
+
+// BC7 with the lane layout of k_decode_bc (four lanes per block, one row
+// each) and the tables in shared memory.
+__global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc7(const uint8_t* __restrict__ blocks, uint32_t w,
+                                                                  uint32_t h, uint32_t* __restrict__ rgba) {
+    __shared__ Bc7Tables T;
+    bc7_load_tables(T);
+    pdl_begin();
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t r = lane & 3u;
+    const uint32_t bx = (blockIdx.x * kDecodeWarps + warp) * 8 + (lane >> 2);
+    const uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
+    if (bx >= bw) return;
+    uint4 q[kDecodeDepth];
+#pragma unroll
+    for (int k = 0; k < kDecodeDepth; ++k) {
+        const uint32_t by = blockIdx.y * kDecodeDepth + k;
+        q[k] = by < bh ? __ldg(reinterpret_cast<const uint4*>(blocks) + ((size_t)by * bw + bx)) : make_uint4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int k = 0; k < kDecodeDepth; ++k) {
+        const uint32_t y = (blockIdx.y * kDecodeDepth + k) * 4 + r;
+        if (y >= h) break;
+        uint32_t texel[4];
+        bc7_row(T, q[k], r, texel);
         uint32_t* dst = rgba + (size_t)y * w + (size_t)bx * 4;
         if (bx * 4 + 4 <= w && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
             __stcs(reinterpret_cast<uint4*>(dst), make_uint4(texel[0], texel[1], texel[2], texel[3]));
@@ -430,8 +469,11 @@ void launch_decode_bc(const uint8_t* blocks, uint32_t format, uint32_t w, uint32
                       cudaStream_t stream) {
     const uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
     const uint32_t per_cta = 8 * kDecodeWarps;
-    launch_pdl(k_decode_bc, dim3((bw + per_cta - 1) / per_cta, (bh + kDecodeDepth - 1) / kDecodeDepth),
-               dim3(kDecodeWarps * 32), 0, stream, blocks, format, w, h, rgba);
+    const dim3 grid((bw + per_cta - 1) / per_cta, (bh + kDecodeDepth - 1) / kDecodeDepth);
+    if (format == VKGV_BC7)
+        launch_pdl(k_decode_bc7, grid, dim3(kDecodeWarps * 32), 0, stream, blocks, w, h, rgba);
+    else
+        launch_pdl(k_decode_bc, grid, dim3(kDecodeWarps * 32), 0, stream, blocks, format, w, h, rgba);
 }
 
 }  // namespace vkgv
