@@ -164,6 +164,22 @@ def test_ktx2_through_load_image(renderer):
         assert np.array_equal(got.view(np.uint32)[..., 0], ob.decode_bc(fmt, blocks, 37, 22))
 
 
+def test_bc7_through_load_image(renderer):
+    """BC7 in a DDS (DX10 header, DXGI 98 / 99) and in a KTX2 (vkFormat 145 /
+    146) decodes through load_image to the oracle's texels."""
+    from test_texture_decode import _dds, _ktx2
+
+    rng = np.random.default_rng(77)
+    blocks = _bc7_blocks(rng, 10 * 6)
+    exp = ob.decode_bc(abi.BC7, blocks, 37, 22)
+    for data, kind in ((_dds(b"DX10", 37, 22, blocks.tobytes(), dxgi=98), abi.IMAGE_DDS),
+                       (_dds(b"DX10", 37, 22, blocks.tobytes(), dxgi=99), abi.IMAGE_DDS),
+                       (_ktx2(145, 37, 22, blocks.tobytes()), abi.IMAGE_KTX2),
+                       (_ktx2(146, 37, 22, blocks.tobytes()), abi.IMAGE_KTX2)):
+        got = texture.load_image(data, kind, renderer)
+        assert np.array_equal(got.view(np.uint32)[..., 0], exp)
+
+
 def test_zstd_ktx2_through_load_image(renderer):
     """Zstandard-supercompressed KTX2 levels (committed libzstd frames of
     block data) inflate on the host and decode on the device to the oracle's

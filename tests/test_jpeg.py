@@ -131,6 +131,10 @@ def test_errors(built):
     huge = bytearray(data)  # a 16000 x 16000 frame over a few hundred bytes of data
     huge[sof + 5:sof + 9] = bytes([0x3E, 0x80, 0x3E, 0x80])
     cases["too short"] = bytes(huge)
+    # a DHT with three 1-bit codes: refused before its third code is placed
+    # (it would index past the 9-bit lookahead table)
+    dht = bytes([0xFF, 0xC4, 0x00, 2 + 17 + 3, 0x00, 3] + [0] * 15 + [1, 2, 3])
+    cases["over-subscribed"] = data[:2] + dht + data[2:]
     for match, bad in cases.items():
         with pytest.raises(abi.VkgvError, match=match):
             texture.Jpeg(bad)

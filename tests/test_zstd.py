@@ -136,6 +136,21 @@ def test_mutated_frames_return_a_status(built, tmp_path):
     assert abi.INVALID_ARG in codes
 
 
+def test_four_stream_literals_need_six_bytes(built):
+    """Four Huffman streams of literals split (n + 3) / 4 to each of the
+    first three; a section of 5 literals would give them 6 and the fourth
+    a negative count: refused before any stream is decoded."""
+    lit_hdr = (2 | (1 << 2) | (5 << 4) | (12 << 14)).to_bytes(3, "little")  # Huffman, 4 streams, 5 literals
+    tree = bytes([0x80, 0x10])                       # two symbols of weight 1: 1-bit codes
+    jump = (1).to_bytes(2, "little") * 3              # streams of one byte each
+    streams = bytes([0x04]) * 4                      # two 1-bit codes, then the end marker
+    block = lit_hdr + tree + jump + streams + bytes([0])  # no sequences
+    frame = (bytes.fromhex("28b52ffd") + bytes([0x20, 5])
+             + (1 | (2 << 1) | (len(block) << 3)).to_bytes(3, "little") + block)
+    rc, _ = _decode(frame, 64)
+    assert rc == abi.INVALID_ARG
+
+
 def test_ktx2_zstd_level(built):
     """A KTX2 file whose level is Zstandard-supercompressed (scheme 2) parses
     to the inflated BC1 blocks; a wrong uncompressed length or a corrupt

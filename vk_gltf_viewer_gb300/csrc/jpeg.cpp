@@ -80,14 +80,17 @@ struct Huffman {
         for (int len = 1; len <= 16; ++len) {
             first_code[len] = code;
             first_index[len] = k;
-            for (int i = 0; i < counts[len - 1]; ++i, ++k, ++code)
+            for (int i = 0; i < counts[len - 1]; ++i, ++k, ++code) {
+                // an over-subscribed length is refused before its code can
+                // index past the lookahead table
+                if (code >= (1 << len)) bad("over-subscribed Huffman table");
                 if (len <= 9)
                     for (int f = code << (9 - len), e = (code + 1) << (9 - len); f < e; ++f) {
                         fast_len[f] = uint8_t(len);
                         fast_sym[f] = vals[k];
                     }
+            }
             last_code[len] = code - 1;  // below first_code when the length is unused
-            if (code > (1 << len)) bad("over-subscribed Huffman table");
             code <<= 1;
         }
         defined = true;

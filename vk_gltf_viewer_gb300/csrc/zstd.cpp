@@ -369,6 +369,7 @@ size_t seq_table(int mode, const uint8_t* p, size_t n, const std::vector<int16_t
 }
 
 void put(FrameState& f, const uint8_t* src, size_t n) {
+    if (n == 0) return;
     if (n > f.cap - f.pos) throw Fail{VKGV_LIMIT_EXCEEDED};
     std::memcpy(f.out + f.pos, src, n);
     f.pos += n;
@@ -442,12 +443,14 @@ void compressed_block(FrameState& f, const uint8_t* p, size_t n) {
             const size_t s1 = rd_le(q, 2), s2 = rd_le(q + 2, 2), s3 = rd_le(q + 4, 2);
             if (6 + s1 + s2 + s3 > qn) bad();
             const size_t s4 = qn - 6 - s1 - s2 - s3;
+            // the first three streams hold (regen + 3) / 4 literals each, the
+            // fourth the rest, which must not be negative
             const size_t per = (regen + 3) / 4;
+            if (3 * per > regen) bad();
             const uint8_t* sp = q + 6;
             const size_t sizes[4] = {s1, s2, s3, s4};
             for (int k = 0; k < 4; ++k) {
                 const size_t cnt = k < 3 ? per : regen - 3 * per;
-                if (k == 3 && 3 * per > regen) bad();
                 huff_stream(sp, sizes[k], f.huff, lit.data() + k * per, cnt);
                 sp += sizes[k];
             }
