@@ -91,9 +91,89 @@ __device__ void raster_rect(const int32_t* X, const int32_t* Y, const int32_t* b
     }
 }
 
-// Triangle setup on snapped vertices and dispatch to inline or binned raster.
+// A large triangle of the slow instance, set up and waiting for its binned
+// rectangles to be queued: the lanes of a warp collect their jobs while they
+// diverge over clipping and setup, then queue all of them with one atomic
+// per warp.  (One atomic per triangle on the shared queue counter
+// serialised: 23,700 slow triangles in one single-view frame.)
+struct BinJob {
+    int32_t x[3], y[3];       // oriented snapped vertices, 28.8
+    float z0, pa, pb;         // depth plane
+    uint32_t id;
+    int32_t px0, py0, px1, py1;  // clamped pixel bounding box
+    uint32_t n;               // rectangles of c.chunk x c.chunk pixels
+};
+// A clipped triangle fans into at most 10 triangles.
+constexpr uint32_t kMaxJobs = 10;
+struct JobList {
+    BinJob job[kMaxJobs];
+    uint32_t count;
+};
+
+// The rectangles of one job, queued at c.big[at, at + n) (past the queue's
+// capacity they are drawn in place and the overflow is reported).
+__device__ void queue_job(const BinJob& j, uint32_t at, const RasterCtx& c) {
+    const int64_t cs = c.chunk;
+    const int64_t ncx = ((int64_t)(j.px1 - j.px0 + 1) + cs - 1) / cs;
+    for (uint32_t i = 0; i < j.n; ++i, ++at) {
+        const int64_t cx = i % ncx, cy = i / ncx;
+        const int qx0 = (int)(j.px0 + cx * cs), qy0 = (int)(j.py0 + cy * cs);
+        const int qx1 = (int)min((int64_t)j.px1, j.px0 + (cx + 1) * cs - 1);
+        const int qy1 = (int)min((int64_t)j.py1, j.py0 + (cy + 1) * cs - 1);
+        if (at < c.big_cap) {
+            BigTri t;
+            t.x[0] = j.x[0], t.x[1] = j.x[1], t.x[2] = j.x[2];
+            t.y[0] = j.y[0], t.y[1] = j.y[1], t.y[2] = j.y[2];
+            t.z0 = j.z0, t.pa = j.pa, t.pb = j.pb;
+            t.id = j.id;
+            t.px0 = (uint16_t)qx0, t.py0 = (uint16_t)qy0, t.px1 = (uint16_t)qx1, t.py1 = (uint16_t)qy1;
+            t.view = c.view;
+            t._pad = 0;
+            c.big[at] = t;
+        } else {
+            report(c.status, kStatusQueueOverflow, at);
+            int32_t bias[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int32_t dx = j.x[(k + 1) % 3] - j.x[k], dy = j.y[(k + 1) % 3] - j.y[k];
+                bias[k] = (dy < 0 || (dy == 0 && dx > 0)) ? 0 : 1;
+            }
+            raster_rect(j.x, j.y, bias, j.z0, j.pa, j.pb, j.id, qx0, qy0, qx1, qy1, c.depth, c.w);
+        }
+    }
+}
+
+// Queues the jobs of every lane (the whole warp, converged): an exclusive
+// scan of the lanes' rectangle counts, one atomic on the queue counter.
+__device__ void flush_jobs(JobList& jobs, const RasterCtx& c, int lane) {
+    uint32_t mine = 0;
+    for (uint32_t i = 0; i < jobs.count; ++i) mine += jobs.job[i].n;
+    uint32_t incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) {
+        jobs.count = 0;
+        return;
+    }
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(c.big_count, total);
+    base = __shfl_sync(0xffffffffu, base, 0) + (incl - mine);
+    for (uint32_t i = 0; i < jobs.count; ++i) {
+        queue_job(jobs.job[i], base, c);
+        base += jobs.job[i].n;
+    }
+    jobs.count = 0;
+}
+
+// Triangle setup on snapped vertices and dispatch to inline or binned
+// raster; a triangle to bin becomes a job in `jobs` (queued directly when
+// the list is full).
 __device__ __noinline__ void setup_and_raster(int32_t X0, int32_t Y0, float Z0, int32_t X1, int32_t Y1, float Z1, int32_t X2,
-                                 int32_t Y2, float Z2, uint32_t id, const RasterCtx& c) {
+                                 int32_t Y2, float Z2, uint32_t id, const RasterCtx& c, JobList& jobs) {
     int64_t A = (int64_t)(X1 - X0) * (Y2 - Y0) - (int64_t)(Y1 - Y0) * (X2 - X0);
     if (A == 0) return;
     if (A < 0) {
@@ -135,26 +215,17 @@ __device__ __noinline__ void setup_and_raster(int32_t X0, int32_t Y0, float Z0, 
     }
     const int64_t cs = c.chunk;
     const int64_t ncx = (bw + cs - 1) / cs, ncy = (bh + cs - 1) / cs;
-    const uint32_t n = (uint32_t)(ncx * ncy);
-    const uint32_t base = atomicAdd(c.big_count, n);
-    for (uint32_t i = 0; i < n; ++i) {
-        const int64_t cx = i % ncx, cy = i / ncx;
-        const int qx0 = (int)(px0 + cx * cs), qy0 = (int)(py0 + cy * cs);
-        const int qx1 = (int)min(px1, px0 + (cx + 1) * cs - 1), qy1 = (int)min(py1, py0 + (cy + 1) * cs - 1);
-        if (base + i < c.big_cap) {
-            BigTri t;
-            t.x[0] = X0, t.x[1] = X1, t.x[2] = X2;
-            t.y[0] = Y0, t.y[1] = Y1, t.y[2] = Y2;
-            t.z0 = Z0, t.pa = pa, t.pb = pb;
-            t.id = id;
-            t.px0 = (uint16_t)qx0, t.py0 = (uint16_t)qy0, t.px1 = (uint16_t)qx1, t.py1 = (uint16_t)qy1;
-            t.view = c.view;
-            t._pad = 0;
-            c.big[base + i] = t;
-        } else {
-            report(c.status, kStatusQueueOverflow, base + i);
-            raster_rect(X, Y, bias, Z0, pa, pb, id, qx0, qy0, qx1, qy1, c.depth, c.w);
-        }
+    BinJob j;
+    j.x[0] = X0, j.x[1] = X1, j.x[2] = X2;
+    j.y[0] = Y0, j.y[1] = Y1, j.y[2] = Y2;
+    j.z0 = Z0, j.pa = pa, j.pb = pb;
+    j.id = id;
+    j.px0 = (int32_t)px0, j.py0 = (int32_t)py0, j.px1 = (int32_t)px1, j.py1 = (int32_t)py1;
+    j.n = (uint32_t)(ncx * ncy);
+    if (jobs.count < kMaxJobs) {
+        jobs.job[jobs.count++] = j;
+    } else {
+        queue_job(j, atomicAdd(c.big_count, j.n), c);
     }
 }
 
@@ -202,7 +273,7 @@ __device__ int clip_poly(const float4* in, int n, float4* out, int plane) {
 
 // Slow path: homogeneous clipping (near/far, then guard band) and a fan.
 __device__ __noinline__ void raster_clipped(float4 v0, float4 v1, float4 v2, bool clipz, uint32_t id,
-                                            const RasterCtx& c) {
+                                            const RasterCtx& c, JobList& jobs) {
     float4 bufa[12], bufb[12];
     bufa[0] = v0, bufa[1] = v1, bufa[2] = v2;
     float4* cur = bufa;
@@ -232,7 +303,7 @@ __device__ __noinline__ void raster_clipped(float4 v0, float4 v1, float4 v2, boo
     for (int k = 0; k < n; ++k)
         if (!snap(cur[k], c, X[k], Y[k], Z[k])) return;
     for (int k = 1; k + 1 < n; ++k)
-        setup_and_raster(X[0], Y[0], Z[0], X[k], Y[k], Z[k], X[k + 1], Y[k + 1], Z[k + 1], id, c);
+        setup_and_raster(X[0], Y[0], Z[0], X[k], Y[k], Z[k], X[k + 1], Y[k + 1], Z[k + 1], id, c, jobs);
 }
 
 // Views per raster launch (the launcher splits larger batches).
@@ -809,19 +880,29 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
             __syncwarp();
             bool any_slow = false;
             if constexpr (SLOW) {
-                // Deferred meshlet: only the triangles the fast instance skipped.
-                for (uint32_t t = lane; t < tc; t += 32) {
-                    TriClass k;
-                    const uint32_t i0 = sidx8[3 * t], i1 = sidx8[3 * t + 1], i2 = sidx8[3 * t + 2];
-                    const int kind = classify<true>(i0, i1, i2, vc, svtx, clip, double_sided, tdet, c, d, k);
-                    if (kind == kSlowClip) {
-                        raster_clipped(clip[i0], clip[i1], clip[i2],
-                                       (((uint32_t)k.q0.w | (uint32_t)k.q1.w | (uint32_t)k.q2.w) & (OC_ZLO | OC_ZHI)) != 0,
-                                       (d << 7) | t, c);
-                    } else if (kind == kSlowSetup) {
-                        setup_and_raster(k.q0.x, k.q0.y, __int_as_float(k.q0.z), k.q1.x, k.q1.y, __int_as_float(k.q1.z),
-                                         k.q2.x, k.q2.y, __int_as_float(k.q2.z), (d << 7) | t, c);
+                // Deferred meshlet: only the triangles the fast instance
+                // skipped, 32 per round; the round's binned triangles are
+                // queued together when the warp has reconverged.
+                JobList jobs;
+                jobs.count = 0;
+                for (uint32_t tb = 0; tb < tc; tb += 32) {
+                    const uint32_t t = tb + (uint32_t)lane;
+                    if (t < tc) {
+                        TriClass k;
+                        const uint32_t i0 = sidx8[3 * t], i1 = sidx8[3 * t + 1], i2 = sidx8[3 * t + 2];
+                        const int kind = classify<true>(i0, i1, i2, vc, svtx, clip, double_sided, tdet, c, d, k);
+                        if (kind == kSlowClip) {
+                            raster_clipped(clip[i0], clip[i1], clip[i2],
+                                           (((uint32_t)k.q0.w | (uint32_t)k.q1.w | (uint32_t)k.q2.w) & (OC_ZLO | OC_ZHI)) != 0,
+                                           (d << 7) | t, c, jobs);
+                        } else if (kind == kSlowSetup) {
+                            setup_and_raster(k.q0.x, k.q0.y, __int_as_float(k.q0.z), k.q1.x, k.q1.y,
+                                             __int_as_float(k.q1.z), k.q2.x, k.q2.y, __int_as_float(k.q2.z),
+                                             (d << 7) | t, c, jobs);
+                        }
                     }
+                    __syncwarp();
+                    flush_jobs(jobs, c, lane);
                 }
             } else {
                 // Pre-filter 32 triangles per round (outcodes, snap, a pixel
