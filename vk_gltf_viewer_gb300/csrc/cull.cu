@@ -424,10 +424,16 @@ void launch_cull(const SceneArgs& S, const DeviceView* views, uint32_t nviews, u
                  uint32_t* status, uint32_t sm_count, cudaStream_t stream) {
     const uint32_t threads = 256;
     const uint32_t want = (S.draw_count + threads - 1) / threads;
-    // Pass 1 covers every draw once.  Pass-2 candidate counts live on the
-    // device, so its grid fills the GPU and strides over the reject list.
-    const uint32_t fill = (sm_count * 8 + nviews - 1) / nviews;
-    uint32_t per_view = pass == 1 ? want : (want < fill ? want : fill);
+    // Both passes stride over their candidates (pass 1: every draw; pass 2:
+    // the reject list, whose length lives on the device) with at most about
+    // sm_count * f CTAs over all views: a CTA's prologue (frustum planes,
+    // occlusion view-projection, the raster eye from an inverse, in one
+    // thread before a barrier) is then paid once per many draws.  256-view
+    // batch: pass 1 7.46 -> 5.96 ms, pass 2 1.40 -> 1.19 ms (f = 8 stays
+    // best for a single view's short pass-2 list).
+    const uint32_t f = pass == 1 ? 128u : (nviews == 1 ? 8u : 40u);
+    const uint32_t fill = (sm_count * f + nviews - 1) / nviews;
+    uint32_t per_view = want < fill ? want : fill;
     if (per_view > 65535u) per_view = 65535u;
     if (per_view == 0) per_view = 1;
     dim3 grid(per_view, nviews);
