@@ -108,32 +108,37 @@ struct FwdBits {
 // Backward reader (Huffman streams, FSE-coded data): the stream is read from
 // its last bit towards its first; the last byte's highest set bit marks the
 // end of the padding.  Reads past the first bit return zeros and flag an
-// overflow.
+// overflow.  A read of k bits takes the k bits below the read position as
+// one little-endian window (the first bit read is the value's highest).
 struct BackBits {
     const uint8_t* p;
+    size_t n;
     int64_t left;  // bits not yet read
-    BackBits(const uint8_t* data, size_t n) : p(data) {
-        if (n == 0 || data[n - 1] == 0) bad();
-        left = int64_t(n - 1) * 8 + highbit(data[n - 1]);
+    BackBits(const uint8_t* data, size_t size) : p(data), n(size) {
+        if (size == 0 || data[size - 1] == 0) bad();
+        left = int64_t(size - 1) * 8 + highbit(data[size - 1]);
+    }
+    // bits [pos, pos + k) of the stream (k <= 32), zeros below bit 0
+    uint32_t window(int64_t pos, int k) const {
+        if (k == 0) return 0u;
+        if (pos < 0) {  // past the first bit: the missing low bits are zeros
+            if (pos + k <= 0) return 0u;
+            return window(0, int(pos + k)) << int(-pos);
+        }
+        const size_t byte = size_t(pos >> 3);
+        uint64_t v = 0;
+        if (byte + 8 <= n) {
+            std::memcpy(&v, p + byte, 8);  // little-endian hosts (x86-64, aarch64)
+        } else {
+            for (size_t i = 0; byte + i < n; ++i) v |= uint64_t(p[byte + i]) << (8 * i);
+        }
+        return uint32_t((v >> (pos & 7)) & ((uint64_t(1) << k) - 1u));
     }
     uint32_t get(int k) {
-        uint32_t v = 0;
-        for (int i = 0; i < k; ++i) {
-            --left;
-            const uint32_t bit = left >= 0 ? (p[left >> 3] >> (left & 7)) & 1u : 0u;
-            v = (v << 1) | bit;
-        }
-        return v;
+        left -= k;
+        return window(left, k);
     }
-    uint32_t peek(int k) const {
-        uint32_t v = 0;
-        int64_t l = left;
-        for (int i = 0; i < k; ++i) {
-            --l;
-            v = (v << 1) | (l >= 0 ? (p[l >> 3] >> (l & 7)) & 1u : 0u);
-        }
-        return v;
-    }
+    uint32_t peek(int k) const { return window(left - k, k); }
     bool overflow() const { return left < 0; }
 };
 
@@ -314,7 +319,7 @@ void huff_stream(const uint8_t* p, size_t n, const Huff& h, uint8_t* out, size_t
     for (size_t i = 0; i < count; ++i) {
         const uint32_t k = b.peek(h.max_bits);
         out[i] = h.sym[k];
-        b.get(h.len[k]);
+        b.left -= h.len[k];
     }
     if (b.left != 0) bad();  // a stream ends exactly on its first bit
 }
@@ -520,7 +525,13 @@ void compressed_block(FrameState& f, const uint8_t* p, size_t n) {
             if (ml > f.cap - f.pos) throw Fail{VKGV_LIMIT_EXCEEDED};
             uint8_t* d = f.out + f.pos;
             const uint8_t* src = d - off;
-            for (size_t k = 0; k < ml; ++k) d[k] = src[k];
+            if (off >= 16) {  // 16-byte pieces never overlap their own source
+                size_t k = 0;
+                for (; k + 16 <= ml; k += 16) std::memcpy(d + k, src + k, 16);
+                for (; k < ml; ++k) d[k] = src[k];
+            } else {
+                for (size_t k = 0; k < ml; ++k) d[k] = src[k];
+            }
             f.pos += ml;
             if (i + 1 < nseq) {  // state updates: literal length, match length, offset
                 sll = cll.base + b.get(cll.bits);
