@@ -43,6 +43,20 @@ public:
         cnt_ -= k;
         return v;
     }
+    // The next k bits without taking them; past the end of the stream the
+    // missing bits read as zeros (taking them then fails).
+    uint32_t peek(int k) {
+        while (cnt_ <= 56 && pos_ < n_) {
+            acc_ |= uint64_t(p_[pos_++]) << cnt_;
+            cnt_ += 8;
+        }
+        return uint32_t(acc_ & ((1ull << k) - 1));
+    }
+    void consume(int k) {
+        if (k > cnt_) fail("DEFLATE stream is truncated");
+        acc_ >>= k;
+        cnt_ -= k;
+    }
     void align() {
         acc_ >>= cnt_ & 7;
         cnt_ -= cnt_ & 7;
@@ -64,15 +78,19 @@ private:
 };
 
 // Canonical Huffman code (RFC 1951 3.2.2): codes of each length are
-// consecutive, starting at next_code[len] as the RFC assigns them.  Decoding
-// reads one bit at a time (codes are stored most-significant bit first) and,
-// at each length, checks whether the code read so far falls in that length's
-// range.
+// consecutive, starting at next_code[len] as the RFC assigns them.  Codes of
+// at most kFastBits bits decode with one lookup of the next kFastBits stream
+// bits (the code is stored most-significant bit first, so the table is
+// indexed by its bit-reversed form, every value of the bits after it filled
+// in); longer codes are read one bit at a time, checking at each length
+// whether the code read so far falls in that length's range.
+constexpr int kFastBits = 10;
 struct Huffman {
     int32_t first[16] = {};   // first code of each length
     int32_t count[16] = {};   // codes of each length
     int32_t offset[16] = {};  // index in `symbol` of each length's first code
     std::vector<uint16_t> symbol;  // symbols ordered by (length, value)
+    uint16_t fast[1 << kFastBits] = {};  // symbol << 4 | length, 0 = a longer code
 
     void build(const uint8_t* lengths, int n) {
         std::memset(count, 0, sizeof(count));
@@ -91,9 +109,23 @@ struct Huffman {
         std::vector<int32_t> fill(offset, offset + 16);
         for (int i = 0; i < n; ++i)
             if (lengths[i]) symbol[size_t(fill[lengths[i]]++)] = uint16_t(i);
+        std::memset(fast, 0, sizeof(fast));
+        for (int len = 1; len <= kFastBits; ++len)
+            for (int32_t k = 0; k < count[len]; ++k) {
+                const uint32_t code = uint32_t(first[len] + k);
+                uint32_t rev = 0;
+                for (int b = 0; b < len; ++b) rev |= ((code >> b) & 1u) << (len - 1 - b);
+                const uint16_t e = uint16_t((uint32_t(symbol[size_t(offset[len] + k)]) << 4) | uint32_t(len));
+                for (uint32_t f = rev; f < (1u << kFastBits); f += 1u << len) fast[f] = e;
+            }
     }
 
     int decode(BitReader& br) const {
+        const uint16_t e = fast[br.peek(kFastBits)];
+        if (e) {
+            br.consume(e & 15);
+            return e >> 4;
+        }
         int32_t code = 0;
         for (int len = 1; len < 16; ++len) {
             code = (code << 1) | int32_t(br.bits(1));
@@ -114,12 +146,23 @@ const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 
 // Order of the code-length code lengths (RFC 1951 3.2.7).
 const uint8_t kClOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
 
-void inflate_block(BitReader& br, const Huffman& lit, const Huffman& dist, std::vector<uint8_t>& out, size_t limit) {
+// Inflated bytes: out[0, pos), the vector grown by doubling up to `limit`.
+struct Output {
+    std::vector<uint8_t> buf;
+    size_t pos = 0, limit = 0;
+    uint8_t* room(size_t n) {
+        if (n > limit - pos) fail("inflated data exceeds the image size");
+        if (pos + n > buf.size()) buf.resize(std::min(limit, std::max(pos + n, 2 * buf.size())));
+        return buf.data() + pos;
+    }
+};
+
+void inflate_block(BitReader& br, const Huffman& lit, const Huffman& dist, Output& out) {
     for (;;) {
         const int sym = lit.decode(br);
         if (sym < 256) {
-            if (out.size() >= limit) fail("inflated data exceeds the image size");
-            out.push_back(uint8_t(sym));
+            *out.room(1) = uint8_t(sym);
+            ++out.pos;
         } else if (sym == 256) {
             return;
         } else {
@@ -129,10 +172,11 @@ void inflate_block(BitReader& br, const Huffman& lit, const Huffman& dist, std::
             const int di = dist.decode(br);
             if (di >= 30) fail("invalid distance symbol");
             const size_t d = kDistBase[di] + br.bits(kDistExtra[di]);
-            if (d > out.size()) fail("distance beyond the start of the output");
-            if (out.size() + len > limit) fail("inflated data exceeds the image size");
-            const size_t from = out.size() - d;
-            for (size_t k = 0; k < len; ++k) out.push_back(out[from + k]);
+            if (d > out.pos) fail("distance beyond the start of the output");
+            uint8_t* o = out.room(len);
+            const uint8_t* from = o - d;
+            for (size_t k = 0; k < len; ++k) o[k] = from[k];  // may overlap its own output
+            out.pos += len;
         }
     }
 }
@@ -144,10 +188,11 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t size, size_t limit
     if ((cmf & 15) != 8 || ((uint32_t(cmf) << 8) | flg) % 31 != 0) fail("not a zlib DEFLATE stream");
     if (flg & 0x20) fail("zlib preset dictionaries are not supported");
     BitReader br(data + 2, size - 2);
-    std::vector<uint8_t> out;
+    Output out;
+    out.limit = limit;
     // DEFLATE expands at most about 1032:1 (258-byte matches coded in 2 bits),
     // so a small stream cannot claim a huge buffer up front
-    out.reserve(std::min(limit, size * 1032 + 1024));
+    out.buf.resize(std::min(limit, size * 1032 + 1024));
     int last = 0;
     while (!last) {
         last = int(br.bits(1));
@@ -158,8 +203,8 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t size, size_t limit
             if ((len ^ 0xFFFFu) != nlen) fail("stored block length mismatch");
             const size_t at = br.byte_pos();
             if (at + len > br.size()) fail("stored block is truncated");
-            if (out.size() + len > limit) fail("inflated data exceeds the image size");
-            out.insert(out.end(), br.data() + at, br.data() + at + len);
+            if (len) std::memcpy(out.room(len), br.data() + at, len);
+            out.pos += len;
             br.skip_to(at + len);
         } else if (type == 1) {
             // the fixed codes of RFC 1951 3.2.6, built once (thread-safely)
@@ -177,7 +222,7 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t size, size_t limit
                 }
             };
             static const Fixed fixed;
-            inflate_block(br, fixed.lit, fixed.dist, out, limit);
+            inflate_block(br, fixed.lit, fixed.dist, out);
         } else if (type == 2) {
             const int hlit = int(br.bits(5)) + 257, hdist = int(br.bits(5)) + 1, hclen = int(br.bits(4)) + 4;
             uint8_t cl[19] = {};
@@ -210,7 +255,7 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t size, size_t limit
             Huffman lit, dist;
             lit.build(lens, hlit);
             dist.build(lens + hlit, hdist);
-            inflate_block(br, lit, dist, out, limit);
+            inflate_block(br, lit, dist, out);
         } else {
             fail("reserved DEFLATE block type");
         }
@@ -219,15 +264,22 @@ std::vector<uint8_t> zlib_inflate(const uint8_t* data, size_t size, size_t limit
     br.align();
     const size_t at = br.byte_pos() + 2;
     if (at + 4 > size) fail("zlib checksum is missing");
+    out.buf.resize(out.pos);
+    // the sums are reduced every 5552 bytes, the most that keeps b in 32 bits
     uint32_t a = 1, b = 0;
-    for (uint8_t v : out) {
-        a = (a + v) % 65521u;
-        b = (b + a) % 65521u;
+    for (size_t i = 0; i < out.pos;) {
+        const size_t end = std::min(out.pos, i + 5552);
+        for (; i < end; ++i) {
+            a += out.buf[i];
+            b += a;
+        }
+        a %= 65521u;
+        b %= 65521u;
     }
     const uint32_t want = (uint32_t(data[at]) << 24) | (uint32_t(data[at + 1]) << 16) | (uint32_t(data[at + 2]) << 8) |
                           uint32_t(data[at + 3]);
     if (((b << 16) | a) != want) fail("zlib checksum mismatch");
-    return out;
+    return std::move(out.buf);
 }
 
 // ------------------------------------------------------------------ PNG
@@ -261,24 +313,35 @@ uint8_t paeth(int a, int b, int c) {
     return uint8_t(pb <= pc ? b : c);
 }
 
-// Reverses the per-scanline filters of one (sub)image in place.
+// Reverses the per-scanline filters of one (sub)image in place: one loop
+// per filter type, the first pixel's bytes (no left neighbour) apart.
 void unfilter(uint8_t* data, uint32_t rows, size_t stride, size_t bpp) {
     std::vector<uint8_t> zero(stride, 0);
+    const size_t head = std::min(bpp, stride);
     for (uint32_t y = 0; y < rows; ++y) {
         uint8_t* line = data + size_t(y) * (stride + 1);
         const uint8_t ft = line[0];
         uint8_t* cur = line + 1;
         const uint8_t* prev = y ? data + size_t(y - 1) * (stride + 1) + 1 : zero.data();
-        for (size_t i = 0; i < stride; ++i) {
-            const int a = i >= bpp ? cur[i - bpp] : 0, b = prev[i], c = i >= bpp ? prev[i - bpp] : 0;
-            switch (ft) {
-                case 0: break;
-                case 1: cur[i] = uint8_t(cur[i] + a); break;
-                case 2: cur[i] = uint8_t(cur[i] + b); break;
-                case 3: cur[i] = uint8_t(cur[i] + ((a + b) >> 1)); break;
-                case 4: cur[i] = uint8_t(cur[i] + paeth(a, b, c)); break;
-                default: fail("unknown PNG filter type");
-            }
+        switch (ft) {
+            case 0:
+                break;
+            case 1:
+                for (size_t i = bpp; i < stride; ++i) cur[i] = uint8_t(cur[i] + cur[i - bpp]);
+                break;
+            case 2:
+                for (size_t i = 0; i < stride; ++i) cur[i] = uint8_t(cur[i] + prev[i]);
+                break;
+            case 3:
+                for (size_t i = 0; i < head; ++i) cur[i] = uint8_t(cur[i] + (prev[i] >> 1));
+                for (size_t i = bpp; i < stride; ++i) cur[i] = uint8_t(cur[i] + ((cur[i - bpp] + prev[i]) >> 1));
+                break;
+            case 4:
+                for (size_t i = 0; i < head; ++i) cur[i] = uint8_t(cur[i] + prev[i]);  // paeth(0, b, 0) = b
+                for (size_t i = bpp; i < stride; ++i) cur[i] = uint8_t(cur[i] + paeth(cur[i - bpp], prev[i], prev[i - bpp]));
+                break;
+            default:
+                fail("unknown PNG filter type");
         }
     }
 }
@@ -427,9 +490,16 @@ void decode_png(const uint8_t* p, size_t n, vkgv_image& img) {
         unfilter(raw.data() + off, ps.h, stride, bpp);
         for (uint32_t y = 0; y < ps.h; ++y) {
             const uint8_t* row = raw.data() + off + size_t(y) * (stride + 1) + 1;
-            for (uint32_t x = 0; x < ps.w; ++x) {
-                const uint32_t X = ps.ox + x * ps.sx, Y = ps.oy + y * ps.sy;
-                put_pixel(I, row, x, &img.rgba[(size_t(Y) * I.w + X) * 4]);
+            uint8_t* out_row = &img.rgba[size_t(ps.oy + y * ps.sy) * I.w * 4];
+            if (I.depth == 8 && I.ctype == 6 && ps.sx == 1) {  // RGBA8 rows as they are
+                std::memcpy(out_row, row, size_t(ps.w) * 4);
+            } else if (I.depth == 8 && I.ctype == 2 && !I.has_key) {
+                for (uint32_t x = 0; x < ps.w; ++x) {
+                    uint8_t* d = out_row + size_t(ps.ox + x * ps.sx) * 4;
+                    d[0] = row[3 * x], d[1] = row[3 * x + 1], d[2] = row[3 * x + 2], d[3] = 255;
+                }
+            } else {
+                for (uint32_t x = 0; x < ps.w; ++x) put_pixel(I, row, x, out_row + size_t(ps.ox + x * ps.sx) * 4);
             }
         }
         off += size_t(ps.h) * (stride + 1);
