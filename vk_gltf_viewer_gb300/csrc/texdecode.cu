@@ -165,17 +165,16 @@ __device__ void bc7_load_tables(Bc7Tables& t) {
     for (uint32_t i = threadIdx.x; i < 80; i += blockDim.x) t.mode[i / 10][i % 10] = c_bc7_mode[i / 10][i % 10];
 }
 
-// Row r (4 texels) of one BC7 block.  The end points of each subset are
-// unpacked once into registers (RGBA8 after the p-bits and the bit
-// replication), then every texel selects its subset's pair.
-__device__ void bc7_row(const Bc7Tables& T, const uint4& q, uint32_t r, uint32_t texel[4]) {
+// Row r (4 texels) of one BC7 block, called by all 32 lanes together: the
+// four lanes of a quad hold the same block (one row each) and share its end
+// points, lane r unpacking end points r and r + 4 (RGBA8 after the p-bits and
+// the bit replication) and the quad exchanging them by shuffles; then every
+// texel selects its subset's pair.
+__device__ void bc7_row(const Bc7Tables& T, const uint4& q, uint32_t r, uint32_t lane, uint32_t texel[4]) {
     const uint64_t lo = (uint64_t)q.x | ((uint64_t)q.y << 32), hi = (uint64_t)q.z | ((uint64_t)q.w << 32);
     const uint32_t first = q.x & 0xFFu;
-    if (first == 0) {  // reserved mode
-        texel[0] = texel[1] = texel[2] = texel[3] = 0u;
-        return;
-    }
-    const uint32_t mode = (uint32_t)(__ffs((int)first) - 1);
+    const bool reserved = first == 0;  // decodes to transparent black
+    const uint32_t mode = reserved ? 0u : (uint32_t)(__ffs((int)first) - 1);
     const uint8_t* m = T.mode[mode];
     const uint32_t ns = m[0], cb = m[4], ab = m[5], ib = m[8], ib2 = m[9];
     uint32_t pos = mode + 1;
@@ -192,10 +191,11 @@ __device__ void bc7_row(const Bc7Tables& T, const uint4& q, uint32_t r, uint32_t
     const uint32_t alpha_base = pos + 3 * nep * cb, pbit_base = alpha_base + nep * ab;
     const uint32_t cbits = cb + ((m[6] | m[7]) ? 1u : 0u);
     const uint32_t abits = ab ? ab + m[6] : 0u;
-    uint32_t epk[6];  // packed RGBA8 of end point k
+    uint32_t mine[2];  // this lane's end points r and r + 4, packed RGBA8
 #pragma unroll
-    for (uint32_t k = 0; k < 6; ++k) {
-        epk[k] = 0u;
+    for (uint32_t j = 0; j < 2; ++j) {
+        const uint32_t k = r + 4 * j;
+        mine[j] = 0u;
         if (k < nep) {
             // a p-bit per end point (modes 0, 3, 6, 7) or per subset (mode 1)
             const uint32_t pb = m[6] ? bc7_bits(lo, hi, pbit_base + k, 1) : (m[7] ? bc7_bits(lo, hi, pbit_base + k / 2, 1) : 0u);
@@ -212,9 +212,12 @@ __device__ void bc7_row(const Bc7Tables& T, const uint4& q, uint32_t r, uint32_t
                 if (m[6]) a = (a << 1) | pb;
                 a = bc7_expand(a, abits);
             }
-            epk[k] = v | (a << 24);
+            mine[j] = v | (a << 24);
         }
     }
+    uint32_t epk[6];  // packed RGBA8 of end point k, from lane k % 4 of the quad
+#pragma unroll
+    for (uint32_t k = 0; k < 6; ++k) epk[k] = __shfl_sync(0xffffffffu, mine[k >> 2], (lane & ~3u) | (k & 3u));
     const uint32_t a1 = ns == 2 ? T.a2[part] : (ns == 3 ? T.a3a[part] : 16u);
     const uint32_t a2 = ns == 3 ? T.a3b[part] : 16u;
     const uint32_t idx_start = pbit_base + (m[6] ? nep : (m[7] ? ns : 0u));
@@ -248,7 +251,7 @@ __device__ void bc7_row(const Bc7Tables& T, const uint4& q, uint32_t r, uint32_t
             px[3] = px[rot - 1];
             px[rot - 1] = t;
         }
-        texel[x] = px[0] | (px[1] << 8) | (px[2] << 16) | (px[3] << 24);
+        texel[x] = reserved ? 0u : (px[0] | (px[1] << 8) | (px[2] << 16) | (px[3] << 24));
     }
 }
 
@@ -327,7 +330,9 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc(const uint8_t* 
 }
 
 // BC7 with the lane layout of k_decode_bc (four lanes per block, one row
-// each) and the tables in shared memory.
+// each) and the tables in shared memory.  Every lane runs every step (the
+// end points are shared by shuffles); lanes past the image edge decode a
+// zero block and store nothing.
 __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc7(const uint8_t* __restrict__ blocks, uint32_t w,
                                                                   uint32_t h, uint32_t* __restrict__ rgba) {
     __shared__ Bc7Tables T;
@@ -338,19 +343,19 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc7(const uint8_t*
     const uint32_t r = lane & 3u;
     const uint32_t bx = (blockIdx.x * kDecodeWarps + warp) * 8 + (lane >> 2);
     const uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
-    if (bx >= bw) return;
     uint4 q[kDecodeDepth];
 #pragma unroll
     for (int k = 0; k < kDecodeDepth; ++k) {
         const uint32_t by = blockIdx.y * kDecodeDepth + k;
-        q[k] = by < bh ? __ldg(reinterpret_cast<const uint4*>(blocks) + ((size_t)by * bw + bx)) : make_uint4(0, 0, 0, 0);
+        q[k] = (bx < bw && by < bh) ? __ldg(reinterpret_cast<const uint4*>(blocks) + ((size_t)by * bw + bx))
+                                    : make_uint4(0, 0, 0, 0);
     }
 #pragma unroll
     for (int k = 0; k < kDecodeDepth; ++k) {
         const uint32_t y = (blockIdx.y * kDecodeDepth + k) * 4 + r;
-        if (y >= h) break;
         uint32_t texel[4];
-        bc7_row(T, q[k], r, texel);
+        bc7_row(T, q[k], r, lane, texel);
+        if (bx >= bw || y >= h) continue;
         uint32_t* dst = rgba + (size_t)y * w + (size_t)bx * 4;
         if (bx * 4 + 4 <= w && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
             __stcs(reinterpret_cast<uint4*>(dst), make_uint4(texel[0], texel[1], texel[2], texel[3]));
