@@ -703,7 +703,7 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
     // no warp idles while work is left.
     const uint32_t warps_total = gridDim.x * WARPS;
     const uint32_t grab = max(1u, min(32u, total / (warps_total * 8u)));
-    uint32_t cur_v = 0xffffffffu;
+    uint32_t cur_v = 0xffffffffu, cur_t = 0xffffffffu;  // view and node of s_vp / s_mvp
     const DeviceView* Vp = P.views;
     // the warp's raster context lives in shared memory (fewer live registers)
     __shared__ RasterCtx s_ctx[WARPS];
@@ -786,6 +786,7 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
             }
             if (v != cur_v) {
                 cur_v = v;
+                cur_t = 0xffffffffu;
                 Vp = P.views + v;
                 __syncwarp();
                 if (lane == 0) {
@@ -808,9 +809,14 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
             const uint32_t transform_index = H.transform;
             // mvp = VP * M, one element per lane (lanes 0-15); lane 16 takes the
             // sign source determinant(M) of visbuffer.mesh.glsl:71.
+            // Consecutive items of a run mostly come from one node (the draw
+            // list is node-major): its matrix and sign are then already here.
             const float* Mg = P.S.transforms + 16 * (size_t)transform_index;
             const bool have_tdet = P.S.tdets != nullptr && transform_index < P.S.transform_count;
-            if (lane < 16 && V.mvps && transform_index < P.S.transform_count) {
+            const bool same_node = transform_index == cur_t;
+            cur_t = transform_index;
+            if (same_node) {
+            } else if (lane < 16 && V.mvps && transform_index < P.S.transform_count) {
                 s_mvp[warp][lane] = __ldg(V.mvps + 16 * (size_t)transform_index + lane);
             } else if (lane < 16) {
                 const int cc = lane >> 2, j = lane & 3;
@@ -826,7 +832,7 @@ __global__ void __launch_bounds__(WARPS * 32, (SLOW ? 16 : VKGV_RASTER_WARPS_PER
                 for (int q = 0; q < 16; ++q) M[q] = __ldg(Mg + q);
                 s_tdet[warp] = det4(M);
             }
-            __syncwarp();
+            if (!same_node) __syncwarp();
             const float tdet = s_tdet[warp];
             const float* mvp = s_mvp[warp];
             // Vertex stage: clip position, outcode, guard flag and the 28.8 snap,
