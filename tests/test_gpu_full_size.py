@@ -86,3 +86,46 @@ def test_full_size_fine_occlusion_bit_exact(renderer, full):
         assert np.array_equal(u32(v.visbuffer), e["ids"])
         assert np.array_equal(u32(v.visbuffer), u32(b.visbuffer))
         assert v.survivor_list().size < b.survivor_list().size
+
+
+def test_all_256_batched_views_equal_single_view_frames(renderer, full):
+    """Every one of the benchmark's 256 uneven poses, rendered together in one
+    batched frame (steady state, each view reading its own previous pyramid,
+    fine occlusion test on as in the benchmark), equals the same pose
+    rendered alone through the single-view path: depth|id, visibility ids,
+    colour, pyramid and survivor set bit for bit.  With the twenty poses
+    checked against the oracle above, this carries the oracle's parity to
+    the whole batch."""
+    from vk_gltf_viewer_gb300.renderer import ViewBuffers
+
+    flags = FLAGS | abi.CULL_OCCLUSION_FINE
+    poses = scene.batch_views(256, seed=3)
+
+    def make():
+        out = []
+        for cam, w, h in poses:
+            vb = ViewBuffers.allocate(w, h, cam, full.host.draw_count, prev_pyramid="alias")
+            vb.use_prev = False
+            out.append(vb)
+        return out
+
+    batched, single = make(), make()
+    renderer.frame(full.dev, batched, flags)
+    for vb in batched:
+        vb.use_prev = True
+    renderer.frame(full.dev, batched, flags)
+    for vb in single:
+        renderer.frame(full.dev, [vb], flags)
+        vb.use_prev = True
+        renderer.frame(full.dev, [vb], flags)
+    torch.cuda.synchronize()
+    assert renderer.device_status() == (0, 0)
+    for i, (a, b) in enumerate(zip(batched, single)):
+        where = (i, a.width, a.height)
+        assert torch.equal(a.depth_id, b.depth_id), where
+        assert torch.equal(a.visbuffer, b.visbuffer), where
+        assert torch.equal(a.color, b.color), where
+        assert torch.equal(a.pyramid, b.pyramid), where
+        na, nb = int(a.survivor_count.item()), int(b.survivor_count.item())
+        assert na == nb, where
+        assert torch.equal(torch.sort(a.survivors[:na])[0], torch.sort(b.survivors[:nb])[0]), where
