@@ -18,7 +18,9 @@
 // footprint of the level above it (a halo of a few texels, recomputed rather
 // than exchanged), keeping levels 1-3 in shared memory and reading the depth
 // image once.  The last CTA of a view to finish computes the remaining top
-// levels from global memory.
+// levels: the footprints of all their columns and rows in one table, the
+// first of them from the top tiled mip in L2, the rest from shared memory
+// with one barrier per level.
 #include <atomic>
 
 #include "kernels.cuh"
@@ -38,7 +40,11 @@ constexpr int kThreads = 256;
 constexpr int kOff2 = kCap1 * kCap1, kOff3 = kOff2 + kCap2 * kCap2, kOff4 = kOff3 + kCap3 * kCap3;
 constexpr int kTileFloats = kOff4 + kCap4 * kCap4;
 constexpr int kTailMax = 40960;
-constexpr int kTailAxis = 1024;  // largest tail level edge with per-axis footprint tables
+constexpr int kTailAxis = 1024;  // footprint-table entries per axis over all tail levels
+#ifndef VKGV_HIZ_TAIL_BATCH
+#define VKGV_HIZ_TAIL_BATCH 4
+#endif
+constexpr int kTailBatch = VKGV_HIZ_TAIL_BATCH;  // first tail level: texels per thread with loads in flight
 
 struct Range {
     int lo, hi;  // inclusive; empty when lo > hi
@@ -205,9 +211,7 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
             __syncthreads();
         }
     }
-    // The last CTA of this view finishes levels Kp+1..L.  When the top tiled
-    // mip fits in shared memory the tail works there (ping-pong A/B) and
-    // only writes each level out; otherwise it reads back from global.
+    // The last CTA of this view finishes levels Kp+1..L.
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_last = atomicAdd(&V.counters[3], 1u) == ntx * nty - 1;
@@ -216,89 +220,135 @@ __global__ void __launch_bounds__(kThreads) k_hiz(const DeviceView* __restrict__
     __threadfence();
     const uint32_t top_w = Kp > 0 ? (w >> Kp) : 0, top_h = Kp > 0 ? (h >> Kp) : 0;
     const uint32_t next_px = Kp > 0 ? (w >> (Kp + 1)) * (h >> (Kp + 1)) : 0;
-    const bool in_smem = Kp > 0 && top_w * top_h <= tail_a && next_px <= tail_b;
-    float* cur = smem;
-    float* nxt = smem + tail_a;
-    if (in_smem) {
-        // eight loads in flight per thread before the first store
-        const float* src = V.pyr + mip_offset(w0, h0, (uint32_t)(Kp - 1));
-        const uint32_t n = top_w * top_h;
-        for (uint32_t i0 = threadIdx.x; i0 < n; i0 += 8 * kThreads) {
-            float t[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const uint32_t i = i0 + (uint32_t)k * kThreads;
-                t[k] = i < n ? __ldcg(src + i) : 0.0f;
+    // Levels Kp+1..Lv have both dimensions non-zero; the ones above are 0.
+    uint32_t Lv = (uint32_t)Kp, sum_w = 0, sum_h = 0;
+    while (Lv < L && (w >> (Lv + 1)) != 0 && (h >> (Lv + 1)) != 0) {
+        ++Lv;
+        sum_w += w >> Lv;
+        sum_h += h >> Lv;
+    }
+    // Shared-memory tail: the footprints of every column and row of every
+    // tail level are tabulated in one pass; level Kp+1 reads the top tiled
+    // mip straight from L2 (all of a thread's loads in flight) into buffer
+    // B, and each level above it reads the previous one from shared memory
+    // (ping-pong B/A), one barrier per level.
+    __shared__ uint32_t s_fx[kTailAxis], s_fy[kTailAxis];
+    const bool fast = Kp > 0 && Lv > (uint32_t)Kp && top_w * top_h <= tail_a && next_px <= tail_b &&
+                      sum_w <= (uint32_t)kTailAxis && sum_h <= (uint32_t)kTailAxis;
+    uint32_t first_zero = (uint32_t)Kp + 1;
+    if (fast) {
+        // entry: x0 | x1 << 14 | n << 28 (x1 = x0 when n = 1)
+        for (uint32_t i = threadIdx.x; i < sum_w + sum_h; i += blockDim.x) {
+            const bool isx = i < sum_w;
+            const uint32_t full = isx ? w : h;
+            uint32_t k = isx ? i : i - sum_w, j = (uint32_t)Kp + 1;
+            while (k >= (full >> j)) {
+                k -= full >> j;
+                ++j;
             }
+            int a = 0, b = 0;
+            const int n = axis_footprint((int)k, full >> j, full >> (j - 1), a, b);
+            if (n == 1) b = a;
+            const uint32_t packed = (uint32_t)a | ((uint32_t)b << 14) | ((uint32_t)n << 28);
+            if (isx) s_fx[i] = packed;
+            else s_fy[i - sum_w] = packed;
+        }
+        __syncthreads();
+        float* cur = smem + tail_a;
+        float* nxt = smem;
+        uint64_t off = mip_offset(w0, h0, (uint32_t)Kp - 1);  // the top tiled mip
+        {
+            const float* src = V.pyr + off;
+            off += (uint64_t)top_w * top_h;
+            float* dst = V.pyr + off;
+            const uint32_t dw = w >> (Kp + 1), sw = top_w, n = next_px;
+            for (uint32_t i0 = threadIdx.x; i0 < n; i0 += kTailBatch * kThreads) {
+                float t[kTailBatch][4];
+                uint32_t two[kTailBatch];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const uint32_t i = i0 + (uint32_t)k * kThreads;
-                if (i < n) cur[i] = t[k];
+                for (int k = 0; k < kTailBatch; ++k) {
+                    const uint32_t i = i0 + (uint32_t)k * kThreads;
+                    if (i < n) {
+                        const uint32_t y = i / dw, x = i - y * dw;
+                        const uint32_t fx = s_fx[x], fy = s_fy[y];
+                        const uint32_t x0 = fx & 0x3fffu, x1 = (fx >> 14) & 0x3fffu;
+                        const uint32_t r0 = (fy & 0x3fffu) * sw, r1 = ((fy >> 14) & 0x3fffu) * sw;
+                        two[k] = (fx >> 28) | ((fy >> 28) << 2);
+                        t[k][0] = __ldcg(src + r0 + x0);
+                        t[k][1] = __ldcg(src + r0 + x1);
+                        t[k][2] = __ldcg(src + r1 + x0);
+                        t[k][3] = __ldcg(src + r1 + x1);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < kTailBatch; ++k) {
+                    const uint32_t i = i0 + (uint32_t)k * kThreads;
+                    if (i < n) {
+                        const bool nx2 = (two[k] & 3u) == 2u, ny2 = (two[k] >> 2) == 2u;
+                        float r = t[k][0];
+                        if (nx2) r = gmin(r, t[k][1]);
+                        if (ny2) {
+                            r = gmin(r, t[k][2]);
+                            if (nx2) r = gmin(r, t[k][3]);
+                        }
+                        cur[i] = r;
+                        dst[i] = r;
+                    }
+                }
             }
         }
         __syncthreads();
+        uint32_t ox = w >> (Kp + 1), oy = h >> (Kp + 1);
+        for (uint32_t j = (uint32_t)Kp + 2; j <= Lv; ++j) {
+            const uint32_t dw = w >> j, dh = h >> j, sw = w >> (j - 1);
+            off += (uint64_t)sw * (h >> (j - 1));
+            float* dst = V.pyr + off;
+            for (uint32_t i = threadIdx.x; i < dw * dh; i += kThreads) {
+                const uint32_t y = i / dw, x = i - y * dw;
+                const uint32_t fx = s_fx[ox + x], fy = s_fy[oy + y];
+                const uint32_t x0 = fx & 0x3fffu, x1 = (fx >> 14) & 0x3fffu;
+                const uint32_t r0 = (fy & 0x3fffu) * sw, r1 = ((fy >> 14) & 0x3fffu) * sw;
+                const bool nx2 = (fx >> 28) == 2u, ny2 = (fy >> 28) == 2u;
+                float r = cur[r0 + x0];
+                if (nx2) r = gmin(r, cur[r0 + x1]);
+                if (ny2) {
+                    r = gmin(r, cur[r1 + x0]);
+                    if (nx2) r = gmin(r, cur[r1 + x1]);
+                }
+                nxt[i] = r;
+                dst[i] = r;
+            }
+            ox += dw;
+            oy += dh;
+            __syncthreads();
+            float* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+        first_zero = Lv + 1;
     }
-    // per-axis footprints of the current tail level: x0 | x1 << 14 | n << 28
-    __shared__ uint32_t s_fx[kTailAxis], s_fy[kTailAxis];
-    const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
-    for (uint32_t j = (uint32_t)Kp + 1; j <= L; ++j) {
+    // Otherwise each texel reads its footprint from global memory.
+    for (uint32_t j = first_zero; j <= L; ++j) {
         const uint32_t dw = w >> j, dh = h >> j;
         const uint32_t mw = mip_dim(w0, j - 1), mh = mip_dim(h0, j - 1);
         float* dst = V.pyr + mip_offset(w0, h0, j - 1);
         if (dw == 0 || dh == 0) {
             for (uint32_t i = threadIdx.x; i < mw * mh; i += blockDim.x) dst[i] = 0.0f;
-        } else if (in_smem && dw <= (uint32_t)kTailAxis && dh <= (uint32_t)kTailAxis) {
-            // One footprint per column and per row (dw + dh of them instead
-            // of two per texel), then warps take rows and lanes columns.
-            const uint32_t sw = mip_dim(w0, j - 2), sh = mip_dim(h0, j - 2);
-            for (uint32_t i = threadIdx.x; i < dw + dh; i += blockDim.x) {
-                int a = 0, b = 0;
-                const bool isx = i < dw;
-                const int n = isx ? axis_footprint((int)i, dw, sw, a, b) : axis_footprint((int)(i - dw), dh, sh, a, b);
-                const uint32_t packed = (uint32_t)a | ((uint32_t)b << 14) | ((uint32_t)n << 28);
-                if (isx) s_fx[i] = packed;
-                else s_fy[i - dw] = packed;
-            }
-            __syncthreads();
-            for (uint32_t y = (uint32_t)warp; y < dh; y += kThreads / 32) {
-                const uint32_t fy = s_fy[y];
-                const int y0 = (int)(fy & 0x3fffu), y1 = (int)((fy >> 14) & 0x3fffu), ny = (int)(fy >> 28);
-                for (uint32_t x = (uint32_t)lane; x < dw; x += 32) {
-                    const uint32_t fx = s_fx[x];
-                    const int x0 = (int)(fx & 0x3fffu), x1 = (int)((fx >> 14) & 0x3fffu), nx = (int)(fx >> 28);
-                    float r = cur[y0 * (int)sw + x0];
-                    if (nx == 2) r = gmin(r, cur[y0 * (int)sw + x1]);
-                    if (ny == 2) {
-                        r = gmin(r, cur[y1 * (int)sw + x0]);
-                        if (nx == 2) r = gmin(r, cur[y1 * (int)sw + x1]);
-                    }
-                    nxt[y * dw + x] = r;
-                    dst[y * dw + x] = r;
-                }
-            }
         } else {
             const uint32_t sw = j == 1 ? w : mip_dim(w0, j - 2), sh = j == 1 ? h : mip_dim(h0, j - 2);
             const float* src = j == 1 ? nullptr : V.pyr + mip_offset(w0, h0, j - 2);
             for (uint32_t i = threadIdx.x; i < dw * dh; i += blockDim.x) {
                 const int x = (int)(i % dw), y = (int)(i / dw);
                 float r;
-                if (in_smem)
-                    r = reduce_texel(x, y, dw, dh, sw, sh, [&](int sx, int sy) { return cur[sy * (int)sw + sx]; });
-                else if (j == 1)
+                if (j == 1)
                     r = reduce_texel(x, y, dw, dh, sw, sh, [&](int sx, int sy) { return depth_at(V.depth_id, w, sx, sy); });
                 else
                     r = reduce_texel(x, y, dw, dh, sw, sh,
                                      [&](int sx, int sy) { return __ldcg(src + (size_t)sy * sw + sx); });
-                if (in_smem) nxt[i] = r;
                 dst[i] = r;
             }
         }
         __syncthreads();
-        if (in_smem) {
-            float* t = cur;
-            cur = nxt;
-            nxt = t;
-        }
     }
     if (threadIdx.x == 0) V.counters[3] = 0;  // ready for the next reduce of this view
 }
