@@ -197,7 +197,7 @@ struct Prepared {
     uint32_t max_w = 0, max_h = 0;
     uint64_t max_px = 0;
     uint32_t hiz_tx = 1, hiz_ty = 1;  // single-pass HiZ grid (max over views)
-    uint32_t hiz_ta = 0, hiz_tb = 0;  // its tail's shared-memory floats (max over views)
+    uint32_t hiz_tail = 0;            // its tail's shared-memory floats (max over views)
     float* tdets = nullptr;           // node tables filled by the clear (whole frames only)
     float* mvps = nullptr;
 };
@@ -279,10 +279,7 @@ int build_views(vkgv_ctx* ctx, const vkgv_scene* scene, const vkgv_view* views, 
             hiz_tiles(v.width, v.height, v.pyramid.levels, &tx, &ty);
             P.hiz_tx = std::max(P.hiz_tx, tx);
             P.hiz_ty = std::max(P.hiz_ty, ty);
-            uint32_t ta = 0, tb = 0;
-            hiz_tail_floats(v.width, v.height, v.pyramid.levels, &ta, &tb);
-            P.hiz_ta = std::max(P.hiz_ta, ta);
-            P.hiz_tb = std::max(P.hiz_tb, tb);
+            P.hiz_tail = std::max(P.hiz_tail, hiz_tail_floats(v.width, v.height, v.pyramid.levels));
         }
         P.max_px = std::max<uint64_t>(P.max_px, (uint64_t)v.width * v.height);
     }
@@ -333,7 +330,7 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
                   zones ? zones[3] : nullptr);
     zone(4);
     const bool two = (flags & VKGV_CULL_TWO_PASS) && (flags & VKGV_CULL_OCCLUSION);
-    if (two) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, P.hiz_ta, P.hiz_tb, ctx->status, stream);
+    if (two) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, P.hiz_tail, ctx->status, stream);
     zone(5);
     if (two) launch_cull(P.S, dv, n, flags, 2, ctx->status, ctx->sm_count, stream);
     zone(6);
@@ -354,12 +351,12 @@ void record_frame(vkgv_ctx* ctx, const Prepared& P, const DeviceView* dv, uint32
         // depth_id: the reduce runs on a side stream beside the resolve
         cudaEventRecord(ctx->fork_ev, stream);
         cudaStreamWaitEvent(ctx->side_stream, ctx->fork_ev, 0);
-        launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, P.hiz_ta, P.hiz_tb, ctx->status, ctx->side_stream);
+        launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, P.hiz_tail, ctx->status, ctx->side_stream);
         cudaEventRecord(ctx->join_ev, ctx->side_stream);
         launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, ctx->counters + 4, ctx->sm_count, stream);
         cudaStreamWaitEvent(stream, ctx->join_ev, 0);
     } else {
-        if (pyramid) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, P.hiz_ta, P.hiz_tb, ctx->status, stream);
+        if (pyramid) launch_hiz(dv, n, P.hiz_tx, P.hiz_ty, P.hiz_tail, ctx->status, stream);
         zone(9);
         if (resolve) launch_resolve(P.S, dv, n, P.max_w, P.max_h, flags, ctx->counters + 4, ctx->sm_count, stream);
     }
@@ -664,7 +661,7 @@ int vkgv_hiz_reduce(vkgv_ctx* ctx, const vkgv_view* view, void* stream_) {
     if (rc) return rc;
     rc = commit_views(ctx, slot, 1, stream);
     if (rc) return rc;
-    launch_hiz(dv, 1, P.hiz_tx, P.hiz_ty, P.hiz_ta, P.hiz_tb, ctx->status, stream);
+    launch_hiz(dv, 1, P.hiz_tx, P.hiz_ty, P.hiz_tail, ctx->status, stream);
     rc = check_launch(ctx);
     if (rc) return rc;
     return close_slot(ctx, slot, stream);

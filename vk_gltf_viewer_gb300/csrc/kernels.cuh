@@ -59,11 +59,11 @@ void launch_raster(const SceneArgs& S, const DeviceView* views, uint32_t nviews,
                    const RasterConfig& cfg, BigTri* big, uint32_t* big_count, uint32_t big_capacity,
                    uint32_t* work, uint32_t* status, uint32_t sm_count, cudaStream_t stream,
                    cudaEvent_t between = nullptr);
-// Shared-memory floats the HiZ tail needs for a view: its top tiled mip (a)
-// and the level above it (b).
-void hiz_tail_floats(uint32_t w, uint32_t h, uint32_t levels, uint32_t* a, uint32_t* b);
-void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t tail_a,
-                uint32_t tail_b, uint32_t* status, cudaStream_t stream);
+// Shared-memory floats the HiZ tail needs for a view: the texels of its
+// levels above the tiled ones.
+uint32_t hiz_tail_floats(uint32_t w, uint32_t h, uint32_t levels);
+void launch_hiz(const DeviceView* views, uint32_t nviews, uint32_t tiles_x, uint32_t tiles_y, uint32_t tail,
+                uint32_t* status, cudaStream_t stream);
 void launch_resolve(const SceneArgs& S, const DeviceView* views, uint32_t nviews, uint32_t max_w, uint32_t max_h,
                     uint32_t flags, uint32_t* work, uint32_t sm_count, cudaStream_t stream);
 void launch_finalize(const DeviceView* views, uint32_t nviews, cudaStream_t stream);
