@@ -42,7 +42,7 @@ constexpr int kTileFloats = kOff4 + kCap4 * kCap4;
 constexpr int kTailMax = 40960;
 constexpr int kTailAxis = 1024;  // footprint-table entries per axis over all tail levels
 #ifndef VKGV_HIZ_TAIL_BATCH
-#define VKGV_HIZ_TAIL_BATCH 4
+#define VKGV_HIZ_TAIL_BATCH 2
 #endif
 constexpr int kTailBatch = VKGV_HIZ_TAIL_BATCH;  // first tail level: texels per thread with loads in flight
 
