@@ -641,7 +641,10 @@ enum vkgv_block_format {
                           * mode's fourth entry is opaque black                      */
     VKGV_RGBA8 = 7, /* uncompressed RGBA8 texels (reported by vkgv_ktx2_parse only;
                      * not a vkgv_decode_bc format)                                 */
-    VKGV_BC7 = 8    /* BPTC UNORM: eight modes of 1-3 subsets, 16-byte blocks       */
+    VKGV_BC7 = 8,   /* BPTC UNORM: eight modes of 1-3 subsets, 16-byte blocks       */
+    VKGV_BC6H_UF16 = 9,  /* BPTC float, unsigned: fourteen modes of 1-2 regions,
+                          * binary16 RGB texels (vkgv_decode_bc6h)                  */
+    VKGV_BC6H_SF16 = 10  /* BPTC float, signed                                      */
 };
 
 typedef struct vkgv_dds_info {
@@ -658,14 +661,15 @@ typedef struct vkgv_dds_info {
 } vkgv_dds_info;
 
 /* Reads a DDS header (FourCC DXT1-5 / ATI1 / ATI2 / BC4U / BC5U, or DX10
- * with a BC1-BC5 or BC7 DXGI format); VKGV_INVALID_ARG for anything else
- * (BC6H, uncompressed pixel formats). */
+ * with a BC1-BC5, BC6H (UF16 / SF16) or BC7 DXGI format); VKGV_INVALID_ARG
+ * for anything else (uncompressed pixel formats). */
 int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* out);
 /* Reads a KTX 2.0 header (the container of KHR_texture_basisu, which the
  * reference enables in fastgltf, assets.cpp:539, and links ktx_read for):
  * a 2D texture (one layer, one face), without supercompression or with
  * Zstandard supercompression (scheme 2), whose vkFormat is BC1-BC5 UNORM /
- * SRGB (131-139, 141), BC7 UNORM / SRGB (145, 146) or R8G8B8A8 UNORM / SRGB
+ * SRGB (131-139, 141), BC6H UFLOAT / SFLOAT (143, 144), BC7 UNORM / SRGB
+ * (145, 146) or R8G8B8A8 UNORM / SRGB
  * (37, 43), into the same
  * fields as a DDS file (level 0; format VKGV_BC1_OPAQUE for BC1_RGB,
  * VKGV_RGBA8 for R8G8B8A8; `supercompression` set to 2 for a zstd level,
@@ -688,6 +692,15 @@ uint64_t vkgv_xxh64(const void* data, uint64_t size);
  * (device uint32[width * height], 4-byte aligned). */
 int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
                    uint64_t rgba_out, void* stream);
+/* Decodes width x height texels of BC6H blocks (format VKGV_BC6H_UF16 or
+ * VKGV_BC6H_SF16; device, row-major 16-byte blocks, 16-byte aligned) into
+ * float32 R, G, B per texel (device float[width * height * 3], 4-byte
+ * aligned): the binary16 values of the format, exactly, for a linear
+ * VKGV_TEXTURE_RGB32F texture.  Reserved modes decode to 0.  (The
+ * reference enables MSFT_texture_dds, assets.cpp:540, whose DDS files may
+ * hold BC6H.) */
+int vkgv_decode_bc6h(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
+                     uint64_t rgb_out, void* stream);
 
 /* JPEG (the reference links wuffs for it, wuffs_implementation.cpp:1-5):
  * sequential or progressive DCT, Huffman, 8-bit; 1 component or 3 (YCbCr,

@@ -159,6 +159,7 @@ def load() -> C.CDLL:
         lib.orc_asin_series.restype = C.c_float
         lib.orc_asin_series.argtypes = [C.c_float]
         lib.orc_decode_bc.argtypes = [U32, P, U32, U32, P]
+        lib.orc_decode_bc6h.argtypes = [P, U32, U32, C.c_int, P]
         lib.orc_jpeg_idct.argtypes = [P, U32, U32, P]
         lib.orc_jpeg_color.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, P]
         lib.orc_half_rn.restype = C.c_uint16
@@ -491,6 +492,17 @@ def decode_bc(fmt: int, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
     out = np.zeros(w * h, np.uint32)
     load().orc_decode_bc(fmt, _addr(blocks), w, h, _addr(out))
     return out.reshape(h, w)
+
+
+def decode_bc6h(blocks: np.ndarray, w: int, h: int, signed: bool) -> np.ndarray:
+    """BC6H blocks -> (h, w, 3) uint16 binary16 bits (SF16 when `signed`)."""
+    blocks = np.ascontiguousarray(blocks, np.uint8)
+    need = ((w + 3) // 4) * ((h + 3) // 4) * 16
+    if blocks.size < need:
+        raise ValueError(f"{blocks.size} block bytes, {need} needed")
+    out = np.zeros(w * h * 3, np.uint16)
+    load().orc_decode_bc6h(_addr(blocks), w, h, 1 if signed else 0, _addr(out))
+    return out.reshape(h, w, 3)
 
 
 def jpeg_rgba(info, planes) -> np.ndarray:

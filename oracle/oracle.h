@@ -242,6 +242,8 @@ float orc_asin_series(float z);
 /* BC1-BC5 blocks (format 1..5, row-major blocks of 8 or 16 bytes) into
  * RGBA8 texels (R in the low byte). */
 void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t h, uint32_t* rgba);
+/* BC6H blocks -> binary16 bits, R, G, B per texel (is_signed: SF16). */
+void orc_decode_bc6h(const uint8_t* blocks, uint32_t w, uint32_t h, int is_signed, uint16_t* rgb);
 /* JPEG pixels from dequantized natural-order coefficient blocks: one
  * component's IDCT into an 8-bit plane (blocks_w * 8 wide), then the
  * upsampled colour conversion of 1 or 3 planes into RGBA8. */

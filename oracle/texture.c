@@ -267,6 +267,160 @@ void orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t 
         }
 }
 
+/* ------------------------------------------------------------------ BC6H
+ * BC6H (BPTC float; UF16 unsigned, SF16 signed), restated from the published
+ * format: a 2-bit mode (values 0, 1) or a 5-bit one; fourteen modes of one or
+ * two regions whose 77-80 header bits hold the endpoint channels in a
+ * mode-specific order (the token tables below; three modes store the top
+ * bits of their base endpoint reversed) and, for two regions, a 5-bit
+ * partition (the first 32 two-subset partitions of BC7, with their
+ * anchors).  Transformed modes store the other endpoints as signed deltas
+ * from the base, added and wrapped to the endpoint precision (then sign-
+ * extended for SF16); untransformed SF16 endpoints are sign-extended.
+ * Endpoints are unquantised to 16 bits (unsigned: 0 and the top code map to
+ * 0 and 0xFFFF, others to ((c << 16) + 0x8000) >> bits; signed: on the
+ * magnitude, 0x7FFF from 2^(bits-1) - 1 up, ((c << 15) + 0x4000) >> (bits-1)
+ * otherwise), texels interpolated as ((64 - w) e0 + w e1 + 32) >> 6 with the
+ * 3-bit (two regions) or 4-bit weights (the anchors store one index bit
+ * less), and scaled into binary16 bits: unsigned v * 31 >> 6; signed the
+ * magnitude * 31 >> 5, the sign bit set only on a non-zero result.
+ * Reserved modes decode to 0.  Matches the GPU texture unit's BC6H decode bit
+ * for bit on every mode (tests/golden/bc6h_texture_unit.json). */
+
+/* header tokens: field (bits 0-3: endpoint w, x, y, z x channel R, G, B, or
+ * 12 = partition), lowest field bit (4-7), bit count - 1 (8-11), reversed
+ * (12: the first stream bit is the highest field bit) */
+static const uint16_t kBc6Tok[14][23] = {
+    {0x0047, 0x0048, 0x004B, 0x0900, 0x0901, 0x0902, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x00 */
+    {0x0057, 0x014A, 0x0600, 0x010B, 0x0048, 0x0601, 0x0058, 0x002B, 0x0047, 0x0602, 0x003B, 0x005B, 0x004B, 0x0503, 0x0307, 0x0504, 0x030A, 0x0505, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x01 */
+    {0x0900, 0x0901, 0x0902, 0x0403, 0x00A0, 0x0307, 0x0304, 0x00A1, 0x000B, 0x030A, 0x0305, 0x00A2, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x02 */
+    {0x0900, 0x0901, 0x0902, 0x0303, 0x00A0, 0x004A, 0x0307, 0x0404, 0x00A1, 0x030A, 0x0305, 0x00A2, 0x001B, 0x0308, 0x0306, 0x000B, 0x002B, 0x0309, 0x0047, 0x003B, 0x040C},  /* mode 0x06 */
+    {0x0900, 0x0901, 0x0902, 0x0303, 0x00A0, 0x0048, 0x0307, 0x0304, 0x00A1, 0x000B, 0x030A, 0x0405, 0x00A2, 0x0308, 0x0306, 0x011B, 0x0309, 0x004B, 0x003B, 0x040C},  /* mode 0x0A */
+    {0x0800, 0x0048, 0x0801, 0x0047, 0x0802, 0x004B, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x0E */
+    {0x0700, 0x004A, 0x0048, 0x0701, 0x002B, 0x0047, 0x0702, 0x013B, 0x0503, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x12 */
+    {0x0700, 0x000B, 0x0048, 0x0701, 0x0057, 0x0047, 0x0702, 0x005A, 0x004B, 0x0403, 0x004A, 0x0307, 0x0504, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x16 */
+    {0x0700, 0x001B, 0x0048, 0x0701, 0x0058, 0x0047, 0x0702, 0x005B, 0x004B, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0505, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x1A */
+    {0x0500, 0x004A, 0x010B, 0x0048, 0x0501, 0x0057, 0x0058, 0x002B, 0x0047, 0x0502, 0x005A, 0x003B, 0x005B, 0x004B, 0x0503, 0x0307, 0x0504, 0x030A, 0x0505, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x1E */
+    {0x0900, 0x0901, 0x0902, 0x0903, 0x0904, 0x0905},  /* mode 0x03 */
+    {0x0900, 0x0901, 0x0902, 0x0803, 0x00A0, 0x0804, 0x00A1, 0x0805, 0x00A2},  /* mode 0x07 */
+    {0x0900, 0x0901, 0x0902, 0x0703, 0x11A0, 0x0704, 0x11A1, 0x0705, 0x11A2},  /* mode 0x0B */
+    {0x0900, 0x0901, 0x0902, 0x0303, 0x15A0, 0x0304, 0x15A1, 0x0305, 0x15A2},  /* mode 0x0F */
+};
+/* mode value, transformed, endpoint bits, delta bits R, G, B, regions, tokens */
+static const uint8_t kBc6Mode[14][8] = {
+    {0x00, 1, 10, 5, 5, 5, 2, 20},
+    {0x01, 1, 7, 6, 6, 6, 2, 22},
+    {0x02, 1, 11, 5, 4, 4, 2, 19},
+    {0x06, 1, 11, 4, 5, 4, 2, 21},
+    {0x0A, 1, 11, 4, 4, 5, 2, 20},
+    {0x0E, 1, 9, 5, 5, 5, 2, 20},
+    {0x12, 1, 8, 6, 5, 5, 2, 19},
+    {0x16, 1, 8, 5, 6, 5, 2, 22},
+    {0x1A, 1, 8, 5, 5, 6, 2, 22},
+    {0x1E, 0, 6, 6, 6, 6, 2, 23},
+    {0x03, 0, 10, 10, 10, 10, 1, 6},
+    {0x07, 1, 11, 9, 9, 9, 1, 9},
+    {0x0B, 1, 12, 8, 8, 8, 1, 9},
+    {0x0F, 1, 16, 4, 4, 4, 1, 9}};
+
+static int32_t bc6_sext(uint32_t v, unsigned n) {
+    v &= (n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u));
+    return (v >> (n - 1)) & 1u ? (int32_t)v - (int32_t)(1u << n) : (int32_t)v;
+}
+
+static int32_t bc6_unquantize(int32_t c, unsigned bits, int sgn) {
+    if (!sgn) {
+        if (bits >= 15) return c;
+        if (c == 0) return 0;
+        if (c == (int32_t)((1u << bits) - 1u)) return 0xFFFF;
+        return (int32_t)((((uint32_t)c << 16) + 0x8000u) >> bits);
+    }
+    if (bits >= 16) return c;
+    const int neg = c < 0;
+    int32_t m = neg ? -c : c, u;
+    if (m == 0)
+        u = 0;
+    else if (m >= (int32_t)((1u << (bits - 1)) - 1u))
+        u = 0x7FFF;
+    else
+        u = (int32_t)((((uint32_t)m << 15) + 0x4000u) >> (bits - 1));
+    return neg ? -u : u;
+}
+
+/* floor(v / 64) */
+static int32_t bc6_asr6(int32_t v) { return v >= 0 ? v >> 6 : -((-v - 1) >> 6) - 1; }
+
+static uint16_t bc6_finish(int32_t v, int sgn) {
+    if (!sgn) return (uint16_t)((v * 31) >> 6);
+    if (v < 0) {
+        const int32_t m = ((-v) * 31) >> 5;
+        return (uint16_t)(m ? (m | 0x8000) : 0);
+    }
+    return (uint16_t)((v * 31) >> 5);
+}
+
+static void bc6_block(const uint8_t* b, int sgn, uint16_t out[16][3]) {
+    unsigned pos = 0;
+    unsigned m = bc7_bits(b, &pos, 2);
+    if (m >= 2) m |= bc7_bits(b, &pos, 3) << 2;
+    int mi = -1;
+    for (int i = 0; i < 14; ++i)
+        if (kBc6Mode[i][0] == m) mi = i;
+    if (mi < 0) {
+        for (int i = 0; i < 16; ++i) out[i][0] = out[i][1] = out[i][2] = 0;
+        return;
+    }
+    const uint8_t* M = kBc6Mode[mi];
+    uint32_t f[13] = {0};
+    for (unsigned t = 0; t < M[7]; ++t) {
+        const unsigned tok = kBc6Tok[mi][t], fid = tok & 15u, lo = (tok >> 4) & 15u, n = ((tok >> 8) & 15u) + 1u;
+        uint32_t v = bc7_bits(b, &pos, n);
+        if (tok >> 12) {
+            uint32_t r = 0;
+            for (unsigned k = 0; k < n; ++k) r |= ((v >> k) & 1u) << (n - 1u - k);
+            v = r;
+        }
+        f[fid] |= v << lo;
+    }
+    const unsigned tr = M[1], bits = M[2], ns = M[6];
+    int32_t ep[4][3];
+    for (unsigned e = 0; e < 2 * ns; ++e)
+        for (unsigned c = 0; c < 3; ++c) {
+            const uint32_t raw = f[e * 3 + c];
+            int32_t v;
+            if (e == 0 || !tr) {
+                v = sgn ? bc6_sext(raw, bits) : (int32_t)raw;
+            } else {
+                const int32_t d = bc6_sext(raw, M[3 + c]);
+                const uint32_t sum = (uint32_t)((int32_t)f[c] + d) & ((1u << bits) - 1u);
+                v = sgn ? bc6_sext(sum, bits) : (int32_t)sum;
+            }
+            ep[e][c] = bc6_unquantize(v, bits, sgn);
+        }
+    const unsigned part = f[12] & 31u, anchor = ns == 2 ? kBc7A2[part] : 16u, ib = ns == 2 ? 3u : 4u;
+    for (unsigned i = 0; i < 16; ++i) {
+        const unsigned idx = bc7_bits(b, &pos, ib - ((i == 0 || i == anchor) ? 1u : 0u));
+        const unsigned s = ns == 2 ? ((kBc7P2[part] >> i) & 1u) : 0u;
+        const int32_t w = ns == 2 ? kBc7W3[idx] : kBc7W4[idx];
+        for (unsigned c = 0; c < 3; ++c)
+            out[i][c] = bc6_finish(bc6_asr6((64 - w) * ep[2 * s][c] + w * ep[2 * s + 1][c] + 32), sgn);
+    }
+}
+
+void orc_decode_bc6h(const uint8_t* blocks, uint32_t w, uint32_t h, int is_signed, uint16_t* rgb) {
+    const uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
+    for (uint32_t by = 0; by < bh; ++by)
+        for (uint32_t bx = 0; bx < bw; ++bx) {
+            uint16_t tex[16][3];
+            bc6_block(blocks + ((size_t)by * bw + bx) * 16, is_signed, tex);
+            for (int i = 0; i < 16; ++i) {
+                const uint32_t x = bx * 4 + (uint32_t)(i % 4), y = by * 4 + (uint32_t)(i / 4);
+                if (x < w && y < h)
+                    for (int c = 0; c < 3; ++c) rgb[((size_t)y * w + x) * 3 + c] = tex[i][c];
+            }
+        }
+}
+
 /*
  * JPEG, the pixel half (the reference links wuffs for JPEG,
  * src/vk_gltf_viewer/wuffs_implementation.cpp:1-5; it is absent, so parity

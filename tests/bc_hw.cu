@@ -2,16 +2,23 @@
 // the GPU's own texture unit.  The blocks go into a block-compressed CUDA
 // array, one thread per texel reads it through a point-sampled texture
 // object, and the normalised texels come back as RGBA8 (channels a format
-// lacks read as the texture unit returns them).
-//   bc_hw <format> <blocks.bin> <rgba.bin> <width> <height>
-// format: the library's numbering (VKGV_BC1-VKGV_BC5 = 1-5, VKGV_BC7 = 8); width,
-// height: multiples of 4.
+// lacks read as the texture unit returns them); BC6H texels come back as
+// four float32 values (R, G, B, A) each.
+//   bc_hw <format> <blocks.bin> <out.bin> <width> <height>
+// format: the library's numbering (VKGV_BC1-VKGV_BC5 = 1-5, VKGV_BC7 = 8,
+// VKGV_BC6H_UF16 = 9, VKGV_BC6H_SF16 = 10); width, height: multiples of 4.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
+
+__global__ void k_fetch_float(cudaTextureObject_t tex, unsigned w, unsigned h, float4* out) {
+    const unsigned x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= w || y >= h) return;
+    out[(size_t)y * w + x] = tex2D<float4>(tex, x + 0.5f, y + 0.5f);
+}
 
 __global__ void k_fetch(cudaTextureObject_t tex, unsigned w, unsigned h, unsigned* out) {
     const unsigned x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
@@ -53,6 +60,8 @@ int main(int argc, char** argv) {
             break;
         case 5: desc = cudaCreateChannelDesc(8, 8, 0, 0, cudaChannelFormatKindUnsignedBlockCompressed5); break;
         case 8: desc = cudaCreateChannelDesc(8, 8, 8, 8, cudaChannelFormatKindUnsignedBlockCompressed7); break;
+        case 9: desc = cudaCreateChannelDesc(16, 16, 16, 0, cudaChannelFormatKindUnsignedBlockCompressed6H); break;
+        case 10: desc = cudaCreateChannelDesc(16, 16, 16, 0, cudaChannelFormatKindSignedBlockCompressed6H); break;
         default: std::fprintf(stderr, "unknown format %d\n", format); return 2;
     }
     if (w == 0 || h == 0 || w % 4 || h % 4 || w > 4096 || h > 4096) {
@@ -78,16 +87,21 @@ int main(int argc, char** argv) {
     cudaTextureDesc td = {};
     td.addressMode[0] = td.addressMode[1] = cudaAddressModeClamp;
     td.filterMode = cudaFilterModePoint;
-    td.readMode = cudaReadModeNormalizedFloat;
+    const bool hdr = format == 9 || format == 10;
+    td.readMode = hdr ? cudaReadModeElementType : cudaReadModeNormalizedFloat;
     td.normalizedCoords = 0;
     cudaTextureObject_t tex = 0;
     CHECK(cudaCreateTextureObject(&tex, &res, &td, nullptr));
+    const size_t words = (size_t)w * h * (hdr ? 4 : 1);
     unsigned* out = nullptr;
-    CHECK(cudaMalloc(&out, (size_t)w * h * 4));
-    k_fetch<<<dim3((w + 127) / 128, h), 128>>>(tex, w, h, out);
+    CHECK(cudaMalloc(&out, words * 4));
+    if (hdr)
+        k_fetch_float<<<dim3((w + 127) / 128, h), 128>>>(tex, w, h, reinterpret_cast<float4*>(out));
+    else
+        k_fetch<<<dim3((w + 127) / 128, h), 128>>>(tex, w, h, out);
     CHECK(cudaGetLastError());
     CHECK(cudaDeviceSynchronize());
-    std::vector<unsigned> host((size_t)w * h);
+    std::vector<unsigned> host(words);
     CHECK(cudaMemcpy(host.data(), out, host.size() * 4, cudaMemcpyDeviceToHost));
     CHECK(cudaDestroyTextureObject(tex));
     CHECK(cudaFreeArray(array));

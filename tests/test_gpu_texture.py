@@ -1,6 +1,7 @@
-"""Block-compressed textures decoded on the device (k_decode_bc) are
-bit-identical to the oracle's decoder for BC1-BC5 at block-aligned and ragged
-sizes; JPEG pixels (k_jpeg_idct, k_jpeg_color) are bit-identical to the
+"""Block-compressed textures decoded on the device (k_decode_bc,
+k_decode_bc7, k_decode_bc6h) are bit-identical to the oracle's decoder for
+BC1-BC5, BC7 and BC6H at block-aligned and ragged sizes, and the BC6H and
+BC7 oracles to the GPU texture unit's own decode; JPEG pixels (k_jpeg_idct, k_jpeg_color) are bit-identical to the
 oracle's from the same coefficients; and a glTF asset whose base colour comes from an embedded DDS
 (MSFT_texture_dds) and PNG renders, textured, like the oracle frame of the
 same decoded images."""
@@ -80,10 +81,13 @@ def texture_unit(tmp_path_factory):
                    check=True, capture_output=True, timeout=300)
 
     def decode(fmt: int, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
+        """(h, w) uint32 RGBA8, or for BC6H (h, w, 4) float32 RGBA."""
         (tmp / "blocks.bin").write_bytes(blocks.tobytes())
         run = subprocess.run([str(exe), str(fmt), str(tmp / "blocks.bin"), str(tmp / "rgba.bin"), str(w), str(h)],
                              capture_output=True, text=True, timeout=120)
         assert run.returncode == 0, run.stderr
+        if fmt in (abi.BC6H_UF16, abi.BC6H_SF16):
+            return np.fromfile(tmp / "rgba.bin", np.float32).reshape(h, w, 4)
         return np.fromfile(tmp / "rgba.bin", np.uint32).reshape(h, w)
 
     return decode
@@ -103,6 +107,72 @@ def test_bc7_oracle_matches_texture_unit(texture_unit):
         blk = blocks.reshape(h // 4, w // 4, 16)[by, bx]
         raise AssertionError(f"{len(bad)} texels differ; first at {tuple(bad[0])}: texture unit "
                              f"{hw[tuple(bad[0])]:08x}, oracle {exp[tuple(bad[0])]:08x}, block {blk.tobytes().hex()}")
+
+
+# The 5-bit mode fields BC6H defines (0 and 1 are 2-bit modes), then the
+# four reserved ones, which decode to 0.
+_BC6H_MODES = [0x00, 0x01, 0x02, 0x06, 0x0A, 0x0E, 0x12, 0x16, 0x1A, 0x1E, 0x03, 0x07, 0x0B, 0x0F,
+               0x13, 0x17, 0x1B, 0x1F]
+
+
+def _bc6h_blocks(rng, n: int) -> np.ndarray:
+    """n random BC6H blocks, every mode field value equally often: any bits
+    after the mode field are a valid block."""
+    blocks = rng.integers(0, 256, size=(n, 16), dtype=np.uint8)
+    modes = np.array(_BC6H_MODES, np.uint8)[np.arange(n) % len(_BC6H_MODES)]
+    rng.shuffle(modes)
+    keep = np.where(modes < 2, 0xFC, 0xE0).astype(np.uint8)  # 2- or 5-bit field
+    blocks[:, 0] = (blocks[:, 0] & keep) | modes
+    return blocks.reshape(-1)
+
+
+def _half_to_f32(bits: np.ndarray) -> np.ndarray:
+    return bits.view(np.float16).astype(np.float32)
+
+
+@pytest.mark.parametrize("fmt", [abi.BC6H_UF16, abi.BC6H_SF16])
+@pytest.mark.parametrize("size", [(4, 4), (37, 21), (256, 128), (3, 5), (1024, 1000)])
+def test_bc6h_decode_matches_oracle(renderer, fmt, size):
+    """k_decode_bc6h's float32 RGB is the oracle's binary16 texels, bit for
+    bit (signed zeros included), at block-aligned and ragged sizes."""
+    w, h = size
+    rng = np.random.default_rng(w * 13 + h + fmt)
+    blocks = _bc6h_blocks(rng, ((w + 3) // 4) * ((h + 3) // 4))
+    got = texture.decode_bc6h(renderer, fmt, blocks, w, h)
+    torch.cuda.synchronize()
+    exp = _half_to_f32(ob.decode_bc6h(blocks, w, h, fmt == abi.BC6H_SF16))
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), exp.view(np.uint32))
+
+
+@pytest.mark.parametrize("fmt", [abi.BC6H_UF16, abi.BC6H_SF16])
+def test_bc6h_oracle_matches_texture_unit(texture_unit, fmt):
+    """Pins the BC6H oracle (its fourteen header layouts, sign extension,
+    delta transform, unquantisation, weights and binary16 scaling) to the GPU
+    texture unit's BC6H decode of the same random blocks of every mode."""
+    w, h = 256, 144  # 2,304 blocks, 128 per mode field value
+    blocks = _bc6h_blocks(np.random.default_rng(606 + fmt), (w // 4) * (h // 4))
+    hw = texture_unit(fmt, blocks, w, h)
+    assert (hw[..., 3] == 1.0).all()
+    exp = ob.decode_bc6h(blocks, w, h, fmt == abi.BC6H_SF16)
+    got = hw[..., :3].astype(np.float16).view(np.uint16)
+    bad = np.argwhere((got != exp).any(axis=2))
+    assert not len(bad), f"{len(bad)} texels differ; first at {tuple(bad[0])}"
+
+
+def test_bc6h_through_load_image(renderer):
+    """BC6H in a DDS (DX10 header, DXGI 95 / 96) and in a KTX2 (vkFormat 143
+    / 144) decodes through load_image to the oracle's texels, float32 RGB."""
+    from test_texture_decode import _dds, _ktx2
+
+    blocks = _bc6h_blocks(np.random.default_rng(78), 10 * 6)
+    for data, kind, signed in ((_dds(b"DX10", 37, 22, blocks.tobytes(), dxgi=95), abi.IMAGE_DDS, False),
+                               (_dds(b"DX10", 37, 22, blocks.tobytes(), dxgi=96), abi.IMAGE_DDS, True),
+                               (_ktx2(143, 37, 22, blocks.tobytes()), abi.IMAGE_KTX2, False),
+                               (_ktx2(144, 37, 22, blocks.tobytes()), abi.IMAGE_KTX2, True)):
+        got = texture.load_image(data, kind, renderer)
+        assert got.dtype == np.float32 and got.shape == (22, 37, 3)
+        exp = _half_to_f32(ob.decode_bc6h(blocks, 37, 22, signed))
+        assert np.array_equal(got.view(np.uint32), exp.view(np.uint32))
 
 
 # Largest per-channel difference between the texture unit and the pinned
@@ -232,7 +302,10 @@ def test_jpeg_through_load_image_and_freed_source(renderer):
     assert np.array_equal(got.cpu().numpy().view(np.uint32)[..., 0], exp)
 
 
-def test_gltf_with_dds_and_png_textures(renderer, tmp_path):
+@pytest.mark.parametrize("dds_format", ["bc3", "bc6h"])
+def test_gltf_with_dds_and_png_textures(renderer, tmp_path, dds_format):
+    """The DDS texture is BC3 (an RGBA8 texture) or BC6H UF16 (a linear
+    float32 RGB texture)."""
     base = small_grid()
     mesh = base.meshes[0]
     world = grid_world(mesh.meshlet_count, mesh.position_scale, grid=(4, 4, 2), animated=False)
@@ -244,8 +317,12 @@ def test_gltf_with_dds_and_png_textures(renderer, tmp_path):
     for material in (0, 1):  # mesh 0 uses the DDS texture, mesh 1 the PNG one
         b.add("meshes", {"primitives": [{"attributes": {"POSITION": pos, "TEXCOORD_0": uv}, "indices": idx,
                                          "material": material}]})
-    dds_blocks = rng.integers(0, 256, size=16 * 16 * 16, dtype=np.uint8)  # 64 x 64 texels of BC3
-    dds = _dds(b"DXT5", 64, 64, dds_blocks.tobytes())
+    if dds_format == "bc3":
+        dds_blocks = rng.integers(0, 256, size=16 * 16 * 16, dtype=np.uint8)  # 64 x 64 texels of BC3
+        dds = _dds(b"DXT5", 64, 64, dds_blocks.tobytes())
+    else:
+        dds_blocks = _bc6h_blocks(rng, 16 * 16)  # 64 x 64 texels of BC6H UF16
+        dds = _dds(b"DX10", 64, 64, dds_blocks.tobytes(), dxgi=95)
     png_pixels = rng.integers(0, 256, size=(32, 48, 4))
     png = encode(png_pixels, 6, 8, rng)
     img_dds = b.add("images", {"bufferView": b._view(dds), "mimeType": "image/vnd-ms.dds"})
@@ -269,8 +346,14 @@ def test_gltf_with_dds_and_png_textures(renderer, tmp_path):
 
     host, iworld = gltf.load(path, images=True, renderer=renderer)
     assert len(host.textures) == 2
-    assert np.array_equal(host.textures[0].data.reshape(64, 64, 4).view(np.uint32)[..., 0],
-                          ob.decode_bc(abi.BC3, dds_blocks, 64, 64))
+    if dds_format == "bc3":
+        assert host.textures[0].format == abi.TEXTURE_RGBA8
+        assert np.array_equal(host.textures[0].data.reshape(64, 64, 4).view(np.uint32)[..., 0],
+                              ob.decode_bc(abi.BC3, dds_blocks, 64, 64))
+    else:
+        assert host.textures[0].format == abi.TEXTURE_RGB32F
+        exp = _half_to_f32(ob.decode_bc6h(dds_blocks, 64, 64, False))
+        assert np.array_equal(host.textures[0].data.view(np.uint32), exp.view(np.uint32))
     assert np.array_equal(host.textures[1].data, png_pixels.astype(np.uint8))
     assert host.materials[1]["albedo_index"] == 0 and host.materials[2]["albedo_index"] == 1
     dev, dw = gltf.device_scene(renderer, host, iworld)

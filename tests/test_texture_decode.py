@@ -108,8 +108,12 @@ def test_dds_headers(built):
     assert (info.format, info.srgb, info.data_size) == (abi.BC7, 0, 32)
     info, _ = texture.parse_dds(_dds(b"DX10", 8, 4, bytes(32), dxgi=99))  # BC7_UNORM_SRGB
     assert (info.format, info.srgb) == (abi.BC7, 1)
+    info, _ = texture.parse_dds(_dds(b"DX10", 8, 4, bytes(32), dxgi=95))  # BC6H_UF16
+    assert (info.format, info.srgb, info.data_size) == (abi.BC6H_UF16, 0, 32)
+    info, _ = texture.parse_dds(_dds(b"DX10", 5, 5, bytes(64), dxgi=96))  # BC6H_SF16
+    assert (info.format, info.data_size) == (abi.BC6H_SF16, 64)
     with pytest.raises(abi.VkgvError):
-        texture.parse_dds(_dds(b"DX10", 4, 4, bytes(16), dxgi=95))  # BC6H is not decoded
+        texture.parse_dds(_dds(b"DX10", 4, 4, bytes(16), dxgi=94))  # BC6H_TYPELESS: no sign to read it with
 
 
 def _rgba(r, g, b, a=255):
@@ -169,6 +173,9 @@ def test_ktx2_headers(built):
     for vk, srgb in ((145, 0), (146, 1)):
         info, got = texture.parse_ktx2(_ktx2(vk, 5, 4, bytes(range(32))))
         assert (info.format, info.srgb, got.tobytes()) == (abi.BC7, srgb, bytes(range(32)))
+    for vk, fmt in ((143, abi.BC6H_UF16), (144, abi.BC6H_SF16)):
+        info, got = texture.parse_ktx2(_ktx2(vk, 5, 4, bytes(range(32))))
+        assert (info.format, info.srgb, got.tobytes()) == (fmt, 0, bytes(range(32)))
     rgba = bytes(range(256)) * 3
     info, got = texture.parse_ktx2(_ktx2(43, 16, 12, rgba))
     assert (info.format, info.srgb, info.data_size) == (abi.RGBA8, 1, 768)
@@ -178,12 +185,58 @@ def test_ktx2_headers(built):
            _ktx2(133, 4, 4, bytes(8), scheme=1),       # BasisLZ supercompression
            _ktx2(133, 4, 4, bytes(48), faces=6),       # cube map
            _ktx2(140, 4, 4, bytes(8)),                 # BC4 SNORM
-           _ktx2(143, 4, 4, bytes(16)),                # BC6H
            _ktx2(133, 16, 16, bytes(8)),               # too little data
            b"DDS " + bytes(200)]
     for data in bad:
         with pytest.raises(abi.VkgvError):
             texture.parse_ktx2(data)
+
+
+def _bc6h_kat_block(v: int) -> np.ndarray:
+    return np.frombuffer(v.to_bytes(16, "little"), np.uint8)
+
+
+def test_oracle_bc6h_known_answers(built):
+    """BC6H answers derived by hand from the format's steps (not from the
+    oracle).  Mode 0x03: one region, 10-bit untransformed end points
+    (R, G, B) = (1023, 0, 512) and (0, 1023, 512), texels 0, 1, 2 at indices
+    0, 15, 7 (weights 0, 64, 30).  Unsigned: 1023 -> 0xFFFF, 512 ->
+    ((512 << 16) + 0x8000) >> 10 = 32800, texel 2 R = (34 * 65535 + 32) >> 6
+    = 34815, G = (30 * 65535 + 32) >> 6 = 30720; binary16 = v * 31 >> 6.
+    Signed: 1023 is -1 -> -(((1 << 15) + 0x4000) >> 9) = -96, 512 is -512 ->
+    -0x7FFF; texel 2 R = floor(-3232 / 64) = -51 -> -(51 * 31 >> 5) = -49,
+    G = floor(-2848 / 64) = -45 -> -43."""
+    v = 0x03 | 1023 << 5 | 0 << 15 | 512 << 25 | 0 << 35 | 1023 << 45 | 512 << 55 | 15 << 68 | 7 << 72
+    blk = _bc6h_kat_block(v)
+    uf = ob.decode_bc6h(blk, 4, 4, False).reshape(16, 3)
+    assert uf[:3].tolist() == [[0x7BFF, 0, 0x3E0F], [0, 0x7BFF, 0x3E0F], [0x41DF, 0x3A20, 0x3E0F]]
+    assert uf[3:].tolist() == [[0x7BFF, 0, 0x3E0F]] * 13
+    sf = ob.decode_bc6h(blk, 4, 4, True).reshape(16, 3)
+    assert sf[:3].tolist() == [[0x805D, 0, 0xFBFF], [0, 0x805D, 0xFBFF], [0x8031, 0x802B, 0xFBFF]]
+    # Mode 0x0F stores the base end point's bits 10-15 reversed: block bit
+    # 39 is R[15], so R = 0x8000 (unquantised as is at 16 bits), binary16
+    # 0x8000 * 31 >> 6 = 0x3E00 (1.5) on every texel (index 0)
+    uf = ob.decode_bc6h(_bc6h_kat_block(0x0F | 1 << 39), 4, 4, False).reshape(16, 3)
+    assert uf.tolist() == [[0x3E00, 0, 0]] * 16
+    # a reserved mode decodes to 0; an interpolated -0 is +0
+    assert not ob.decode_bc6h(_bc6h_kat_block(0x13 | 0xFFFF << 20), 4, 4, True).any()
+
+
+def test_oracle_bc6h_matches_texture_unit_golden(built):
+    """The BC6H oracle against the GPU texture unit's decodes of seeded
+    blocks of every mode field value, committed by
+    tests/golden/make_bc6h_golden.py: identical binary16 texels, UF16 and
+    SF16."""
+    import base64
+    import json
+    from pathlib import Path
+
+    g = json.loads((Path(__file__).resolve().parent / "golden" / "bc6h_texture_unit.json").read_text())
+    w, h = g["width"], g["height"]
+    blocks = np.frombuffer(base64.b64decode(g["blocks"]), np.uint8)
+    for key, signed in (("uf16", False), ("sf16", True)):
+        exp = np.frombuffer(base64.b64decode(g[key]), np.uint16).reshape(h, w, 3)
+        assert np.array_equal(ob.decode_bc6h(blocks, w, h, signed), exp), key
 
 
 def test_oracle_bc1_opaque_known_answer(built):

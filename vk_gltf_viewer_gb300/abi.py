@@ -209,7 +209,7 @@ class JpegInfo(C.Structure):
 GLTF_TEXTURE_REFERENCES = 1
 GLTF_IMAGES = 2
 IMAGE_UNKNOWN, IMAGE_PNG, IMAGE_DDS, IMAGE_JPEG, IMAGE_KTX2 = 0, 1, 2, 3, 4
-BC1, BC2, BC3, BC4, BC5, BC1_OPAQUE, RGBA8, BC7 = 1, 2, 3, 4, 5, 6, 7, 8
+BC1, BC2, BC3, BC4, BC5, BC1_OPAQUE, RGBA8, BC7, BC6H_UF16, BC6H_SF16 = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
 PATH_TRANSLATION, PATH_ROTATION, PATH_SCALE, PATH_WEIGHTS = 1, 2, 3, 4
 INTERP_LINEAR, INTERP_STEP, INTERP_CUBICSPLINE = 0, 1, 2
 MAX_NODE_DEPTH = 64
@@ -281,6 +281,7 @@ _PROTOS = {
     "vkgv_dds_parse": (C.c_int, [_P, _U64, C.POINTER(DdsInfo)]),
     "vkgv_ktx2_parse": (C.c_int, [_P, _U64, C.POINTER(DdsInfo)]),
     "vkgv_decode_bc": (C.c_int, [_P, _U32, _U64, _U32, _U32, _U64, _P]),
+    "vkgv_decode_bc6h": (C.c_int, [_P, _U32, _U64, _U32, _U32, _U64, _P]),
     "vkgv_jpeg_decode_coefficients": (C.c_int, [_P, _U64, C.POINTER(_P), C.c_char_p, _U32]),
     "vkgv_jpeg_get_info": (C.c_int, [_P, C.POINTER(JpegInfo)]),
     "vkgv_jpeg_get_coefficients": (C.c_int, [_P, _U32, C.POINTER(_P)]),

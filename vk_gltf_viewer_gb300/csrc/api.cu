@@ -703,6 +703,19 @@ int vkgv_decode_bc(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t wid
     return check_launch(ctx);
 }
 
+int vkgv_decode_bc6h(vkgv_ctx* ctx, uint32_t format, uint64_t blocks, uint32_t width, uint32_t height,
+                     uint64_t rgb_out, void* stream_) {
+    if (!ctx) return VKGV_INVALID_ARG;
+    if (format != VKGV_BC6H_UF16 && format != VKGV_BC6H_SF16) return fail(ctx, VKGV_INVALID_ARG, "not a BC6H format");
+    if (width == 0 || height == 0) return VKGV_OK;
+    if (width > 16384 || height > 16384) return fail(ctx, VKGV_LIMIT_EXCEEDED, "texture edge exceeds 16384");
+    if (!blocks || !rgb_out || (blocks & 15u) || (rgb_out & 3u))
+        return fail(ctx, VKGV_INVALID_ARG, "blocks must be 16-byte aligned and rgb_out 4-byte aligned");
+    launch_decode_bc6h(reinterpret_cast<const uint8_t*>(blocks), format == VKGV_BC6H_SF16, width, height,
+                       reinterpret_cast<float*>(rgb_out), reinterpret_cast<cudaStream_t>(stream_));
+    return check_launch(ctx);
+}
+
 int vkgv_jpeg_to_rgba(vkgv_ctx* ctx, const vkgv_jpeg* jpeg, uint64_t rgba_out, void* stream_) {
     if (!ctx) return VKGV_INVALID_ARG;
     vkgv_jpeg_info I;

@@ -579,6 +579,8 @@ extern "C" int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* ou
             case 80: fmt = VKGV_BC4; break;
             case 83: fmt = VKGV_BC5; break;
             case 98: case 99: fmt = VKGV_BC7; break;  // DXGI_FORMAT_BC7_UNORM(_SRGB)
+            case 95: fmt = VKGV_BC6H_UF16; break;     // DXGI_FORMAT_BC6H_UF16
+            case 96: fmt = VKGV_BC6H_SF16; break;     // DXGI_FORMAT_BC6H_SF16
             default: return VKGV_INVALID_ARG;
         }
         out->srgb = (dxgi == 72 || dxgi == 75 || dxgi == 78 || dxgi == 99) ? 1u : 0u;
@@ -623,6 +625,8 @@ extern "C" int vkgv_ktx2_parse(const void* data, uint64_t size, vkgv_dds_info* o
         case 141: fmt = VKGV_BC5; break;                   // BC5_UNORM_BLOCK
         case 145: fmt = VKGV_BC7; break;                   // BC7_UNORM_BLOCK
         case 146: fmt = VKGV_BC7; srgb = 1; break;         // BC7_SRGB_BLOCK
+        case 143: fmt = VKGV_BC6H_UF16; break;             // BC6H_UFLOAT_BLOCK
+        case 144: fmt = VKGV_BC6H_SF16; break;             // BC6H_SFLOAT_BLOCK
         case 37: fmt = VKGV_RGBA8; break;                  // R8G8B8A8_UNORM
         case 43: fmt = VKGV_RGBA8; srgb = 1; break;        // R8G8B8A8_SRGB
         default: return VKGV_INVALID_ARG;

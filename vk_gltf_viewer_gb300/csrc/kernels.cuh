@@ -196,5 +196,7 @@ void launch_jpeg_idct(const int16_t* coef, uint32_t blocks_w, uint32_t blocks_h,
 void launch_jpeg_color(const JpegPlanes& P, uint32_t* rgba, cudaStream_t stream);
 void launch_decode_bc(const uint8_t* blocks, uint32_t format, uint32_t w, uint32_t h, uint32_t* rgba,
                       cudaStream_t stream);
+void launch_decode_bc6h(const uint8_t* blocks, bool is_signed, uint32_t w, uint32_t h, float* rgb,
+                        cudaStream_t stream);
 
 }  // namespace vkgv

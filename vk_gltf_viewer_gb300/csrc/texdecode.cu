@@ -1,6 +1,6 @@
 // Block-compressed texture decode on the device: BC1-BC5 (the DXT1-5 /
 // RGTC formats a DDS base-colour texture holds, MSFT_texture_dds) and BC7 into RGBA8
-// for the textured resolve.  The reference loads no images
+// for the textured resolve, and BC6H into float32 RGB.  The reference loads no images
 // (src/vk_gltf_viewer/assets.cpp:467-471); the formats are the published
 // ones, with the interpolation rounding, which they leave to the
 // implementation, pinned here and in the oracle:
@@ -17,6 +17,8 @@
 //   BC4 -> (r, 0, 0, 255), BC5 -> (r, g, 0, 255)
 // One thread per block row: the four rows of a block share its load and
 // each writes 4 texels, so a warp stores four contiguous 128-byte rows.
+#include <cuda_fp16.h>
+
 #include "kernels.cuh"
 
 namespace vkgv {
@@ -367,6 +369,196 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc7(const uint8_t*
     }
 }
 
+// ------------------------------------------------------------------- BC6H
+// BC6H (BPTC float; UF16 unsigned, SF16 signed) into float32 RGB (a linear
+// VKGV_TEXTURE_RGB32F texture): the published format and the steps the
+// oracle restates (oracle/texture.c), with the same tables.  A 2-bit mode
+// (values 0, 1) or a 5-bit one selects one of fourteen header layouts
+// (tokens: field = endpoint w/x/y/z x channel R/G/B or 12 = partition,
+// lowest field bit, bit count, reversed), transformed modes add signed
+// deltas to the base endpoint, endpoints are unquantised to 16 bits, texels
+// interpolated with the 3- or 4-bit BC7 weights and scaled to binary16
+// (unsigned v * 31 >> 6; signed magnitude * 31 >> 5, sign only on a
+// non-zero result).  Reserved modes decode to 0.  Four lanes per block, one
+// row each, like k_decode_bc7; each lane parses the header itself.
+__constant__ uint16_t c_bc6_tok[14][23] = {
+    {0x0047, 0x0048, 0x004B, 0x0900, 0x0901, 0x0902, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x00 */
+    {0x0057, 0x014A, 0x0600, 0x010B, 0x0048, 0x0601, 0x0058, 0x002B, 0x0047, 0x0602, 0x003B, 0x005B, 0x004B, 0x0503, 0x0307, 0x0504, 0x030A, 0x0505, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x01 */
+    {0x0900, 0x0901, 0x0902, 0x0403, 0x00A0, 0x0307, 0x0304, 0x00A1, 0x000B, 0x030A, 0x0305, 0x00A2, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x02 */
+    {0x0900, 0x0901, 0x0902, 0x0303, 0x00A0, 0x004A, 0x0307, 0x0404, 0x00A1, 0x030A, 0x0305, 0x00A2, 0x001B, 0x0308, 0x0306, 0x000B, 0x002B, 0x0309, 0x0047, 0x003B, 0x040C},  /* mode 0x06 */
+    {0x0900, 0x0901, 0x0902, 0x0303, 0x00A0, 0x0048, 0x0307, 0x0304, 0x00A1, 0x000B, 0x030A, 0x0405, 0x00A2, 0x0308, 0x0306, 0x011B, 0x0309, 0x004B, 0x003B, 0x040C},  /* mode 0x0A */
+    {0x0800, 0x0048, 0x0801, 0x0047, 0x0802, 0x004B, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x0E */
+    {0x0700, 0x004A, 0x0048, 0x0701, 0x002B, 0x0047, 0x0702, 0x013B, 0x0503, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x12 */
+    {0x0700, 0x000B, 0x0048, 0x0701, 0x0057, 0x0047, 0x0702, 0x005A, 0x004B, 0x0403, 0x004A, 0x0307, 0x0504, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x16 */
+    {0x0700, 0x001B, 0x0048, 0x0701, 0x0058, 0x0047, 0x0702, 0x005B, 0x004B, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0505, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x1A */
+    {0x0500, 0x004A, 0x010B, 0x0048, 0x0501, 0x0057, 0x0058, 0x002B, 0x0047, 0x0502, 0x005A, 0x003B, 0x005B, 0x004B, 0x0503, 0x0307, 0x0504, 0x030A, 0x0505, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x1E */
+    {0x0900, 0x0901, 0x0902, 0x0903, 0x0904, 0x0905},  /* mode 0x03 */
+    {0x0900, 0x0901, 0x0902, 0x0803, 0x00A0, 0x0804, 0x00A1, 0x0805, 0x00A2},  /* mode 0x07 */
+    {0x0900, 0x0901, 0x0902, 0x0703, 0x11A0, 0x0704, 0x11A1, 0x0705, 0x11A2},  /* mode 0x0B */
+    {0x0900, 0x0901, 0x0902, 0x0303, 0x15A0, 0x0304, 0x15A1, 0x0305, 0x15A2},  /* mode 0x0F */
+};
+// mode value, transformed, endpoint bits, delta bits R, G, B, regions, tokens
+__constant__ uint8_t c_bc6_mode[14][8] = {
+    {0x00, 1, 10, 5, 5, 5, 2, 20}, {0x01, 1, 7, 6, 6, 6, 2, 22},   {0x02, 1, 11, 5, 4, 4, 2, 19},
+    {0x06, 1, 11, 4, 5, 4, 2, 21}, {0x0A, 1, 11, 4, 4, 5, 2, 20},  {0x0E, 1, 9, 5, 5, 5, 2, 20},
+    {0x12, 1, 8, 6, 5, 5, 2, 19},  {0x16, 1, 8, 5, 6, 5, 2, 22},   {0x1A, 1, 8, 5, 5, 6, 2, 22},
+    {0x1E, 0, 6, 6, 6, 6, 2, 23},  {0x03, 0, 10, 10, 10, 10, 1, 6}, {0x07, 1, 11, 9, 9, 9, 1, 9},
+    {0x0B, 1, 12, 8, 8, 8, 1, 9},  {0x0F, 1, 16, 4, 4, 4, 1, 9}};
+
+struct Bc6Tables {
+    uint16_t tok[14][23];
+    uint8_t mode[14][8];
+    int8_t row[32];  // 5-bit mode field -> mode row, -1 for a reserved mode
+    uint16_t p2[32];
+    uint8_t a2[32];
+    uint8_t w3[8], w4[16];
+};
+
+__device__ void bc6_load_tables(Bc6Tables& t) {
+    for (uint32_t i = threadIdx.x; i < 14 * 23; i += blockDim.x) t.tok[i / 23][i % 23] = c_bc6_tok[i / 23][i % 23];
+    for (uint32_t i = threadIdx.x; i < 14 * 8; i += blockDim.x) t.mode[i / 8][i % 8] = c_bc6_mode[i / 8][i % 8];
+    for (uint32_t i = threadIdx.x; i < 32; i += blockDim.x) {
+        // a field whose two low bits are 0 or 1 is a 2-bit mode
+        const uint32_t m = (i & 3u) < 2u ? (i & 3u) : i;
+        int8_t r = -1;
+        for (int k = 0; k < 14; ++k)
+            if (c_bc6_mode[k][0] == m) r = (int8_t)k;
+        t.row[i] = r;
+        t.p2[i] = c_bc7_p2[i];
+        t.a2[i] = c_bc7_a2[i];
+    }
+    for (uint32_t i = threadIdx.x; i < 8; i += blockDim.x) t.w3[i] = c_bc7_w[1][i];
+    for (uint32_t i = threadIdx.x; i < 16; i += blockDim.x) t.w4[i] = c_bc7_w[2][i];
+}
+
+__device__ __forceinline__ int32_t bc6_sext(uint32_t v, uint32_t n) {
+    const uint32_t s = 32u - n;
+    return (int32_t)(v << s) >> s;
+}
+
+__device__ __forceinline__ int32_t bc6_unquantize(int32_t c, uint32_t bits, bool sgn) {
+    if (!sgn) {
+        if (bits >= 15u) return c;
+        if (c == 0) return 0;
+        if (c == (int32_t)((1u << bits) - 1u)) return 0xFFFF;
+        return (int32_t)((((uint32_t)c << 16) + 0x8000u) >> bits);
+    }
+    if (bits >= 16u) return c;
+    const bool neg = c < 0;
+    const int32_t m = neg ? -c : c;
+    int32_t u;
+    if (m == 0) u = 0;
+    else if (m >= (int32_t)((1u << (bits - 1u)) - 1u)) u = 0x7FFF;
+    else u = (int32_t)((((uint32_t)m << 15) + 0x4000u) >> (bits - 1u));
+    return neg ? -u : u;
+}
+
+__device__ __forceinline__ uint16_t bc6_finish(int32_t v, bool sgn) {
+    if (!sgn) return (uint16_t)((v * 31) >> 6);
+    if (v < 0) {
+        const int32_t m = ((-v) * 31) >> 5;
+        return (uint16_t)(m ? (m | 0x8000) : 0);
+    }
+    return (uint16_t)((v * 31) >> 5);
+}
+
+// Row r (4 texels, R, G, B as float32) of one BC6H block.
+__device__ __forceinline__ void bc6_row(const Bc6Tables& T, const uint4& q, uint32_t r, bool sgn, float out[12]) {
+    const uint64_t lo = (uint64_t)q.x | ((uint64_t)q.y << 32), hi = (uint64_t)q.z | ((uint64_t)q.w << 32);
+    const int mi = T.row[q.x & 31u];
+    if (mi < 0) {
+#pragma unroll
+        for (int k = 0; k < 12; ++k) out[k] = 0.0f;
+        return;
+    }
+    const uint8_t* M = T.mode[mi];
+    uint32_t f[13];
+#pragma unroll
+    for (int k = 0; k < 13; ++k) f[k] = 0u;
+    uint32_t pos = (q.x & 3u) < 2u ? 2u : 5u;
+    for (uint32_t t = 0; t < M[7]; ++t) {
+        const uint32_t tok = T.tok[mi][t], n = ((tok >> 8) & 15u) + 1u;
+        uint32_t v = bc7_bits(lo, hi, pos, n);
+        pos += n;
+        if (tok >> 12) v = __brev(v) >> (32u - n);
+        const uint32_t fid = tok & 15u, sh = (tok >> 4) & 15u;
+        // a dynamic index into f would put it in local memory
+#pragma unroll
+        for (int k = 0; k < 13; ++k)
+            if ((uint32_t)k == fid) f[k] |= v << sh;
+    }
+    const bool tr = M[1] != 0;
+    const uint32_t bits = M[2], ns = M[6];
+    int32_t ep[4][3];
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const uint32_t raw = f[e * 3 + c];
+            int32_t v;
+            if (e == 0 || !tr) {
+                v = sgn ? bc6_sext(raw, bits) : (int32_t)raw;
+            } else {
+                const uint32_t sum = (f[c] + (uint32_t)bc6_sext(raw, M[3 + c])) & ((1u << bits) - 1u);
+                v = sgn ? bc6_sext(sum, bits) : (int32_t)sum;
+            }
+            ep[e][c] = bc6_unquantize(v, bits, sgn);
+        }
+    const uint32_t part = f[12] & 31u, anchor = ns == 2u ? T.a2[part] : 16u, ib = ns == 2u ? 3u : 4u;
+    // index bits of texels 4r .. 4r + 3: the header, then ib bits a texel,
+    // one less for texel 0 and the second region's anchor
+    uint32_t ipos = pos + 4u * r * ib - (r > 0 ? 1u : 0u) - ((anchor < 4u * r) ? 1u : 0u);
+#pragma unroll
+    for (int x = 0; x < 4; ++x) {
+        const uint32_t i = 4u * r + (uint32_t)x;
+        const uint32_t n = ib - ((i == 0u || i == anchor) ? 1u : 0u);
+        const uint32_t idx = bc7_bits(lo, hi, ipos, n);
+        ipos += n;
+        const uint32_t s = ns == 2u ? ((T.p2[part] >> i) & 1u) : 0u;
+        const int32_t w = ns == 2u ? T.w3[idx] : T.w4[idx];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int32_t e0 = s ? ep[2][c] : ep[0][c], e1 = s ? ep[3][c] : ep[1][c];
+            const int32_t v = ((64 - w) * e0 + w * e1 + 32) >> 6;  // arithmetic: floor division
+            out[3 * x + c] = __half2float(__ushort_as_half(bc6_finish(v, sgn)));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc6h(const uint8_t* __restrict__ blocks, uint32_t w,
+                                                                   uint32_t h, uint32_t is_signed,
+                                                                   float* __restrict__ rgb) {
+    __shared__ Bc6Tables T;
+    bc6_load_tables(T);
+    pdl_begin();
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t r = lane & 3u;
+    const uint32_t bx = (blockIdx.x * kDecodeWarps + warp) * 8 + (lane >> 2);
+    const uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
+    const bool sgn = is_signed != 0;
+    // the header parse dominates, so each block row is loaded when needed
+#pragma unroll 1
+    for (int k = 0; k < kDecodeDepth; ++k) {
+        const uint32_t by = blockIdx.y * kDecodeDepth + k, y = by * 4 + r;
+        if (bx >= bw || by >= bh || y >= h) continue;
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(blocks) + ((size_t)by * bw + bx));
+        float t[12];
+        bc6_row(T, q, r, sgn, t);
+        float* dst = rgb + ((size_t)y * w + (size_t)bx * 4) * 3;
+        if (bx * 4 + 4 <= w && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+            float4* d4 = reinterpret_cast<float4*>(dst);
+            __stcs(d4, make_float4(t[0], t[1], t[2], t[3]));
+            __stcs(d4 + 1, make_float4(t[4], t[5], t[6], t[7]));
+            __stcs(d4 + 2, make_float4(t[8], t[9], t[10], t[11]));
+        } else {
+            for (uint32_t x = 0; x < 4 && bx * 4 + x < w; ++x)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) __stcs(dst + 3 * x + c, t[3 * x + c]);
+        }
+    }
+}
+
 // ------------------------------------------------------------------- JPEG
 // The device half of a JPEG decode (the host half, jpeg.cpp, writes the
 // dequantized coefficient planes).  Pinned fixed-point arithmetic, shared
@@ -468,6 +660,14 @@ void launch_jpeg_idct(const int16_t* coef, uint32_t blocks_w, uint32_t blocks_h,
 
 void launch_jpeg_color(const JpegPlanes& P, uint32_t* rgba, cudaStream_t stream) {
     launch_pdl(k_jpeg_color, dim3((P.width + 31) / 32, (P.height + 7) / 8), dim3(256), 0, stream, P, rgba);
+}
+
+void launch_decode_bc6h(const uint8_t* blocks, bool is_signed, uint32_t w, uint32_t h, float* rgb,
+                        cudaStream_t stream) {
+    const uint32_t bw = (w + 3) / 4, bh = (h + 3) / 4;
+    const uint32_t per_cta = 8 * kDecodeWarps;
+    const dim3 grid((bw + per_cta - 1) / per_cta, (bh + kDecodeDepth - 1) / kDecodeDepth);
+    launch_pdl(k_decode_bc6h, grid, dim3(kDecodeWarps * 32), 0, stream, blocks, w, h, is_signed ? 1u : 0u, rgb);
 }
 
 void launch_decode_bc(const uint8_t* blocks, uint32_t format, uint32_t w, uint32_t h, uint32_t* rgba,

@@ -56,7 +56,8 @@ def load(path, texture_references: bool = False, images: bool = False,
                     rgba = np.full((1, 1, 4), 255, np.uint8)  # a texture without an image samples white
                 else:
                     rgba = texture.load_image(C.string_at(gi.data, gi.size), gi.kind, renderer)
-                textures.append(scene.Texture(np.ascontiguousarray(rgba), abi.TEXTURE_RGBA8))
+                fmt = abi.TEXTURE_RGB32F if rgba.dtype == np.float32 else abi.TEXTURE_RGBA8  # BC6H: linear float RGB
+                textures.append(scene.Texture(np.ascontiguousarray(rgba), fmt))
     finally:
         lib.vkgv_gltf_free(h)
     draws = world.draw_list()

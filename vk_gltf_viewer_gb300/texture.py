@@ -1,10 +1,11 @@
 """Base-colour images for the textured resolve (``vkgv_image_*``,
-``vkgv_dds_parse``, ``vkgv_decode_bc``).
+``vkgv_dds_parse``, ``vkgv_decode_bc``, ``vkgv_decode_bc6h``).
 
-PNG decodes on the host into RGBA8; DDS files hold BC1-BC5 blocks, which the
-device decodes into RGBA8; JPEG is entropy-decoded on the host and turned
-into pixels on the device.  The reference loads no images
-(src/vk_gltf_viewer/assets.cpp:467-471).
+PNG decodes on the host into RGBA8; DDS and KTX2 files hold BC1-BC5 or BC7
+blocks, which the device decodes into RGBA8, or BC6H blocks, which it
+decodes into float32 RGB (a linear ``TEXTURE_RGB32F`` texture); JPEG is
+entropy-decoded on the host and turned into pixels on the device.  The
+reference loads no images (src/vk_gltf_viewer/assets.cpp:467-471).
 """
 from __future__ import annotations
 
@@ -41,7 +42,7 @@ def parse_dds(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
     info = abi.DdsInfo()
     rc = abi.load().vkgv_dds_parse(buf.ctypes.data, buf.size, C.byref(info))
     if rc != abi.OK:
-        raise abi.VkgvError(rc, "not a DDS file with BC1-BC5 or BC7 data")
+        raise abi.VkgvError(rc, "not a DDS file with BC1-BC5, BC6H or BC7 data")
     blocks = buf[info.data_offset:info.data_offset + info.data_size].copy()
     return info, blocks
 
@@ -67,7 +68,7 @@ def parse_ktx2(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
     info = abi.DdsInfo()
     rc = abi.load().vkgv_ktx2_parse(buf.ctypes.data, buf.size, C.byref(info))
     if rc != abi.OK:
-        raise abi.VkgvError(rc, "not a KTX2 file with BC1-BC5, BC7 or RGBA8 data, uncompressed or Zstandard-"
+        raise abi.VkgvError(rc, "not a KTX2 file with BC1-BC5, BC6H, BC7 or RGBA8 data, uncompressed or Zstandard-"
                                 "supercompressed (BasisU files are not decoded)")
     level = buf[info.data_offset:info.data_offset + info.data_size]
     if info.supercompression == 2:
@@ -90,6 +91,29 @@ def decode_bc(renderer, fmt: int, blocks, width: int, height: int, stream=None) 
     abi.check(abi.load().vkgv_decode_bc(renderer.ctx, fmt, blocks.data_ptr(), width, height, out.data_ptr(),
                                         _stream_handle(stream)), renderer.ctx)
     return out
+
+
+def decode_bc6h(renderer, fmt: int, blocks, width: int, height: int, stream=None) -> torch.Tensor:
+    """BC6H blocks (``abi.BC6H_UF16`` or ``abi.BC6H_SF16``) -> device
+    (height, width, 3) float32 RGB, the format's binary16 values exactly,
+    decoded by k_decode_bc6h.  `blocks` is a numpy array or a device tensor
+    of bytes."""
+    dev = torch.device("cuda", renderer.device)
+    if isinstance(blocks, np.ndarray):
+        blocks = torch.from_numpy(np.ascontiguousarray(blocks, np.uint8)).to(dev)
+    out = torch.empty((height, width, 3), dtype=torch.float32, device=blocks.device)
+    abi.check(abi.load().vkgv_decode_bc6h(renderer.ctx, fmt, blocks.data_ptr(), width, height, out.data_ptr(),
+                                          _stream_handle(stream)), renderer.ctx)
+    return out
+
+
+def _decode_blocks(renderer, info, blocks) -> np.ndarray:
+    if info.format in (abi.BC6H_UF16, abi.BC6H_SF16):
+        img = decode_bc6h(renderer, info.format, blocks, info.width, info.height)
+    else:
+        img = decode_bc(renderer, info.format, blocks, info.width, info.height)
+    torch.cuda.synchronize()
+    return img.cpu().numpy()
 
 
 class Jpeg:
@@ -149,18 +173,16 @@ def decode_jpeg(data: bytes, renderer, stream=None) -> torch.Tensor:
 
 
 def load_image(data: bytes, kind: int, renderer=None) -> np.ndarray:
-    """Encoded image -> host (H, W, 4) uint8 RGBA: PNG and RGBA8 KTX2 on the
-    host; DDS, block-compressed KTX2 and JPEG on the device (they need a
-    renderer)."""
+    """Encoded image -> host (H, W, 4) uint8 RGBA, or (H, W, 3) float32 RGB
+    for BC6H: PNG and RGBA8 KTX2 on the host; DDS, block-compressed KTX2 and
+    JPEG on the device (they need a renderer)."""
     if kind == abi.IMAGE_PNG:
         return decode_png(data)
     if kind == abi.IMAGE_DDS:
         if renderer is None:
             raise ValueError("DDS images decode on the device: pass a renderer")
         info, blocks = parse_dds(data)
-        img = decode_bc(renderer, info.format, blocks, info.width, info.height)
-        torch.cuda.synchronize()
-        return img.cpu().numpy()
+        return _decode_blocks(renderer, info, blocks)
     if kind == abi.IMAGE_JPEG:
         if renderer is None:
             raise ValueError("JPEG images decode on the device: pass a renderer")
@@ -173,7 +195,5 @@ def load_image(data: bytes, kind: int, renderer=None) -> np.ndarray:
             return payload.reshape(info.height, info.width, 4)
         if renderer is None:
             raise ValueError("KTX2 block-compressed images decode on the device: pass a renderer")
-        img = decode_bc(renderer, info.format, payload, info.width, info.height)
-        torch.cuda.synchronize()
-        return img.cpu().numpy()
+        return _decode_blocks(renderer, info, payload)
     raise abi.VkgvError(abi.INVALID_ARG, "unknown image format")
