@@ -546,8 +546,9 @@ def run_world(r, host, local, args, stream, peak):
 def run_texture(r, local, args, stream, peak):
     """Base-colour texture decode: BC1, BC3 and BC7 blocks of an 8192^2
     texture into RGBA8 on the device (k_decode_bc; the BC7 blocks take the
-    eight modes equally often), and a 2048^2 RGBA8 PNG on the host (the C2
-    texture size)."""
+    eight modes equally often), BC6H UF16 blocks (the fourteen modes equally
+    often) into float32 RGB (k_decode_bc6h), and a 2048^2 RGBA8 PNG on the
+    host (the C2 texture size)."""
     import zlib
 
     import numpy as np
@@ -558,28 +559,38 @@ def run_texture(r, local, args, stream, peak):
     out = {}
     rng = np.random.default_rng(3)
     w = h = 8192
-    for name, fmt, bsize in (("bc1", abi.BC1, 8), ("bc3", abi.BC3, 16), ("bc7", abi.BC7, 16)):
+    bc6h_modes = np.array([0x00, 0x01, 0x02, 0x06, 0x0A, 0x0E, 0x12, 0x16, 0x1A, 0x1E, 0x03, 0x07, 0x0B, 0x0F],
+                          np.uint8)
+    for name, fmt, bsize in (("bc1", abi.BC1, 8), ("bc3", abi.BC3, 16), ("bc7", abi.BC7, 16),
+                             ("bc6h", abi.BC6H_UF16, 16)):
         host_blocks = rng.integers(0, 256, size=((w // 4) * (h // 4), bsize), dtype=np.uint8)
         if fmt == abi.BC7:  # mode m: the lowest set bit of the first byte is bit m
             modes = np.arange(host_blocks.shape[0]) % 8
             first = host_blocks[:, 0].astype(np.uint32)
             host_blocks[:, 0] = (((first >> (modes + 1)) << (modes + 1)) | (1 << modes)).astype(np.uint8)
+        if fmt == abi.BC6H_UF16:  # a 2-bit (0, 1) or 5-bit mode field
+            modes = bc6h_modes[np.arange(host_blocks.shape[0]) % bc6h_modes.size]
+            keep = np.where(modes < 2, 0xFC, 0xE0).astype(np.uint8)
+            host_blocks[:, 0] = (host_blocks[:, 0] & keep) | modes
         blocks = torch.from_numpy(host_blocks.reshape(-1)).cuda(local)
-        rgba = torch.empty((h, w, 4), dtype=torch.uint8, device=f"cuda:{local}")
+        hdr = fmt == abi.BC6H_UF16
+        rgba = torch.empty((h, w, 3) if hdr else (h, w, 4), dtype=torch.float32 if hdr else torch.uint8,
+                           device=f"cuda:{local}")
         lib = abi.load()
+        decode = lib.vkgv_decode_bc6h if hdr else lib.vkgv_decode_bc
         for _ in range(3):
-            abi.check(lib.vkgv_decode_bc(r.ctx, fmt, blocks.data_ptr(), w, h, rgba.data_ptr(), stream.cuda_stream), r.ctx)
+            abi.check(decode(r.ctx, fmt, blocks.data_ptr(), w, h, rgba.data_ptr(), stream.cuda_stream), r.ctx)
         torch.cuda.synchronize()
         ts = []
         for _ in range(10):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            lib.vkgv_decode_bc(r.ctx, fmt, blocks.data_ptr(), w, h, rgba.data_ptr(), stream.cuda_stream)
+            decode(r.ctx, fmt, blocks.data_ptr(), w, h, rgba.data_ptr(), stream.cuda_stream)
             e1.record(stream)
             ts.append((e0, e1))
         torch.cuda.synchronize()
         ms = statistics.median(a.elapsed_time(b) for a, b in ts)
-        nbytes = blocks.numel() + rgba.numel()
+        nbytes = blocks.numel() + rgba.numel() * rgba.element_size()
         gbs = nbytes / (ms / 1000.0) / 1e9
         out[name + "_8192"] = {"ms": ms, "bytes": nbytes, "achieved_gbs": gbs, "frac": gbs / peak,
                                "texels_per_s": w * h / (ms / 1000.0)}
