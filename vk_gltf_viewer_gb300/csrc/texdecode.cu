@@ -374,30 +374,51 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc7(const uint8_t*
 // VKGV_TEXTURE_RGB32F texture): the published format and the steps the
 // oracle restates (oracle/texture.c), with the same tables.  A 2-bit mode
 // (values 0, 1) or a 5-bit one selects one of fourteen header layouts
-// (tokens: field = endpoint w/x/y/z x channel R/G/B or 12 = partition,
-// lowest field bit, bit count, reversed), transformed modes add signed
+// (the oracle's stream-order tokens regrouped by field, so that each field
+// is assembled in its own register), transformed modes add signed
 // deltas to the base endpoint, endpoints are unquantised to 16 bits, texels
 // interpolated with the 3- or 4-bit BC7 weights and scaled to binary16
 // (unsigned v * 31 >> 6; signed magnitude * 31 >> 5, sign only on a
 // non-zero result).  Reserved modes decode to 0.  Four lanes per block, one
 // row each, like k_decode_bc7; each lane parses the header itself.
-__constant__ uint16_t c_bc6_tok[14][23] = {
-    {0x0047, 0x0048, 0x004B, 0x0900, 0x0901, 0x0902, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x00 */
-    {0x0057, 0x014A, 0x0600, 0x010B, 0x0048, 0x0601, 0x0058, 0x002B, 0x0047, 0x0602, 0x003B, 0x005B, 0x004B, 0x0503, 0x0307, 0x0504, 0x030A, 0x0505, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x01 */
-    {0x0900, 0x0901, 0x0902, 0x0403, 0x00A0, 0x0307, 0x0304, 0x00A1, 0x000B, 0x030A, 0x0305, 0x00A2, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x02 */
-    {0x0900, 0x0901, 0x0902, 0x0303, 0x00A0, 0x004A, 0x0307, 0x0404, 0x00A1, 0x030A, 0x0305, 0x00A2, 0x001B, 0x0308, 0x0306, 0x000B, 0x002B, 0x0309, 0x0047, 0x003B, 0x040C},  /* mode 0x06 */
-    {0x0900, 0x0901, 0x0902, 0x0303, 0x00A0, 0x0048, 0x0307, 0x0304, 0x00A1, 0x000B, 0x030A, 0x0405, 0x00A2, 0x0308, 0x0306, 0x011B, 0x0309, 0x004B, 0x003B, 0x040C},  /* mode 0x0A */
-    {0x0800, 0x0048, 0x0801, 0x0047, 0x0802, 0x004B, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x0E */
-    {0x0700, 0x004A, 0x0048, 0x0701, 0x002B, 0x0047, 0x0702, 0x013B, 0x0503, 0x0307, 0x0404, 0x000B, 0x030A, 0x0405, 0x001B, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x12 */
-    {0x0700, 0x000B, 0x0048, 0x0701, 0x0057, 0x0047, 0x0702, 0x005A, 0x004B, 0x0403, 0x004A, 0x0307, 0x0504, 0x030A, 0x0405, 0x001B, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x16 */
-    {0x0700, 0x001B, 0x0048, 0x0701, 0x0058, 0x0047, 0x0702, 0x005B, 0x004B, 0x0403, 0x004A, 0x0307, 0x0404, 0x000B, 0x030A, 0x0505, 0x0308, 0x0406, 0x002B, 0x0409, 0x003B, 0x040C},  /* mode 0x1A */
-    {0x0500, 0x004A, 0x010B, 0x0048, 0x0501, 0x0057, 0x0058, 0x002B, 0x0047, 0x0502, 0x005A, 0x003B, 0x005B, 0x004B, 0x0503, 0x0307, 0x0504, 0x030A, 0x0505, 0x0308, 0x0506, 0x0509, 0x040C},  /* mode 0x1E */
-    {0x0900, 0x0901, 0x0902, 0x0903, 0x0904, 0x0905},  /* mode 0x03 */
-    {0x0900, 0x0901, 0x0902, 0x0803, 0x00A0, 0x0804, 0x00A1, 0x0805, 0x00A2},  /* mode 0x07 */
-    {0x0900, 0x0901, 0x0902, 0x0703, 0x11A0, 0x0704, 0x11A1, 0x0705, 0x11A2},  /* mode 0x0B */
-    {0x0900, 0x0901, 0x0902, 0x0303, 0x15A0, 0x0304, 0x15A1, 0x0305, 0x15A2},  /* mode 0x0F */
+// Header tokens grouped by field (endpoint w, x, y, z x channel R, G, B;
+// 12 = partition), per mode: the bit position in the block (bits 0-6), the
+// lowest field bit (7-10), bit count - 1 (11-14) and reversed (15: the first
+// block bit is the highest field bit); the counts follow.
+__constant__ uint16_t c_bc6_ftok[14][13][6] = {
+    {{0x4805, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x480F, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4819, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2023, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x202D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2037, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2041, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0202, 0x1829, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0203, 0x183D, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2047, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0228, 0x1833, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0204, 0x0032, 0x00BC, 0x0146, 0x01CC, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x00
+    {{0x3005, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x300F, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x3019, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2823, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x282D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2837, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2841, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0282, 0x0218, 0x1829, 0x0000, 0x0000, 0x0000}, {0x020E, 0x0296, 0x183D, 0x0000, 0x0000, 0x0000}, {0x2847, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0A03, 0x1833, 0x0000, 0x0000, 0x0000, 0x0000}, {0x080C, 0x0117, 0x01A0, 0x02A1, 0x0222, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x01
+    {{0x4805, 0x0528, 0x0000, 0x0000, 0x0000, 0x0000}, {0x480F, 0x0531, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4819, 0x053B, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2023, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x182D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1837, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2041, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1829, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x183D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2047, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1833, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0032, 0x00BC, 0x0146, 0x01CC, 0x0000, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x02
+    {{0x4805, 0x0527, 0x0000, 0x0000, 0x0000, 0x0000}, {0x480F, 0x0532, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4819, 0x053B, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1823, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x202D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1837, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1841, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1829, 0x024B, 0x0000, 0x0000, 0x0000, 0x0000}, {0x183D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1847, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0228, 0x1833, 0x0000, 0x0000, 0x0000, 0x0000}, {0x00BC, 0x0045, 0x0146, 0x01CC, 0x0000, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x06
+    {{0x4805, 0x0527, 0x0000, 0x0000, 0x0000, 0x0000}, {0x480F, 0x0531, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4819, 0x053C, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1823, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x182D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2037, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1841, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1829, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0228, 0x183D, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1847, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1833, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0032, 0x08C5, 0x024B, 0x01CC, 0x0000, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x0A
+    {{0x4005, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x400F, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4019, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2023, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x202D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2037, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2041, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0218, 0x1829, 0x0000, 0x0000, 0x0000, 0x0000}, {0x020E, 0x183D, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2047, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0228, 0x1833, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0222, 0x0032, 0x00BC, 0x0146, 0x01CC, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x0E
+    {{0x3805, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x380F, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x3819, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2823, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x202D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2037, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2841, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0218, 0x1829, 0x0000, 0x0000, 0x0000, 0x0000}, {0x020E, 0x183D, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2847, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x020D, 0x1833, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0117, 0x09A1, 0x0032, 0x00BC, 0x0000, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x12
+    {{0x3805, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x380F, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x3819, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2023, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x282D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2037, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2041, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0297, 0x0218, 0x1829, 0x0000, 0x0000, 0x0000}, {0x020E, 0x183D, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2047, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x02A1, 0x0228, 0x1833, 0x0000, 0x0000, 0x0000}, {0x000D, 0x0222, 0x00BC, 0x0146, 0x01CC, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x16
+    {{0x3805, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x380F, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x3819, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2023, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x202D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2837, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2041, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0218, 0x1829, 0x0000, 0x0000, 0x0000, 0x0000}, {0x020E, 0x0297, 0x183D, 0x0000, 0x0000, 0x0000}, {0x2047, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0228, 0x1833, 0x0000, 0x0000, 0x0000, 0x0000}, {0x008D, 0x02A1, 0x0222, 0x0032, 0x0146, 0x01CC}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x1A
+    {{0x2805, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x280F, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2819, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2823, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x282D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2837, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x2841, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0295, 0x0218, 0x1829, 0x0000, 0x0000, 0x0000}, {0x020E, 0x0296, 0x183D, 0x0000, 0x0000, 0x0000}, {0x2847, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x020B, 0x029F, 0x1833, 0x0000, 0x0000, 0x0000}, {0x080C, 0x0117, 0x01A0, 0x02A1, 0x0222, 0x0000}, {0x204D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x1E
+    {{0x4805, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x480F, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4819, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4823, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x482D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4837, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x03
+    {{0x4805, 0x052C, 0x0000, 0x0000, 0x0000, 0x0000}, {0x480F, 0x0536, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4819, 0x0540, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4023, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x402D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4037, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x07
+    {{0x4805, 0x8D2B, 0x0000, 0x0000, 0x0000, 0x0000}, {0x480F, 0x8D35, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4819, 0x8D3F, 0x0000, 0x0000, 0x0000, 0x0000}, {0x3823, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x382D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x3837, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x0B
+    {{0x4805, 0xAD27, 0x0000, 0x0000, 0x0000, 0x0000}, {0x480F, 0xAD31, 0x0000, 0x0000, 0x0000, 0x0000}, {0x4819, 0xAD3B, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1823, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x182D, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x1837, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}, {0x0000, 0x0000, 0x0000, 0x0000, 0x0000, 0x0000}},  // mode 0x0F
+};
+__constant__ uint8_t c_bc6_fcount[14][13] = {
+    {1, 1, 1, 1, 1, 1, 1, 2, 2, 1, 2, 5, 1},  // mode 0x00
+    {1, 1, 1, 1, 1, 1, 1, 3, 3, 1, 2, 5, 1},  // mode 0x01
+    {2, 2, 2, 1, 1, 1, 1, 1, 1, 1, 1, 4, 1},  // mode 0x02
+    {2, 2, 2, 1, 1, 1, 1, 2, 1, 1, 2, 4, 1},  // mode 0x06
+    {2, 2, 2, 1, 1, 1, 1, 1, 2, 1, 1, 4, 1},  // mode 0x0A
+    {1, 1, 1, 1, 1, 1, 1, 2, 2, 1, 2, 5, 1},  // mode 0x0E
+    {1, 1, 1, 1, 1, 1, 1, 2, 2, 1, 2, 4, 1},  // mode 0x12
+    {1, 1, 1, 1, 1, 1, 1, 3, 2, 1, 3, 5, 1},  // mode 0x16
+    {1, 1, 1, 1, 1, 1, 1, 2, 3, 1, 2, 6, 1},  // mode 0x1A
+    {1, 1, 1, 1, 1, 1, 1, 3, 3, 1, 3, 5, 1},  // mode 0x1E
+    {1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0},  // mode 0x03
+    {2, 2, 2, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0},  // mode 0x07
+    {2, 2, 2, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0},  // mode 0x0B
+    {2, 2, 2, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0},  // mode 0x0F
 };
 // mode value, transformed, endpoint bits, delta bits R, G, B, regions, tokens
+// (the oracle's stream-order count)
 __constant__ uint8_t c_bc6_mode[14][8] = {
     {0x00, 1, 10, 5, 5, 5, 2, 20}, {0x01, 1, 7, 6, 6, 6, 2, 22},   {0x02, 1, 11, 5, 4, 4, 2, 19},
     {0x06, 1, 11, 4, 5, 4, 2, 21}, {0x0A, 1, 11, 4, 4, 5, 2, 20},  {0x0E, 1, 9, 5, 5, 5, 2, 20},
@@ -406,7 +427,8 @@ __constant__ uint8_t c_bc6_mode[14][8] = {
     {0x0B, 1, 12, 8, 8, 8, 1, 9},  {0x0F, 1, 16, 4, 4, 4, 1, 9}};
 
 struct Bc6Tables {
-    uint16_t tok[14][23];
+    uint16_t ftok[14][13][6];
+    uint8_t fcount[14][13];
     uint8_t mode[14][8];
     int8_t row[32];  // 5-bit mode field -> mode row, -1 for a reserved mode
     uint16_t p2[32];
@@ -415,7 +437,9 @@ struct Bc6Tables {
 };
 
 __device__ void bc6_load_tables(Bc6Tables& t) {
-    for (uint32_t i = threadIdx.x; i < 14 * 23; i += blockDim.x) t.tok[i / 23][i % 23] = c_bc6_tok[i / 23][i % 23];
+    for (uint32_t i = threadIdx.x; i < 14 * 13 * 6; i += blockDim.x)
+        t.ftok[i / 78][(i / 6) % 13][i % 6] = c_bc6_ftok[i / 78][(i / 6) % 13][i % 6];
+    for (uint32_t i = threadIdx.x; i < 14 * 13; i += blockDim.x) t.fcount[i / 13][i % 13] = c_bc6_fcount[i / 13][i % 13];
     for (uint32_t i = threadIdx.x; i < 14 * 8; i += blockDim.x) t.mode[i / 8][i % 8] = c_bc6_mode[i / 8][i % 8];
     for (uint32_t i = threadIdx.x; i < 32; i += blockDim.x) {
         // a field whose two low bits are 0 or 1 is a 2-bit mode
@@ -474,19 +498,19 @@ __device__ __forceinline__ void bc6_row(const Bc6Tables& T, const uint4& q, uint
     const uint8_t* M = T.mode[mi];
     uint32_t f[13];
 #pragma unroll
-    for (int k = 0; k < 13; ++k) f[k] = 0u;
-    uint32_t pos = (q.x & 3u) < 2u ? 2u : 5u;
-    for (uint32_t t = 0; t < M[7]; ++t) {
-        const uint32_t tok = T.tok[mi][t], n = ((tok >> 8) & 15u) + 1u;
-        uint32_t v = bc7_bits(lo, hi, pos, n);
-        pos += n;
-        if (tok >> 12) v = __brev(v) >> (32u - n);
-        const uint32_t fid = tok & 15u, sh = (tok >> 4) & 15u;
-        // a dynamic index into f would put it in local memory
-#pragma unroll
-        for (int k = 0; k < 13; ++k)
-            if ((uint32_t)k == fid) f[k] |= v << sh;
+    for (int k = 0; k < 13; ++k) {
+        uint32_t acc = 0u;
+        for (uint32_t t = 0; t < T.fcount[mi][k]; ++t) {
+            const uint32_t tok = T.ftok[mi][k][t], n = ((tok >> 11) & 15u) + 1u;
+            uint32_t v = bc7_bits(lo, hi, tok & 127u, n);
+            if (tok >> 15) v = __brev(v) >> (32u - n);
+            acc |= v << ((tok >> 7) & 15u);
+        }
+        f[k] = acc;
     }
+    // the header ends after the partition field (two regions) or the
+    // last end point (one region)
+    const uint32_t pos = M[6] == 2u ? 82u : 65u;
     const bool tr = M[1] != 0;
     const uint32_t bits = M[2], ns = M[6];
     int32_t ep[4][3];
