@@ -151,6 +151,30 @@ def test_frame_matches_oracle(renderer, grid, name):
     assert renderer.device_status() == (0, 0)
 
 
+def test_frame_at_the_maximum_view_size(renderer, ico):
+    """A whole frame (cull, raster, HiZ, resolve) at the largest view the
+    library accepts, 8192 x 8192, with the icosphere covering 27M pixels:
+    survivors, depth|id, ids and pyramid bit-exact, RGBA within 1/255.  The
+    pyramid's top levels exceed the HiZ tail's shared-memory budget here."""
+    w = h = abi.MAX_VIEW_DIM
+    flags = abi.CULL_FRUSTUM | abi.BUILD_PYRAMID | abi.RESOLVE_FLAT | abi.WRITE_IDS
+    cam = scene.camera((0.0, 0.0, 2.6), (0, 0, 0), (0, 1, 0), 60.0, 1.0)
+    exp = ob.frame(ico.orc, cam, w, h, oracle_flags(flags))
+    v = view(ico, cam, w, h)
+    renderer.frame(ico.dev, [v], flags)
+    torch.cuda.synchronize()
+    assert np.array_equal(np.sort(v.survivor_list()), np.sort(exp["survivors"]))
+    assert np.array_equal(u64(v.depth_id), exp["depth_id"])
+    ids = u32(v.visbuffer)
+    assert np.array_equal(ids, exp["ids"]) and (ids != 0xFFFFFFFF).sum() > 20_000_000
+    assert np.array_equal(v.pyramid.cpu().numpy()[: exp["pyramid"].size], exp["pyramid"])
+    ok, bad = rgba_close(u32(v.color), exp["rgba"])
+    assert ok, f"{bad} pixels off"
+    assert renderer.device_status() == (0, 0)
+    del v
+    torch.cuda.empty_cache()
+
+
 def test_batched_frame_matches_single_views(renderer, grid):
     flags = abi.CULL_FRUSTUM | abi.BUILD_PYRAMID | abi.RESOLVE_FLAT | abi.WRITE_IDS
     sizes = [(256, 256), (512, 384), (640, 360), (97, 61), (1024, 576)]
