@@ -236,6 +236,31 @@ def test_empty_view(renderer, ico):
     assert int(v.survivor_count.item()) == 0
 
 
+def test_scene_without_draws(renderer, ico):
+    """A scene with no meshlet draws goes through every stage of a two-pass
+    textured frame (cull, raster, HiZ, resolve) to a background image, an
+    empty survivor list and a pyramid of the cleared depth (0.0)."""
+    import ctypes as C
+
+    lib = abi.load()
+    empty = abi.Scene.from_buffer_copy(ico.dev.scene)
+    empty.meshlet_draw_count = 0
+    w, h = 320, 200
+    cam = scene.camera((0, 0, 3), (0, 0, 0), (0, 1, 0), 60, w / h)
+    v = view(ico, cam, w, h)
+    v.pyramid.fill_(-1.0)
+    flags = (abi.CULL_FRUSTUM | abi.CULL_OCCLUSION | abi.CULL_TWO_PASS | abi.BUILD_PYRAMID | abi.RESOLVE_TEXTURED
+             | abi.WRITE_IDS)
+    s = v.struct(0)
+    assert lib.vkgv_frame(renderer.ctx, C.byref(empty), C.byref(s), 1, flags, 0) == abi.OK
+    torch.cuda.synchronize()
+    assert np.all(u32(v.visbuffer) == 0xFFFFFFFF) and np.all(u32(v.color) == 0)
+    assert np.all(u64(v.depth_id) == 0)
+    assert int(v.survivor_count.item()) == 0
+    assert np.all(v.pyramid.cpu().numpy()[: ob.pyramid_floats(w, h)] == 0.0)
+    assert renderer.device_status() == (0, 0)
+
+
 def test_invalid_arguments(renderer, ico):
     cam = scene.camera((0, 0, 3), (0, 0, 0), (0, 1, 0), 60, 1.0)
     v = view(ico, cam, 64, 64)
