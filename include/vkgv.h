@@ -644,7 +644,13 @@ enum vkgv_block_format {
     VKGV_BC7 = 8,   /* BPTC UNORM: eight modes of 1-3 subsets, 16-byte blocks       */
     VKGV_BC6H_UF16 = 9,  /* BPTC float, unsigned: fourteen modes of 1-2 regions,
                           * binary16 RGB texels (vkgv_decode_bc6h)                  */
-    VKGV_BC6H_SF16 = 10  /* BPTC float, signed                                      */
+    VKGV_BC6H_SF16 = 10, /* BPTC float, signed                                      */
+    /* uncompressed 32-bit DDS texels (reported by vkgv_dds_parse; decoded on
+     * the host): B, G, R, A bytes; and R, G, B / B, G, R bytes with a fourth
+     * byte that is not alpha (read as 255) */
+    VKGV_BGRA8 = 11,
+    VKGV_RGBX8 = 12,
+    VKGV_BGRX8 = 13
 };
 
 typedef struct vkgv_dds_info {
@@ -661,8 +667,11 @@ typedef struct vkgv_dds_info {
 } vkgv_dds_info;
 
 /* Reads a DDS header (FourCC DXT1-5 / ATI1 / ATI2 / BC4U / BC5U, or DX10
- * with a BC1-BC5, BC6H (UF16 / SF16) or BC7 DXGI format); VKGV_INVALID_ARG
- * for anything else (uncompressed pixel formats). */
+ * with a BC1-BC5, BC6H (UF16 / SF16) or BC7 DXGI format), or an uncompressed
+ * 32-bit one: DX10 R8G8B8A8 (28, 29), B8G8R8A8 (87, 91), B8G8R8X8 (88, 93),
+ * or a DDPF_RGB pixel format with RGBA / BGRA byte masks (format VKGV_RGBA8,
+ * VKGV_BGRA8, or VKGV_RGBX8 / VKGV_BGRX8 without DDPF_ALPHAPIXELS);
+ * VKGV_INVALID_ARG for anything else. */
 int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* out);
 /* Reads a KTX 2.0 header (the container of KHR_texture_basisu, which the
  * reference enables in fastgltf, assets.cpp:539, and links ktx_read for):

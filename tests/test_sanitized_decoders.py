@@ -103,7 +103,7 @@ def test_image_decoders_under_sanitizers(driver, kind):
         seeds = _jpeg()
     elif kind == "dds":
         seeds = [_dds(b"DXT1", 11, 6, bytes(range(8)) * 6), _dds(b"DX10", 8, 4, bytes(32), dxgi=98),
-                 _dds(b"DX10", 8, 4, bytes(32), dxgi=96)]
+                 _dds(b"DX10", 8, 4, bytes(32), dxgi=96), _dds(b"DX10", 3, 5, bytes(60), dxgi=87)]
     elif kind == "ktx2":
         frames = json.loads((ROOT / "tests" / "golden" / "zstd_frames.json").read_text())["cases"]
         bc1 = next(c for c in frames if c["name"] == "bc1_blocks" and c["level"] == 1)

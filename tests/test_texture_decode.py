@@ -116,6 +116,49 @@ def test_dds_headers(built):
         texture.parse_dds(_dds(b"DX10", 4, 4, bytes(16), dxgi=94))  # BC6H_TYPELESS: no sign to read it with
 
 
+def _dds_rgb(w: int, h: int, pf_flags: int, masks, payload: bytes) -> bytes:
+    """A legacy DDS header with an uncompressed DDPF_RGB pixel format."""
+    hdr = bytearray(128)
+    hdr[0:4] = b"DDS "
+    struct.pack_into("<IIIII", hdr, 4, 124, 0x100F, h, w, w * 4)
+    struct.pack_into("<I", hdr, 28, 1)
+    struct.pack_into("<IIIIIIII", hdr, 76, 32, pf_flags, 0, 32, *masks)
+    return bytes(hdr) + payload
+
+
+def test_uncompressed_dds(built):
+    """32-bit DDS texels decode on the host: DX10 R8G8B8A8 / B8G8R8A8 /
+    B8G8R8X8, and legacy RGB pixel formats with RGBA or BGRA byte masks, with
+    or without an alpha channel (without one, alpha reads 255)."""
+    rng = np.random.default_rng(9)
+    px = rng.integers(0, 256, size=(5, 7, 4), dtype=np.uint8)
+    bgra = px[..., [2, 1, 0, 3]].copy()
+    opaque = px.copy()
+    opaque[..., 3] = 255
+    rgba_masks = (0x000000FF, 0x0000FF00, 0x00FF0000, 0xFF000000)
+    bgra_masks = (0x00FF0000, 0x0000FF00, 0x000000FF, 0xFF000000)
+    cases = [(_dds(b"DX10", 7, 5, px.tobytes(), dxgi=28), abi.RGBA8, 0, px),
+             (_dds(b"DX10", 7, 5, px.tobytes(), dxgi=29), abi.RGBA8, 1, px),
+             (_dds(b"DX10", 7, 5, bgra.tobytes(), dxgi=87), abi.BGRA8, 0, px),
+             (_dds(b"DX10", 7, 5, bgra.tobytes(), dxgi=91), abi.BGRA8, 1, px),
+             (_dds(b"DX10", 7, 5, bgra.tobytes(), dxgi=88), abi.BGRX8, 0, opaque),
+             (_dds_rgb(7, 5, 0x41, rgba_masks, px.tobytes()), abi.RGBA8, 0, px),
+             (_dds_rgb(7, 5, 0x41, bgra_masks, bgra.tobytes()), abi.BGRA8, 0, px),
+             (_dds_rgb(7, 5, 0x40, rgba_masks, px.tobytes()), abi.RGBX8, 0, opaque),
+             (_dds_rgb(7, 5, 0x40, bgra_masks, bgra.tobytes()), abi.BGRX8, 0, opaque)]
+    for data, fmt, srgb, exp in cases:
+        info, _ = texture.parse_dds(data)
+        assert (info.width, info.height, info.format, info.srgb, info.data_size) == (7, 5, fmt, srgb, 140)
+        assert np.array_equal(texture.load_image(data, abi.IMAGE_DDS), exp)  # no renderer needed
+    bad = [_dds(b"DX10", 7, 5, px.tobytes()[:-1], dxgi=28),                 # one byte short
+           _dds_rgb(7, 5, 0x41, (0xF800, 0x07E0, 0x001F, 0), px.tobytes()),  # 565 masks
+           _dds_rgb(7, 5, 0x1, rgba_masks, px.tobytes()),                     # neither RGB nor FourCC
+           _dds(b"DX10", 1 << 21, 4, px.tobytes(), dxgi=28)]                 # absurd width
+    for data in bad:
+        with pytest.raises(abi.VkgvError):
+            texture.parse_dds(data)
+
+
 def _rgba(r, g, b, a=255):
     return r | (g << 8) | (b << 16) | (a << 24)
 

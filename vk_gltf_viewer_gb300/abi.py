@@ -210,6 +210,7 @@ GLTF_TEXTURE_REFERENCES = 1
 GLTF_IMAGES = 2
 IMAGE_UNKNOWN, IMAGE_PNG, IMAGE_DDS, IMAGE_JPEG, IMAGE_KTX2 = 0, 1, 2, 3, 4
 BC1, BC2, BC3, BC4, BC5, BC1_OPAQUE, RGBA8, BC7, BC6H_UF16, BC6H_SF16 = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
+BGRA8, RGBX8, BGRX8 = 11, 12, 13  # uncompressed DDS texels (host)
 PATH_TRANSLATION, PATH_ROTATION, PATH_SCALE, PATH_WEIGHTS = 1, 2, 3, 4
 INTERP_LINEAR, INTERP_STEP, INTERP_CUBICSPLINE = 0, 1, 2
 MAX_NODE_DEPTH = 64

@@ -558,10 +558,32 @@ extern "C" int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* ou
     out->height = le32(p + 12);
     out->width = le32(p + 16);
     out->mip_count = std::max<uint32_t>(1, le32(p + 28));
+    // far beyond any texture edge the decoders accept; keeps the byte counts
+    // below 2^64
+    if (out->width > (1u << 20) || out->height > (1u << 20)) return VKGV_INVALID_ARG;
     const uint32_t pf_flags = le32(p + 80), fourcc = le32(p + 84);
     uint64_t offset = 128;
     uint32_t fmt = 0;
-    if (!(pf_flags & 0x4)) return VKGV_INVALID_ARG;  // DDPF_FOURCC: only block-compressed data
+    auto finish = [&](uint32_t format, uint64_t bytes) {
+        out->format = format;
+        out->data_offset = offset;
+        out->data_size = bytes;
+        if (out->width == 0 || out->height == 0 || offset + bytes > size) return VKGV_INVALID_ARG;
+        return VKGV_OK;
+    };
+    const uint64_t texels = uint64_t(out->width) * out->height;
+    if (!(pf_flags & 0x4)) {
+        // DDPF_RGB (0x40): 32-bit texels whose channel masks are RGBA or
+        // BGRA bytes (DDPF_ALPHAPIXELS 0x1 says the top byte is alpha;
+        // without it the texels are opaque and read as alpha 255)
+        const uint32_t bits = le32(p + 88), rm = le32(p + 92), gm = le32(p + 96), bm = le32(p + 100);
+        if (!(pf_flags & 0x40) || bits != 32 || gm != 0x0000FF00u) return VKGV_INVALID_ARG;
+        const bool alpha = (pf_flags & 0x1) != 0;
+        if (rm == 0x000000FFu && bm == 0x00FF0000u) fmt = alpha ? VKGV_RGBA8 : VKGV_RGBX8;
+        else if (rm == 0x00FF0000u && bm == 0x000000FFu) fmt = alpha ? VKGV_BGRA8 : VKGV_BGRX8;
+        else return VKGV_INVALID_ARG;
+        return finish(fmt, texels * 4);
+    }
     auto cc = [](const char* s) { return uint32_t(s[0]) | (uint32_t(s[1]) << 8) | (uint32_t(s[2]) << 16) | (uint32_t(s[3]) << 24); };
     if (fourcc == cc("DXT1")) fmt = VKGV_BC1;
     else if (fourcc == cc("DXT2") || fourcc == cc("DXT3")) fmt = VKGV_BC2;
@@ -573,6 +595,9 @@ extern "C" int vkgv_dds_parse(const void* data, uint64_t size, vkgv_dds_info* ou
         const uint32_t dxgi = le32(p + 128);
         offset = 148;
         switch (dxgi) {  // DXGI_FORMAT_BC*_UNORM and *_UNORM_SRGB
+            case 28: case 29: return (out->srgb = dxgi == 29, finish(VKGV_RGBA8, texels * 4));  // R8G8B8A8_UNORM(_SRGB)
+            case 87: case 91: return (out->srgb = dxgi == 91, finish(VKGV_BGRA8, texels * 4));  // B8G8R8A8_UNORM(_SRGB)
+            case 88: case 93: return (out->srgb = dxgi == 93, finish(VKGV_BGRX8, texels * 4));  // B8G8R8X8_UNORM(_SRGB)
             case 71: case 72: fmt = VKGV_BC1; break;
             case 74: case 75: fmt = VKGV_BC2; break;
             case 77: case 78: fmt = VKGV_BC3; break;
@@ -611,6 +636,7 @@ extern "C" int vkgv_ktx2_parse(const void* data, uint64_t size, vkgv_dds_info* o
     const uint32_t levels = le32(p + 40), scheme = le32(p + 44);
     if ((scheme != 0 && scheme != 2) || vk_format == 0) return VKGV_INVALID_ARG;  // BasisU / BasisLZ
     if (width == 0 || height == 0 || depth > 1 || layers > 1 || faces != 1) return VKGV_INVALID_ARG;
+    if (width > (1u << 20) || height > (1u << 20)) return VKGV_INVALID_ARG;  // byte counts stay below 2^64
     uint32_t fmt = 0, srgb = 0;
     switch (vk_format) {  // VkFormat values
         case 131: fmt = VKGV_BC1_OPAQUE; break;           // BC1_RGB_UNORM_BLOCK

@@ -42,7 +42,7 @@ def parse_dds(data: bytes) -> tuple[abi.DdsInfo, np.ndarray]:
     info = abi.DdsInfo()
     rc = abi.load().vkgv_dds_parse(buf.ctypes.data, buf.size, C.byref(info))
     if rc != abi.OK:
-        raise abi.VkgvError(rc, "not a DDS file with BC1-BC5, BC6H or BC7 data")
+        raise abi.VkgvError(rc, "not a DDS file with BC1-BC5, BC6H, BC7 or 32-bit RGBA / BGRA data")
     blocks = buf[info.data_offset:info.data_offset + info.data_size].copy()
     return info, blocks
 
@@ -105,6 +105,17 @@ def decode_bc6h(renderer, fmt: int, blocks, width: int, height: int, stream=None
     abi.check(abi.load().vkgv_decode_bc6h(renderer.ctx, fmt, blocks.data_ptr(), width, height, out.data_ptr(),
                                           _stream_handle(stream)), renderer.ctx)
     return out
+
+
+def _uncompressed_dds(info, texels: np.ndarray) -> np.ndarray:
+    """32-bit DDS texels -> (H, W, 4) uint8 RGBA: B, G, R byte orders
+    swapped, a fourth byte that is not alpha read as 255."""
+    px = np.array(texels, np.uint8).reshape(info.height, info.width, 4)
+    if info.format in (abi.BGRA8, abi.BGRX8):
+        px = px[..., [2, 1, 0, 3]].copy()
+    if info.format in (abi.RGBX8, abi.BGRX8):
+        px[..., 3] = 255
+    return px
 
 
 def _decode_blocks(renderer, info, blocks) -> np.ndarray:
@@ -174,14 +185,17 @@ def decode_jpeg(data: bytes, renderer, stream=None) -> torch.Tensor:
 
 def load_image(data: bytes, kind: int, renderer=None) -> np.ndarray:
     """Encoded image -> host (H, W, 4) uint8 RGBA, or (H, W, 3) float32 RGB
-    for BC6H: PNG and RGBA8 KTX2 on the host; DDS, block-compressed KTX2 and
-    JPEG on the device (they need a renderer)."""
+    for BC6H: PNG, RGBA8 KTX2 and uncompressed DDS on the host;
+    block-compressed DDS and KTX2, and JPEG, on the device (they need a
+    renderer)."""
     if kind == abi.IMAGE_PNG:
         return decode_png(data)
     if kind == abi.IMAGE_DDS:
-        if renderer is None:
-            raise ValueError("DDS images decode on the device: pass a renderer")
         info, blocks = parse_dds(data)
+        if info.format in (abi.RGBA8, abi.BGRA8, abi.RGBX8, abi.BGRX8):
+            return _uncompressed_dds(info, blocks)
+        if renderer is None:
+            raise ValueError("block-compressed DDS images decode on the device: pass a renderer")
         return _decode_blocks(renderer, info, blocks)
     if kind == abi.IMAGE_JPEG:
         if renderer is None:
