@@ -429,9 +429,11 @@ void launch_cull(const SceneArgs& S, const DeviceView* views, uint32_t nviews, u
     // sm_count * f CTAs over all views: a CTA's prologue (frustum planes,
     // occlusion view-projection, the raster eye from an inverse, in one
     // thread before a barrier) is then paid once per many draws.  256-view
-    // batch: pass 1 7.46 -> 5.96 ms, pass 2 1.40 -> 1.19 ms (f = 8 stays
-    // best for a single view's short pass-2 list).
-    const uint32_t f = pass == 1 ? 128u : (nviews == 1 ? 8u : 40u);
+    // batch: pass 1 7.46 -> 5.96 ms, pass 2 1.40 -> 1.19 ms.  A single view
+    // takes f = 16 in pass 1 (843,776 draws: 2,432 CTAs instead of one
+    // 256-draw CTA per draw block, cull 36 -> 35 us; 8 and 32 were no
+    // faster) and f = 8 for its short pass-2 list.
+    const uint32_t f = pass == 1 ? (nviews == 1 ? 16u : 128u) : (nviews == 1 ? 8u : 40u);
     const uint32_t fill = (sm_count * f + nviews - 1) / nviews;
     uint32_t per_view = want < fill ? want : fill;
     if (per_view > 65535u) per_view = 65535u;
