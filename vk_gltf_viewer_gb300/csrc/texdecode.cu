@@ -372,10 +372,11 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_decode_bc7(const uint8_t*
 // ------------------------------------------------------------------- BC6H
 // BC6H (BPTC float; UF16 unsigned, SF16 signed) into float32 RGB (a linear
 // VKGV_TEXTURE_RGB32F texture): the published format and the steps the
-// oracle restates (oracle/texture.c), with the same tables.  A 2-bit mode
-// (values 0, 1) or a 5-bit one selects one of fourteen header layouts
-// (the oracle's stream-order tokens regrouped by field, so that each field
-// is assembled in its own register), transformed modes add signed
+// oracle restates (oracle/texture.c), with the same partition, anchor and
+// weight tables.  A 2-bit mode (values 0, 1) or a 5-bit one selects one of
+// fourteen header layouts (the oracle's stream-order tokens regrouped by
+// field, so that each field is assembled in its own register), transformed
+// modes add signed
 // deltas to the base endpoint, endpoints are unquantised to 16 bits, texels
 // interpolated with the 3- or 4-bit BC7 weights and scaled to binary16
 // (unsigned v * 31 >> 6; signed magnitude * 31 >> 5, sign only on a
